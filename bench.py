@@ -1,0 +1,375 @@
+#!/usr/bin/env python
+"""Throughput and latency of the per-batch sorting path on GB300.
+
+Workload (the streamed drop-in case): 384 channels at 30 kHz, 500 templates (6 PCs, nt = 61),
+a seeded 60 s recording with a 0-20 um rigid drift cut into 1500-sample batches with nt of
+context on each side, 50 matching iterations, FP32 arithmetic.  One step = one group of
+``--group`` consecutive batches through preprocessing, projection, the matching loop and
+PC features.
+
+* ``value``   device throughput (ch*samples/s of new samples) with the recording resident in
+              HBM, timed with CUDA events on the sorter's stream, max over ranks;
+* ``e2e``     the same through the public C ABI from host int16 buffers (lss_push_batch /
+              lss_poll), host-to-device copies and spike read-back inside the timed region;
+* ``latency`` per-batch push-to-spikes wall time with one batch per launch (p50 / p99);
+* ``roofline`` of the dominant kernel from per-stage CUDA events;
+* ``cpu_baseline`` the float32 CPU oracle port of the same batches on the host cores.
+
+``--impl reference`` times the CPU oracle port (the reference's Kilosort CPU path restated)
+on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NT = 1500
+METRIC = "ch*samples/s & p99 batch latency, chosen vs plain FP32 at >=99.5% spike match"
+UNIT = "ch*samples/s"
+SPIKE_REC_BYTES = 288
+
+
+def args_():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=18)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--seconds", type=float, default=60.0)
+    ap.add_argument("--group", type=int, default=64, help="batches per step")
+    ap.add_argument("--latency-batches", type=int, default=200)
+    ap.add_argument("--cpu-sample", type=int, default=6, help="batches timed on the CPU oracle")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="one short pass (for ncu)")
+    return ap.parse_args()
+
+
+def dataset(seconds: float):
+    from livespikesorter_gb300 import synth
+    cfg = synth.config_stream(seconds=seconds, seed=1)
+    oss_dir, data, _ = synth.cached_dataset(cfg)
+    return cfg, oss_dir, data
+
+
+def workload_config(a, cfg, group):
+    return {"workload": "drop-in streaming, 384 ch x 30 kHz int16, 500 templates, 1500-sample batches "
+                        "+ 2*61 context, 50 iterations, FP32",
+            "channels": cfg.n_chan, "templates": cfg.n_units, "batch_samples": NT, "nt": cfg.nt,
+            "recording_s": a.seconds, "batches_per_step": group, "max_iters": 50,
+            "l2": "inputs larger than L2: every step reads a fresh slice of the HBM-resident recording "
+                  "and streams > 1 GB of intermediates",
+            "parallelism": "replicas" if a.gpus > 1 else "single"}
+
+
+# -------------------------------------------------------------------------------------------
+# CPU oracle port (reference arm and cpu_baseline)
+# -------------------------------------------------------------------------------------------
+def cpu_oracle_rate(data, oss_dir, n_batches, warm=1):
+    from oracle import ks_oracle as ko
+    oss = ko.load_oss_input(oss_dir)
+    nt = oss.wPCA.shape[1]
+    nbat = ko.n_batches(data.shape[0], NT)
+    ids = [1 + (i * 7) % (nbat - 2) for i in range(n_batches + warm)]
+    times = []
+    for i, ib in enumerate(ids):
+        X = ko.padded_batch(data, ib, NT, nt)
+        t0 = time.perf_counter()
+        ko.sort_window(X, oss, max_iters=50, dtype=np.float32)
+        dt = time.perf_counter() - t0
+        if i >= warm:
+            times.append(dt)
+    total = sum(times)
+    return n_batches * NT * data.shape[1] / total, times
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cfg, oss_dir, data = dataset(a.seconds)
+    t0 = time.perf_counter()
+    rate, times = cpu_oracle_rate(data, oss_dir, a.steps, warm=a.warmup)
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, shapes of the named config)",
+            "config": workload_config(a, cfg, 1),
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{a.steps} batches of 1500 new samples (+2*61 context) of the 60 s "
+                                       f"recording through the float32 numpy oracle (Kilosort filter + "
+                                       f"run_matching + xfeat + positions), {cores} host threads"},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t0}
+    print(json.dumps(line))
+    return 0
+
+
+# -------------------------------------------------------------------------------------------
+# GPU arm
+# -------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        load = sorted(sm)[len(sm) // 4:] or sm
+        return {"sm_mhz": float(np.median(load)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops_sustained", 1700.0), "measured"
+    return 6800.0, 1700.0, "fallback"
+
+
+def roofline(stage_ms, n_groups, group, C, T, K, nt, W, ntaps, spikes_per_batch):
+    """Achieved vs peak for the dominant kernel (per-launch algorithmic work / mean duration)."""
+    hbm, tflops, src = peaks()
+    per = {k: v / max(n_groups, 1) for k, v in stage_ms.items()}
+    kern = max((k for k in per if k not in ("h2d", "d2h")), key=lambda k: per[k])
+    ms = per[kern]
+    if kern == "project":
+        work, unit, bound, peak = 2.0 * T * K * C * W * group / 1e12, "TFLOP/s", "tensor", tflops
+    elif kern == "highpass":
+        work, unit, bound, peak = 2.0 * C * W * ntaps * group / 1e12, "TFLOP/s", "tensor", tflops
+    elif kern == "whiten":
+        work, unit, bound, peak = 2.0 * C * C * W * group / 1e12, "TFLOP/s", "tensor", tflops
+    elif kern == "basis_conv":
+        work, unit, bound, peak = 2.0 * C * K * nt * W * group / 1e12, "TFLOP/s", "tensor", tflops
+    elif kern == "match":
+        per_spike = T * (2 * nt + 1) * (4 + 8) + nt * C * (4 + 8)
+        work = group * (4.0 * T * W + spikes_per_batch * per_spike) / 1e9
+        unit, bound, peak = "GB/s", "hbm", hbm
+    else:
+        work = group * (2.0 * W * C + 4.0 * W * C) / 1e9
+        unit, bound, peak = "GB/s", "hbm", hbm
+    achieved = work / (ms / 1e3)
+    return {"kernel": kern, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak, "peak_source": src, "traffic": None, "ms_per_launch": ms,
+            "stage_ms_per_launch": per}
+
+
+def run_gpu(a):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+        torch.cuda.set_device(local)
+    dev = local
+    torch.cuda.set_device(dev)
+    from livespikesorter_gb300 import sorter
+
+    cfg, oss_dir, data = dataset(a.seconds)
+    C, nt, T, K = cfg.n_chan, cfg.nt, cfg.n_units, cfg.n_pcs
+    W = NT + 2 * nt
+    G = a.group
+    n_usable = (data.shape[0] - 2 * nt) // NT
+    n_groups = max(1, n_usable // G)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident throughput -------------------------------------------------------
+    d_data = torch.from_numpy(data).to(f"cuda:{dev}")
+    base_ptr = d_data.data_ptr()
+    row_bytes = C * 2
+    s = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1)
+    ext = torch.cuda.ExternalStream(s.cuda_stream(), device=f"cuda:{dev}")
+    spikes_seen = [0]
+
+    def step(i):
+        g0 = (i % n_groups) * G
+        s.push_device_span(base_ptr + g0 * NT * row_bytes, G, g0 * NT)
+
+    def drain(srt):
+        n = srt.pending()
+        srt.poll(max(n, 1))
+        return n
+
+    for i in range(a.warmup):
+        step(i)
+    drain(s)
+    t_base, n_base = s.stage_times()
+    launches_per_step = s.kernel_launches()
+    barrier()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        with torch.cuda.stream(ext):
+            e0.record(ext)
+        for i in range(a.steps):
+            step(a.warmup + i)
+        with torch.cuda.stream(ext):
+            e1.record(ext)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    spikes_seen[0] = drain(s)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    units = a.steps * G * NT * C
+    value = world * units / (ms / 1e3)
+    t_all, n_all = s.stage_times()
+    stage = {k: t_all[k] - t_base[k] for k in t_all}
+    n_timed = n_all - n_base
+    spikes_per_batch = spikes_seen[0] / max(1, a.steps * G)
+    ntaps = 1281
+    roof = roofline(stage, n_timed, G, C, T, K, nt, W, ntaps, spikes_per_batch)
+    s.close()
+    del d_data
+
+    # ---- end to end through the host API ---------------------------------------------------
+    s2 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G)
+    chunk = G * NT
+    pos = [0]
+    obuf = np.zeros(1 << 16, sorter.SPIKE_DTYPE)
+
+    def host_step():
+        if pos[0] + chunk > data.shape[0]:
+            s2.flush()
+            drain(s2)
+            pos[0] = 0
+        s2.push(data[pos[0]: pos[0] + chunk], pos[0])
+        pos[0] += chunk
+        return len(s2.poll(out=obuf))
+
+    for _ in range(a.warmup + 1):
+        host_step()
+    barrier()
+    torch.cuda.synchronize(dev)
+    n_sp = 0
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        n_sp += host_step()
+    n_sp += drain(s2)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * units / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": chunk * C * 2, "d2h_bytes_per_step": int(n_sp / a.steps * SPIKE_REC_BYTES),
+           "path": "lss_push_batch + lss_poll from pageable host int16 rows"}
+    s2.close()
+
+    # ---- per-batch latency (one batch per launch) --------------------------------------------
+    s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1)
+    lat = []
+    s3.push(data[:NT + 2 * nt], 0)
+    drain(s3)
+    p = NT + 2 * nt
+    for i in range(a.latency_batches + 5):
+        if p + NT > data.shape[0]:
+            break
+        t1 = time.perf_counter()
+        s3.push(data[p: p + NT])
+        s3.poll(out=obuf)
+        if i >= 5:
+            lat.append(1e3 * (time.perf_counter() - t1))
+        p += NT
+    s3.close()
+    latency = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+               "batches": len(lat), "batch_ms_of_signal": 1e3 * NT / 30000.0,
+               "path": "lss_push_batch of 1500 new samples -> lss_poll, group_batches=1"}
+
+    # ---- CPU baseline (rank 0) ----------------------------------------------------------------
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        rate, times = cpu_oracle_rate(data, oss_dir, a.cpu_sample)
+        cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{a.cpu_sample} batches of 1500 new samples (+2*61) through the float32 numpy oracle "
+                         f"(Kilosort filter + run_matching + xfeat + positions), {os.cpu_count()} host threads, "
+                         f"{sum(times):.1f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded generator, shapes of the named config)",
+                "config": workload_config(a, cfg, G), "e2e": e2e, "latency": latency, "roofline": roof,
+                "cpu_baseline": cpu, "clocks": clk.summary(),
+                "gpu_launches": launches_per_step * a.steps,
+                "spikes_per_batch": spikes_per_batch,
+                "realtime_factor": value / (C * 30000.0)}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    a = args_()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_gpu(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,175 @@
+/*
+ * lss_gb300.h -- C ABI of the GB300-native LiveSpikeSorter per-batch sorting path.
+ *
+ * One handle = one probe stream (one sorter instance of the reference) on one CUDA device,
+ * with its own non-blocking CUDA stream and device-resident state.  Handles are independent
+ * and may be driven from different host threads; a single handle is single-producer.
+ *
+ * Every function returns an int status (LSS_OK = 0); no C++ exception crosses this
+ * boundary and nothing calls exit().  lss_last_error() gives the message of the last
+ * failure on a handle.  No CUDA or torch type appears in a signature.
+ *
+ * Semantics of one batch follow Kilosort 4.0.13 as vendored in the reference
+ * (src/Python/run_online_spikes/Lib/site-packages/kilosort/): io.py:757-790 (filter),
+ * template_matching.py:128-202 (run_matching), template_matching.py:50-51,68 (features and
+ * spike time), postprocessing.py:9-46 (duplicates, positions).
+ */
+#ifndef LSS_GB300_H
+#define LSS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LSS_ABI_VERSION 1
+#define LSS_MAX_PCFEAT 64 /* nearest channels x PCs carried per spike */
+
+enum lss_status {
+    LSS_OK = 0,
+    LSS_ERR_ARG = 1,      /* bad argument / size */
+    LSS_ERR_IO = 2,       /* file missing or unreadable */
+    LSS_ERR_FORMAT = 3,   /* .npy word size / rank / shape mismatch, bad misc.txt */
+    LSS_ERR_CUDA = 4,     /* CUDA runtime failure (message has the CUDA error string) */
+    LSS_ERR_NOMEM = 5,    /* device or pinned allocation failed / over the memory budget */
+    LSS_ERR_OVERFLOW = 6, /* a per-batch spike buffer overflowed (spikes beyond it dropped) */
+    LSS_ERR_STATE = 7,    /* call not valid in the handle's state */
+    LSS_ERR_INTERNAL = 8
+};
+
+/* Per-handle options.  Fill with lss_default_params() and override fields. */
+typedef struct lss_params {
+    int32_t abi_version;    /* = LSS_ABI_VERSION */
+    int32_t device;         /* CUDA ordinal (InputParameters.uSelectedDevice) */
+    int32_t batch_samples;  /* NT: new samples per batch (InputParameters.iMaxScanWindow), default 1500 */
+    int32_t max_iters;      /* matching-pursuit iterations per batch, default 50 (OnlineSpikesV2.cu:933) */
+    int32_t group_batches;  /* batches launched together, default 1 (lowest latency); larger = throughput */
+    int32_t n_chan_in;      /* channels per input row; 0 = C of the oss_input; > C selects channelMap */
+    int32_t hp_half_taps;   /* high-pass FIR half length (taps beyond are < 1e-8 of the centre); 0 = 640 */
+    int32_t dedup;          /* 1 = drop same-cluster spikes within duplicate_spike_bins (default 1) */
+    float th_override;      /* > 0 replaces Th_learned of misc.txt */
+    int32_t spike_cap;      /* per-batch spike buffer; 0 = automatic */
+    int64_t mem_budget;     /* device bytes this handle may hold; 0 = no limit (admission check) */
+    int32_t profile;        /* 1 = time every stage with CUDA events (lss_stage_times) */
+    int32_t reserved[5];
+} lss_params;
+
+/* One sorted spike.  time is the stream sample (Kilosort template_matching.py:68). */
+typedef struct lss_spike {
+    int64_t time;       /* stream sample of the spike */
+    int32_t tmpl;       /* pre-clustered template id (row of Wall3), Kilosort iY */
+    int32_t cluster;    /* final cluster: nearest centroid in (x, y) */
+    float amp;          /* B[iY, iX] / nm[iY] */
+    float x, y;         /* feature-energy weighted position (um) */
+    int32_t batch;      /* batch index within the stream */
+    int32_t n_feat;     /* = nearest_chans * n_pcs */
+    int32_t iter;       /* matching iteration that accepted the spike */
+    float pcfeat[LSS_MAX_PCFEAT]; /* [nearest_chans][n_pcs] PC features */
+} lss_spike;
+
+typedef struct lss_info {
+    int32_t C;          /* channels */
+    int32_t T;          /* pre-clustered templates (Wall3 rows) */
+    int32_t T_final;    /* final clusters (templates.npy rows / centroids) */
+    int32_t K;          /* PCs */
+    int32_t nt;         /* template length */
+    int32_t nC;         /* nearest channels */
+    int32_t nt0min;
+    int32_t dup_bins;
+    float th;           /* Th_learned in use */
+    int32_t NT;         /* new samples per batch */
+    int32_t W;          /* window = NT + 2 nt */
+    int32_t group_batches;
+    int64_t device_bytes;   /* device memory held by the handle */
+    int64_t batches_done;
+    int64_t spikes_done;
+} lss_info;
+
+typedef struct lss_handle lss_handle;
+
+/* Defaults. */
+int lss_default_params(lss_params* p);
+
+/* Load an oss_input/ directory (cnpy semantics: row-major, fortran_order ignored) and
+ * allocate all device state.  Replaces OnlineSpikesV2::OnlineSpikesV2 + initializeSorter +
+ * allocateMemory + initializeStaticMemory (src/SpikeSorter/OnlineSpikesV2.cu:248-281,
+ * 322-382, 410-660) minus the UDP handshake (establishDecoderConnection, :384-406). */
+int lss_open(const char* oss_dir, const lss_params* p, lss_handle** out);
+
+/* Shapes and counters. */
+int lss_get_info(const lss_handle* h, lss_info* info);
+
+/* Push n_samples rows of int16 [n_samples][n_chan_in] (channel fastest, SpikeGLX order).
+ * stream_sample_ct = stream index of row 0, or -1 for "continues the previous push"; a
+ * discontinuity flushes the current segment and starts a new one (the skip / behind policy
+ * of OnlineSpikesV2::runSpikeSorting, OnlineSpikesV2.cu:698-761).  The rows are copied into
+ * pinned staging before the call returns; every batch whose window is complete is launched
+ * asynchronously on the handle's stream.  Replaces DataSocket::fetchLatest / fetchFromPlace +
+ * the H2D copy + the per-batch body of runSpikeSorting (dataSocket.cpp:103-171,
+ * OnlineSpikesV2.cu:747-822). */
+int lss_push_batch(lss_handle* h, const int16_t* samples, int64_t n_samples, int64_t stream_sample_ct);
+
+/* Process the samples still buffered as a final batch (last sample replicated to fill the
+ * window, Kilosort io.py:626-629). */
+int lss_flush(lss_handle* h);
+
+/* Copy out finished spikes in time order (blocking until the oldest launched batch group is
+ * done, if any).  *n_out = number written; if cap is too small the rest stay queued and
+ * *n_out = cap.  Replaces saveSpikes + writeSpikesToFile + the payload vectors
+ * (OnlineSpikesV2.cu:1148-1205, onlineSpikesPayload.h:8-48). */
+int lss_poll(lss_handle* h, lss_spike* out, int64_t cap, int64_t* n_out);
+
+/* Number of finished spikes waiting in the queue after waiting for all launched work. */
+int lss_pending(lss_handle* h, int64_t* n);
+
+/* Free everything (OnlineSpikesV2::~OnlineSpikesV2, OnlineSpikesV2.cu:283-320). */
+int lss_close(lss_handle* h);
+
+/* Message of the last failure on h (or of the last failed lss_open when h is NULL). */
+const char* lss_last_error(const lss_handle* h);
+
+/* Sort explicit windows without stream framing: windows = int16 [n_windows][W][n_chan_in].
+ * Spikes of window i carry batch = i and time = the window sample shifted like Kilosort
+ * (s - nt//2 + nt0min).  counts[i] = spikes of window i; out receives them window by window,
+ * each window in (time, template) order, no duplicate removal.  Replaces
+ * OnlineSpikesV2::kilosortMatchingPursuit + computeClosestClusters for one batch
+ * (OnlineSpikesV2.cu:853-1001) with the preprocessing before it (:771-808). */
+int lss_sort_windows(lss_handle* h, const int16_t* windows, int32_t n_windows, int32_t W,
+                     lss_spike* out, int64_t cap, int64_t* counts);
+
+/* Stage outputs of one window for parity checks (float32):
+ *   LSS_STAGE_PREPROCESSED  [W][C]  after mean, median CAR, high-pass, (M @ Wrot)
+ *   LSS_STAGE_SCORES        [W][T]  B before the matching loop (transposed)
+ *   LSS_STAGE_RESIDUAL      [W][C]  Xres after the loop */
+enum lss_stage { LSS_STAGE_PREPROCESSED = 1, LSS_STAGE_SCORES = 2, LSS_STAGE_RESIDUAL = 3 };
+int lss_debug_stage(lss_handle* h, const int16_t* window, int32_t W, int32_t stage, float* out, int64_t out_len);
+
+/* Device kernels launched by the last lss_push_batch / lss_push_device_span / lss_sort_windows /
+ * lss_flush call. */
+int lss_kernel_launches(const lss_handle* h, int64_t* n);
+
+/* Sort n_batches batches whose samples are already in device memory: dev_rows = int16
+ * [n_batches*NT + 2*nt][n_chan_in] on the handle's device; batch b uses rows
+ * [b*NT, b*NT + NT + 2*nt) and its spikes get stream times from first_row_sample = the stream
+ * sample of row 0 (so batch b covers new samples first_row_sample + nt + b*NT ...).  The rows must
+ * stay valid until the batches are collected (lss_poll / lss_pending).  For acquisition that
+ * lands on the GPU directly; no host staging copy.  Replaces the H2D copy of
+ * OnlineSpikesV2::runSpikeSorting (OnlineSpikesV2.cu:747-761) for device-resident input. */
+int lss_push_device_span(lss_handle* h, const int16_t* dev_rows, int64_t n_batches, int64_t first_row_sample);
+
+/* The handle's CUDA stream (a cudaStream_t) as an opaque pointer, for callers that order their
+ * own device work or timing events against the sorter's. */
+int lss_cuda_stream(const lss_handle* h, void** stream);
+
+/* Per-stage device time accumulated with CUDA events since the handle opened (profile = 1):
+ * ms[0..LSS_N_STAGES-1] = h2d, colsum, car, highpass, whiten, basis_conv, project, match,
+ * features, d2h; *n_groups = batch groups timed.  The reference's per-stage Timer
+ * (Timer.h:7-21) prints nothing; this is its working counterpart. */
+#define LSS_N_STAGES 10
+int lss_stage_times(lss_handle* h, double* ms, int32_t n, int64_t* n_groups);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LSS_GB300_H */

@@ -1,0 +1,285 @@
+// kernels_pre.cu -- preprocessing of a group of windows (Kilosort io.py:757-790):
+// exact integer channel sums, mean removal + median CAR (one warp per time sample), the
+// circular zero-phase high-pass as an FIR in registers, and the temporal-basis convolution
+// (Kilosort template_matching.py:145, conv1d with padding nt//2).
+#include "lss_kernels.cuh"
+
+#include <cstdio>
+
+namespace lss {
+
+// ---------------------------------------------------------------------------------------
+// channel sums over each window, exact in integers (mean = sum / W, rounded once)
+// ---------------------------------------------------------------------------------------
+constexpr int kSumRows = 128;
+
+__global__ void colsum_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan,
+                              int C, int W, int NT, long long* __restrict__ colsum) {
+    const int b = blockIdx.z;
+    const int r0 = blockIdx.y * kSumRows;
+    const int r1 = min(W, r0 + kSumRows);
+    const int64_t base = (int64_t)b * NT;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+        const int src = chan ? chan[c] : c;
+        int acc = 0;
+        for (int r = r0; r < r1; ++r) acc += raw[(base + r) * row_stride + src];
+        atomicAdd(reinterpret_cast<unsigned long long*>(colsum + (int64_t)b * C + c),
+                  (unsigned long long)(long long)acc);
+    }
+}
+
+void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
+                   long long* colsum, cudaStream_t s) {
+    cudaMemsetAsync(colsum, 0, sizeof(long long) * (size_t)nb * C, s);
+    dim3 grid((C + 255) / 256, (W + kSumRows - 1) / kSumRows, nb);
+    colsum_kernel<<<grid, 256, 0, s>>>(raw, row_stride, chan, C, W, NT, colsum);
+}
+
+// ---------------------------------------------------------------------------------------
+// mean removal + lower median across channels (torch.median semantics), one warp per row
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t f2key(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key2f(uint32_t k) {
+    uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+
+constexpr int kCarWarps = 8;
+constexpr int kMaxChanPerLane = 32;   // C <= 1024
+
+__global__ void __launch_bounds__(kCarWarps * 32)
+car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C, int W,
+           int NT, const long long* __restrict__ colsum, int L, int R, float* __restrict__ Xw) {
+    const int b = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kCarWarps + (threadIdx.x >> 5);
+    if (w >= W) return;
+    const int64_t rowp = ((int64_t)b * NT + w) * row_stride;
+    const int nj = (C + 31) >> 5;
+    float v[kMaxChanPerLane];
+    uint32_t key[kMaxChanPerLane];
+    const double invW = 1.0 / (double)W;
+#pragma unroll
+    for (int j = 0; j < kMaxChanPerLane; ++j) {
+        const int c = lane + 32 * j;
+        if (j < nj && c < C) {
+            const float mean = (float)((double)colsum[(int64_t)b * C + c] * invW);
+            const float x = (float)raw[rowp + (chan ? chan[c] : c)] - mean;
+            v[j] = x;
+            key[j] = f2key(x);
+        } else {
+            v[j] = 0.f;
+            key[j] = 0xffffffffu;   // sorts after every real value, never selected (k < C)
+        }
+    }
+    // k-th smallest by MSB-first bit selection over order-preserving keys
+    uint32_t prefix = 0;
+    int k = (C - 1) >> 1;
+    for (int bit = 31; bit >= 0; --bit) {
+        const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
+        int cnt = 0;
+#pragma unroll
+        for (int j = 0; j < kMaxChanPerLane; ++j) {
+            if (j < nj) cnt += ((key[j] & hi_mask) == prefix) && !((key[j] >> bit) & 1u);
+        }
+        cnt = __reduce_add_sync(0xffffffffu, cnt);
+        if (k >= cnt) {
+            k -= cnt;
+            prefix |= (1u << bit);
+        }
+    }
+    const float med = key2f(prefix);
+    const int rows = W + L + R;
+    float* xb = Xw + (int64_t)b * rows * C;
+    const bool wrapL = (w >= W - L);   // also lands in the left pad
+    const bool wrapR = (w < R);        // also lands in the right pad
+#pragma unroll
+    for (int j = 0; j < kMaxChanPerLane; ++j) {
+        const int c = lane + 32 * j;
+        if (j < nj && c < C) {
+            const float y = v[j] - med;
+            xb[(int64_t)(w + L) * C + c] = y;
+            if (wrapL) xb[(int64_t)(w + L - W) * C + c] = y;
+            if (wrapR) xb[(int64_t)(w + L + W) * C + c] = y;
+        }
+    }
+}
+
+void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
+                const long long* colsum, int L, int R, float* Xw, cudaStream_t s) {
+    dim3 grid((W + kCarWarps - 1) / kCarWarps, nb);
+    car_kernel<<<grid, kCarWarps * 32, 0, s>>>(raw, row_stride, chan, C, W, NT, colsum, L, R, Xw);
+}
+
+// ---------------------------------------------------------------------------------------
+// circular high-pass: Y[w][c] = sum_j taps[j] * Xw[w + j][c]   (taps zero-padded to kHpChunk)
+// CTA = 32 channels x 128 rows; a thread owns one channel and 32 consecutive rows; each
+// chunk of 32 taps is applied from a shared-memory tile of 159 rows.
+// ---------------------------------------------------------------------------------------
+constexpr int kHpRows = 128;
+constexpr int kHpRowsPerThread = 32;
+constexpr int kHpChunk = 32;
+constexpr int kHpTile = kHpRows + kHpChunk - 1;
+
+__global__ void __launch_bounds__(128)
+highpass_kernel(const float* __restrict__ Xw, int C, int W, int rows_in, const float* __restrict__ taps, int ntaps,
+                float* __restrict__ Y) {
+    __shared__ float xs[kHpTile][32];
+    __shared__ float ts[kHpChunk];
+    const int b = blockIdx.z;
+    const int c0 = blockIdx.y * 32;
+    const int w0 = blockIdx.x * kHpRows;
+    const int tc = threadIdx.x & 31;
+    const int rg = threadIdx.x >> 5;   // 0..3
+    const float* xb = Xw + (int64_t)b * rows_in * C;
+    float acc[kHpRowsPerThread];
+#pragma unroll
+    for (int r = 0; r < kHpRowsPerThread; ++r) acc[r] = 0.f;
+
+    for (int j0 = 0; j0 < ntaps; j0 += kHpChunk) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < kHpTile * 32; i += blockDim.x) {
+            const int rr = i >> 5, cc = i & 31;
+            const int row = w0 + j0 + rr, ch = c0 + cc;
+            xs[rr][cc] = (row < rows_in && ch < C) ? xb[(int64_t)row * C + ch] : 0.f;
+        }
+        if (threadIdx.x < kHpChunk) ts[threadIdx.x] = taps[j0 + threadIdx.x];
+        __syncthreads();
+        float xv[kHpRowsPerThread + kHpChunk - 1];
+#pragma unroll
+        for (int u = 0; u < kHpRowsPerThread + kHpChunk - 1; ++u) xv[u] = xs[rg * kHpRowsPerThread + u][tc];
+#pragma unroll
+        for (int jj = 0; jj < kHpChunk; ++jj) {
+            const float t = ts[jj];
+#pragma unroll
+            for (int r = 0; r < kHpRowsPerThread; ++r) acc[r] = fmaf(t, xv[r + jj], acc[r]);
+        }
+    }
+    const int ch = c0 + tc;
+    if (ch >= C) return;
+    float* yb = Y + (int64_t)b * W * C;
+#pragma unroll
+    for (int r = 0; r < kHpRowsPerThread; ++r) {
+        const int w = w0 + rg * kHpRowsPerThread + r;
+        if (w < W) yb[(int64_t)w * C + ch] = acc[r];
+    }
+}
+
+void launch_highpass(const float* Xw, int C, int W, int L, int R, const float* taps, int nb, float* Y,
+                     cudaStream_t s) {
+    const int ntaps = L + R + 1;
+    dim3 grid((W + kHpRows - 1) / kHpRows, (C + 31) / 32, nb);
+    highpass_kernel<<<grid, 128, 0, s>>>(Xw, C, W, W + L + R, taps, ntaps, Y);
+}
+
+// ---------------------------------------------------------------------------------------
+// temporal basis convolution: Bpc[w][k][c] = sum_m wPCA[k][m] * Z[w + m - nt/2][c]
+// ---------------------------------------------------------------------------------------
+constexpr int kConvRows = 8;        // rows per thread
+constexpr int kConvMaxK = 8;
+
+template <int NT_, int K_>
+struct BasisParam {
+    float w[K_ * NT_];
+};
+
+// Specialised for the common (nt, K): the basis lives in the kernel parameter bank so every
+// multiply-add takes it as an immediate constant operand.
+template <int NT_, int K_>
+__global__ void __launch_bounds__(128)
+basis_conv_fixed(const float* __restrict__ Z, int C, int W, BasisParam<NT_, K_> bp, float* __restrict__ Bpc) {
+    const int b = blockIdx.z;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w0 = blockIdx.y * kConvRows;
+    if (c >= C) return;
+    const float* zb = Z + (int64_t)b * W * C;
+    constexpr int H = NT_ / 2;
+    float acc[kConvRows][K_];
+#pragma unroll
+    for (int r = 0; r < kConvRows; ++r)
+#pragma unroll
+        for (int k = 0; k < K_; ++k) acc[r][k] = 0.f;
+#pragma unroll
+    for (int u = 0; u < kConvRows + NT_ - 1; ++u) {
+        const int row = w0 + u - H;
+        const float x = (row >= 0 && row < W) ? __ldg(zb + (int64_t)row * C + c) : 0.f;
+#pragma unroll
+        for (int r = 0; r < kConvRows; ++r) {
+            const int m = u - r;
+            if (m >= 0 && m < NT_) {
+#pragma unroll
+                for (int k = 0; k < K_; ++k) acc[r][k] = fmaf(x, bp.w[k * NT_ + m], acc[r][k]);
+            }
+        }
+    }
+    float* ob = Bpc + (int64_t)b * W * K_ * C;
+#pragma unroll
+    for (int r = 0; r < kConvRows; ++r) {
+        const int w = w0 + r;
+        if (w < W) {
+#pragma unroll
+            for (int k = 0; k < K_; ++k) ob[((int64_t)w * K_ + k) * C + c] = acc[r][k];
+        }
+    }
+}
+
+// Any (nt, K <= 8): basis read from global memory (cached).
+__global__ void __launch_bounds__(128)
+basis_conv_generic(const float* __restrict__ Z, int C, int W, const float* __restrict__ wPCA, int K, int nt,
+                   float* __restrict__ Bpc) {
+    const int b = blockIdx.z;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w0 = blockIdx.y * kConvRows;
+    if (c >= C) return;
+    const float* zb = Z + (int64_t)b * W * C;
+    const int H = nt / 2;
+    float acc[kConvRows][kConvMaxK];
+#pragma unroll
+    for (int r = 0; r < kConvRows; ++r)
+#pragma unroll
+        for (int k = 0; k < kConvMaxK; ++k) acc[r][k] = 0.f;
+    for (int u = 0; u < kConvRows + nt - 1; ++u) {
+        const int row = w0 + u - H;
+        const float x = (row >= 0 && row < W) ? __ldg(zb + (int64_t)row * C + c) : 0.f;
+#pragma unroll
+        for (int r = 0; r < kConvRows; ++r) {
+            const int m = u - r;
+            if (m >= 0 && m < nt) {
+#pragma unroll
+                for (int k = 0; k < kConvMaxK; ++k)
+                    if (k < K) acc[r][k] = fmaf(x, __ldg(wPCA + k * nt + m), acc[r][k]);
+            }
+        }
+    }
+    float* ob = Bpc + (int64_t)b * W * K * C;
+#pragma unroll
+    for (int r = 0; r < kConvRows; ++r) {
+        const int w = w0 + r;
+        if (w < W)
+            for (int k = 0; k < K; ++k) ob[((int64_t)w * K + k) * C + c] = acc[r][k];
+    }
+}
+
+void launch_basis_conv(const float* Z, int C, int W, const float* wPCA_dev, int K, int nt, int nb, float* Bpc,
+                       cudaStream_t s) {
+    dim3 grid((C + 127) / 128, (W + kConvRows - 1) / kConvRows, nb);
+    basis_conv_generic<<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, K, nt, Bpc);
+}
+
+// Host-side basis (needed for the parameter-bank specialisation).
+void launch_basis_conv_host(const float* Z, int C, int W, const float* wPCA_dev, const float* wPCA_host, int K,
+                            int nt, int nb, float* Bpc, cudaStream_t s) {
+    dim3 grid((C + 127) / 128, (W + kConvRows - 1) / kConvRows, nb);
+    if (nt == 61 && K == 6 && wPCA_host) {
+        BasisParam<61, 6> bp;
+        for (int i = 0; i < 6 * 61; ++i) bp.w[i] = wPCA_host[i];
+        basis_conv_fixed<61, 6><<<grid, 128, 0, s>>>(Z, C, W, bp, Bpc);
+    } else {
+        basis_conv_generic<<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, K, nt, Bpc);
+    }
+}
+
+}  // namespace lss

@@ -1,0 +1,74 @@
+// lss_kernels.cuh -- device kernels of the per-batch sorting path and their launchers.
+//
+// Data layout in HBM (time-major everywhere, so every stage reads and writes rows that are
+// contiguous across channels or templates):
+//   raw      int16 [S][Cin]            one contiguous span; window b starts at row b*NT
+//   Xw       f32   [nb][W+L+R][C]      median-CAR'd window, circularly wrapped by L/R rows
+//   Y        f32   [nb][W][C]          high-passed
+//   Z        f32   [nb][W][C]          whitened + drift-corrected (M @ Wrot); becomes Xres
+//   Bpc      f32   [nb][W][K][C]       temporal-basis convolution
+//   Bt       f32   [nb][W][T]          template scores B transposed (templates contiguous)
+//   ctcP     f32   [T][2nt+1][T]       ctcP[s][l][t] = ctc[t][s][l]  (target template contiguous)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lss {
+
+// Per-batch results of the matching loop (device).
+struct MatchOut {
+    int* n_spikes;     // [nb] spikes accepted (may exceed cap: then the list is truncated)
+    int* n_iters;      // [nb] iterations that accepted spikes
+    int* status;       // [nb] bit 0 = spike list overflow, bit 1 = bad launch shape
+    int* sp_w;         // [nb][cap] window sample
+    int* sp_t;         // [nb][cap] template
+    float* sp_amp;     // [nb][cap]
+    int* sp_iter;      // [nb][cap]
+    int cap;
+};
+
+// Scratch of the matching loop (device), per batch.
+struct MatchScratch {
+    float* cfmax;      // [nb][W]
+    int* imax;         // [nb][W]
+    int* at_t;         // [nb][W]   template of the spike accepted at w this iteration, -1 if none
+    float* at_amp;     // [nb][W]
+    unsigned char* dirty;  // [nb][W]
+    int* cta_cnt;      // [nb][2][G]
+};
+
+// One spike record as written by the feature kernel (host-mapped memory).
+struct SpikeRec {
+    int32_t batch, w, t, iter;
+    float amp, x, y;
+    int32_t cluster;
+    float feat[64];
+};
+
+constexpr int kMatchCluster = 8;   // CTAs per batch in the matching loop (one thread-block cluster)
+constexpr int kMatchThreads = 512;
+
+void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT,
+                   int nb, long long* colsum, cudaStream_t s);
+void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
+                const long long* colsum, int L, int R, float* Xw, cudaStream_t s);
+void launch_highpass(const float* Xw, int C, int W, int L, int R, const float* taps, int nb, float* Y,
+                     cudaStream_t s);
+void launch_sgemm_nt(const float* A, int64_t lda, int64_t strideA, const float* B, int64_t ldb,
+                     float* Cm, int64_t ldc, int64_t strideC, int M, int N, int K, int nb, cudaStream_t s);
+void launch_basis_conv(const float* Z, int C, int W, const float* wPCA, int K, int nt, int nb, float* Bpc,
+                       cudaStream_t s);
+// wPCA_host (K*nt floats) enables the specialisation with the basis in the parameter bank.
+void launch_basis_conv_host(const float* Z, int C, int W, const float* wPCA_dev, const float* wPCA_host, int K,
+                            int nt, int nb, float* Bpc, cudaStream_t s);
+cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
+                         float th2, int W, int T, int C, int nt, int max_iters, int nb,
+                         const MatchScratch& sc, const MatchOut& out, cudaStream_t s);
+void launch_features(const float* Xres, const MatchOut& out, int nb, int W, int C, int T, int K, int nt, int nC,
+                     const float* wPCA, const int64_t* iCC, const int64_t* iU, const float* Ucc, const float* xc,
+                     const float* yc, const float* centroids, int n_final, const int* rec_offset, SpikeRec* recs,
+                     int batch_base, cudaStream_t s);
+void launch_rec_offsets(const MatchOut& out, int nb, int* rec_offset, cudaStream_t s);
+
+}  // namespace lss

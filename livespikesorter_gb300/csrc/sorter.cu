@@ -1,0 +1,845 @@
+// sorter.cu -- host side of one sorter handle: device-resident state, stream framing,
+// launch sequence of a group of batches, egress, and the C ABI of include/lss_gb300.h.
+//
+// Stream framing follows Kilosort's batching (io.py:584-637, template_matching.py:56-68): batch j
+// of a segment covers the new samples [s0 + j*NT, s0 + (j+1)*NT) and is sorted on the window
+// [s0 + j*NT - nt, s0 + (j+1)*NT + nt); the first window's left pad repeats the first sample, the
+// last window's right side repeats the last sample.  Detections are limited to the interior of a
+// window (Cf is zeroed on nt samples at both ends), so consecutive windows tile the stream
+// without double counting.  The reference's own loop overlaps windows by lookback = 2M samples
+// (OnlineSpikesV2.cu:844) -- the same 2*nt overlap -- and computes the spike time as
+// start + s - M/2 - M + nt0min - lookback (OnlineSpikesV2.cu:1186-1187) for its framing; here the
+// time is window_start + s - nt//2 + nt0min, Kilosort's formula.
+#include "../../include/lss_gb300.h"
+#include "lss_kernels.cuh"
+#include "oss_input.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace lss {
+
+struct CudaError {
+    std::string msg;
+};
+
+#define LSS_CUDA(call)                                                                             \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            throw ::lss::CudaError{std::string(#call) + ": " + cudaGetErrorString(e_) + " (" +            \
+                            std::to_string((int)e_) + ")"};                                        \
+    } while (0)
+
+template <typename T>
+static T* dev_alloc(size_t n, int64_t& tally) {
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) throw LoadError{LSS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    tally += (int64_t)(n * sizeof(T));
+    return static_cast<T*>(p);
+}
+
+template <typename T>
+static T* dev_upload(const std::vector<T>& v, int64_t& tally, cudaStream_t s) {
+    T* p = dev_alloc<T>(v.size(), tally);
+    LSS_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return p;
+}
+
+struct TapSet {
+    float* d = nullptr;
+    int L = 0, R = 0;
+};
+
+struct Slot {
+    int16_t* h_stage = nullptr;
+    size_t stage_rows = 0;
+    SpikeRec* h_recs = nullptr;
+    SpikeRec* d_recs = nullptr;
+    int* h_off = nullptr;
+    int* d_off = nullptr;
+    int* h_nsp = nullptr;     // [nbcap] spikes found (may exceed cap)
+    int* h_status = nullptr;  // [nbcap]
+    cudaEvent_t ev = nullptr;
+    cudaEvent_t tev[LSS_N_STAGES + 1] = {};   // stage boundaries (profile = 1)
+    bool busy = false;
+    int nb = 0, W = 0;
+    bool windows_api = false;
+    std::vector<int64_t> win_start;   // stream sample of each window's first row
+    std::vector<int64_t> batch_id;
+    std::vector<int64_t> drop_before; // spikes earlier than this are dropped (first batch of a segment)
+};
+
+struct Handle {
+    lss_params p{};
+    OssModel m;
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    int C = 0, T = 0, K = 0, nt = 0, nC = 0, Tf = 0, Cin = 0, NT = 0, W = 0, G = 1, cap = 0, max_iters = 50;
+    float th = 8.f;
+    int64_t dev_bytes = 0;
+    std::string err;
+    int64_t launches_last = 0;
+    int64_t batches_done = 0, spikes_done = 0;
+    bool overflow_pending = false;
+    double stage_ms[LSS_N_STAGES] = {};
+    int64_t groups_timed = 0;
+
+    // static device state
+    float *d_WD = nullptr, *d_Wall3 = nullptr, *d_ctcP = nullptr, *d_pre_wf = nullptr, *d_nm = nullptr;
+    float *d_wPCA = nullptr, *d_Ucc = nullptr, *d_xc = nullptr, *d_yc = nullptr, *d_cent = nullptr;
+    int64_t *d_iCC = nullptr, *d_iU = nullptr;
+    int32_t* d_chan = nullptr;
+    std::map<int, TapSet> taps;
+
+    // work buffers
+    int Wcap = 0, nbcap = 0;
+    size_t raw_rows_cap = 0;
+    int16_t* d_raw = nullptr;
+    long long* d_colsum = nullptr;
+    float *d_Xw = nullptr, *d_Y = nullptr, *d_Z = nullptr, *d_Bpc = nullptr, *d_Bt = nullptr;
+    MatchScratch sc{};
+    MatchOut mo{};
+    int64_t work_bytes = 0;
+
+    // output slots (in flight groups) and the finished-spike queue
+    std::vector<Slot> slots;
+    std::deque<int> inflight;   // slot indices in launch order
+    std::deque<lss_spike> ready;
+
+    // stream framing
+    bool seg_active = false;
+    int64_t seg_s0 = 0, next_batch = 0, expected_ct = 0, batch_counter = 0;
+    std::vector<int16_t> buf;   // rows from the next window's first row on
+    std::map<int, int64_t> last_kept;   // per final cluster (duplicate removal)
+
+    ~Handle();
+    void init(const char* dir, const lss_params* prm);
+    TapSet& taps_for(int Wn);
+    void ensure_work(int Wn, int nb);
+    void free_work();
+    int acquire_slot();
+    void launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, int stage_rows,
+                      const int16_t* dev_src = nullptr);
+    void push_device(const int16_t* rows, int64_t n_batches, int64_t first_row_sample);
+    void collect(int slot_idx, std::vector<lss_spike>* direct, std::vector<int64_t>* counts);
+    void drain_all();
+    void push(const int16_t* x, int64_t n, int64_t ct);
+    void flush();
+    void launch_windows_from_buf(int g, bool pad_to_end);
+};
+
+Handle::~Handle() {
+    if (dev >= 0) cudaSetDevice(dev);
+    if (st) cudaStreamSynchronize(st);
+    free_work();
+    for (auto& kv : taps) cudaFree(kv.second.d);
+    for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
+                    (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
+                    (void*)d_chan})
+        if (p) cudaFree(p);
+    for (auto& s : slots) {
+        if (s.h_stage) cudaFreeHost(s.h_stage);
+        if (s.h_recs) cudaFreeHost(s.h_recs);
+        if (s.h_off) cudaFreeHost(s.h_off);
+        if (s.h_nsp) cudaFreeHost(s.h_nsp);
+        if (s.h_status) cudaFreeHost(s.h_status);
+        if (s.ev) cudaEventDestroy(s.ev);
+        for (cudaEvent_t e : s.tev)
+            if (e) cudaEventDestroy(e);
+    }
+    if (st) cudaStreamDestroy(st);
+}
+
+void Handle::free_work() {
+    for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
+                    (void*)sc.cfmax, (void*)sc.imax, (void*)sc.at_t, (void*)sc.at_amp, (void*)sc.dirty,
+                    (void*)sc.cta_cnt, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
+                    (void*)mo.sp_t, (void*)mo.sp_amp, (void*)mo.sp_iter})
+        if (p) cudaFree(p);
+    d_raw = nullptr;
+    d_colsum = nullptr;
+    d_Xw = d_Y = d_Z = d_Bpc = d_Bt = nullptr;
+    sc = MatchScratch{};
+    mo = MatchOut{};
+    dev_bytes -= work_bytes;
+    work_bytes = 0;
+    Wcap = nbcap = 0;
+}
+
+void Handle::init(const char* dir, const lss_params* prm) {
+    lss_default_params(&p);
+    if (prm) {
+        if (prm->abi_version != LSS_ABI_VERSION) throw LoadError{LSS_ERR_ARG, "lss_params.abi_version mismatch"};
+        p = *prm;
+    }
+    if (p.batch_samples <= 0 || p.max_iters <= 0 || p.group_batches <= 0 || p.hp_half_taps < 0)
+        throw LoadError{LSS_ERR_ARG, "lss_params: non-positive batch_samples / max_iters / group_batches"};
+    m = load_oss_input(dir ? dir : "");
+    if (m.nt % 2 == 0) throw LoadError{LSS_ERR_FORMAT, "template length must be odd"};
+    if (m.C > 1024) throw LoadError{LSS_ERR_FORMAT, "more than 1024 channels"};
+    C = (int)m.C;
+    T = (int)m.T;
+    K = (int)m.K;
+    nt = (int)m.nt;
+    nC = (int)m.nC;
+    Tf = (int)(m.centroids.size() / 2);
+    if (K > 8) throw LoadError{LSS_ERR_FORMAT, "more than 8 PCs"};
+    Cin = p.n_chan_in > 0 ? p.n_chan_in : C;
+    if (Cin < C) throw LoadError{LSS_ERR_ARG, "n_chan_in smaller than the channel count"};
+    NT = p.batch_samples;
+    W = NT + 2 * nt;
+    G = p.group_batches;
+    max_iters = p.max_iters;
+    th = p.th_override > 0.f ? p.th_override : m.th;
+    if (Cin > C) {
+        for (int64_t v : m.channel_map)
+            if (v < 0 || v >= Cin) throw LoadError{LSS_ERR_FORMAT, "channelMap entry outside n_chan_in"};
+    }
+
+    dev = p.device;
+    int ndev = 0;
+    LSS_CUDA(cudaGetDeviceCount(&ndev));
+    if (dev < 0 || dev >= ndev) throw LoadError{LSS_ERR_ARG, "device ordinal out of range"};
+    LSS_CUDA(cudaSetDevice(dev));
+    LSS_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+
+    // derived host arrays: (M @ Wrot) in float64, ctc permuted so the target template is
+    // contiguous, squared template norms
+    std::vector<float> WD((size_t)C * C);
+    for (int i = 0; i < C; ++i)
+        for (int j = 0; j < C; ++j) {
+            double acc = 0.0;
+            for (int k = 0; k < C; ++k) acc += (double)m.drift[(size_t)i * C + k] * (double)m.whitening[(size_t)k * C + j];
+            WD[(size_t)i * C + j] = (float)acc;
+        }
+    const int L2 = 2 * nt + 1;
+    std::vector<float> ctcP((size_t)T * L2 * T);
+    for (int t = 0; t < T; ++t)
+        for (int s = 0; s < T; ++s) {
+            const float* src = &m.ctc[((size_t)t * T + s) * L2];
+            for (int l = 0; l < L2; ++l) ctcP[((size_t)s * L2 + l) * T + t] = src[l];
+        }
+    std::vector<float> nm(T);
+    for (int t = 0; t < T; ++t) {
+        double acc = 0.0;
+        for (size_t i = 0; i < (size_t)K * C; ++i) {
+            const double v = m.Wall3[(size_t)t * K * C + i];
+            acc += v * v;
+        }
+        nm[t] = (float)acc;
+    }
+    std::vector<int32_t> chan(C);
+    for (int c = 0; c < C; ++c) chan[c] = (int32_t)(Cin > C ? m.channel_map[c] : c);
+
+    d_WD = dev_upload(WD, dev_bytes, st);
+    d_Wall3 = dev_upload(m.Wall3, dev_bytes, st);
+    d_ctcP = dev_upload(ctcP, dev_bytes, st);
+    d_pre_wf = dev_upload(m.pre_wf, dev_bytes, st);
+    d_nm = dev_upload(nm, dev_bytes, st);
+    d_wPCA = dev_upload(m.wPCA, dev_bytes, st);
+    d_Ucc = dev_upload(m.Ucc, dev_bytes, st);
+    d_xc = dev_upload(m.xc, dev_bytes, st);
+    d_yc = dev_upload(m.yc, dev_bytes, st);
+    d_cent = dev_upload(m.centroids, dev_bytes, st);
+    d_iCC = dev_upload(m.iCC, dev_bytes, st);
+    d_iU = dev_upload(m.iU, dev_bytes, st);
+    d_chan = (Cin > C) ? dev_upload(chan, dev_bytes, st) : nullptr;
+    LSS_CUDA(cudaStreamSynchronize(st));
+    m.ctc.clear();
+    m.ctc.shrink_to_fit();
+
+    taps_for(W);
+    ensure_work(W, G);
+    slots.resize(3);
+    for (auto& s : slots) {
+        LSS_CUDA(cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming));
+        if (p.profile)
+            for (cudaEvent_t& e : s.tev) LSS_CUDA(cudaEventCreate(&e));
+    }
+}
+
+TapSet& Handle::taps_for(int Wn) {
+    auto it = taps.find(Wn);
+    if (it != taps.end()) return it->second;
+    std::vector<float> tv;
+    int64_t L = 0, R = 0;
+    highpass_taps(m.hp_filter, Wn, p.hp_half_taps > 0 ? p.hp_half_taps : 640, tv, L, R);
+    tv.resize(((tv.size() + 31) / 32) * 32, 0.f);   // the FIR kernel reads taps in chunks of 32
+    TapSet ts;
+    ts.L = (int)L;
+    ts.R = (int)R;
+    ts.d = dev_upload(tv, dev_bytes, st);
+    LSS_CUDA(cudaStreamSynchronize(st));
+    return taps.emplace(Wn, ts).first->second;
+}
+
+void Handle::ensure_work(int Wn, int nb) {
+    if (Wn <= Wcap && nb <= nbcap) return;
+    if (st) LSS_CUDA(cudaStreamSynchronize(st));
+    const int Wa = std::max(Wn, Wcap), nba = std::max(nb, nbcap);
+    free_work();
+    int64_t before = dev_bytes;
+    const int LRmax = Wa;   // wrap rows never exceed the window length
+    cap = p.spike_cap > 0 ? p.spike_cap : std::max(2048, Wa);
+    raw_rows_cap = (size_t)nba * (size_t)std::max(Wa, NT) + 2 * (size_t)nt;
+    const int64_t need = (int64_t)raw_rows_cap * Cin * 2 + (int64_t)nba * C * 8 +
+                         (int64_t)nba * (Wa + LRmax) * C * 4 + 2LL * nba * Wa * C * 4 +
+                         (int64_t)nba * Wa * K * C * 4 + (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 +
+                         (int64_t)nba * cap * 16;
+    if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
+        throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
+                                           " device bytes, budget " + std::to_string(p.mem_budget)};
+    d_raw = dev_alloc<int16_t>(raw_rows_cap * Cin, dev_bytes);
+    d_colsum = dev_alloc<long long>((size_t)nba * C, dev_bytes);
+    d_Xw = dev_alloc<float>((size_t)nba * (Wa + LRmax) * C, dev_bytes);
+    d_Y = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
+    d_Z = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
+    d_Bpc = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
+    d_Bt = dev_alloc<float>((size_t)nba * Wa * T, dev_bytes);
+    sc.cfmax = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
+    sc.imax = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
+    sc.at_t = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
+    sc.at_amp = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
+    sc.dirty = dev_alloc<unsigned char>((size_t)nba * Wa, dev_bytes);
+    sc.cta_cnt = dev_alloc<int>((size_t)nba * 2 * kMatchCluster, dev_bytes);
+    mo.n_spikes = dev_alloc<int>(nba, dev_bytes);
+    mo.n_iters = dev_alloc<int>(nba, dev_bytes);
+    mo.status = dev_alloc<int>(nba, dev_bytes);
+    mo.sp_w = dev_alloc<int>((size_t)nba * cap, dev_bytes);
+    mo.sp_t = dev_alloc<int>((size_t)nba * cap, dev_bytes);
+    mo.sp_amp = dev_alloc<float>((size_t)nba * cap, dev_bytes);
+    mo.sp_iter = dev_alloc<int>((size_t)nba * cap, dev_bytes);
+    mo.cap = cap;
+    work_bytes = dev_bytes - before;
+    Wcap = Wa;
+    nbcap = nba;
+    // pinned staging + mapped outputs of every slot follow the new capacity
+    for (auto& s : slots) {
+        if (s.busy) continue;
+        if (s.h_stage) cudaFreeHost(s.h_stage), s.h_stage = nullptr;
+        if (s.h_recs) cudaFreeHost(s.h_recs), s.h_recs = nullptr;
+        if (s.h_off) cudaFreeHost(s.h_off), s.h_off = nullptr;
+        if (s.h_nsp) cudaFreeHost(s.h_nsp), s.h_nsp = nullptr;
+        if (s.h_status) cudaFreeHost(s.h_status), s.h_status = nullptr;
+    }
+}
+
+int Handle::acquire_slot() {
+    // finish the oldest group if every slot is in flight
+    for (;;) {
+        for (size_t i = 0; i < slots.size(); ++i)
+            if (!slots[i].busy) {
+                Slot& s = slots[i];
+                if (!s.h_stage) {
+                    s.stage_rows = raw_rows_cap;
+                    LSS_CUDA(cudaHostAlloc((void**)&s.h_stage, s.stage_rows * Cin * sizeof(int16_t), cudaHostAllocPortable));
+                    LSS_CUDA(cudaHostAlloc((void**)&s.h_recs, (size_t)nbcap * cap * sizeof(SpikeRec),
+                                           cudaHostAllocMapped | cudaHostAllocPortable));
+                    LSS_CUDA(cudaHostGetDevicePointer((void**)&s.d_recs, s.h_recs, 0));
+                    LSS_CUDA(cudaHostAlloc((void**)&s.h_off, (size_t)(nbcap + 1) * sizeof(int),
+                                           cudaHostAllocMapped | cudaHostAllocPortable));
+                    LSS_CUDA(cudaHostGetDevicePointer((void**)&s.d_off, s.h_off, 0));
+                    LSS_CUDA(cudaHostAlloc((void**)&s.h_nsp, (size_t)nbcap * sizeof(int), cudaHostAllocPortable));
+                    LSS_CUDA(cudaHostAlloc((void**)&s.h_status, (size_t)nbcap * sizeof(int), cudaHostAllocPortable));
+                }
+                return (int)i;
+            }
+        collect(inflight.front(), nullptr, nullptr);
+    }
+}
+
+// Enqueue the kernels of one group: windows b = 0..nb-1 start at row b*NTs of the staging copy
+// (or of dev_src, rows already on the device).
+void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, int stage_rows, const int16_t* dev_src) {
+    const bool prof = p.profile != 0;
+    int stage = 0;
+    auto mark = [&]() {
+        if (prof) LSS_CUDA(cudaEventRecord(s.tev[stage], st));
+        ++stage;
+    };
+    mark();
+    const int16_t* raw = dev_src;
+    if (!raw) {
+        LSS_CUDA(cudaMemcpyAsync(d_raw, s.h_stage, (size_t)stage_rows * Cin * sizeof(int16_t), cudaMemcpyHostToDevice, st));
+        raw = d_raw;
+    }
+    mark();
+    int64_t nl = 0;
+    launch_colsum(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, st), ++nl;
+    mark();
+    launch_car(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, d_Xw, st), ++nl;
+    mark();
+    launch_highpass(d_Xw, C, Wn, ts.L, ts.R, ts.d, nb, d_Y, st), ++nl;
+    mark();
+    launch_sgemm_nt(d_Y, C, (int64_t)Wn * C, d_WD, C, d_Z, C, (int64_t)Wn * C, Wn, C, C, nb, st), ++nl;
+    mark();
+    launch_basis_conv_host(d_Z, C, Wn, d_wPCA, m.wPCA.data(), K, nt, nb, d_Bpc, st), ++nl;
+    mark();
+    launch_sgemm_nt(d_Bpc, (int64_t)K * C, (int64_t)Wn * K * C, d_Wall3, (int64_t)K * C, d_Bt, T, (int64_t)Wn * T, Wn, T,
+                    K * C, nb, st), ++nl;
+    LSS_CUDA(cudaGetLastError());
+    mark();
+    LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
+    LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st));
+    ++nl;
+    mark();
+    launch_rec_offsets(mo, nb, s.d_off, st), ++nl;
+    launch_features(d_Z, mo, nb, Wn, C, T, K, nt, nC, d_wPCA, d_iCC, d_iU, d_Ucc, d_xc, d_yc, d_cent, Tf, s.d_off,
+                    s.d_recs, 0, st), ++nl;
+    LSS_CUDA(cudaGetLastError());
+    mark();
+    LSS_CUDA(cudaMemcpyAsync(s.h_nsp, mo.n_spikes, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
+    LSS_CUDA(cudaMemcpyAsync(s.h_status, mo.status, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
+    mark();
+    LSS_CUDA(cudaEventRecord(s.ev, st));
+    s.busy = true;
+    s.nb = nb;
+    s.W = Wn;
+    launches_last += nl;
+}
+
+void Handle::push_device(const int16_t* rows, int64_t n_batches, int64_t first_row_sample) {
+    if (!rows || n_batches <= 0) throw LoadError{LSS_ERR_ARG, "lss_push_device_span: bad rows / n_batches"};
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, rows) != cudaSuccess || pa.type != cudaMemoryTypeDevice || pa.device != dev) {
+        cudaGetLastError();
+        throw LoadError{LSS_ERR_ARG, "lss_push_device_span: rows are not device memory of the handle's device"};
+    }
+    for (int64_t b0 = 0; b0 < n_batches; b0 += G) {
+        const int g = (int)std::min<int64_t>(G, n_batches - b0);
+        const int si = acquire_slot();
+        Slot& s = slots[si];
+        s.windows_api = false;
+        s.win_start.assign(g, 0);
+        s.batch_id.assign(g, 0);
+        s.drop_before.assign(g, INT64_MIN);
+        for (int b = 0; b < g; ++b) {
+            s.win_start[b] = first_row_sample + (b0 + b) * (int64_t)NT;
+            s.batch_id[b] = batch_counter + b;
+        }
+        launch_group(s, g, W, NT, taps_for(W), 0, rows + (size_t)b0 * NT * Cin);
+        inflight.push_back(si);
+        batch_counter += g;
+    }
+}
+
+// Turn a finished group into lss_spike records.  direct != nullptr: windows API (results
+// returned to the caller, no duplicate removal); otherwise appended to the ready queue.
+void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t>* counts) {
+    Slot& s = slots[si];
+    LSS_CUDA(cudaEventSynchronize(s.ev));
+    if (!inflight.empty() && inflight.front() == si) inflight.pop_front();
+    if (p.profile && s.tev[0]) {
+        for (int i = 0; i < LSS_N_STAGES; ++i) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, s.tev[i], s.tev[i + 1]) == cudaSuccess) stage_ms[i] += ms;
+        }
+        ++groups_timed;
+    }
+    const int hw = nt / 2;
+    const int nf = nC * K;
+    std::vector<lss_spike> batch;
+    for (int b = 0; b < s.nb; ++b) {
+        const int n = s.h_off[b + 1] - s.h_off[b];
+        if (s.h_status[b] & 1) overflow_pending = true;
+        batch.clear();
+        batch.reserve(n);
+        for (int i = 0; i < n; ++i) {
+            const SpikeRec& r = s.h_recs[s.h_off[b] + i];
+            lss_spike o;
+            std::memset(&o, 0, sizeof(o));
+            o.time = s.win_start[b] + r.w - hw + m.nt0min;
+            if (o.time < s.drop_before[b]) continue;
+            o.tmpl = r.t;
+            o.cluster = r.cluster;
+            o.amp = r.amp;
+            o.x = r.x;
+            o.y = r.y;
+            o.batch = (int32_t)s.batch_id[b];
+            o.n_feat = nf;
+            o.iter = r.iter;
+            std::memcpy(o.pcfeat, r.feat, sizeof(float) * nf);
+            batch.push_back(o);
+        }
+        std::stable_sort(batch.begin(), batch.end(), [](const lss_spike& a, const lss_spike& c) {
+            return a.time != c.time ? a.time < c.time : a.tmpl < c.tmpl;
+        });
+        if (direct) {
+            direct->insert(direct->end(), batch.begin(), batch.end());
+            if (counts) counts->push_back((int64_t)batch.size());
+        } else {
+            for (const lss_spike& o : batch) {
+                if (p.dedup) {
+                    // Kilosort postprocessing.py:9-30: keep when t >= last kept + dt
+                    auto it = last_kept.find(o.cluster);
+                    if (it != last_kept.end() && o.time < it->second + m.dup_bins) continue;
+                    last_kept[o.cluster] = o.time;
+                }
+                ready.push_back(o);
+            }
+        }
+        spikes_done += (int64_t)batch.size();
+    }
+    batches_done += s.nb;
+    s.busy = false;
+}
+
+void Handle::drain_all() {
+    while (!inflight.empty()) collect(inflight.front(), nullptr, nullptr);
+}
+
+// Launch g windows from the front of buf; with pad_to_end the rows past the end of buf repeat
+// the last row (Kilosort's last batch).
+void Handle::launch_windows_from_buf(int g, bool pad_to_end) {
+    const int64_t rows_have = (int64_t)(buf.size() / Cin);
+    const int64_t rows_need = (int64_t)g * NT + 2 * nt;
+    const int si = acquire_slot();
+    Slot& s = slots[si];
+    const int64_t copy_rows = std::min(rows_have, rows_need);
+    std::memcpy(s.h_stage, buf.data(), (size_t)copy_rows * Cin * sizeof(int16_t));
+    if (copy_rows < rows_need) {
+        if (!pad_to_end || copy_rows == 0) throw LoadError{LSS_ERR_INTERNAL, "window underflow"};
+        for (int64_t r = copy_rows; r < rows_need; ++r)
+            std::memcpy(s.h_stage + r * Cin, s.h_stage + (copy_rows - 1) * Cin, (size_t)Cin * sizeof(int16_t));
+    }
+    s.windows_api = false;
+    s.win_start.assign(g, 0);
+    s.batch_id.assign(g, 0);
+    s.drop_before.assign(g, INT64_MIN);
+    for (int b = 0; b < g; ++b) {
+        const int64_t j = next_batch + b;
+        s.win_start[b] = seg_s0 + j * NT - nt;
+        s.batch_id[b] = batch_counter + b;
+        if (j == 0) s.drop_before[b] = seg_s0;   // Kilosort drops negative times of batch 0
+    }
+    launch_group(s, g, W, NT, taps_for(W), (int)rows_need);
+    inflight.push_back(si);
+    next_batch += g;
+    batch_counter += g;
+    const int64_t drop = std::min<int64_t>((int64_t)g * NT, rows_have);
+    buf.erase(buf.begin(), buf.begin() + (size_t)drop * Cin);
+}
+
+void Handle::push(const int16_t* x, int64_t n, int64_t ct) {
+    if (n < 0 || (n > 0 && !x)) throw LoadError{LSS_ERR_ARG, "lss_push_batch: bad samples"};
+    if (seg_active && ct >= 0 && ct != expected_ct) flush();   // discontinuity: close the segment
+    if (n == 0) return;
+    if (!seg_active) {
+        seg_active = true;
+        seg_s0 = ct >= 0 ? ct : expected_ct;
+        next_batch = 0;
+        buf.clear();
+        for (int r = 0; r < nt; ++r) buf.insert(buf.end(), x, x + Cin);   // left pad = first sample
+        expected_ct = seg_s0;
+    }
+    buf.insert(buf.end(), x, x + (size_t)n * Cin);
+    expected_ct += n;
+    for (;;) {
+        const int64_t rows = (int64_t)(buf.size() / Cin);
+        if (rows < (int64_t)G * NT + 2 * nt) break;
+        launch_windows_from_buf(G, false);
+    }
+}
+
+void Handle::flush() {
+    if (!seg_active) return;
+    // pending new samples: rows past the nt context rows at the front of buf
+    for (;;) {
+        const int64_t rows = (int64_t)(buf.size() / Cin);
+        const int64_t fresh = rows - nt;
+        if (fresh <= 0) break;
+        const int64_t nbat = (fresh + NT - 1) / NT;
+        const int g = (int)std::min<int64_t>(nbat, G);
+        launch_windows_from_buf(g, true);
+    }
+    seg_active = false;
+    buf.clear();
+}
+
+}  // namespace lss
+
+// =========================================================================================
+// C ABI
+// =========================================================================================
+using lss::Handle;
+
+struct lss_handle {
+    Handle h;
+};
+
+static thread_local std::string g_open_error;
+
+#define LSS_TRY(hptr, ...)                                                                         \
+    try {                                                                                          \
+        __VA_ARGS__;                                                                               \
+        return LSS_OK;                                                                             \
+    } catch (const lss::LoadError& e) {                                                            \
+        (hptr)->h.err = e.msg;                                                                     \
+        return e.status;                                                                           \
+    } catch (const lss::CudaError& e) {                                                            \
+        (hptr)->h.err = e.msg;                                                                     \
+        return LSS_ERR_CUDA;                                                                       \
+    } catch (const std::bad_alloc&) {                                                              \
+        (hptr)->h.err = "host allocation failed";                                                  \
+        return LSS_ERR_NOMEM;                                                                      \
+    } catch (const std::exception& e) {                                                            \
+        (hptr)->h.err = e.what();                                                                  \
+        return LSS_ERR_INTERNAL;                                                                   \
+    }
+
+extern "C" {
+
+int lss_default_params(lss_params* p) {
+    if (!p) return LSS_ERR_ARG;
+    std::memset(p, 0, sizeof(*p));
+    p->abi_version = LSS_ABI_VERSION;
+    p->device = 0;
+    p->batch_samples = 1500;
+    p->max_iters = 50;
+    p->group_batches = 1;
+    p->n_chan_in = 0;
+    p->hp_half_taps = 640;
+    p->dedup = 1;
+    p->th_override = 0.f;
+    p->spike_cap = 0;
+    p->mem_budget = 0;
+    p->profile = 0;
+    return LSS_OK;
+}
+
+int lss_open(const char* oss_dir, const lss_params* p, lss_handle** out) {
+    if (!out) return LSS_ERR_ARG;
+    *out = nullptr;
+    lss_handle* h = nullptr;
+    try {
+        h = new lss_handle();
+        h->h.init(oss_dir, p);
+        *out = h;
+        return LSS_OK;
+    } catch (const lss::LoadError& e) {
+        g_open_error = e.msg;
+        delete h;
+        return e.status;
+    } catch (const lss::CudaError& e) {
+        g_open_error = e.msg;
+        delete h;
+        return LSS_ERR_CUDA;
+    } catch (const std::exception& e) {
+        g_open_error = e.what();
+        delete h;
+        return LSS_ERR_INTERNAL;
+    }
+}
+
+int lss_get_info(const lss_handle* hp, lss_info* info) {
+    if (!hp || !info) return LSS_ERR_ARG;
+    const Handle& h = hp->h;
+    info->C = h.C;
+    info->T = h.T;
+    info->T_final = h.Tf;
+    info->K = h.K;
+    info->nt = h.nt;
+    info->nC = h.nC;
+    info->nt0min = (int32_t)h.m.nt0min;
+    info->dup_bins = (int32_t)h.m.dup_bins;
+    info->th = h.th;
+    info->NT = h.NT;
+    info->W = h.W;
+    info->group_batches = h.G;
+    info->device_bytes = h.dev_bytes;
+    info->batches_done = h.batches_done;
+    info->spikes_done = h.spikes_done;
+    return LSS_OK;
+}
+
+int lss_push_batch(lss_handle* hp, const int16_t* samples, int64_t n_samples, int64_t stream_sample_ct) {
+    if (!hp) return LSS_ERR_ARG;
+    LSS_TRY(hp, {
+        cudaSetDevice(hp->h.dev);
+        hp->h.launches_last = 0;
+        hp->h.push(samples, n_samples, stream_sample_ct);
+    })
+}
+
+int lss_flush(lss_handle* hp) {
+    if (!hp) return LSS_ERR_ARG;
+    LSS_TRY(hp, {
+        cudaSetDevice(hp->h.dev);
+        hp->h.launches_last = 0;
+        hp->h.flush();
+    })
+}
+
+int lss_poll(lss_handle* hp, lss_spike* out, int64_t cap, int64_t* n_out) {
+    if (!hp || !n_out || cap < 0 || (cap > 0 && !out)) return LSS_ERR_ARG;
+    *n_out = 0;
+    try {
+        Handle& h = hp->h;
+        cudaSetDevice(h.dev);
+        // everything already finished, plus the oldest group if nothing is ready yet
+        while (!h.inflight.empty() && cudaEventQuery(h.slots[h.inflight.front()].ev) == cudaSuccess)
+            h.collect(h.inflight.front(), nullptr, nullptr);
+        if (h.ready.empty() && !h.inflight.empty()) h.collect(h.inflight.front(), nullptr, nullptr);
+        int64_t n = std::min<int64_t>(cap, (int64_t)h.ready.size());
+        for (int64_t i = 0; i < n; ++i) {
+            out[i] = h.ready.front();
+            h.ready.pop_front();
+        }
+        *n_out = n;
+        if (h.overflow_pending) {
+            h.overflow_pending = false;
+            h.err = "a batch found more spikes than its spike buffer holds; raise spike_cap";
+            return LSS_ERR_OVERFLOW;
+        }
+        return LSS_OK;
+    } catch (const lss::LoadError& e) {
+        hp->h.err = e.msg;
+        return e.status;
+    } catch (const lss::CudaError& e) {
+        hp->h.err = e.msg;
+        return LSS_ERR_CUDA;
+    }
+}
+
+int lss_pending(lss_handle* hp, int64_t* n) {
+    if (!hp || !n) return LSS_ERR_ARG;
+    LSS_TRY(hp, {
+        cudaSetDevice(hp->h.dev);
+        hp->h.drain_all();
+        *n = (int64_t)hp->h.ready.size();
+    })
+}
+
+int lss_close(lss_handle* hp) {
+    if (!hp) return LSS_ERR_ARG;
+    delete hp;
+    return LSS_OK;
+}
+
+const char* lss_last_error(const lss_handle* hp) {
+    if (!hp) return g_open_error.c_str();
+    return hp->h.err.c_str();
+}
+
+int lss_sort_windows(lss_handle* hp, const int16_t* windows, int32_t n_windows, int32_t W, lss_spike* out,
+                     int64_t cap, int64_t* counts) {
+    if (!hp || !windows || n_windows <= 0 || !counts || cap < 0 || (cap > 0 && !out)) return LSS_ERR_ARG;
+    Handle& h = hp->h;
+    if (W <= 2 * h.nt + 1) {
+        h.err = "window shorter than 2*nt+2 samples";
+        return LSS_ERR_ARG;
+    }
+    LSS_TRY(hp, {
+        cudaSetDevice(h.dev);
+        h.launches_last = 0;
+        h.drain_all();
+        const int per = std::max(1, h.G);
+        h.ensure_work(W, per);
+        std::vector<lss_spike> all;
+        std::vector<int64_t> cnt;
+        for (int w0 = 0; w0 < n_windows; w0 += per) {
+            const int g = std::min(per, n_windows - w0);
+            const int si = h.acquire_slot();
+            lss::Slot& s = h.slots[si];
+            std::memcpy(s.h_stage, windows + (size_t)w0 * W * h.Cin, (size_t)g * W * h.Cin * sizeof(int16_t));
+            s.windows_api = true;
+            s.win_start.assign(g, 0);
+            s.drop_before.assign(g, INT64_MIN);
+            s.batch_id.resize(g);
+            for (int b = 0; b < g; ++b) s.batch_id[b] = w0 + b;
+            h.launch_group(s, g, W, W, h.taps_for(W), g * W);
+            h.collect(si, &all, &cnt);
+        }
+        int64_t written = 0;
+        for (int i = 0; i < n_windows; ++i) counts[i] = cnt[i];
+        for (const lss_spike& o : all) {
+            if (written >= cap) break;
+            out[written++] = o;
+        }
+        if ((int64_t)all.size() > cap) throw lss::LoadError{LSS_ERR_ARG, "output capacity too small"};
+        if (h.overflow_pending) {
+            h.overflow_pending = false;
+            throw lss::LoadError{LSS_ERR_OVERFLOW, "a window found more spikes than its spike buffer holds"};
+        }
+    })
+}
+
+int lss_debug_stage(lss_handle* hp, const int16_t* window, int32_t W, int32_t stage, float* out, int64_t out_len) {
+    if (!hp || !window || !out) return LSS_ERR_ARG;
+    Handle& h = hp->h;
+    if (W <= 2 * h.nt + 1) return LSS_ERR_ARG;
+    const int64_t need = (stage == LSS_STAGE_SCORES) ? (int64_t)W * h.T : (int64_t)W * h.C;
+    if (out_len < need || stage < 1 || stage > 3) return LSS_ERR_ARG;
+    LSS_TRY(hp, {
+        cudaSetDevice(h.dev);
+        h.drain_all();
+        h.ensure_work(W, 1);
+        const int si = h.acquire_slot();
+        lss::Slot& s = h.slots[si];
+        std::memcpy(s.h_stage, window, (size_t)W * h.Cin * sizeof(int16_t));
+        lss::TapSet& ts = h.taps_for(W);
+        cudaStream_t st = h.st;
+        LSS_CUDA(cudaMemcpyAsync(h.d_raw, s.h_stage, (size_t)W * h.Cin * 2, cudaMemcpyHostToDevice, st));
+        lss::launch_colsum(h.d_raw, h.Cin, h.d_chan, h.C, W, W, 1, h.d_colsum, st);
+        lss::launch_car(h.d_raw, h.Cin, h.d_chan, h.C, W, W, 1, h.d_colsum, ts.L, ts.R, h.d_Xw, st);
+        lss::launch_highpass(h.d_Xw, h.C, W, ts.L, ts.R, ts.d, 1, h.d_Y, st);
+        lss::launch_sgemm_nt(h.d_Y, h.C, (int64_t)W * h.C, h.d_WD, h.C, h.d_Z, h.C, (int64_t)W * h.C, W, h.C, h.C, 1, st);
+        if (stage == LSS_STAGE_PREPROCESSED) {
+            LSS_CUDA(cudaMemcpyAsync(out, h.d_Z, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
+        } else {
+            lss::launch_basis_conv_host(h.d_Z, h.C, W, h.d_wPCA, h.m.wPCA.data(), h.K, h.nt, 1, h.d_Bpc, st);
+            lss::launch_sgemm_nt(h.d_Bpc, (int64_t)h.K * h.C, (int64_t)W * h.K * h.C, h.d_Wall3, (int64_t)h.K * h.C,
+                                 h.d_Bt, h.T, (int64_t)W * h.T, W, h.T, h.K * h.C, 1, st);
+            if (stage == LSS_STAGE_SCORES) {
+                LSS_CUDA(cudaMemcpyAsync(out, h.d_Bt, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
+            } else {
+                LSS_CUDA(cudaMemsetAsync(h.mo.status, 0, sizeof(int), st));
+                LSS_CUDA(lss::launch_match(h.d_Bt, h.d_Z, h.d_ctcP, h.d_pre_wf, h.d_nm, h.th * h.th, W, h.T, h.C, h.nt,
+                                           h.max_iters, 1, h.sc, h.mo, st));
+                LSS_CUDA(cudaMemcpyAsync(out, h.d_Z, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
+            }
+        }
+        LSS_CUDA(cudaGetLastError());
+        LSS_CUDA(cudaStreamSynchronize(st));
+    })
+}
+
+int lss_push_device_span(lss_handle* hp, const int16_t* dev_rows, int64_t n_batches, int64_t first_row_sample) {
+    if (!hp) return LSS_ERR_ARG;
+    LSS_TRY(hp, {
+        cudaSetDevice(hp->h.dev);
+        hp->h.launches_last = 0;
+        hp->h.push_device(dev_rows, n_batches, first_row_sample);
+    })
+}
+
+int lss_cuda_stream(const lss_handle* hp, void** stream) {
+    if (!hp || !stream) return LSS_ERR_ARG;
+    *stream = (void*)hp->h.st;
+    return LSS_OK;
+}
+
+int lss_stage_times(lss_handle* hp, double* ms, int32_t n, int64_t* n_groups) {
+    if (!hp || !ms || n < 0) return LSS_ERR_ARG;
+    for (int i = 0; i < n && i < LSS_N_STAGES; ++i) ms[i] = hp->h.stage_ms[i];
+    if (n_groups) *n_groups = hp->h.groups_timed;
+    return LSS_OK;
+}
+
+int lss_kernel_launches(const lss_handle* hp, int64_t* n) {
+    if (!hp || !n) return LSS_ERR_ARG;
+    *n = hp->h.launches_last;
+    return LSS_OK;
+}
+
+}  // extern "C"

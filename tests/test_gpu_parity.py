@@ -1,0 +1,232 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the vendored Kilosort
+fixtures.  Tolerances: stage outputs within 2e-5 (preprocessed) / 5e-5 (scores, residual) of
+the largest magnitude; spike sets agree at >= 99.5% (same template, |dt| <= 1 sample) with
+>= 99.5% of the matched amplitudes within 1e-3 relative of the float64 oracle."""
+import numpy as np
+import pytest
+
+from livespikesorter_gb300 import sorter, synth
+from oracle import ks_oracle as ko
+
+from lss_testutil import agreement, make_dataset, write_oss_from_arrays
+
+pytestmark = pytest.mark.gpu
+
+AGREE = 0.995
+
+
+@pytest.fixture(scope="module")
+def win(golden_dir):
+    return np.load(golden_dir / "ks_window.npz")
+
+
+@pytest.fixture(scope="module")
+def win_oss(win, tmp_path_factory):
+    return write_oss_from_arrays(win, tmp_path_factory.mktemp("win") / "oss_input")
+
+
+@pytest.fixture(scope="module")
+def win_sorter(win_oss, win):
+    with sorter.OnlineSorter(win_oss, max_iters=int(win["max_iters"]), batch_samples=int(win["NT"])) as s:
+        yield s
+
+
+def _rel_close(got, ref, frac):
+    scale = np.abs(ref).max()
+    err = np.abs(got - ref).max()
+    assert err <= frac * scale, f"max err {err:.3e} vs scale {scale:.3e}"
+
+
+# ---------------------------------------------------------------- stage parity (golden window)
+def test_stage_preprocessed(win_sorter, win):
+    oss = ko.oss_from_arrays(win)
+    ref = ko.preprocess(win["window"].T, oss)            # float64 oracle
+    got = win_sorter.debug_stage(win["window"], sorter.STAGE_PREPROCESSED)
+    _rel_close(got.T.astype(np.float64), ref, 2e-5)
+    _rel_close(got.T.astype(np.float64), win["X"].astype(np.float64), 2e-5)   # the vendored filter
+
+
+def test_stage_scores(win_sorter, win):
+    oss = ko.oss_from_arrays(win)
+    X = ko.preprocess(win["window"].T, oss)
+    ref = ko.project(X, win["Wall3"].astype(np.float64), win["wPCA"].astype(np.float64))
+    got = win_sorter.debug_stage(win["window"], sorter.STAGE_SCORES)
+    _rel_close(got.T.astype(np.float64), ref, 5e-5)
+
+
+def test_stage_residual(win_sorter, win):
+    oss = ko.oss_from_arrays(win)
+    r = ko.sort_window(win["window"].T, oss, max_iters=int(win["max_iters"]))
+    got = win_sorter.debug_stage(win["window"], sorter.STAGE_RESIDUAL)
+    _rel_close(got.T.astype(np.float64), r.match.Xres, 5e-5)
+
+
+def test_window_spikes_match_kilosort(win_sorter, win):
+    """Spikes of the golden window against the vendored run_matching output."""
+    nt, nt0 = win["wPCA"].shape[1], int(win["misc"][0])
+    (sp,) = win_sorter.sort_windows(win["window"])
+    t_ref = win["st"][:, 0] - nt // 2 + nt0
+    a, amp_ok, amax = agreement(t_ref, win["st"][:, 1], win["amps"], sp["time"], sp["tmpl"], sp["amp"])
+    assert len(sp) == len(win["st"])
+    assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
+
+
+def test_window_features_and_positions(win_sorter, win):
+    oss = ko.oss_from_arrays(win)
+    r = ko.sort_window(win["window"].T, oss, max_iters=int(win["max_iters"]))
+    (sp,) = win_sorter.sort_windows(win["window"])
+    nt, nt0 = oss.wPCA.shape[1], oss.nt0min
+    order = np.lexsort((r.match.st[:, 1], r.match.st[:, 0]))
+    nf = oss.iCC.shape[0] * oss.wPCA.shape[0]
+    tF = r.tF[order].reshape(len(order), -1)
+    np.testing.assert_array_equal(sp["time"], r.match.st[order, 0] - nt // 2 + nt0)
+    np.testing.assert_allclose(sp["pcfeat"][:, :nf], tF, atol=2e-4 * np.abs(tF).max())
+    np.testing.assert_allclose(sp["x"], r.xs[order], atol=5e-3)
+    np.testing.assert_allclose(sp["y"], r.ys[order], atol=5e-3)
+    clu = ko.nearest_centroid(r.xs[order], r.ys[order], oss.centroids)
+    assert (sp["cluster"] == clu).mean() >= 0.99
+
+
+# ---------------------------------------------------------------- stream (golden Kilosort extract)
+def test_stream_matches_kilosort_extract(golden_dir, tmp_path):
+    z = np.load(golden_dir / "ks_stream.npz")
+    d = write_oss_from_arrays(z, tmp_path / "oss_input")
+    with sorter.OnlineSorter(d, batch_samples=int(z["NT"]), max_iters=int(z["max_iters"]), dedup=1) as s:
+        sp = s.sort_stream(z["data"], chunk=777)
+    keep = z["keep"].astype(bool)
+    st = z["st"]
+    a, amp_ok, amax = agreement(st[keep, 0], st[keep, 1], st[keep, 2], sp["time"], sp["tmpl"], sp["amp"])
+    assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
+    assert np.all(np.diff(sp["time"]) >= 0)
+
+
+def test_stream_chunking_is_invisible(golden_dir, tmp_path):
+    z = np.load(golden_dir / "ks_stream.npz")
+    d = write_oss_from_arrays(z, tmp_path / "oss_input")
+    outs = []
+    for chunk, group in ((0, 1), (333, 1), (1999, 2), (64, 3)):
+        with sorter.OnlineSorter(d, batch_samples=int(z["NT"]), max_iters=100, group_batches=group) as s:
+            outs.append(s.sort_stream(z["data"], chunk=chunk))
+    for o in outs[1:]:
+        assert len(o) == len(outs[0])
+        for f in ("time", "tmpl", "cluster", "amp", "x", "y", "pcfeat"):
+            np.testing.assert_array_equal(o[f], outs[0][f])   # bitwise: deterministic kernels
+
+
+# ---------------------------------------------------------------- seeded configs vs the oracle
+@pytest.fixture(scope="module")
+def cfg_small(tmp_path_factory):
+    """96 channels, 64 units, one 60000-sample batch (+2*61)."""
+    return make_dataset(synth.config_small(seed=11), tmp_path_factory.mktemp("cfg1"))
+
+
+def test_config_small_one_batch(cfg_small):
+    d, data, _ = cfg_small
+    oss = ko.load_oss_input(d)
+    with sorter.OnlineSorter(d, max_iters=50) as s:
+        (sp,) = s.sort_windows(data[: 60000 + 122])
+    r = ko.sort_window(data[: 60000 + 122].T, oss, max_iters=50)
+    nt, nt0 = oss.wPCA.shape[1], oss.nt0min
+    a, amp_ok, amax = agreement(r.match.st[:, 0] - nt // 2 + nt0, r.match.st[:, 1], r.match.amps,
+                                sp["time"], sp["tmpl"], sp["amp"])
+    assert len(r.match.st) > 500
+    assert a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax, len(sp), len(r.match.st))
+
+
+@pytest.fixture(scope="module")
+def cfg_stream(tmp_path_factory):
+    """384 channels, 500 templates, 6 batches of 1500 new samples with a rigid drift."""
+    cfg = synth.SynthConfig(n_chan=384, n_units=500, n_samples=6 * 1500 + 300, drift_um=20.0,
+                            whiten_batch=3000, whiten_batches=3, seed=5)
+    return make_dataset(cfg, tmp_path_factory.mktemp("cfg2"))
+
+
+def test_config_stream_384ch(cfg_stream):
+    d, data, _ = cfg_stream
+    oss = ko.load_oss_input(d)
+    ref = ko.sort_stream(data, oss, 1500, max_iters=50)
+    with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=4) as s:
+        sp = s.sort_stream(data)
+    k = ref["keep"]
+    a, amp_ok, amax = agreement(ref["time"][k], ref["template"][k], ref["amp"][k], sp["time"], sp["tmpl"], sp["amp"])
+    assert k.sum() > 300
+    assert a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax, len(sp), int(k.sum()))
+
+
+# ---------------------------------------------------------------- edge cases
+def test_silent_window_has_no_spikes(win_sorter, win):
+    (sp,) = win_sorter.sort_windows(np.zeros_like(win["window"]))
+    assert len(sp) == 0
+
+
+def test_short_stream_and_empty_push(golden_dir, tmp_path):
+    z = np.load(golden_dir / "ks_stream.npz")
+    d = write_oss_from_arrays(z, tmp_path / "oss_input")
+    oss = ko.oss_from_arrays(z)
+    data = z["data"][:700]                      # shorter than one batch
+    with sorter.OnlineSorter(d, batch_samples=2000, max_iters=100) as s:
+        s.push(data[:0])
+        s.push(data)
+        assert len(s.poll()) == 0               # nothing launched before the flush
+        s.flush()
+        sp = s.poll_all()
+    ref = ko.sort_stream(data, oss, 2000, max_iters=100)
+    k = ref["keep"]
+    a, _, _ = agreement(ref["time"][k], ref["template"][k], ref["amp"][k], sp["time"], sp["tmpl"], sp["amp"])
+    assert a == 1.0
+
+
+def test_discontinuity_starts_a_new_segment(golden_dir, tmp_path):
+    z = np.load(golden_dir / "ks_stream.npz")
+    d = write_oss_from_arrays(z, tmp_path / "oss_input")
+    oss = ko.oss_from_arrays(z)
+    A, B = z["data"][:2500], z["data"][3000:]
+    with sorter.OnlineSorter(d, batch_samples=2000, max_iters=100) as s:
+        s.push(A, 0)
+        s.push(B, 3000)                         # jumps: the first segment is flushed
+        s.flush()
+        sp = s.poll_all()
+    ra = ko.sort_stream(A, oss, 2000, max_iters=100)
+    rb = ko.sort_stream(B, oss, 2000, max_iters=100)
+    t_ref = np.concatenate([ra["time"][ra["keep"]], rb["time"][rb["keep"]] + 3000])
+    k_ref = np.concatenate([ra["template"][ra["keep"]], rb["template"][rb["keep"]]])
+    a_ref = np.concatenate([ra["amp"][ra["keep"]], rb["amp"][rb["keep"]]])
+    a, _, _ = agreement(t_ref, k_ref, a_ref, sp["time"], sp["tmpl"], sp["amp"])
+    assert a == 1.0
+
+
+def test_spike_buffer_overflow_is_reported(win_oss, win):
+    with sorter.OnlineSorter(win_oss, max_iters=100, spike_cap=2) as s:
+        with pytest.raises(sorter.SorterError) as e:
+            s.sort_windows(win["window"])
+        assert e.value.status == 6
+
+
+def test_channel_subset_via_channel_map(golden_dir, tmp_path):
+    """n_chan_in > C: the sorter picks channelMap columns out of wider rows (the DataSocket's
+    channel subset, dataSocket.h:17-21)."""
+    z = np.load(golden_dir / "ks_window.npz")
+    d = write_oss_from_arrays(z, tmp_path / "oss_input")
+    C = z["window"].shape[1]
+    perm = np.random.default_rng(0).permutation(C + 9)[:C].astype(np.int32)
+    np.save(d / "channelMap.npy", perm)
+    wide = np.zeros((z["window"].shape[0], C + 9), np.int16)
+    wide[:, perm] = z["window"]
+    with sorter.OnlineSorter(d, max_iters=100) as s0:
+        (ref,) = s0.sort_windows(z["window"])
+    with sorter.OnlineSorter(d, max_iters=100, n_chan_in=C + 9) as s1:
+        (got,) = s1.sort_windows(wide)
+    np.testing.assert_array_equal(got["time"], ref["time"])
+    np.testing.assert_array_equal(got["amp"], ref["amp"])
+
+
+def test_admission_by_memory_budget(win_oss):
+    with pytest.raises(sorter.SorterError) as e:
+        sorter.OnlineSorter(win_oss, mem_budget=1 << 20)
+    assert e.value.status == 5
+
+
+def test_kernel_launch_count(win_oss, win):
+    with sorter.OnlineSorter(win_oss, max_iters=100) as s:
+        s.sort_windows(win["window"])
+        assert s.kernel_launches() == 9
