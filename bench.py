@@ -242,8 +242,9 @@ def run_gpu(a):
     spikes_seen = [0]
 
     def step(i):
+        # cycle over the recording; stream times keep increasing (a continuous stream)
         g0 = (i % n_groups) * G
-        s.push_device_span(base_ptr + g0 * NT * row_bytes, G, g0 * NT)
+        s.push_device_span(base_ptr + g0 * NT * row_bytes, G, i * G * NT)
 
     def drain(srt):
         n = srt.pending()
@@ -320,7 +321,7 @@ def run_gpu(a):
     s2.close()
 
     # ---- per-batch latency (one batch per launch) --------------------------------------------
-    s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1)
+    s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1, profile=1)
     lat = []
     s3.push(data[:NT + 2 * nt], 0)
     drain(s3)
@@ -334,10 +335,12 @@ def run_gpu(a):
         if i >= 5:
             lat.append(1e3 * (time.perf_counter() - t1))
         p += NT
+    st3, ng3 = s3.stage_times()
     s3.close()
     latency = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                "batches": len(lat), "batch_ms_of_signal": 1e3 * NT / 30000.0,
-               "path": "lss_push_batch of 1500 new samples -> lss_poll, group_batches=1"}
+               "path": "lss_push_batch of 1500 new samples -> lss_poll, group_batches=1",
+               "stage_ms_per_batch": {k: v / max(ng3, 1) for k, v in st3.items()}}
 
     # ---- CPU baseline (rank 0) ----------------------------------------------------------------
     cpu = None

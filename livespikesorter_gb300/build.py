@@ -19,6 +19,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "lib"
 OBJ = PKG / "_build"
 LIB = OUT / "liblss_gb300.so"
+REPLAY = OUT / "lss_replay"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
@@ -68,6 +69,13 @@ def build(verbose: bool = False, extra=()) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
         os.replace(tmp, LIB)
+    ex_src = CSRC / "examples" / "lss_replay.cpp"
+    if not REPLAY.exists() or REPLAY.stat().st_mtime < max(ex_src.stat().st_mtime, LIB.stat().st_mtime):
+        cmd = [nvcc(), *ARCH, "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(ex_src), "-o", str(REPLAY),
+               "-L", str(OUT), "-llss_gb300", "-Xlinker", "-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"lss_replay build failed:\n{r.stderr}")
     if verbose:
         print(f"built {LIB}")
     return LIB

@@ -135,7 +135,7 @@ struct Handle {
     void drain_all();
     void push(const int16_t* x, int64_t n, int64_t ct);
     void flush();
-    void launch_windows_from_buf(int g, bool pad_to_end);
+    void launch_windows_from_buf(int g, int pad_mode);
 };
 
 Handle::~Handle() {
@@ -498,9 +498,11 @@ void Handle::drain_all() {
     while (!inflight.empty()) collect(inflight.front(), nullptr, nullptr);
 }
 
-// Launch g windows from the front of buf; with pad_to_end the rows past the end of buf repeat
-// the last row (Kilosort's last batch).
-void Handle::launch_windows_from_buf(int g, bool pad_to_end) {
+// Launch g windows from the front of buf.  Rows past the end of buf (only at a flush, g = 1):
+// pad_mode 1 repeats the last row (Kilosort's last batch, io.py:626-629); pad_mode 2 leaves them
+// zero, which is what Kilosort does when the first batch is also the last one (its ibatch == 0
+// branch, io.py:621-625, runs first and never fills the right side).
+void Handle::launch_windows_from_buf(int g, int pad_mode) {
     const int64_t rows_have = (int64_t)(buf.size() / Cin);
     const int64_t rows_need = (int64_t)g * NT + 2 * nt;
     const int si = acquire_slot();
@@ -508,9 +510,13 @@ void Handle::launch_windows_from_buf(int g, bool pad_to_end) {
     const int64_t copy_rows = std::min(rows_have, rows_need);
     std::memcpy(s.h_stage, buf.data(), (size_t)copy_rows * Cin * sizeof(int16_t));
     if (copy_rows < rows_need) {
-        if (!pad_to_end || copy_rows == 0) throw LoadError{LSS_ERR_INTERNAL, "window underflow"};
-        for (int64_t r = copy_rows; r < rows_need; ++r)
-            std::memcpy(s.h_stage + r * Cin, s.h_stage + (copy_rows - 1) * Cin, (size_t)Cin * sizeof(int16_t));
+        if (pad_mode == 0 || copy_rows == 0 || g != 1) throw LoadError{LSS_ERR_INTERNAL, "window underflow"};
+        for (int64_t r = copy_rows; r < rows_need; ++r) {
+            if (pad_mode == 2)
+                std::memset(s.h_stage + r * Cin, 0, (size_t)Cin * sizeof(int16_t));
+            else
+                std::memcpy(s.h_stage + r * Cin, s.h_stage + (copy_rows - 1) * Cin, (size_t)Cin * sizeof(int16_t));
+        }
     }
     s.windows_api = false;
     s.win_start.assign(g, 0);
@@ -547,20 +553,23 @@ void Handle::push(const int16_t* x, int64_t n, int64_t ct) {
     for (;;) {
         const int64_t rows = (int64_t)(buf.size() / Cin);
         if (rows < (int64_t)G * NT + 2 * nt) break;
-        launch_windows_from_buf(G, false);
+        launch_windows_from_buf(G, 0);
     }
 }
 
 void Handle::flush() {
     if (!seg_active) return;
-    // pending new samples: rows past the nt context rows at the front of buf
+    // pending new samples: rows past the nt context rows at the front of buf.  Complete windows
+    // go out in groups; a window that runs past the data is padded and launched on its own.
     for (;;) {
         const int64_t rows = (int64_t)(buf.size() / Cin);
-        const int64_t fresh = rows - nt;
-        if (fresh <= 0) break;
-        const int64_t nbat = (fresh + NT - 1) / NT;
-        const int g = (int)std::min<int64_t>(nbat, G);
-        launch_windows_from_buf(g, true);
+        if (rows - nt <= 0) break;
+        const int64_t complete = rows >= W ? (rows - W) / NT + 1 : 0;
+        if (complete > 0) {
+            launch_windows_from_buf((int)std::min<int64_t>(complete, G), 0);
+        } else {
+            launch_windows_from_buf(1, next_batch == 0 ? 2 : 1);
+        }
     }
     seg_active = false;
     buf.clear();

@@ -230,3 +230,27 @@ def test_kernel_launch_count(win_oss, win):
     with sorter.OnlineSorter(win_oss, max_iters=100) as s:
         s.sort_windows(win["window"])
         assert s.kernel_launches() == 9
+
+
+def test_cpp_dropin_replay(golden_dir, tmp_path):
+    """The C++ drop-in class (lss::OnlineSpikesV2 over a DataSocket) driven by the replay program
+    writes spikeOutput.txt lines "time,cluster,amplitude,y" equal to the Kilosort fixture."""
+    import subprocess
+    from livespikesorter_gb300 import build
+    z = np.load(golden_dir / "ks_stream.npz")
+    d = write_oss_from_arrays(z, tmp_path / "oss_input")
+    rec = tmp_path / "rec.i16"
+    z["data"].astype(np.int16).tofile(rec)
+    out = tmp_path / "out"
+    r = subprocess.run([str(build.REPLAY), str(d), str(rec), str(z["data"].shape[1]), str(out), str(int(z["NT"])), "613"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    rows = np.loadtxt(out / "spikeOutput.txt", delimiter=",", ndmin=2)
+    keep = z["keep"].astype(bool)
+    st = z["st"][keep]
+    order = np.lexsort((st[:, 1], st[:, 0]))
+    st = st[order]
+    assert rows.shape[0] == len(st)
+    np.testing.assert_array_equal(rows[:, 0].astype(np.int64), st[:, 0].astype(np.int64))
+    np.testing.assert_array_equal(rows[:, 1].astype(np.int64), z["clu"][keep][order])
+    np.testing.assert_allclose(rows[:, 2], st[:, 2], rtol=1e-4)
