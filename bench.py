@@ -293,12 +293,14 @@ def run_gpu(a):
     obuf = np.zeros(1 << 16, sorter.SPIKE_DTYPE)
 
     def host_step():
+        # a continuous stream: the recording is replayed from the start when it runs out
         if pos[0] + chunk > data.shape[0]:
-            s2.flush()
-            drain(s2)
-            pos[0] = 0
-        s2.push(data[pos[0]: pos[0] + chunk], pos[0])
-        pos[0] += chunk
+            rows = np.concatenate([data[pos[0]:], data[: pos[0] + chunk - data.shape[0]]])
+            pos[0] = pos[0] + chunk - data.shape[0]
+        else:
+            rows = data[pos[0]: pos[0] + chunk]
+            pos[0] += chunk
+        s2.push(rows)
         return len(s2.poll(out=obuf))
 
     for _ in range(a.warmup + 1):

@@ -19,9 +19,11 @@ public:
     ReplaySocket(std::vector<int16_t> data, int nchan, long tick) : d_(std::move(data)), c_(nchan), tick_(tick) {
         n_ = (lss::t_ull)(d_.size() / (size_t)c_);
     }
+    // the stream starts empty; every query afterwards finds rows_per_tick more rows
     lss::t_ull getStreamSampleCt(int, const lss::OSSSpecificParams&) override {
+        const lss::t_ull now = avail_;
         avail_ = std::min(n_, avail_ + (lss::t_ull)tick_);
-        return avail_;
+        return now;
     }
     lss::t_ull fetchLatest(int16_t* out, long maxRows, const lss::OSSSpecificParams& p, lss::t_ull start) override {
         lss::t_ull s = std::max(start, avail_ > (lss::t_ull)maxRows ? avail_ - (lss::t_ull)maxRows : 0ULL);
@@ -35,6 +37,7 @@ public:
         return end;
     }
     bool isRunning() override { return fetched_ < n_; }
+    void waitUntil(lss::t_ull, const lss::OSSSpecificParams&) override {}
 
 private:
     std::vector<int16_t> d_;

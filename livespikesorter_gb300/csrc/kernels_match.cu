@@ -12,10 +12,12 @@
 //      per output sample (each CTA updates only its own samples, so no atomics and a fixed
 //      summation order).
 //
-// Phases are separated by hardware cluster barriers (barrier.cluster arrive.release /
-// wait.acquire); data shared between CTAs goes through L2 with .cg loads.  No spin-waits,
-// no host round trips; the loop ends when an iteration accepts nothing (the same decision
-// in every CTA) or after max_iters.
+// When the CTA's slice of the score matrix fits (G = 16: ceil(W/16) samples x T templates x 4 B
+// <= ~220 KB), it stays in shared memory for the whole loop; otherwise it is read and written in
+// place in global memory (L2).  Phases are separated by hardware cluster barriers
+// (barrier.cluster arrive.release / wait.acquire); data shared between CTAs goes through L2
+// with .cg loads.  No spin-waits, no host round trips; the loop ends when an iteration accepts
+// nothing (the same decision in every CTA) or after max_iters.
 #include "lss_kernels.cuh"
 
 #include <cfloat>
@@ -39,7 +41,17 @@ __device__ __forceinline__ unsigned cluster_rank() {
     return r;
 }
 
-template <int G>
+constexpr int kWarps = kMatchThreads / 32;
+constexpr int kMaxRounds = 64;   // slice <= 64 * 512 samples per CTA
+
+// dynamic shared memory of one CTA: [score slice if SMEM_B][s_cf][s_t][s_amp], floats/ints
+__host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, bool smem_b) {
+    const int span = (W + G - 1) / G;
+    const size_t halo = (size_t)span + 2 * nt;
+    return (smem_b ? (size_t)span * T * 4 : 0) + halo * 12;
+}
+
+template <int G, bool SMEM_B>
 __global__ void __launch_bounds__(kMatchThreads)
 match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __restrict__ ctcP,
              const float* __restrict__ pre_wf, const float* __restrict__ nm, float th2, int W, int T, int C,
@@ -49,16 +61,21 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     const int rank = (G == 1) ? 0 : (int)cluster_rank();
     const int span = (W + G - 1) / G;
     const int lo = min(W, rank * span), hi = min(W, lo + span);
-    const int halo = hi - lo + 2 * nt;
-    float* s_cf = smem;                                   // [halo]
-    int* s_t = reinterpret_cast<int*>(s_cf + halo);      // [halo]
-    float* s_amp = reinterpret_cast<float*>(s_t + halo); // [halo]
+    const int halo = span + 2 * nt;
+    float* Bs = smem;                                                  // [span][T] when SMEM_B
+    float* s_cf = smem + (SMEM_B ? (size_t)span * T : 0);            // [halo]
+    int* s_t = reinterpret_cast<int*>(s_cf + halo);                    // [halo]
+    float* s_amp = reinterpret_cast<float*>(s_t + halo);               // [halo]
     __shared__ int s_cnt[G];
-    __shared__ int s_red[kMatchThreads / 32];
+    __shared__ int s_woff[kMaxRounds * kWarps];
+    __shared__ int s_total;
 
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = kMatchThreads / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int L2 = 2 * nt + 1, hw = nt / 2;
-    float* B = Bt + (int64_t)b * W * T;
+    const int rounds = (hi - lo + kMatchThreads - 1) / kMatchThreads;
+    float* Bg = Bt + (int64_t)b * W * T;
+    // row pointer of sample w (own slice only)
+    auto brow = [&](int w) -> float* { return SMEM_B ? Bs + (size_t)(w - lo) * T : Bg + (int64_t)w * T; };
     float* X = Xres + (int64_t)b * W * C;
     float* cfmax = sc.cfmax + (int64_t)b * W;
     int* imax = sc.imax + (int64_t)b * W;
@@ -71,24 +88,37 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     float* sp_amp = out.sp_amp + (int64_t)b * out.cap;
     int* sp_iter = out.sp_iter + (int64_t)b * out.cap;
 
-    if (G > 1 && rank != (unsigned)(blockIdx.x % G) && tid == 0) atomicOr(out.status + b, 2);
+    if (G > 1 && rank != (int)(blockIdx.x % G) && tid == 0) atomicOr(out.status + b, 2);
+    if (rounds > kMaxRounds && tid == 0) atomicOr(out.status + b, 2);
+    if constexpr (SMEM_B) {
+        // the slice [lo, hi) x T is contiguous in global memory
+        const int64_t n = (int64_t)(hi - lo) * T;
+        const float* src = Bg + (int64_t)lo * T;
+        if ((((uintptr_t)src) & 15) == 0 && (n & 3) == 0) {
+            const float4* s4 = reinterpret_cast<const float4*>(src);
+            float4* d4 = reinterpret_cast<float4*>(Bs);
+            for (int64_t i = tid; i < n / 4; i += kMatchThreads) d4[i] = __ldcs(s4 + i);
+        } else {
+            for (int64_t i = tid; i < n; i += kMatchThreads) Bs[i] = __ldcs(src + i);
+        }
+    }
     for (int w = lo + tid; w < hi; w += kMatchThreads) dirty[w] = 1;
     __syncthreads();
 
     int n_total = 0, iters = 0;
-    for (int it = 0; it < max_iters; ++it) {
+    for (int it = 0; it < max_iters && rounds <= kMaxRounds; ++it) {
         // ---- A: per-sample max / argmax over templates (changed samples only) ----
-        for (int w = lo + warp; w < hi; w += nwarps) {
+        for (int w = lo + warp; w < hi; w += kWarps) {
             if (!dirty[w]) continue;
             float best = 0.f;
             int bi = 0;
             if (w >= nt && w < W - nt) {
                 best = -1.f;
                 bi = 0x7fffffff;
-                const float* row = B + (int64_t)w * T;
+                const float* row = brow(w);
                 for (int t = lane; t < T; t += 32) {
                     const float r = fmaxf(row[t], 0.f);
-                    const float v = r * r / nm[t];
+                    const float v = r * r / __ldg(nm + t);
                     if (v > best) { best = v; bi = t; }
                 }
 #pragma unroll
@@ -102,66 +132,74 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
         }
         group_barrier<G>();
 
-        // ---- B1: pooled max and acceptance on the own slice ----
+        // ---- B1: pooled max and acceptance on the own slice; per-warp counts per round ----
         for (int i = tid; i < halo; i += kMatchThreads) {
             const int w = lo - nt + i;
             s_cf[i] = (w >= 0 && w < W) ? __ldcg(cfmax + w) : -FLT_MAX;
         }
         __syncthreads();
-        int my_cnt = 0;
-        for (int w = lo + tid; w < hi; w += kMatchThreads) {
-            const int i = w - lo + nt;
-            float cm = -FLT_MAX;
-            for (int d = -nt; d <= nt; ++d) cm = fmaxf(cm, s_cf[i + d]);
-            const float cf = s_cf[i];
-            int tt = -1;
-            float amp = 0.f;
-            if (cm > th2 && cf == cm) {
-                tt = imax[w];
-                amp = B[(int64_t)w * T + tt] / nm[tt];
-                ++my_cnt;
+        for (int r = 0; r < rounds; ++r) {
+            const int w = lo + r * kMatchThreads + tid;
+            bool acc = false;
+            if (w < hi) {
+                const int i = w - lo + nt;
+                float cm = -FLT_MAX;
+                for (int d = -nt; d <= nt; ++d) cm = fmaxf(cm, s_cf[i + d]);
+                const float cf = s_cf[i];
+                int tt = -1;
+                float amp = 0.f;
+                if (cm > th2 && cf == cm) {
+                    tt = imax[w];
+                    amp = brow(w)[tt] / __ldg(nm + tt);
+                    acc = true;
+                }
+                at_t[w] = tt;
+                at_amp[w] = amp;
             }
-            at_t[w] = tt;
-            at_amp[w] = amp;
+            const unsigned m = __ballot_sync(0xffffffffu, acc);
+            if (lane == 0) s_woff[r * kWarps + warp] = __popc(m);
         }
-        my_cnt = __reduce_add_sync(0xffffffffu, my_cnt);
-        if (lane == 0) s_red[warp] = my_cnt;
         __syncthreads();
         if (tid == 0) {
-            int c = 0;
-            for (int i = 0; i < nwarps; ++i) c += s_red[i];
-            cta_cnt[(it & 1) * G + rank] = c;
+            // exclusive prefix over (round, warp) = sample order within the slice
+            int acc = 0;
+            for (int i = 0; i < rounds * kWarps; ++i) {
+                const int c = s_woff[i];
+                s_woff[i] = acc;
+                acc += c;
+            }
+            cta_cnt[(it & 1) * G + rank] = acc;
         }
         group_barrier<G>();
 
         // ---- totals: the same numbers in every CTA of the cluster ----
         if (tid < G) s_cnt[tid] = __ldcg(cta_cnt + (it & 1) * G + tid);
         __syncthreads();
-        int total = 0, base = n_total;
-        for (int r = 0; r < G; ++r) {
-            total += s_cnt[r];
-            if (r < rank) base += s_cnt[r];
+        if (tid == 0) {
+            int total = 0;
+            for (int r = 0; r < G; ++r) total += s_cnt[r];
+            s_total = total;
         }
+        __syncthreads();
+        const int total = s_total;
         if (total == 0) break;
         ++iters;
+        int base = n_total;
+        for (int r = 0; r < rank; ++r) base += s_cnt[r];
 
-        // ---- B2: record the own slice's spikes in sample order ----
-        if (warp == 0) {
-            int run = base;
-            for (int w0 = lo; w0 < hi; w0 += 32) {
-                const int w = w0 + lane;
-                const int tt = (w < hi) ? at_t[w] : -1;
-                const unsigned m = __ballot_sync(0xffffffffu, tt >= 0);
-                if (tt >= 0) {
-                    const int slot = run + __popc(m & ((1u << lane) - 1u));
-                    if (slot < out.cap) {
-                        sp_w[slot] = w;
-                        sp_t[slot] = tt;
-                        sp_amp[slot] = at_amp[w];
-                        sp_iter[slot] = it;
-                    }
+        // ---- B2: record the own slice's spikes in sample order (all threads) ----
+        for (int r = 0; r < rounds; ++r) {
+            const int w = lo + r * kMatchThreads + tid;
+            const int tt = (w < hi) ? at_t[w] : -1;
+            const unsigned m = __ballot_sync(0xffffffffu, tt >= 0);
+            if (tt >= 0) {
+                const int slot = base + s_woff[r * kWarps + warp] + __popc(m & ((1u << lane) - 1u));
+                if (slot < out.cap) {
+                    sp_w[slot] = w;
+                    sp_t[slot] = tt;
+                    sp_amp[slot] = at_amp[w];
+                    sp_iter[slot] = it;
                 }
-                run += __popc(m);
             }
         }
 
@@ -173,9 +211,10 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             s_amp[i] = in ? __ldcg(at_amp + w) : 0.f;
         }
         __syncthreads();
-        for (int wp = lo + warp; wp < hi; wp += nwarps) {
+        for (int wp = lo + warp; wp < hi; wp += kWarps) {
             const int i0 = wp - lo;   // s_t[i0 + e] is the sample wp - nt + e
             bool any = false;
+            float* br = brow(wp);
             for (int e0 = 0; e0 < L2; e0 += 32) {
                 const int e = e0 + lane;
                 unsigned m = __ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0);
@@ -187,8 +226,7 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                     const float a = s_amp[i0 + ee];
                     const int l = 2 * nt - ee;               // = wp - w + nt
                     const float* crow = ctcP + ((int64_t)ts * L2 + l) * T;
-                    float* brow = B + (int64_t)wp * T;
-                    for (int t = lane; t < T; t += 32) brow[t] = fmaf(-a, __ldg(crow + t), brow[t]);
+                    for (int t = lane; t < T; t += 32) br[t] = fmaf(-a, __ldg(crow + t), br[t]);
                     const int dw = nt - ee;                   // = wp - w
                     if (dw >= -hw && dw <= hw) {
                         const float* wrow = pre_wf + ((int64_t)ts * nt + (dw + hw)) * C;
@@ -209,15 +247,18 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     }
 }
 
-cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm, float th2,
-                         int W, int T, int C, int nt, int max_iters, int nb, const MatchScratch& sc,
-                         const MatchOut& out, cudaStream_t s) {
-    constexpr int G = kMatchCluster;
-    const int span = (W + G - 1) / G;
-    const size_t smem = (size_t)(span + 2 * nt) * 12;
-    auto kern = match_kernel<G>;
+template <int G, bool SMEM_B>
+static cudaError_t launch_match_cfg(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
+                                    float th2, int W, int T, int C, int nt, int max_iters, int nb,
+                                    const MatchScratch& sc, const MatchOut& out, cudaStream_t s) {
+    const size_t smem = match_smem_bytes(W, T, nt, G, SMEM_B);
+    auto kern = match_kernel<G, SMEM_B>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    if (G > 8) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb * G, 1, 1);
     cfg.blockDim = dim3(kMatchThreads, 1, 1);
@@ -231,6 +272,55 @@ cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float*
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kern, Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, sc, out);
+}
+
+// Can a cluster of 16 CTAs with the whole score slice in shared memory run on this device?
+static int smem16_ok(int W, int T, int nt) {
+    const size_t smem = match_smem_bytes(W, T, nt, 16, true);
+    int dev = 0, maxopt = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+    if (smem + 8192 > (size_t)maxopt) return 0;   // static shared memory and the driver reserve
+    auto kern = match_kernel<16, true>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16, 1, 1);
+    cfg.blockDim = dim3(kMatchThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int match_variant(int W, int T, int nt) {
+    static thread_local int cW = -1, cT = -1, cnt = -1, cres = 0;
+    if (W != cW || T != cT || nt != cnt) {
+        cres = smem16_ok(W, T, nt) > 0 ? 16 : 8;
+        cW = W, cT = T, cnt = nt;
+    }
+    return cres;
+}
+
+cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm, float th2,
+                         int W, int T, int C, int nt, int max_iters, int nb, const MatchScratch& sc,
+                         const MatchOut& out, cudaStream_t s) {
+    if (match_variant(W, T, nt) == 16)
+        return launch_match_cfg<16, true>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc, out, s);
+    return launch_match_cfg<8, false>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc, out, s);
 }
 
 }  // namespace lss

@@ -46,7 +46,7 @@ struct SpikeRec {
     float feat[64];
 };
 
-constexpr int kMatchCluster = 8;   // CTAs per batch in the matching loop (one thread-block cluster)
+constexpr int kMatchCluster = 16;  // largest cluster (CTAs per batch) the matching loop launches
 constexpr int kMatchThreads = 512;
 
 void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT,

@@ -37,6 +37,8 @@ def agreement(t_ref, k_ref, a_ref, t_got, k_got, a_got, tol: int = 1):
     """(fraction matched over the larger set, fraction of matched pairs with amplitude within
     1e-3 relative, max relative amplitude error)"""
     ri, gi = match_spikes(t_ref, k_ref, t_got, k_got, tol)
+    if len(t_ref) == 0 and len(t_got) == 0:
+        return 1.0, 1.0, 0.0
     denom = max(len(t_ref), len(t_got), 1)
     if len(ri) == 0:
         return len(ri) / denom, 1.0 if denom == 1 else 0.0, 0.0
