@@ -51,7 +51,7 @@ def args_():
     ap.add_argument("--latency-batches", type=int, default=200)
     ap.add_argument("--cpu-sample", type=int, default=6, help="batches timed on the CPU oracle")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile-only", action="store_true", help="one short pass (for ncu)")
+    ap.add_argument("--match-variant", type=int, default=0, help="0 auto, 1 scores in L2, 2 scores in SMEM")
     return ap.parse_args()
 
 
@@ -237,7 +237,8 @@ def run_gpu(a):
     d_data = torch.from_numpy(data).to(f"cuda:{dev}")
     base_ptr = d_data.data_ptr()
     row_bytes = C * 2
-    s = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1)
+    s = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1,
+                           match_variant=a.match_variant)
     ext = torch.cuda.ExternalStream(s.cuda_stream(), device=f"cuda:{dev}")
     spikes_seen = [0]
 
@@ -287,7 +288,8 @@ def run_gpu(a):
     del d_data
 
     # ---- end to end through the host API ---------------------------------------------------
-    s2 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G)
+    s2 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
+                             match_variant=a.match_variant)
     chunk = G * NT
     pos = [0]
     obuf = np.zeros(1 << 16, sorter.SPIKE_DTYPE)
@@ -323,7 +325,8 @@ def run_gpu(a):
     s2.close()
 
     # ---- per-batch latency (one batch per launch) --------------------------------------------
-    s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1, profile=1)
+    s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1, profile=1,
+                             match_variant=a.match_variant)
     lat = []
     s3.push(data[:NT + 2 * nt], 0)
     drain(s3)

@@ -52,7 +52,8 @@ typedef struct lss_params {
     int32_t spike_cap;      /* per-batch spike buffer; 0 = automatic */
     int64_t mem_budget;     /* device bytes this handle may hold; 0 = no limit (admission check) */
     int32_t profile;        /* 1 = time every stage with CUDA events (lss_stage_times) */
-    int32_t reserved[5];
+    int32_t match_variant;  /* 0 = automatic; 1 = scores in L2, 8-CTA clusters; 2 = scores in shared memory */
+    int32_t reserved[4];
 } lss_params;
 
 /* One sorted spike.  time is the stream sample (Kilosort template_matching.py:68). */

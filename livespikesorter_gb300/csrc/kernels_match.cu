@@ -43,6 +43,7 @@ __device__ __forceinline__ unsigned cluster_rank() {
 
 constexpr int kWarps = kMatchThreads / 32;
 constexpr int kMaxRounds = 64;   // slice <= 64 * 512 samples per CTA
+constexpr int kPerLane = 16;     // row elements each lane loads before it stores (512 per warp)
 
 // dynamic shared memory of one CTA: [score slice if SMEM_B][s_cf][s_t][s_amp], floats/ints
 __host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, bool smem_b) {
@@ -108,27 +109,52 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     int n_total = 0, iters = 0;
     for (int it = 0; it < max_iters && rounds <= kMaxRounds; ++it) {
         // ---- A: per-sample max / argmax over templates (changed samples only) ----
-        for (int w = lo + warp; w < hi; w += kWarps) {
-            if (!dirty[w]) continue;
-            float best = 0.f;
-            int bi = 0;
-            if (w >= nt && w < W - nt) {
-                best = -1.f;
-                bi = 0x7fffffff;
-                const float* row = brow(w);
-                for (int t = lane; t < T; t += 32) {
-                    const float r = fmaxf(row[t], 0.f);
-                    const float v = r * r / __ldg(nm + t);
-                    if (v > best) { best = v; bi = t; }
-                }
+        for (int w0 = lo + warp; w0 < hi; w0 += 2 * kWarps) {
+            // two samples per pass: their loads are in flight together
+            float best[2] = {0.f, 0.f};
+            int bi[2] = {0, 0};
+            bool live[2];
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            for (int q = 0; q < 2; ++q) {
+                const int w = w0 + q * kWarps;
+                live[q] = (w < hi) && dirty[w];
+                if (live[q] && w >= nt && w < W - nt) {
+                    best[q] = -1.f;
+                    bi[q] = 0x7fffffff;
                 }
             }
-            if (lane == 0) { cfmax[w] = best; imax[w] = bi; }
+            const bool in0 = live[0] && w0 >= nt && w0 < W - nt;
+            const bool in1 = live[1] && (w0 + kWarps) >= nt && (w0 + kWarps) < W - nt;
+            if (in0 || in1) {
+                const float* r0 = brow(in0 ? w0 : lo);
+                const float* r1 = brow(in1 ? w0 + kWarps : lo);
+                for (int t = lane; t < T; t += 32) {
+                    const float n = __ldg(nm + t);
+                    const float x0 = in0 ? r0[t] : 0.f;
+                    const float x1 = in1 ? r1[t] : 0.f;
+                    const float a0 = fmaxf(x0, 0.f), a1 = fmaxf(x1, 0.f);
+                    const float v0 = a0 * a0 / n, v1 = a1 * a1 / n;
+                    if (in0 && v0 > best[0]) { best[0] = v0; bi[0] = t; }
+                    if (in1 && v1 > best[1]) { best[1] = v1; bi[1] = t; }
+                }
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const float ob = __shfl_xor_sync(0xffffffffu, best[q], o);
+                        const int oi = __shfl_xor_sync(0xffffffffu, bi[q], o);
+                        if (ob > best[q] || (ob == best[q] && oi < bi[q])) { best[q] = ob; bi[q] = oi; }
+                    }
+                }
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int q = 0; q < 2; ++q)
+                    if (live[q]) {
+                        cfmax[w0 + q * kWarps] = best[q];
+                        imax[w0 + q * kWarps] = bi[q];
+                    }
+            }
         }
         group_barrier<G>();
 
@@ -215,6 +241,7 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             const int i0 = wp - lo;   // s_t[i0 + e] is the sample wp - nt + e
             bool any = false;
             float* br = brow(wp);
+            float* xrow = X + (int64_t)wp * C;
             for (int e0 = 0; e0 < L2; e0 += 32) {
                 const int e = e0 + lane;
                 unsigned m = __ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0);
@@ -226,12 +253,44 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                     const float a = s_amp[i0 + ee];
                     const int l = 2 * nt - ee;               // = wp - w + nt
                     const float* crow = ctcP + ((int64_t)ts * L2 + l) * T;
-                    for (int t = lane; t < T; t += 32) br[t] = fmaf(-a, __ldg(crow + t), br[t]);
+                    // every load of the chunk is issued before the first store, so the
+                    // round trips overlap instead of queueing behind each store
+                    for (int t0 = 0; t0 < T; t0 += 32 * kPerLane) {
+                        float cv[kPerLane];
+#pragma unroll
+                        for (int j = 0; j < kPerLane; ++j) {
+                            const int t = t0 + lane + 32 * j;
+                            cv[j] = (t < T) ? __ldg(crow + t) : 0.f;
+                        }
+                        float bv[kPerLane];
+#pragma unroll
+                        for (int j = 0; j < kPerLane; ++j) {
+                            const int t = t0 + lane + 32 * j;
+                            bv[j] = (t < T) ? br[t] : 0.f;
+                        }
+#pragma unroll
+                        for (int j = 0; j < kPerLane; ++j) {
+                            const int t = t0 + lane + 32 * j;
+                            if (t < T) br[t] = fmaf(-a, cv[j], bv[j]);
+                        }
+                    }
                     const int dw = nt - ee;                   // = wp - w
                     if (dw >= -hw && dw <= hw) {
                         const float* wrow = pre_wf + ((int64_t)ts * nt + (dw + hw)) * C;
-                        float* xrow = X + (int64_t)wp * C;
-                        for (int c = lane; c < C; c += 32) xrow[c] = fmaf(-a, __ldg(wrow + c), xrow[c]);
+                        for (int c0 = 0; c0 < C; c0 += 32 * kPerLane) {
+                            float wv[kPerLane], xv[kPerLane];
+#pragma unroll
+                            for (int j = 0; j < kPerLane; ++j) {
+                                const int c = c0 + lane + 32 * j;
+                                wv[j] = (c < C) ? __ldg(wrow + c) : 0.f;
+                                xv[j] = (c < C) ? xrow[c] : 0.f;
+                            }
+#pragma unroll
+                            for (int j = 0; j < kPerLane; ++j) {
+                                const int c = c0 + lane + 32 * j;
+                                if (c < C) xrow[c] = fmaf(-a, wv[j], xv[j]);
+                            }
+                        }
                     }
                 }
             }
@@ -317,8 +376,14 @@ int match_variant(int W, int T, int nt) {
 
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm, float th2,
                          int W, int T, int C, int nt, int max_iters, int nb, const MatchScratch& sc,
-                         const MatchOut& out, cudaStream_t s) {
-    if (match_variant(W, T, nt) == 16)
+                         const MatchOut& out, cudaStream_t s, int variant) {
+    // variant: 0 = automatic (shared-memory scores when they fit and the group is small enough
+    // that 16-CTA clusters do not leave SMs idle), 1 = scores in global memory, 8-CTA clusters,
+    // 2 = scores in shared memory, 16-CTA clusters (falls back to 1 when it cannot launch)
+    bool smem = false;
+    if (variant == 2) smem = match_variant(W, T, nt) == 16;
+    else if (variant == 0) smem = nb <= 8 && match_variant(W, T, nt) == 16;
+    if (smem)
         return launch_match_cfg<16, true>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc, out, s);
     return launch_match_cfg<8, false>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc, out, s);
 }

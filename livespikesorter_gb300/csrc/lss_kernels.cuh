@@ -64,7 +64,7 @@ void launch_basis_conv_host(const float* Z, int C, int W, const float* wPCA_dev,
                             int nt, int nb, float* Bpc, cudaStream_t s);
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                          float th2, int W, int T, int C, int nt, int max_iters, int nb,
-                         const MatchScratch& sc, const MatchOut& out, cudaStream_t s);
+                         const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0);
 void launch_features(const float* Xres, const MatchOut& out, int nb, int W, int C, int T, int K, int nt, int nC,
                      const float* wPCA, const int64_t* iCC, const int64_t* iU, const float* Ucc, const float* xc,
                      const float* yc, const float* centroids, int n_final, const int* rec_offset, SpikeRec* recs,

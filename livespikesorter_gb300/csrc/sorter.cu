@@ -390,7 +390,8 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     LSS_CUDA(cudaGetLastError());
     mark();
     LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
-    LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st));
+    LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st,
+                          p.match_variant));
     ++nl;
     mark();
     launch_rec_offsets(mo, nb, s.d_off, st), ++nl;
@@ -623,6 +624,7 @@ int lss_default_params(lss_params* p) {
     p->spike_cap = 0;
     p->mem_budget = 0;
     p->profile = 0;
+    p->match_variant = 0;
     return LSS_OK;
 }
 
@@ -814,7 +816,7 @@ int lss_debug_stage(lss_handle* hp, const int16_t* window, int32_t W, int32_t st
             } else {
                 LSS_CUDA(cudaMemsetAsync(h.mo.status, 0, sizeof(int), st));
                 LSS_CUDA(lss::launch_match(h.d_Bt, h.d_Z, h.d_ctcP, h.d_pre_wf, h.d_nm, h.th * h.th, W, h.T, h.C, h.nt,
-                                           h.max_iters, 1, h.sc, h.mo, st));
+                                           h.max_iters, 1, h.sc, h.mo, st, h.p.match_variant));
                 LSS_CUDA(cudaMemcpyAsync(out, h.d_Z, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
             }
         }
