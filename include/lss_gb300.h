@@ -127,7 +127,8 @@ int lss_pending(lss_handle* h, int64_t* n);
 /* Free everything (OnlineSpikesV2::~OnlineSpikesV2, OnlineSpikesV2.cu:283-320). */
 int lss_close(lss_handle* h);
 
-/* Message of the last failure on h (or of the last failed lss_open when h is NULL). */
+/* Message of the last failure on h (or, when h is NULL, of the last failed call on this thread
+ * that takes no handle: lss_open, lss_match_noalloc). */
 const char* lss_last_error(const lss_handle* h);
 
 /* Sort explicit windows without stream framing: windows = int16 [n_windows][W][n_chan_in].
@@ -169,6 +170,33 @@ int lss_cuda_stream(const lss_handle* h, void** stream);
  * (Timer.h:7-21) prints nothing; this is its working counterpart. */
 #define LSS_N_STAGES 10
 int lss_stage_times(lss_handle* h, double* ms, int32_t n, int64_t* n_groups);
+
+/* The matching loop of one window on buffers the caller owns, allocating no memory.
+ *
+ * No counterpart in the reference.  For callers that cannot allocate device memory when they
+ * sort -- a real-time acquisition thread that must not wait on the allocator, code confined to a
+ * memory pool owned by another framework, or an application that already keeps the scores and
+ * the residual in its own device buffers.  All pointers are device pointers on the current CUDA
+ * device; stream is a cudaStream_t (NULL = legacy default stream); the call is asynchronous.
+ *   scores          [W][T]  template scores (B transposed); consumed (overwritten)
+ *   residual        [W][C]  preprocessed window in, Xres out
+ *   ctc_perm        [T][2*nt+1][T]  ctc_perm[s][l][t] = ctc[t][s][l]
+ *   waveforms       [T][nt][C]      preclustered_template_waveforms
+ *   template_norms  [T]             sum of squares of each Wall3 template
+ *   n_spikes        [1]     spikes accepted (may exceed cap; the lists then hold the first cap)
+ *   spike_sample / spike_template / spike_amp / spike_iter  [cap]  in (iteration, sample) order
+ * Its working memory is a fixed device array of LSS_NOALLOC_SCRATCH_BYTES inside the library
+ * (held on every GPU that loads it until the process exits), enough for windows of at most
+ * LSS_NOALLOC_MAX_SAMPLES samples; a larger W returns LSS_ERR_ARG.  The first call on a device
+ * looks up that array's device address, so make it before any stream capture.  All calls share
+ * the array: calls whose work overlaps on the GPU race, so serialise them (one stream, or events).
+ * Errors: LSS_ERR_ARG / LSS_ERR_CUDA, message via lss_last_error(NULL). */
+#define LSS_NOALLOC_MAX_SAMPLES 16384
+#define LSS_NOALLOC_SCRATCH_BYTES 279040
+int lss_match_noalloc(float* scores, float* residual, const float* ctc_perm, const float* waveforms,
+                      const float* template_norms, float th, int32_t W, int32_t T, int32_t C, int32_t nt,
+                      int32_t max_iters, int32_t* n_spikes, int32_t* spike_sample, int32_t* spike_template,
+                      float* spike_amp, int32_t* spike_iter, int32_t cap, void* stream);
 
 #ifdef __cplusplus
 }

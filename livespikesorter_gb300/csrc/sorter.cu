@@ -587,7 +587,11 @@ struct lss_handle {
     Handle h;
 };
 
-static thread_local std::string g_open_error;
+namespace lss {
+// message of the last failure of a call that has no handle (lss_open, lss_match_noalloc)
+thread_local std::string g_handleless_error;
+}
+static std::string& g_open_error = lss::g_handleless_error;
 
 #define LSS_TRY(hptr, ...)                                                                         \
     try {                                                                                          \

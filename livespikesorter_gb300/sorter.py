@@ -68,6 +68,9 @@ _SIGS = {
     "lss_push_device_span": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int64]),
     "lss_cuda_stream": (ct.c_int, [ct.c_void_p, _P(ct.c_void_p)]),
     "lss_stage_times": (ct.c_int, [ct.c_void_p, _P(ct.c_double), ct.c_int32, _P(ct.c_int64)]),
+    "lss_match_noalloc": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_float,
+                                     ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p,
+                                     ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_void_p]),
 }
 STAGES = ("h2d", "colsum", "car", "highpass", "whiten", "basis_conv", "project", "match", "features", "d2h")
 
