@@ -7,10 +7,13 @@
 //   B1 (2nt+1) max pool of that per-sample max; accept a sample when the pooled value
 //      exceeds Th^2 and equals the sample's own max; amplitude B[w][iY] / nm[iY];
 //   B2 write the accepted spikes, ordered by (iteration, sample) like the reference;
-//   C  subtract every accepted spike: B[w'][:] -= amp * ctc[:, iY, w'-w+nt] for |w'-w| <= nt
-//      and Xres[w'][:] -= amp * waveform[iY][w'-w+nt/2] for |w'-w| <= nt/2 -- as a gather
-//      per output sample (each CTA updates only its own samples, so no atomics and a fixed
-//      summation order).
+//   C  subtract every accepted spike from the scores: B[w'][:] -= amp * ctc[:, iY, w'-w+nt] for
+//      |w'-w| <= nt -- as a gather per output sample (each CTA updates only its own samples, so
+//      no atomics and a fixed summation order).
+//
+// The loop never reads the residual, so the waveform subtraction Xres[w'][:] -= amp *
+// waveform[iY][w'-w+nt/2] (|w'-w| <= nt/2) runs afterwards in residual_kernel, applying the
+// spikes in the same (iteration, sample) order.
 //
 // When the CTA's slice of the score matrix fits (G = 16: ceil(W/16) samples x T templates x 4 B
 // <= ~220 KB), it stays in shared memory for the whole loop; otherwise it is read and written in
@@ -43,7 +46,7 @@ __device__ __forceinline__ unsigned cluster_rank() {
 
 constexpr int kWarps = kMatchThreads / 32;
 constexpr int kMaxRounds = 64;   // slice <= 64 * 512 samples per CTA
-constexpr int kPerLane = 16;     // row elements each lane loads before it stores (512 per warp)
+constexpr int kPerLane = 8;      // row elements each lane loads before it stores (256 per warp)
 
 // dynamic shared memory of one CTA: [score slice if SMEM_B][s_cf][s_t][s_amp], floats/ints
 __host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, bool smem_b) {
@@ -53,7 +56,7 @@ __host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, 
 }
 
 template <int G, bool SMEM_B>
-__global__ void __launch_bounds__(kMatchThreads)
+__global__ void __launch_bounds__(kMatchThreads, 2)
 match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __restrict__ ctcP,
              const float* __restrict__ pre_wf, const float* __restrict__ nm, float th2, int W, int T, int C,
              int nt, int max_iters, MatchScratch sc, MatchOut out) {
@@ -72,12 +75,11 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     __shared__ int s_total;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int L2 = 2 * nt + 1, hw = nt / 2;
+    const int L2 = 2 * nt + 1;
     const int rounds = (hi - lo + kMatchThreads - 1) / kMatchThreads;
     float* Bg = Bt + (int64_t)b * W * T;
     // row pointer of sample w (own slice only)
     auto brow = [&](int w) -> float* { return SMEM_B ? Bs + (size_t)(w - lo) * T : Bg + (int64_t)w * T; };
-    float* X = Xres + (int64_t)b * W * C;
     float* cfmax = sc.cfmax + (int64_t)b * W;
     int* imax = sc.imax + (int64_t)b * W;
     int* at_t = sc.at_t + (int64_t)b * W;
@@ -241,7 +243,37 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             const int i0 = wp - lo;   // s_t[i0 + e] is the sample wp - nt + e
             bool any = false;
             float* br = brow(wp);
-            float* xrow = X + (int64_t)wp * C;
+            // spikes within +-nt of wp, in increasing sample order, two at a time: both rows of
+            // ctc are loaded before either is applied, and they are applied in order
+            int t0s = 0, l0s = 0, t1s = 0, l1s = 0;
+            float a0s = 0.f, a1s = 0.f;
+            int npend = 0;
+            auto flush = [&]() {
+                const float* c0 = ctcP + ((int64_t)t0s * L2 + l0s) * T;
+                const float* c1 = ctcP + ((int64_t)t1s * L2 + l1s) * T;
+                const bool two = npend == 2;
+                for (int tb = 0; tb < T; tb += 32 * kPerLane) {
+                    float v0[kPerLane], v1[kPerLane], bv[kPerLane];
+#pragma unroll
+                    for (int j = 0; j < kPerLane; ++j) {
+                        const int t = tb + lane + 32 * j;
+                        const bool ok = t < T;
+                        v0[j] = ok ? __ldg(c0 + t) : 0.f;
+                        v1[j] = (ok && two) ? __ldg(c1 + t) : 0.f;
+                        bv[j] = ok ? br[t] : 0.f;
+                    }
+#pragma unroll
+                    for (int j = 0; j < kPerLane; ++j) {
+                        const int t = tb + lane + 32 * j;
+                        if (t < T) {
+                            float x = fmaf(-a0s, v0[j], bv[j]);
+                            if (two) x = fmaf(-a1s, v1[j], x);
+                            br[t] = x;
+                        }
+                    }
+                }
+                npend = 0;
+            };
             for (int e0 = 0; e0 < L2; e0 += 32) {
                 const int e = e0 + lane;
                 unsigned m = __ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0);
@@ -249,51 +281,21 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                     const int ee = e0 + __ffs(m) - 1;
                     m &= m - 1;
                     any = true;
-                    const int ts = s_t[i0 + ee];
-                    const float a = s_amp[i0 + ee];
-                    const int l = 2 * nt - ee;               // = wp - w + nt
-                    const float* crow = ctcP + ((int64_t)ts * L2 + l) * T;
-                    // every load of the chunk is issued before the first store, so the
-                    // round trips overlap instead of queueing behind each store
-                    for (int t0 = 0; t0 < T; t0 += 32 * kPerLane) {
-                        float cv[kPerLane];
-#pragma unroll
-                        for (int j = 0; j < kPerLane; ++j) {
-                            const int t = t0 + lane + 32 * j;
-                            cv[j] = (t < T) ? __ldg(crow + t) : 0.f;
-                        }
-                        float bv[kPerLane];
-#pragma unroll
-                        for (int j = 0; j < kPerLane; ++j) {
-                            const int t = t0 + lane + 32 * j;
-                            bv[j] = (t < T) ? br[t] : 0.f;
-                        }
-#pragma unroll
-                        for (int j = 0; j < kPerLane; ++j) {
-                            const int t = t0 + lane + 32 * j;
-                            if (t < T) br[t] = fmaf(-a, cv[j], bv[j]);
-                        }
-                    }
-                    const int dw = nt - ee;                   // = wp - w
-                    if (dw >= -hw && dw <= hw) {
-                        const float* wrow = pre_wf + ((int64_t)ts * nt + (dw + hw)) * C;
-                        for (int c0 = 0; c0 < C; c0 += 32 * kPerLane) {
-                            float wv[kPerLane], xv[kPerLane];
-#pragma unroll
-                            for (int j = 0; j < kPerLane; ++j) {
-                                const int c = c0 + lane + 32 * j;
-                                wv[j] = (c < C) ? __ldg(wrow + c) : 0.f;
-                                xv[j] = (c < C) ? xrow[c] : 0.f;
-                            }
-#pragma unroll
-                            for (int j = 0; j < kPerLane; ++j) {
-                                const int c = c0 + lane + 32 * j;
-                                if (c < C) xrow[c] = fmaf(-a, wv[j], xv[j]);
-                            }
-                        }
+                    if (npend == 0) {
+                        t0s = s_t[i0 + ee];
+                        a0s = s_amp[i0 + ee];
+                        l0s = 2 * nt - ee;                    // = wp - w + nt
+                        npend = 1;
+                    } else {
+                        t1s = s_t[i0 + ee];
+                        a1s = s_amp[i0 + ee];
+                        l1s = 2 * nt - ee;
+                        npend = 2;
+                        flush();
                     }
                 }
             }
+            if (npend) flush();
             if (lane == 0) dirty[wp] = any ? 1 : 0;
         }
         n_total += total;
@@ -303,6 +305,89 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
         out.n_spikes[b] = n_total;
         out.n_iters[b] = iters;
         if (n_total > out.cap) atomicOr(out.status + b, 1);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// residual: Xres[w][:] -= amp * waveform[t][w - w_s + nt/2][:] for every accepted spike with
+// |w - w_s| <= nt/2, applied in list order = (iteration, sample) -- the order the reference's
+// loop subtracts in.  A CTA owns kResRows rows; it first copies the spikes that can touch them
+// (in list order) into shared memory, then each warp applies them to its rows.
+// ---------------------------------------------------------------------------------------------
+constexpr int kResRows = 64;
+constexpr int kResList = 1024;
+
+__global__ void __launch_bounds__(256)
+residual_kernel(float* __restrict__ Xres, const float* __restrict__ pre_wf, MatchOut out, int W, int C, int nt) {
+    __shared__ int s_w[kResList], s_t[kResList];
+    __shared__ float s_a[kResList];
+    __shared__ int s_n, s_over;
+    const int b = blockIdx.y;
+    const int r0 = blockIdx.x * kResRows, r1 = min(W, r0 + kResRows);
+    const int hw = nt / 2;
+    const int n = min(out.n_spikes[b], out.cap);
+    const int* sw = out.sp_w + (int64_t)b * out.cap;
+    const int* st = out.sp_t + (int64_t)b * out.cap;
+    const float* sa = out.sp_amp + (int64_t)b * out.cap;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) { s_n = 0; s_over = 0; }
+    __syncthreads();
+    // order-preserving compaction of the spikes with r0 - hw <= w_s < r1 + hw
+    for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const bool hit = i < n && sw[i] >= r0 - hw && sw[i] < r1 + hw;
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        __shared__ int s_wc[8];
+        if (lane == 0) s_wc[warp] = __popc(m);
+        __syncthreads();
+        int before = s_n;
+        for (int k = 0; k < warp; ++k) before += s_wc[k];
+        if (hit) {
+            const int pos = before + __popc(m & ((1u << lane) - 1u));
+            if (pos < kResList) {
+                s_w[pos] = sw[i];
+                s_t[pos] = st[i];
+                s_a[pos] = sa[i];
+            } else {
+                s_over = 1;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int k = 0; k < 8; ++k) tot += s_wc[k];
+            s_n += tot;
+        }
+        __syncthreads();
+    }
+    const bool over = s_over != 0;
+    const int ns = min(s_n, kResList);
+    float* X = Xres + (int64_t)b * W * C;
+    for (int w = r0 + warp; w < r1; w += 8) {
+        float* xrow = X + (int64_t)w * C;
+        const int cnt = over ? n : ns;
+        for (int k = 0; k < cnt; ++k) {
+            const int ws = over ? sw[k] : s_w[k];
+            const int dw = w - ws;
+            if (dw < -hw || dw > hw) continue;
+            const int ts = over ? st[k] : s_t[k];
+            const float a = over ? sa[k] : s_a[k];
+            const float* wrow = pre_wf + ((int64_t)ts * nt + (dw + hw)) * C;
+            for (int c0 = 0; c0 < C; c0 += 32 * kPerLane) {
+                float wv[kPerLane], xv[kPerLane];
+#pragma unroll
+                for (int j = 0; j < kPerLane; ++j) {
+                    const int c = c0 + lane + 32 * j;
+                    wv[j] = (c < C) ? __ldg(wrow + c) : 0.f;
+                    xv[j] = (c < C) ? xrow[c] : 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < kPerLane; ++j) {
+                    const int c = c0 + lane + 32 * j;
+                    if (c < C) xrow[c] = fmaf(-a, wv[j], xv[j]);
+                }
+            }
+        }
     }
 }
 
@@ -383,9 +468,14 @@ cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float*
     bool smem = false;
     if (variant == 2) smem = match_variant(W, T, nt) == 16;
     else if (variant == 0) smem = nb <= 8 && match_variant(W, T, nt) == 16;
-    if (smem)
-        return launch_match_cfg<16, true>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc, out, s);
-    return launch_match_cfg<8, false>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc, out, s);
+    cudaError_t e = smem ? launch_match_cfg<16, true>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc,
+                                                      out, s)
+                         : launch_match_cfg<8, false>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc,
+                                                      out, s);
+    if (e != cudaSuccess) return e;
+    dim3 grid((W + kResRows - 1) / kResRows, nb);
+    residual_kernel<<<grid, 256, 0, s>>>(Xres, pre_wf, out, W, C, nt);
+    return cudaGetLastError();
 }
 
 }  // namespace lss

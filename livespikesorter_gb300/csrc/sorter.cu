@@ -392,7 +392,7 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
     LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st,
                           p.match_variant));
-    ++nl;
+    nl += 2;   // the loop and the residual
     mark();
     launch_rec_offsets(mo, nb, s.d_off, st), ++nl;
     launch_features(d_Z, mo, nb, Wn, C, T, K, nt, nC, d_wPCA, d_iCC, d_iU, d_Ucc, d_xc, d_yc, d_cent, Tf, s.d_off,
