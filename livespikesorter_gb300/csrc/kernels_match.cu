@@ -2,8 +2,9 @@
 // persistent kernel per batch: a thread-block cluster of G CTAs owns one window, each CTA a
 // contiguous slice of its time samples.  Per iteration:
 //
-//   A  per-sample max / argmax over templates of Cf = relu(B)^2 / nm (first and last nt
-//      samples zeroed), only for samples whose scores changed in the previous iteration;
+//   A  per-sample max / argmax over templates of Cf = relu(B)^2 * (1/nm) (first and last nt
+//      samples zeroed) -- computed for every sample before the loop, and afterwards only for
+//      the samples phase C changed, by the warp that changed them, from the values it holds;
 //   B1 (2nt+1) max pool of that per-sample max; accept a sample when the pooled value
 //      exceeds Th^2 and equals the sample's own max; amplitude B[w][iY] / nm[iY];
 //   B2 write the accepted spikes, ordered by (iteration, sample) like the reference;
@@ -48,11 +49,11 @@ constexpr int kWarps = kMatchThreads / 32;
 constexpr int kMaxRounds = 64;   // slice <= 64 * 512 samples per CTA
 constexpr int kPerLane = 8;      // row elements each lane loads before it stores (256 per warp)
 
-// dynamic shared memory of one CTA: [score slice if SMEM_B][s_cf][s_t][s_amp], floats/ints
+// dynamic shared memory of one CTA: [score slice if SMEM_B][s_cf][s_t][s_amp][1/nm], floats/ints
 __host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, bool smem_b) {
     const int span = (W + G - 1) / G;
     const size_t halo = (size_t)span + 2 * nt;
-    return (smem_b ? (size_t)span * T * 4 : 0) + halo * 12;
+    return (smem_b ? (size_t)span * T * 4 : 0) + halo * 12 + (size_t)T * 4;
 }
 
 template <int G, bool SMEM_B>
@@ -70,6 +71,7 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     float* s_cf = smem + (SMEM_B ? (size_t)span * T : 0);            // [halo]
     int* s_t = reinterpret_cast<int*>(s_cf + halo);                    // [halo]
     float* s_amp = reinterpret_cast<float*>(s_t + halo);               // [halo]
+    float* s_inm = s_amp + halo;                                       // [T] 1 / nm
     __shared__ int s_cnt[G];
     __shared__ int s_woff[kMaxRounds * kWarps];
     __shared__ int s_total;
@@ -84,7 +86,6 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     int* imax = sc.imax + (int64_t)b * W;
     int* at_t = sc.at_t + (int64_t)b * W;
     float* at_amp = sc.at_amp + (int64_t)b * W;
-    unsigned char* dirty = sc.dirty + (int64_t)b * W;
     int* cta_cnt = sc.cta_cnt + (int64_t)b * 2 * G;
     int* sp_w = out.sp_w + (int64_t)b * out.cap;
     int* sp_t = out.sp_t + (int64_t)b * out.cap;
@@ -105,61 +106,40 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             for (int64_t i = tid; i < n; i += kMatchThreads) Bs[i] = __ldcs(src + i);
         }
     }
-    for (int w = lo + tid; w < hi; w += kMatchThreads) dirty[w] = 1;
+    for (int t = tid; t < T; t += kMatchThreads) s_inm[t] = 1.f / nm[t];
     __syncthreads();
+
+    // warp-wide max / argmax of relu(x)^2 / nm (first index on ties) into cfmax / imax of w
+    auto finish_sample = [&](int w, float best, int bi) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (lane == 0) {
+            const bool inner = w >= nt && w < W - nt;
+            cfmax[w] = inner ? best : 0.f;
+            imax[w] = inner ? bi : 0;
+        }
+    };
+
+    // ---- A (once): per-sample max / argmax over templates of the whole slice ----
+    for (int w = lo + warp; w < hi; w += kWarps) {
+        const float* row = brow(w);
+        float best = -1.f;
+        int bi = 0x7fffffff;
+        for (int t = lane; t < T; t += 32) {
+            const float r = fmaxf(row[t], 0.f);
+            const float v = r * r * s_inm[t];
+            if (v > best) { best = v; bi = t; }
+        }
+        finish_sample(w, best, bi);
+    }
+    group_barrier<G>();
 
     int n_total = 0, iters = 0;
     for (int it = 0; it < max_iters && rounds <= kMaxRounds; ++it) {
-        // ---- A: per-sample max / argmax over templates (changed samples only) ----
-        for (int w0 = lo + warp; w0 < hi; w0 += 2 * kWarps) {
-            // two samples per pass: their loads are in flight together
-            float best[2] = {0.f, 0.f};
-            int bi[2] = {0, 0};
-            bool live[2];
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                const int w = w0 + q * kWarps;
-                live[q] = (w < hi) && dirty[w];
-                if (live[q] && w >= nt && w < W - nt) {
-                    best[q] = -1.f;
-                    bi[q] = 0x7fffffff;
-                }
-            }
-            const bool in0 = live[0] && w0 >= nt && w0 < W - nt;
-            const bool in1 = live[1] && (w0 + kWarps) >= nt && (w0 + kWarps) < W - nt;
-            if (in0 || in1) {
-                const float* r0 = brow(in0 ? w0 : lo);
-                const float* r1 = brow(in1 ? w0 + kWarps : lo);
-                for (int t = lane; t < T; t += 32) {
-                    const float n = __ldg(nm + t);
-                    const float x0 = in0 ? r0[t] : 0.f;
-                    const float x1 = in1 ? r1[t] : 0.f;
-                    const float a0 = fmaxf(x0, 0.f), a1 = fmaxf(x1, 0.f);
-                    const float v0 = a0 * a0 / n, v1 = a1 * a1 / n;
-                    if (in0 && v0 > best[0]) { best[0] = v0; bi[0] = t; }
-                    if (in1 && v1 > best[1]) { best[1] = v1; bi[1] = t; }
-                }
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        const float ob = __shfl_xor_sync(0xffffffffu, best[q], o);
-                        const int oi = __shfl_xor_sync(0xffffffffu, bi[q], o);
-                        if (ob > best[q] || (ob == best[q] && oi < bi[q])) { best[q] = ob; bi[q] = oi; }
-                    }
-                }
-            }
-            if (lane == 0) {
-#pragma unroll
-                for (int q = 0; q < 2; ++q)
-                    if (live[q]) {
-                        cfmax[w0 + q * kWarps] = best[q];
-                        imax[w0 + q * kWarps] = bi[q];
-                    }
-            }
-        }
-        group_barrier<G>();
-
         // ---- B1: pooled max and acceptance on the own slice; per-warp counts per round ----
         for (int i = tid; i < halo; i += kMatchThreads) {
             const int w = lo - nt + i;
@@ -241,14 +221,22 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
         __syncthreads();
         for (int wp = lo + warp; wp < hi; wp += kWarps) {
             const int i0 = wp - lo;   // s_t[i0 + e] is the sample wp - nt + e
-            bool any = false;
+            int n_sp = 0;
+            for (int e0 = 0; e0 < L2; e0 += 32) {
+                const int e = e0 + lane;
+                n_sp += __popc(__ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0));
+            }
+            if (n_sp == 0) continue;   // scores unchanged: cfmax / imax stay valid
             float* br = brow(wp);
             // spikes within +-nt of wp, in increasing sample order, two at a time: both rows of
-            // ctc are loaded before either is applied, and they are applied in order
+            // ctc are loaded before either is applied, and they are applied in order; the pass
+            // that applies the last spike also takes the new max / argmax of the sample
             int t0s = 0, l0s = 0, t1s = 0, l1s = 0;
             float a0s = 0.f, a1s = 0.f;
-            int npend = 0;
-            auto flush = [&]() {
+            int npend = 0, done = 0;
+            float best = -1.f;
+            int bi = 0x7fffffff;
+            auto flush = [&](bool last) {
                 const float* c0 = ctcP + ((int64_t)t0s * L2 + l0s) * T;
                 const float* c1 = ctcP + ((int64_t)t1s * L2 + l1s) * T;
                 const bool two = npend == 2;
@@ -269,6 +257,11 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                             float x = fmaf(-a0s, v0[j], bv[j]);
                             if (two) x = fmaf(-a1s, v1[j], x);
                             br[t] = x;
+                            if (last) {
+                                const float r = fmaxf(x, 0.f);
+                                const float v = r * r * s_inm[t];
+                                if (v > best) { best = v; bi = t; }
+                            }
                         }
                     }
                 }
@@ -280,7 +273,7 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                 while (m) {
                     const int ee = e0 + __ffs(m) - 1;
                     m &= m - 1;
-                    any = true;
+                    ++done;
                     if (npend == 0) {
                         t0s = s_t[i0 + ee];
                         a0s = s_amp[i0 + ee];
@@ -291,15 +284,14 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                         a1s = s_amp[i0 + ee];
                         l1s = 2 * nt - ee;
                         npend = 2;
-                        flush();
                     }
+                    if (npend == 2 || done == n_sp) flush(done == n_sp);
                 }
             }
-            if (npend) flush();
-            if (lane == 0) dirty[wp] = any ? 1 : 0;
+            finish_sample(wp, best, bi);
         }
         n_total += total;
-        __syncthreads();
+        group_barrier<G>();   // cfmax of the changed samples is read by the neighbours in B1
     }
     if (rank == 0 && tid == 0) {
         out.n_spikes[b] = n_total;
