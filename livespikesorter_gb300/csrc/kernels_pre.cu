@@ -115,7 +115,16 @@ void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int
 }
 
 // ---------------------------------------------------------------------------------------
+// tf32 split of an fp32 value: hi = tf32(x) (round to nearest, ties away), lo = x - hi
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    hi = __uint_as_float(h);
+    lo = x - hi;
+}
+
 // circular high-pass: Y[w][c] = sum_j taps[j] * Xw[w + j][c]   (taps zero-padded to kHpChunk)
+// With Ylo != nullptr the output is written as its tf32 split (Y = hi, Ylo = lo).
 // CTA = 32 channels x 128 rows; a thread owns one channel and 32 consecutive rows; each
 // chunk of 32 taps is applied from a shared-memory tile of 159 rows.
 // ---------------------------------------------------------------------------------------
@@ -126,7 +135,7 @@ constexpr int kHpTile = kHpRows + kHpChunk - 1;
 
 __global__ void __launch_bounds__(128)
 highpass_kernel(const float* __restrict__ Xw, int C, int W, int rows_in, const float* __restrict__ taps, int ntaps,
-                float* __restrict__ Y) {
+                float* __restrict__ Y, float* __restrict__ Ylo) {
     __shared__ float xs[kHpTile][32];
     __shared__ float ts[kHpChunk];
     const int b = blockIdx.z;
@@ -161,18 +170,28 @@ highpass_kernel(const float* __restrict__ Xw, int C, int W, int rows_in, const f
     const int ch = c0 + tc;
     if (ch >= C) return;
     float* yb = Y + (int64_t)b * W * C;
+    float* lb = Ylo ? Ylo + (int64_t)b * W * C : nullptr;
 #pragma unroll
     for (int r = 0; r < kHpRowsPerThread; ++r) {
         const int w = w0 + rg * kHpRowsPerThread + r;
-        if (w < W) yb[(int64_t)w * C + ch] = acc[r];
+        if (w < W) {
+            if (lb) {
+                float h, l;
+                tf32_split(acc[r], h, l);
+                yb[(int64_t)w * C + ch] = h;
+                lb[(int64_t)w * C + ch] = l;
+            } else {
+                yb[(int64_t)w * C + ch] = acc[r];
+            }
+        }
     }
 }
 
 void launch_highpass(const float* Xw, int C, int W, int L, int R, const float* taps, int nb, float* Y,
-                     cudaStream_t s) {
+                     cudaStream_t s, float* Ylo) {
     const int ntaps = L + R + 1;
     dim3 grid((W + kHpRows - 1) / kHpRows, (C + 31) / 32, nb);
-    highpass_kernel<<<grid, 128, 0, s>>>(Xw, C, W, W + L + R, taps, ntaps, Y);
+    highpass_kernel<<<grid, 128, 0, s>>>(Xw, C, W, W + L + R, taps, ntaps, Y, Ylo);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -190,7 +209,8 @@ struct BasisParam {
 // multiply-add takes it as an immediate constant operand.
 template <int NT_, int K_>
 __global__ void __launch_bounds__(128)
-basis_conv_fixed(const float* __restrict__ Z, int C, int W, BasisParam<NT_, K_> bp, float* __restrict__ Bpc) {
+basis_conv_fixed(const float* __restrict__ Z, int C, int W, BasisParam<NT_, K_> bp, float* __restrict__ Bpc,
+                 float* __restrict__ Blo) {
     const int b = blockIdx.z;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int w0 = blockIdx.y * kConvRows;
@@ -216,12 +236,23 @@ basis_conv_fixed(const float* __restrict__ Z, int C, int W, BasisParam<NT_, K_> 
         }
     }
     float* ob = Bpc + (int64_t)b * W * K_ * C;
+    float* lb = Blo ? Blo + (int64_t)b * W * K_ * C : nullptr;
 #pragma unroll
     for (int r = 0; r < kConvRows; ++r) {
         const int w = w0 + r;
         if (w < W) {
 #pragma unroll
-            for (int k = 0; k < K_; ++k) ob[((int64_t)w * K_ + k) * C + c] = acc[r][k];
+            for (int k = 0; k < K_; ++k) {
+                const int64_t o = ((int64_t)w * K_ + k) * C + c;
+                if (lb) {
+                    float h, l;
+                    tf32_split(acc[r][k], h, l);
+                    ob[o] = h;
+                    lb[o] = l;
+                } else {
+                    ob[o] = acc[r][k];
+                }
+            }
         }
     }
 }
@@ -229,7 +260,7 @@ basis_conv_fixed(const float* __restrict__ Z, int C, int W, BasisParam<NT_, K_> 
 // Any (nt, K <= 8): basis read from global memory (cached).
 __global__ void __launch_bounds__(128)
 basis_conv_generic(const float* __restrict__ Z, int C, int W, const float* __restrict__ wPCA, int K, int nt,
-                   float* __restrict__ Bpc) {
+                   float* __restrict__ Bpc, float* __restrict__ Blo) {
     const int b = blockIdx.z;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int w0 = blockIdx.y * kConvRows;
@@ -255,30 +286,37 @@ basis_conv_generic(const float* __restrict__ Z, int C, int W, const float* __res
         }
     }
     float* ob = Bpc + (int64_t)b * W * K * C;
+    float* lb = Blo ? Blo + (int64_t)b * W * K * C : nullptr;
 #pragma unroll
     for (int r = 0; r < kConvRows; ++r) {
         const int w = w0 + r;
         if (w < W)
-            for (int k = 0; k < K; ++k) ob[((int64_t)w * K + k) * C + c] = acc[r][k];
+            for (int k = 0; k < K; ++k) {
+                const int64_t o = ((int64_t)w * K + k) * C + c;
+                if (lb) {
+                    float h, l;
+                    tf32_split(acc[r][k], h, l);
+                    ob[o] = h;
+                    lb[o] = l;
+                } else {
+                    ob[o] = acc[r][k];
+                }
+            }
     }
 }
 
-void launch_basis_conv(const float* Z, int C, int W, const float* wPCA_dev, int K, int nt, int nb, float* Bpc,
-                       cudaStream_t s) {
-    dim3 grid((C + 127) / 128, (W + kConvRows - 1) / kConvRows, nb);
-    basis_conv_generic<<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, K, nt, Bpc);
-}
+
 
 // Host-side basis (needed for the parameter-bank specialisation).
 void launch_basis_conv_host(const float* Z, int C, int W, const float* wPCA_dev, const float* wPCA_host, int K,
-                            int nt, int nb, float* Bpc, cudaStream_t s) {
+                            int nt, int nb, float* Bpc, cudaStream_t s, float* Blo) {
     dim3 grid((C + 127) / 128, (W + kConvRows - 1) / kConvRows, nb);
     if (nt == 61 && K == 6 && wPCA_host) {
         BasisParam<61, 6> bp;
         for (int i = 0; i < 6 * 61; ++i) bp.w[i] = wPCA_host[i];
-        basis_conv_fixed<61, 6><<<grid, 128, 0, s>>>(Z, C, W, bp, Bpc);
+        basis_conv_fixed<61, 6><<<grid, 128, 0, s>>>(Z, C, W, bp, Bpc, Blo);
     } else {
-        basis_conv_generic<<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, K, nt, Bpc);
+        basis_conv_generic<<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, K, nt, Bpc, Blo);
     }
 }
 

@@ -53,15 +53,23 @@ void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, 
                    int nb, long long* colsum, cudaStream_t s);
 void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
                 const long long* colsum, int L, int R, float* Xw, cudaStream_t s);
+// Ylo != nullptr: Y receives tf32(y) and Ylo the remainder (operands of the tensor-core GEMM)
 void launch_highpass(const float* Xw, int C, int W, int L, int R, const float* taps, int nb, float* Y,
-                     cudaStream_t s);
+                     cudaStream_t s, float* Ylo = nullptr);
 void launch_sgemm_nt(const float* A, int64_t lda, int64_t strideA, const float* B, int64_t ldb,
                      float* Cm, int64_t ldc, int64_t strideC, int M, int N, int K, int nb, cudaStream_t s);
-void launch_basis_conv(const float* Z, int C, int W, const float* wPCA, int K, int nt, int nb, float* Bpc,
-                       cudaStream_t s);
-// wPCA_host (K*nt floats) enables the specialisation with the basis in the parameter bank.
+// wPCA_host (K*nt floats) enables the specialisation with the basis in the parameter bank;
+// Blo != nullptr writes the tf32 split like launch_highpass.
 void launch_basis_conv_host(const float* Z, int C, int W, const float* wPCA_dev, const float* wPCA_host, int K,
-                            int nt, int nb, float* Bpc, cudaStream_t s);
+                            int nt, int nb, float* Bpc, cudaStream_t s, float* Blo = nullptr);
+
+// tensor-core (tcgen05) FP32-accurate GEMM C[m][n] = sum_k A[m][k] B[n][k] from tf32-split operands
+struct UmmaOperands;
+UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, const float* b_hi, const float* b_lo,
+                        int64_t rows_b, int K);
+void umma_free(UmmaOperands* u);
+cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, int* err, cudaStream_t s);
+void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                          float th2, int W, int T, int C, int nt, int max_iters, int nb,
                          const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0);

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <new>
@@ -97,6 +98,13 @@ struct Handle {
     // static device state
     float *d_WD = nullptr, *d_Wall3 = nullptr, *d_ctcP = nullptr, *d_pre_wf = nullptr, *d_nm = nullptr;
     float *d_wPCA = nullptr, *d_Ucc = nullptr, *d_xc = nullptr, *d_yc = nullptr, *d_cent = nullptr;
+    // tf32 splits of the GEMM's fixed operands (tensor-core path)
+    float *d_WD_hi = nullptr, *d_WD_lo = nullptr, *d_Wall3_hi = nullptr, *d_Wall3_lo = nullptr;
+    bool tc_whiten = false, tc_project = false;   // GEMMs on the tensor cores
+    UmmaOperands* um_whiten = nullptr;
+    UmmaOperands* um_project = nullptr;
+    int* h_gemm_err = nullptr;                    // mapped: device-side wait timeouts
+    int* d_gemm_err = nullptr;
     int64_t *d_iCC = nullptr, *d_iU = nullptr;
     int32_t* d_chan = nullptr;
     std::map<int, TapSet> taps;
@@ -107,6 +115,7 @@ struct Handle {
     int16_t* d_raw = nullptr;
     long long* d_colsum = nullptr;
     float *d_Xw = nullptr, *d_Y = nullptr, *d_Z = nullptr, *d_Bpc = nullptr, *d_Bt = nullptr;
+    float *d_Y_lo = nullptr, *d_Bpc_lo = nullptr;   // tf32 remainders (tensor-core path)
     MatchScratch sc{};
     MatchOut mo{};
     int64_t work_bytes = 0;
@@ -136,6 +145,8 @@ struct Handle {
     void push(const int16_t* x, int64_t n, int64_t ct);
     void flush();
     void launch_windows_from_buf(int g, int pad_mode);
+    void run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
+                              const std::function<void()>& mark);
 };
 
 Handle::~Handle() {
@@ -145,8 +156,9 @@ Handle::~Handle() {
     for (auto& kv : taps) cudaFree(kv.second.d);
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
-                    (void*)d_chan})
+                    (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo})
         if (p) cudaFree(p);
+    if (h_gemm_err) cudaFreeHost(h_gemm_err);
     for (auto& s : slots) {
         if (s.h_stage) cudaFreeHost(s.h_stage);
         if (s.h_recs) cudaFreeHost(s.h_recs);
@@ -161,7 +173,11 @@ Handle::~Handle() {
 }
 
 void Handle::free_work() {
+    umma_free(um_whiten);
+    umma_free(um_project);
+    um_whiten = um_project = nullptr;
     for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
+                    (void*)d_Y_lo, (void*)d_Bpc_lo,
                     (void*)sc.cfmax, (void*)sc.imax, (void*)sc.at_t, (void*)sc.at_amp, (void*)sc.dirty,
                     (void*)sc.cta_cnt, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
                     (void*)mo.sp_t, (void*)mo.sp_amp, (void*)mo.sp_iter})
@@ -169,6 +185,7 @@ void Handle::free_work() {
     d_raw = nullptr;
     d_colsum = nullptr;
     d_Xw = d_Y = d_Z = d_Bpc = d_Bt = nullptr;
+    d_Y_lo = d_Bpc_lo = nullptr;
     sc = MatchScratch{};
     mo = MatchOut{};
     dev_bytes -= work_bytes;
@@ -254,6 +271,27 @@ void Handle::init(const char* dir, const lss_params* prm) {
     d_iCC = dev_upload(m.iCC, dev_bytes, st);
     d_iU = dev_upload(m.iU, dev_bytes, st);
     d_chan = (Cin > C) ? dev_upload(chan, dev_bytes, st) : nullptr;
+    // tensor-core GEMMs need K % 16 == 0 and N <= 512 (C for the whitening, T for the projection)
+    const bool want_tc = p.gemm_path == 0;
+    tc_whiten = want_tc && C % 16 == 0 && C <= 512;
+    tc_project = want_tc && (K * C) % 16 == 0 && T <= 512;
+    if (tc_whiten || tc_project) {
+        if (tc_whiten) {
+            d_WD_hi = dev_alloc<float>((size_t)C * C, dev_bytes);
+            d_WD_lo = dev_alloc<float>((size_t)C * C, dev_bytes);
+            launch_split_tf32(d_WD, d_WD_hi, d_WD_lo, (int64_t)C * C, st);
+        }
+        if (tc_project) {
+            d_Wall3_hi = dev_alloc<float>((size_t)T * K * C, dev_bytes);
+            d_Wall3_lo = dev_alloc<float>((size_t)T * K * C, dev_bytes);
+            launch_split_tf32(d_Wall3, d_Wall3_hi, d_Wall3_lo, (int64_t)T * K * C, st);
+        }
+        LSS_CUDA(cudaGetLastError());
+        LSS_CUDA(cudaStreamSynchronize(st));
+    }
+    LSS_CUDA(cudaHostAlloc((void**)&h_gemm_err, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable));
+    *h_gemm_err = 0;
+    LSS_CUDA(cudaHostGetDevicePointer((void**)&d_gemm_err, h_gemm_err, 0));
     LSS_CUDA(cudaStreamSynchronize(st));
     m.ctc.clear();
     m.ctc.shrink_to_fit();
@@ -294,8 +332,8 @@ void Handle::ensure_work(int Wn, int nb) {
     raw_rows_cap = (size_t)nba * (size_t)std::max(Wa, NT) + 2 * (size_t)nt;
     const int64_t need = (int64_t)raw_rows_cap * Cin * 2 + (int64_t)nba * C * 8 +
                          (int64_t)nba * (Wa + LRmax) * C * 4 + 2LL * nba * Wa * C * 4 +
-                         (int64_t)nba * Wa * K * C * 4 + (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 +
-                         (int64_t)nba * cap * 16;
+                         (int64_t)nba * Wa * K * C * 4 * (tc_project ? 2 : 1) + (int64_t)nba * Wa * C * 4 * (tc_whiten ? 1 : 0) +
+                         (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16;
     if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
         throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
                                            " device bytes, budget " + std::to_string(p.mem_budget)};
@@ -306,6 +344,8 @@ void Handle::ensure_work(int Wn, int nb) {
     d_Z = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     d_Bpc = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
     d_Bt = dev_alloc<float>((size_t)nba * Wa * T, dev_bytes);
+    if (tc_whiten) d_Y_lo = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
+    if (tc_project) d_Bpc_lo = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
     sc.cfmax = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
     sc.imax = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
     sc.at_t = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
@@ -320,6 +360,14 @@ void Handle::ensure_work(int Wn, int nb) {
     mo.sp_amp = dev_alloc<float>((size_t)nba * cap, dev_bytes);
     mo.sp_iter = dev_alloc<int>((size_t)nba * cap, dev_bytes);
     mo.cap = cap;
+    if (tc_whiten) {
+        um_whiten = umma_make(d_Y, d_Y_lo, (int64_t)nba * Wa, d_WD_hi, d_WD_lo, C, C);
+        if (!um_whiten) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (whitening GEMM)"};
+    }
+    if (tc_project) {
+        um_project = umma_make(d_Bpc, d_Bpc_lo, (int64_t)nba * Wa, d_Wall3_hi, d_Wall3_lo, T, K * C);
+        if (!um_project) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (projection GEMM)"};
+    }
     work_bytes = dev_bytes - before;
     Wcap = Wa;
     nbcap = nba;
@@ -358,6 +406,35 @@ int Handle::acquire_slot() {
     }
 }
 
+// Preprocessing, whitening, basis convolution and projection of nb windows (raw rows already on
+// the device) into d_Z (whitened windows) and d_Bt (scores).  mark() is called after each stage.
+void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
+                                  const std::function<void()>& mark) {
+    launch_colsum(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, st), ++nl;
+    mark();
+    launch_car(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, d_Xw, st), ++nl;
+    mark();
+    launch_highpass(d_Xw, C, Wn, ts.L, ts.R, ts.d, nb, d_Y, st, tc_whiten ? d_Y_lo : nullptr), ++nl;
+    mark();
+    if (tc_whiten)
+        LSS_CUDA(launch_umma_gemm(um_whiten, d_Z, nb * Wn, C, C, d_gemm_err, st));
+    else
+        launch_sgemm_nt(d_Y, C, (int64_t)Wn * C, d_WD, C, d_Z, C, (int64_t)Wn * C, Wn, C, C, nb, st);
+    ++nl;
+    mark();
+    launch_basis_conv_host(d_Z, C, Wn, d_wPCA, m.wPCA.data(), K, nt, nb, d_Bpc, st, tc_project ? d_Bpc_lo : nullptr),
+        ++nl;
+    mark();
+    if (tc_project)
+        LSS_CUDA(launch_umma_gemm(um_project, d_Bt, nb * Wn, T, T, d_gemm_err, st));
+    else
+        launch_sgemm_nt(d_Bpc, (int64_t)K * C, (int64_t)Wn * K * C, d_Wall3, (int64_t)K * C, d_Bt, T, (int64_t)Wn * T, Wn,
+                        T, K * C, nb, st);
+    ++nl;
+    LSS_CUDA(cudaGetLastError());
+    mark();
+}
+
 // Enqueue the kernels of one group: windows b = 0..nb-1 start at row b*NTs of the staging copy
 // (or of dev_src, rows already on the device).
 void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, int stage_rows, const int16_t* dev_src) {
@@ -375,20 +452,7 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     }
     mark();
     int64_t nl = 0;
-    launch_colsum(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, st), ++nl;
-    mark();
-    launch_car(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, d_Xw, st), ++nl;
-    mark();
-    launch_highpass(d_Xw, C, Wn, ts.L, ts.R, ts.d, nb, d_Y, st), ++nl;
-    mark();
-    launch_sgemm_nt(d_Y, C, (int64_t)Wn * C, d_WD, C, d_Z, C, (int64_t)Wn * C, Wn, C, C, nb, st), ++nl;
-    mark();
-    launch_basis_conv_host(d_Z, C, Wn, d_wPCA, m.wPCA.data(), K, nt, nb, d_Bpc, st), ++nl;
-    mark();
-    launch_sgemm_nt(d_Bpc, (int64_t)K * C, (int64_t)Wn * K * C, d_Wall3, (int64_t)K * C, d_Bt, T, (int64_t)Wn * T, Wn, T,
-                    K * C, nb, st), ++nl;
-    LSS_CUDA(cudaGetLastError());
-    mark();
+    run_stages_to_scores(raw, nb, Wn, NTs, ts, nl, mark);
     LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
     LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st,
                           p.match_variant));
@@ -440,6 +504,12 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
     Slot& s = slots[si];
     LSS_CUDA(cudaEventSynchronize(s.ev));
     if (!inflight.empty() && inflight.front() == si) inflight.pop_front();
+    if (h_gemm_err && *h_gemm_err) {
+        const int code = *h_gemm_err;
+        *h_gemm_err = 0;
+        s.busy = false;
+        throw CudaError{"tensor-core GEMM gave up waiting on its pipeline (code " + std::to_string(code) + ")"};
+    }
     if (p.profile && s.tev[0]) {
         for (int i = 0; i < LSS_N_STAGES; ++i) {
             float ms = 0.f;
@@ -629,6 +699,7 @@ int lss_default_params(lss_params* p) {
     p->mem_budget = 0;
     p->profile = 0;
     p->match_variant = 0;
+    p->gemm_path = 0;
     return LSS_OK;
 }
 
@@ -805,16 +876,11 @@ int lss_debug_stage(lss_handle* hp, const int16_t* window, int32_t W, int32_t st
         lss::TapSet& ts = h.taps_for(W);
         cudaStream_t st = h.st;
         LSS_CUDA(cudaMemcpyAsync(h.d_raw, s.h_stage, (size_t)W * h.Cin * 2, cudaMemcpyHostToDevice, st));
-        lss::launch_colsum(h.d_raw, h.Cin, h.d_chan, h.C, W, W, 1, h.d_colsum, st);
-        lss::launch_car(h.d_raw, h.Cin, h.d_chan, h.C, W, W, 1, h.d_colsum, ts.L, ts.R, h.d_Xw, st);
-        lss::launch_highpass(h.d_Xw, h.C, W, ts.L, ts.R, ts.d, 1, h.d_Y, st);
-        lss::launch_sgemm_nt(h.d_Y, h.C, (int64_t)W * h.C, h.d_WD, h.C, h.d_Z, h.C, (int64_t)W * h.C, W, h.C, h.C, 1, st);
+        int64_t nl = 0;
+        h.run_stages_to_scores(h.d_raw, 1, W, W, ts, nl, [] {});
         if (stage == LSS_STAGE_PREPROCESSED) {
             LSS_CUDA(cudaMemcpyAsync(out, h.d_Z, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
         } else {
-            lss::launch_basis_conv_host(h.d_Z, h.C, W, h.d_wPCA, h.m.wPCA.data(), h.K, h.nt, 1, h.d_Bpc, st);
-            lss::launch_sgemm_nt(h.d_Bpc, (int64_t)h.K * h.C, (int64_t)W * h.K * h.C, h.d_Wall3, (int64_t)h.K * h.C,
-                                 h.d_Bt, h.T, (int64_t)W * h.T, W, h.T, h.K * h.C, 1, st);
             if (stage == LSS_STAGE_SCORES) {
                 LSS_CUDA(cudaMemcpyAsync(out, h.d_Bt, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
             } else {
@@ -826,6 +892,10 @@ int lss_debug_stage(lss_handle* hp, const int16_t* window, int32_t W, int32_t st
         }
         LSS_CUDA(cudaGetLastError());
         LSS_CUDA(cudaStreamSynchronize(st));
+        if (*h.h_gemm_err) {
+            *h.h_gemm_err = 0;
+            throw lss::CudaError{"tensor-core GEMM gave up waiting on its pipeline"};
+        }
     })
 }
 

@@ -254,3 +254,30 @@ def test_cpp_dropin_replay(golden_dir, tmp_path):
     np.testing.assert_array_equal(rows[:, 0].astype(np.int64), st[:, 0].astype(np.int64))
     np.testing.assert_array_equal(rows[:, 1].astype(np.int64), z["clu"][keep][order])
     np.testing.assert_allclose(rows[:, 2], st[:, 2], rtol=1e-4)
+
+
+def test_tensor_core_and_simt_gemms_agree(win_oss, win):
+    """gemm_path 0 (tcgen05, 3xTF32) and 1 (FP32 SIMT) give the same scores to FP32 accuracy and
+    the same spikes."""
+    outs = {}
+    for path in (0, 1):
+        with sorter.OnlineSorter(win_oss, max_iters=int(win["max_iters"]), gemm_path=path) as s:
+            outs[path] = (s.debug_stage(win["window"], sorter.STAGE_PREPROCESSED),
+                          s.debug_stage(win["window"], sorter.STAGE_SCORES), s.sort_windows(win["window"])[0])
+    _rel_close(outs[0][0].astype(np.float64), outs[1][0].astype(np.float64), 2e-6)
+    _rel_close(outs[0][1].astype(np.float64), outs[1][1].astype(np.float64), 1e-5)
+    a, amp_ok, amax = agreement(outs[1][2]["time"], outs[1][2]["tmpl"], outs[1][2]["amp"],
+                                outs[0][2]["time"], outs[0][2]["tmpl"], outs[0][2]["amp"])
+    assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
+
+
+def test_tensor_core_gemm_384ch(cfg_stream):
+    """The 384-channel / 500-template shapes (two N tiles, ragged last M tile) through both paths."""
+    d, data, _ = cfg_stream
+    win = data[1500 - 61: 3000 + 61]
+    outs = {}
+    for path in (0, 1):
+        with sorter.OnlineSorter(d, gemm_path=path) as s:
+            outs[path] = (s.debug_stage(win, sorter.STAGE_PREPROCESSED), s.debug_stage(win, sorter.STAGE_SCORES))
+    _rel_close(outs[0][0].astype(np.float64), outs[1][0].astype(np.float64), 2e-6)
+    _rel_close(outs[0][1].astype(np.float64), outs[1][1].astype(np.float64), 1e-5)
