@@ -48,11 +48,13 @@ __device__ __forceinline__ float key2f(uint32_t k) {
 }
 
 constexpr int kCarWarps = 8;
-constexpr int kMaxChanPerLane = 32;   // C <= 1024
 
+// NJ = channels per lane (C <= 32 * NJ), so the selection loop runs over live registers only
+template <int NJ>
 __global__ void __launch_bounds__(kCarWarps * 32)
 car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C, int W,
            int NT, const long long* __restrict__ colsum, int L, int R, float* __restrict__ Xw) {
+    constexpr int kMaxChanPerLane = NJ;
     const int b = blockIdx.y;
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * kCarWarps + (threadIdx.x >> 5);
@@ -111,7 +113,15 @@ car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* _
 void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
                 const long long* colsum, int L, int R, float* Xw, cudaStream_t s) {
     dim3 grid((W + kCarWarps - 1) / kCarWarps, nb);
-    car_kernel<<<grid, kCarWarps * 32, 0, s>>>(raw, row_stride, chan, C, W, NT, colsum, L, R, Xw);
+    const int nj = (C + 31) / 32;
+#define LSS_CAR(N) car_kernel<N><<<grid, kCarWarps * 32, 0, s>>>(raw, row_stride, chan, C, W, NT, colsum, L, R, Xw)
+    if (nj <= 4) LSS_CAR(4);
+    else if (nj <= 8) LSS_CAR(8);
+    else if (nj <= 12) LSS_CAR(12);
+    else if (nj <= 16) LSS_CAR(16);
+    else if (nj <= 24) LSS_CAR(24);
+    else LSS_CAR(32);
+#undef LSS_CAR
 }
 
 // ---------------------------------------------------------------------------------------
