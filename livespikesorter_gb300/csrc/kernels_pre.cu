@@ -47,6 +47,14 @@ __device__ __forceinline__ float key2f(uint32_t k) {
     return __uint_as_float(u);
 }
 
+// tf32 split of an fp32 value: hi = tf32(x) (round to nearest, ties away), lo = x - hi
+__device__ __forceinline__ void tf32_split_(float x, float& hi, float& lo) {
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    hi = __uint_as_float(h);
+    lo = x - hi;
+}
+
 constexpr int kCarWarps = 8;
 
 // NJ = channels per lane (C <= 32 * NJ), so the selection loop runs over live registers only
@@ -108,6 +116,104 @@ car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* _
             if (wrapR) xb[(int64_t)(w + L + W) * C + c] = y;
         }
     }
+}
+
+// Channel-major variant for the tensor-core high-pass: a CTA takes 32 consecutive samples, each
+// warp four of them (the same median selection as car_kernel), stages the results in shared
+// memory and writes Xt[(b, c)][w + L] (+ the wrap copies) as coalesced runs of 32 samples per
+// channel, tf32-split into (Xt_hi, Xt_lo); columns past W + L + R up to the row pitch are zeroed.
+constexpr int kCarTRows = 32;
+
+template <int NJ>
+__global__ void __launch_bounds__(kCarWarps * 32)
+car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C, int W,
+             int NT, const long long* __restrict__ colsum, int L, int R, int pitch, float* __restrict__ Xt_hi,
+             float* __restrict__ Xt_lo) {
+    extern __shared__ float s_y[];   // [kCarTRows][C + 1]
+    const int b = blockIdx.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int w0 = blockIdx.x * kCarTRows;
+    const int ld = C + 1;
+    const double invW = 1.0 / (double)W;
+    for (int rr = warp; rr < kCarTRows; rr += kCarWarps) {
+        const int w = w0 + rr;
+        if (w >= W) break;
+        const int64_t rowp = ((int64_t)b * NT + w) * row_stride;
+        float v[NJ];
+        uint32_t key[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int c = lane + 32 * j;
+            if (c < C) {
+                const float mean = (float)((double)colsum[(int64_t)b * C + c] * invW);
+                const float x = (float)raw[rowp + (chan ? chan[c] : c)] - mean;
+                v[j] = x;
+                key[j] = f2key(x);
+            } else {
+                v[j] = 0.f;
+                key[j] = 0xffffffffu;
+            }
+        }
+        uint32_t prefix = 0;
+        int k = (C - 1) >> 1;
+        for (int bit = 31; bit >= 0; --bit) {
+            const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
+            int cnt = 0;
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) cnt += ((key[j] & hi_mask) == prefix) && !((key[j] >> bit) & 1u);
+            cnt = __reduce_add_sync(0xffffffffu, cnt);
+            if (k >= cnt) {
+                k -= cnt;
+                prefix |= (1u << bit);
+            }
+        }
+        const float med = key2f(prefix);
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int c = lane + 32 * j;
+            if (c < C) s_y[rr * ld + c] = v[j] - med;
+        }
+    }
+    __syncthreads();
+    const int nrows = min(kCarTRows, W - w0);
+    const int total = W + L + R;
+    for (int idx = threadIdx.x; idx < kCarTRows * C; idx += blockDim.x) {
+        const int c = idx / kCarTRows, rr = idx - c * kCarTRows;
+        const int64_t rbase = ((int64_t)b * C + c) * pitch;
+        if (rr < nrows) {
+            const int w = w0 + rr;
+            float h, l;
+            tf32_split_(s_y[rr * ld + c], h, l);
+            Xt_hi[rbase + w + L] = h;
+            Xt_lo[rbase + w + L] = l;
+            if (w >= W - L) { Xt_hi[rbase + w + L - W] = h; Xt_lo[rbase + w + L - W] = l; }
+            if (w < R) { Xt_hi[rbase + w + L + W] = h; Xt_lo[rbase + w + L + W] = l; }
+        }
+        if (blockIdx.x == 0 && rr < pitch - total) {   // row padding read by the last tiles' band
+            Xt_hi[rbase + total + rr] = 0.f;
+            Xt_lo[rbase + total + rr] = 0.f;
+        }
+    }
+}
+
+void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
+                  const long long* colsum, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s) {
+    dim3 grid((W + kCarTRows - 1) / kCarTRows, nb);
+    const int nj = (C + 31) / 32;
+    const size_t smem = (size_t)kCarTRows * (C + 1) * sizeof(float);
+#define LSS_CART(N)                                                                                        \
+    do {                                                                                                   \
+        cudaFuncSetAttribute(car_t_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+        car_t_kernel<N><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, L, R,  \
+                                                           pitch, Xt_hi, Xt_lo);                           \
+    } while (0)
+    if (nj <= 4) LSS_CART(4);
+    else if (nj <= 8) LSS_CART(8);
+    else if (nj <= 12) LSS_CART(12);
+    else if (nj <= 16) LSS_CART(16);
+    else if (nj <= 24) LSS_CART(24);
+    else LSS_CART(32);
+#undef LSS_CART
 }
 
 void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,

@@ -23,12 +23,26 @@
 
 namespace lss {
 
-constexpr int kBM = 128, kBN = 256, kBK = 16, kStages = 4;
+constexpr int kBM = 128, kBK = 16;
 constexpr int kTileA = kBM * kBK * 4;                   // 8 KB
-constexpr int kTileB = kBN * kBK * 4;                   // 16 KB
-constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;    // 48 KB
-constexpr int kUmmaSmem = kStages * kStageBytes + 1024;  // + alignment slack
+constexpr int kSmemBudget = 196 * 1024;                 // stage buffers per CTA
 constexpr uint64_t kWaitNs = 2000000000ull;             // 2 s
+
+// Two uses of one kernel:
+//   kPlain     C[m][n] = sum_k A[m][k] B[n][k]; tile N = 256; B rows = n
+//   kToeplitz  the circular high-pass: A = channel-major wrapped windows [(b, c)][time], B = a fixed
+//              128 x K band matrix G[j][k] = taps[k - j]; the tile at output time w0 reads A columns
+//              w0 + k, and the epilogue stores Y[b][w0 + j][c] as its tf32 split (hi, lo)
+enum UmmaMode { kPlain = 0, kToeplitz = 1 };
+
+struct UmmaArgs {
+    float* out;       // kPlain: C; kToeplitz: Y (hi)
+    float* out_lo;    // kToeplitz: Y (lo)
+    int M, N, K;
+    int64_t ldc;      // kPlain
+    int chans, wlen;  // kToeplitz: C and W of a window (rows of A are (b, c) = (r / chans, r % chans))
+    int* err;
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -78,15 +92,19 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     d |= (uint64_t)4u << 61;                          // swizzle 64B
     return d;
 }
-// instruction descriptor: D = F32, A = B = TF32, both K-major, N = 256, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kBN >> 3) << 17) |
-                            ((uint32_t)(kBM >> 4) << 24);
+// instruction descriptor: D = F32, A = B = TF32, both K-major, M = 128, N = BN
+template <int BN>
+struct IdescTf32 {
+    static constexpr uint32_t value =
+        (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+};
 
+template <int BN>
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
-        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(IdescTf32<BN>::value), "r"(accumulate)
         : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
@@ -94,10 +112,16 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                  : "memory");
 }
 
+template <int BN, int MODE>
 __global__ void __launch_bounds__(128, 1)
 umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
-                 const __grid_constant__ CUtensorMap tB_hi, const __grid_constant__ CUtensorMap tB_lo,
-                 float* __restrict__ Cm, int M, int N, int K, int64_t ldc, int* __restrict__ err) {
+                 const __grid_constant__ CUtensorMap tB_hi, const __grid_constant__ CUtensorMap tB_lo, UmmaArgs args) {
+    constexpr int kBN = BN;
+    constexpr int kTileB = kBN * kBK * 4;
+    constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;
+    constexpr int kStages = kSmemBudget / kStageBytes;
+    const int M = args.M, N = args.N, K = args.K;
+    int* err = args.err;
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
     __shared__ uint32_t tmem_base_s;
@@ -147,10 +171,14 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
             const uint32_t fb = smem_u32(&full_bar[s]);
             mbar_expect_tx(fb, kStageBytes);
             const int k0 = kt * kBK;   // a multiple of 16 fp32 = 64 bytes
-            tma_load_2d(sA_hi(s), &tA_hi, fb, k0, m0);
-            tma_load_2d(sA_lo(s), &tA_lo, fb, k0, m0);
-            tma_load_2d(sB_hi(s), &tB_hi, fb, k0, n0);
-            tma_load_2d(sB_lo(s), &tB_lo, fb, k0, n0);
+            // Toeplitz: A columns start at the tile's output time n0 (a multiple of 128), B is the
+            // same band matrix for every tile
+            const int ax = (MODE == kToeplitz) ? n0 + k0 : k0;
+            const int by = (MODE == kToeplitz) ? 0 : n0;
+            tma_load_2d(sA_hi(s), &tA_hi, fb, ax, m0);
+            tma_load_2d(sA_lo(s), &tA_lo, fb, ax, m0);
+            tma_load_2d(sB_hi(s), &tB_hi, fb, k0, by);
+            tma_load_2d(sB_lo(s), &tB_lo, fb, k0, by);
             ++issued;
         }
         // the copies of the last rounds must have landed before the CTA may exit
@@ -172,9 +200,9 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
                 const uint32_t off = (uint32_t)kk * 32u;
                 const uint64_t ah = smem_desc(sA_hi(s) + off), al = smem_desc(sA_lo(s) + off);
                 const uint64_t bh = smem_desc(sB_hi(s) + off), bl = smem_desc(sB_lo(s) + off);
-                mma_tf32(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
-                mma_tf32(tmem, ah, bl, 1u);
-                mma_tf32(tmem, al, bh, 1u);
+                mma_tf32<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
+                mma_tf32<BN>(tmem, ah, bl, 1u);
+                mma_tf32<BN>(tmem, al, bh, 1u);
             }
             mma_commit(smem_u32(&empty_bar[s]));        // frees the stage once these MMAs finish
         }
@@ -199,8 +227,26 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
               "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if constexpr (MODE == kToeplitz) {
+            // row = (b, c); column j = output time n0 + c0 + j; lanes = consecutive channels
+            if (ok && row < M) {
+                const int b = row / args.chans, c = row - b * args.chans;
+                for (int j = 0; j < 32; ++j) {
+                    const int w = n0 + c0 + j;
+                    if (w < args.wlen) {
+                        const float v = __uint_as_float(r[j]);
+                        uint32_t h;
+                        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+                        const int64_t o = ((int64_t)b * args.wlen + w) * args.chans + c;
+                        args.out[o] = __uint_as_float(h);
+                        args.out_lo[o] = v - __uint_as_float(h);
+                    }
+                }
+            }
+            continue;
+        }
         if (ok && row < M) {
-            float* crow = Cm + (int64_t)row * ldc + n0 + c0;
+            float* crow = args.out + (int64_t)row * args.ldc + n0 + c0;
             const int ncol = min(32, N - (n0 + c0));
             if (ncol == 32 && ((((uintptr_t)crow) & 15) == 0)) {
 #pragma unroll
@@ -256,7 +302,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // rows x cols fp32 row-major, boxes of 16 columns (64 B) x box_rows rows, 64-byte swizzle
-static bool make_map(CUtensorMap* m, const float* ptr, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+bool make_map(CUtensorMap* m, const float* ptr, uint64_t rows, uint64_t cols, uint32_t box_rows) {
     auto fn = encode_fn();
     if (!fn || ((uintptr_t)ptr & 15) || (cols * 4) % 16) return false;
     const cuuint64_t dims[2] = {cols, rows};
@@ -271,17 +317,40 @@ static bool make_map(CUtensorMap* m, const float* ptr, uint64_t rows, uint64_t c
 struct UmmaOperands {
     CUtensorMap a_hi, a_lo, b_hi, b_lo;
     int rows_a = 0, rows_b = 0, K = 0;
+    int cols_a = 0;           // Toeplitz: columns of A (wrapped window length, padded)
 };
+
+constexpr int kPlainBN = 256, kToepBN = 128;
+template <int BN>
+constexpr int smem_bytes() {
+    return (kSmemBudget / (2 * kTileA + 2 * BN * kBK * 4)) * (2 * kTileA + 2 * BN * kBK * 4) + 1024;
+}
 
 UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, const float* b_hi, const float* b_lo,
                         int64_t rows_b, int K) {
-    if (K % kBK != 0 || rows_b > 2 * kBN) return nullptr;
+    if (K % kBK != 0 || rows_b > 2 * kPlainBN) return nullptr;
     auto* u = new UmmaOperands();
     u->rows_a = (int)rows_a;
     u->rows_b = (int)rows_b;
     u->K = K;
     if (!make_map(&u->a_hi, a_hi, rows_a, K, kBM) || !make_map(&u->a_lo, a_lo, rows_a, K, kBM) ||
-        !make_map(&u->b_hi, b_hi, rows_b, K, kBN) || !make_map(&u->b_lo, b_lo, rows_b, K, kBN)) {
+        !make_map(&u->b_hi, b_hi, rows_b, K, kPlainBN) || !make_map(&u->b_lo, b_lo, rows_b, K, kPlainBN)) {
+        delete u;
+        return nullptr;
+    }
+    return u;
+}
+
+UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t rows, int64_t cols, const float* g_hi,
+                                 const float* g_lo, int K) {
+    if (K % kBK != 0 || cols % 4 != 0) return nullptr;
+    auto* u = new UmmaOperands();
+    u->rows_a = (int)rows;
+    u->cols_a = (int)cols;
+    u->rows_b = kToepBN;
+    u->K = K;
+    if (!make_map(&u->a_hi, x_hi, rows, cols, kBM) || !make_map(&u->a_lo, x_lo, rows, cols, kBM) ||
+        !make_map(&u->b_hi, g_hi, kToepBN, K, kToepBN) || !make_map(&u->b_lo, g_lo, kToepBN, K, kToepBN)) {
         delete u;
         return nullptr;
     }
@@ -291,12 +360,42 @@ UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, co
 void umma_free(UmmaOperands* u) { delete u; }
 
 cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, int* err, cudaStream_t s) {
-    if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kBN) return cudaErrorInvalidValue;
-    const cudaError_t attr_err =
-        cudaFuncSetAttribute(umma_gemm_3xtf32, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem);
+    if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
+    auto kern = umma_gemm_3xtf32<kPlainBN, kPlain>;
+    constexpr int smem = smem_bytes<kPlainBN>();
+    const cudaError_t attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (attr_err != cudaSuccess) return attr_err;
-    dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM);
-    umma_gemm_3xtf32<<<grid, 128, kUmmaSmem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, Cm, M, N, u->K, ldc, err);
+    UmmaArgs a{};
+    a.out = Cm;
+    a.M = M;
+    a.N = N;
+    a.K = u->K;
+    a.ldc = ldc;
+    a.err = err;
+    dim3 grid((N + kPlainBN - 1) / kPlainBN, (M + kBM - 1) / kBM);
+    kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
+    return cudaGetLastError();
+}
+
+// Y[b][w][c] (tf32 split) = circular high-pass of nb windows held channel-major in the operands
+cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W, int* err,
+                                 cudaStream_t s) {
+    if (!u || nb * C > u->rows_a) return cudaErrorInvalidValue;
+    auto kern = umma_gemm_3xtf32<kToepBN, kToeplitz>;
+    constexpr int smem = smem_bytes<kToepBN>();
+    const cudaError_t attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (attr_err != cudaSuccess) return attr_err;
+    UmmaArgs a{};
+    a.out = Y_hi;
+    a.out_lo = Y_lo;
+    a.M = nb * C;
+    a.N = W;
+    a.K = u->K;
+    a.chans = C;
+    a.wlen = W;
+    a.err = err;
+    dim3 grid((W + kToepBN - 1) / kToepBN, (nb * C + kBM - 1) / kBM);
+    kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     return cudaGetLastError();
 }
 

@@ -53,6 +53,9 @@ void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, 
                    int nb, long long* colsum, cudaStream_t s);
 void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
                 const long long* colsum, int L, int R, float* Xw, cudaStream_t s);
+// channel-major, tf32-split variant feeding the tensor-core high-pass: Xt[(b, c)][pitch]
+void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
+                  const long long* colsum, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s);
 // Ylo != nullptr: Y receives tf32(y) and Ylo the remainder (operands of the tensor-core GEMM)
 void launch_highpass(const float* Xw, int C, int W, int L, int R, const float* taps, int nb, float* Y,
                      cudaStream_t s, float* Ylo = nullptr);
@@ -69,6 +72,12 @@ UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, co
                         int64_t rows_b, int K);
 void umma_free(UmmaOperands* u);
 cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, int* err, cudaStream_t s);
+// circular high-pass on the tensor cores: x = channel-major windows [rows][cols] (tf32 split),
+// g = the 128 x K band matrix of the taps (tf32 split)
+UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t rows, int64_t cols, const float* g_hi,
+                                 const float* g_lo, int K);
+cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W, int* err,
+                                 cudaStream_t s);
 void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                          float th2, int W, int T, int C, int nt, int max_iters, int nb,

@@ -57,8 +57,13 @@ static T* dev_upload(const std::vector<T>& v, int64_t& tally, cudaStream_t s) {
 }
 
 struct TapSet {
-    float* d = nullptr;
+    float* d = nullptr;          // taps, zero-padded to a multiple of 32 (SIMT FIR)
     int L = 0, R = 0;
+    // tensor-core high-pass: the 128 x Kt band matrix G[j][k] = taps[k - j] (tf32 split), the row
+    // pitch of the channel-major window buffer and the tensor maps over it
+    float *g_hi = nullptr, *g_lo = nullptr;
+    int Kt = 0, pitch = 0;
+    UmmaOperands* um = nullptr;
 };
 
 struct Slot {
@@ -101,6 +106,7 @@ struct Handle {
     // tf32 splits of the GEMM's fixed operands (tensor-core path)
     float *d_WD_hi = nullptr, *d_WD_lo = nullptr, *d_Wall3_hi = nullptr, *d_Wall3_lo = nullptr;
     bool tc_whiten = false, tc_project = false;   // GEMMs on the tensor cores
+    bool tc_highpass = false;                     // circular high-pass as a tensor-core band GEMM
     UmmaOperands* um_whiten = nullptr;
     UmmaOperands* um_project = nullptr;
     int* h_gemm_err = nullptr;                    // mapped: device-side wait timeouts
@@ -116,6 +122,7 @@ struct Handle {
     long long* d_colsum = nullptr;
     float *d_Xw = nullptr, *d_Y = nullptr, *d_Z = nullptr, *d_Bpc = nullptr, *d_Bt = nullptr;
     float *d_Y_lo = nullptr, *d_Bpc_lo = nullptr;   // tf32 remainders (tensor-core path)
+    float *d_Xt_hi = nullptr, *d_Xt_lo = nullptr;   // channel-major wrapped windows (tensor-core high-pass)
     MatchScratch sc{};
     MatchOut mo{};
     int64_t work_bytes = 0;
@@ -153,7 +160,11 @@ Handle::~Handle() {
     if (dev >= 0) cudaSetDevice(dev);
     if (st) cudaStreamSynchronize(st);
     free_work();
-    for (auto& kv : taps) cudaFree(kv.second.d);
+    for (auto& kv : taps) {
+        cudaFree(kv.second.d);
+        if (kv.second.g_hi) cudaFree(kv.second.g_hi);
+        if (kv.second.g_lo) cudaFree(kv.second.g_lo);
+    }
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
                     (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo})
@@ -176,8 +187,12 @@ void Handle::free_work() {
     umma_free(um_whiten);
     umma_free(um_project);
     um_whiten = um_project = nullptr;
+    for (auto& kv : taps) {
+        umma_free(kv.second.um);
+        kv.second.um = nullptr;
+    }
     for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
-                    (void*)d_Y_lo, (void*)d_Bpc_lo,
+                    (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo,
                     (void*)sc.cfmax, (void*)sc.imax, (void*)sc.at_t, (void*)sc.at_amp, (void*)sc.dirty,
                     (void*)sc.cta_cnt, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
                     (void*)mo.sp_t, (void*)mo.sp_amp, (void*)mo.sp_iter})
@@ -186,6 +201,7 @@ void Handle::free_work() {
     d_colsum = nullptr;
     d_Xw = d_Y = d_Z = d_Bpc = d_Bt = nullptr;
     d_Y_lo = d_Bpc_lo = nullptr;
+    d_Xt_hi = d_Xt_lo = nullptr;
     sc = MatchScratch{};
     mo = MatchOut{};
     dev_bytes -= work_bytes;
@@ -275,6 +291,7 @@ void Handle::init(const char* dir, const lss_params* prm) {
     const bool want_tc = p.gemm_path == 0;
     tc_whiten = want_tc && C % 16 == 0 && C <= 512;
     tc_project = want_tc && (K * C) % 16 == 0 && T <= 512;
+    tc_highpass = tc_whiten;
     if (tc_whiten || tc_project) {
         if (tc_whiten) {
             d_WD_hi = dev_alloc<float>((size_t)C * C, dev_bytes);
@@ -317,6 +334,22 @@ TapSet& Handle::taps_for(int Wn) {
     ts.L = (int)L;
     ts.R = (int)R;
     ts.d = dev_upload(tv, dev_bytes, st);
+    if (tc_highpass) {
+        const int ntaps = (int)(L + R + 1), TB = 128;
+        ts.Kt = ((TB + ntaps - 1) + 15) / 16 * 16;
+        ts.pitch = (int)(((Wn + L + R) + 3) / 4 * 4);
+        std::vector<float> G((size_t)TB * ts.Kt, 0.f);
+        for (int j = 0; j < TB; ++j)
+            for (int d = 0; d < ntaps; ++d) G[(size_t)j * ts.Kt + j + d] = tv[(size_t)d];
+        float* g = dev_upload(G, dev_bytes, st);
+        ts.g_hi = dev_alloc<float>(G.size(), dev_bytes);
+        ts.g_lo = dev_alloc<float>(G.size(), dev_bytes);
+        launch_split_tf32(g, ts.g_hi, ts.g_lo, (int64_t)G.size(), st);
+        LSS_CUDA(cudaGetLastError());
+        LSS_CUDA(cudaStreamSynchronize(st));
+        cudaFree(g);
+        dev_bytes -= (int64_t)G.size() * 4;
+    }
     LSS_CUDA(cudaStreamSynchronize(st));
     return taps.emplace(Wn, ts).first->second;
 }
@@ -339,7 +372,16 @@ void Handle::ensure_work(int Wn, int nb) {
                                            " device bytes, budget " + std::to_string(p.mem_budget)};
     d_raw = dev_alloc<int16_t>(raw_rows_cap * Cin, dev_bytes);
     d_colsum = dev_alloc<long long>((size_t)nba * C, dev_bytes);
-    d_Xw = dev_alloc<float>((size_t)nba * (Wa + LRmax) * C, dev_bytes);
+    if (tc_highpass) {
+        // row pitch of any window length up to Wa: W + L + R <= 2W - 1, rounded up to 4
+        const size_t n = (size_t)nba * C * (size_t)((2 * Wa + 3) / 4 * 4);
+        d_Xt_hi = dev_alloc<float>(n, dev_bytes);
+        d_Xt_lo = dev_alloc<float>(n, dev_bytes);
+        LSS_CUDA(cudaMemsetAsync(d_Xt_hi, 0, n * sizeof(float), st));
+        LSS_CUDA(cudaMemsetAsync(d_Xt_lo, 0, n * sizeof(float), st));
+    } else {
+        d_Xw = dev_alloc<float>((size_t)nba * (Wa + LRmax) * C, dev_bytes);
+    }
     d_Y = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     d_Z = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     d_Bpc = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
@@ -412,10 +454,23 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
                                   const std::function<void()>& mark) {
     launch_colsum(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, st), ++nl;
     mark();
-    launch_car(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, d_Xw, st), ++nl;
-    mark();
-    launch_highpass(d_Xw, C, Wn, ts.L, ts.R, ts.d, nb, d_Y, st, tc_whiten ? d_Y_lo : nullptr), ++nl;
-    mark();
+    if (tc_highpass) {
+        TapSet& tw = const_cast<TapSet&>(ts);
+        if (!tw.um) {
+            tw.um = umma_make_toeplitz(d_Xt_hi, d_Xt_lo, (int64_t)nbcap * C, tw.pitch, tw.g_hi, tw.g_lo, tw.Kt);
+            if (!tw.um) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (high-pass band GEMM)"};
+        }
+        launch_car_t(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, tw.pitch, d_Xt_hi, d_Xt_lo, st), ++nl;
+        mark();
+        LSS_CUDA(launch_umma_highpass(tw.um, d_Y, d_Y_lo, nb, C, Wn, d_gemm_err, st));
+        ++nl;
+        mark();
+    } else {
+        launch_car(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, d_Xw, st), ++nl;
+        mark();
+        launch_highpass(d_Xw, C, Wn, ts.L, ts.R, ts.d, nb, d_Y, st, tc_whiten ? d_Y_lo : nullptr), ++nl;
+        mark();
+    }
     if (tc_whiten)
         LSS_CUDA(launch_umma_gemm(um_whiten, d_Z, nb * Wn, C, C, d_gemm_err, st));
     else
