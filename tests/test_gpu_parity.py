@@ -257,15 +257,16 @@ def test_cpp_dropin_replay(golden_dir, tmp_path):
 
 
 def test_tensor_core_and_simt_gemms_agree(win_oss, win):
-    """gemm_path 0 (tcgen05, 3xTF32) and 1 (FP32 SIMT) give the same scores to FP32 accuracy and
-    the same spikes."""
+    """gemm_path 0 (tcgen05, 3xTF32: high-pass band GEMM, whitening, projection) and 1 (FP32 SIMT)
+    agree within 1e-5 (preprocessed) / 2e-5 (scores) of the largest magnitude -- inside the
+    oracle tolerances -- and give the same spikes."""
     outs = {}
     for path in (0, 1):
         with sorter.OnlineSorter(win_oss, max_iters=int(win["max_iters"]), gemm_path=path) as s:
             outs[path] = (s.debug_stage(win["window"], sorter.STAGE_PREPROCESSED),
                           s.debug_stage(win["window"], sorter.STAGE_SCORES), s.sort_windows(win["window"])[0])
-    _rel_close(outs[0][0].astype(np.float64), outs[1][0].astype(np.float64), 2e-6)
-    _rel_close(outs[0][1].astype(np.float64), outs[1][1].astype(np.float64), 1e-5)
+    _rel_close(outs[0][0].astype(np.float64), outs[1][0].astype(np.float64), 1e-5)
+    _rel_close(outs[0][1].astype(np.float64), outs[1][1].astype(np.float64), 2e-5)
     a, amp_ok, amax = agreement(outs[1][2]["time"], outs[1][2]["tmpl"], outs[1][2]["amp"],
                                 outs[0][2]["time"], outs[0][2]["tmpl"], outs[0][2]["amp"])
     assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
@@ -279,5 +280,5 @@ def test_tensor_core_gemm_384ch(cfg_stream):
     for path in (0, 1):
         with sorter.OnlineSorter(d, gemm_path=path) as s:
             outs[path] = (s.debug_stage(win, sorter.STAGE_PREPROCESSED), s.debug_stage(win, sorter.STAGE_SCORES))
-    _rel_close(outs[0][0].astype(np.float64), outs[1][0].astype(np.float64), 2e-6)
-    _rel_close(outs[0][1].astype(np.float64), outs[1][1].astype(np.float64), 1e-5)
+    _rel_close(outs[0][0].astype(np.float64), outs[1][0].astype(np.float64), 1e-5)
+    _rel_close(outs[0][1].astype(np.float64), outs[1][1].astype(np.float64), 2e-5)
