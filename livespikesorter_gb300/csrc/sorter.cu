@@ -22,6 +22,7 @@
 #include <map>
 #include <memory>
 #include <new>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -54,6 +55,29 @@ static T* dev_upload(const std::vector<T>& v, int64_t& tally, cudaStream_t s) {
     T* p = dev_alloc<T>(v.size(), tally);
     LSS_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
     return p;
+}
+
+// memcpy split across threads for large host copies (pinned staging fills at several GB/s per
+// core; one thread alone is the bottleneck of the host path for multi-MB groups)
+static void par_memcpy(void* dst, const void* src, size_t bytes) {
+    constexpr size_t kChunk = 4u << 20;
+    const size_t nthr = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency() / 2), 16);
+    if (bytes < 2 * kChunk || nthr < 2) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t k = std::min(nthr, bytes / kChunk);
+    const size_t per = (bytes / k + 63) / 64 * 64;
+    std::vector<std::thread> th;
+    th.reserve(k);
+    for (size_t i = 1; i < k; ++i) {
+        const size_t off = i * per;
+        if (off >= bytes) break;
+        const size_t n = std::min(per, bytes - off);
+        th.emplace_back([=] { std::memcpy((char*)dst + off, (const char*)src + off, n); });
+    }
+    std::memcpy(dst, src, std::min(per, bytes));
+    for (auto& t : th) t.join();
 }
 
 struct TapSet {
@@ -136,7 +160,8 @@ struct Handle {
     bool seg_active = false;
     int64_t seg_s0 = 0, next_batch = 0, expected_ct = 0, batch_counter = 0;
     std::vector<int16_t> buf;   // rows from the next window's first row on
-    std::map<int, int64_t> last_kept;   // per final cluster (duplicate removal)
+    std::vector<int64_t> last_kept;     // per final cluster: last kept spike time (duplicate removal)
+    std::vector<char> has_kept;
 
     ~Handle();
     void init(const char* dir, const lss_params* prm);
@@ -151,7 +176,7 @@ struct Handle {
     void drain_all();
     void push(const int16_t* x, int64_t n, int64_t ct);
     void flush();
-    void launch_windows_from_buf(int g, int pad_mode);
+    int64_t launch_windows(int g, int pad_mode, const int16_t* x, int64_t xr);
     void run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
                               const std::function<void()>& mark);
 };
@@ -313,6 +338,8 @@ void Handle::init(const char* dir, const lss_params* prm) {
     m.ctc.clear();
     m.ctc.shrink_to_fit();
 
+    last_kept.assign(Tf, 0);
+    has_kept.assign(Tf, 0);
     taps_for(W);
     ensure_work(W, G);
     slots.resize(3);
@@ -605,11 +632,11 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
             if (counts) counts->push_back((int64_t)batch.size());
         } else {
             for (const lss_spike& o : batch) {
-                if (p.dedup) {
+                if (p.dedup && o.cluster >= 0 && o.cluster < Tf) {
                     // Kilosort postprocessing.py:9-30: keep when t >= last kept + dt
-                    auto it = last_kept.find(o.cluster);
-                    if (it != last_kept.end() && o.time < it->second + m.dup_bins) continue;
+                    if (has_kept[o.cluster] && o.time < last_kept[o.cluster] + m.dup_bins) continue;
                     last_kept[o.cluster] = o.time;
+                    has_kept[o.cluster] = 1;
                 }
                 ready.push_back(o);
             }
@@ -624,17 +651,23 @@ void Handle::drain_all() {
     while (!inflight.empty()) collect(inflight.front(), nullptr, nullptr);
 }
 
-// Launch g windows from the front of buf.  Rows past the end of buf (only at a flush, g = 1):
-// pad_mode 1 repeats the last row (Kilosort's last batch, io.py:626-629); pad_mode 2 leaves them
-// zero, which is what Kilosort does when the first batch is also the last one (its ibatch == 0
-// branch, io.py:621-625, runs first and never fills the right side).
-void Handle::launch_windows_from_buf(int g, int pad_mode) {
-    const int64_t rows_have = (int64_t)(buf.size() / Cin);
+// Launch g windows whose rows are the concatenation of buf (rows not launched yet) and the
+// caller's rows x[0 .. xr): each row is copied once, straight into the pinned staging slot.  Rows
+// past the end (only at a flush, g = 1): pad_mode 1 repeats the last row (Kilosort's last batch,
+// io.py:626-629); pad_mode 2 leaves them zero, which is what Kilosort does when the first batch is
+// also the last one (its ibatch == 0 branch, io.py:621-625, runs first and never fills the right
+// side).  Returns the number of caller rows consumed (dropped from the front of the stream).
+int64_t Handle::launch_windows(int g, int pad_mode, const int16_t* x, int64_t xr) {
+    const int64_t brows = (int64_t)(buf.size() / Cin);
+    const int64_t rows_have = brows + xr;
     const int64_t rows_need = (int64_t)g * NT + 2 * nt;
     const int si = acquire_slot();
     Slot& s = slots[si];
-    const int64_t copy_rows = std::min(rows_have, rows_need);
-    std::memcpy(s.h_stage, buf.data(), (size_t)copy_rows * Cin * sizeof(int16_t));
+    const int64_t from_buf = std::min(brows, rows_need);
+    const int64_t from_x = std::min(xr, rows_need - from_buf);
+    par_memcpy(s.h_stage, buf.data(), (size_t)from_buf * Cin * sizeof(int16_t));
+    if (from_x > 0) par_memcpy(s.h_stage + from_buf * Cin, x, (size_t)from_x * Cin * sizeof(int16_t));
+    const int64_t copy_rows = from_buf + from_x;
     if (copy_rows < rows_need) {
         if (pad_mode == 0 || copy_rows == 0 || g != 1) throw LoadError{LSS_ERR_INTERNAL, "window underflow"};
         for (int64_t r = copy_rows; r < rows_need; ++r) {
@@ -658,8 +691,14 @@ void Handle::launch_windows_from_buf(int g, int pad_mode) {
     inflight.push_back(si);
     next_batch += g;
     batch_counter += g;
-    const int64_t drop = std::min<int64_t>((int64_t)g * NT, rows_have);
-    buf.erase(buf.begin(), buf.begin() + (size_t)drop * Cin);
+    // advance the stream by g * NT rows
+    const int64_t adv = std::min<int64_t>((int64_t)g * NT, rows_have);
+    if (adv <= brows) {
+        buf.erase(buf.begin(), buf.begin() + (size_t)adv * Cin);
+        return 0;
+    }
+    buf.clear();
+    return adv - brows;
 }
 
 void Handle::push(const int16_t* x, int64_t n, int64_t ct) {
@@ -674,13 +713,14 @@ void Handle::push(const int16_t* x, int64_t n, int64_t ct) {
         for (int r = 0; r < nt; ++r) buf.insert(buf.end(), x, x + Cin);   // left pad = first sample
         expected_ct = seg_s0;
     }
-    buf.insert(buf.end(), x, x + (size_t)n * Cin);
     expected_ct += n;
-    for (;;) {
-        const int64_t rows = (int64_t)(buf.size() / Cin);
-        if (rows < (int64_t)G * NT + 2 * nt) break;
-        launch_windows_from_buf(G, 0);
+    const int64_t need = (int64_t)G * NT + 2 * nt;
+    while ((int64_t)(buf.size() / Cin) + n >= need) {
+        const int64_t used = launch_windows(G, 0, x, n);
+        x += used * Cin;
+        n -= used;
     }
+    buf.insert(buf.end(), x, x + (size_t)n * Cin);
 }
 
 void Handle::flush() {
@@ -692,9 +732,9 @@ void Handle::flush() {
         if (rows - nt <= 0) break;
         const int64_t complete = rows >= W ? (rows - W) / NT + 1 : 0;
         if (complete > 0) {
-            launch_windows_from_buf((int)std::min<int64_t>(complete, G), 0);
+            launch_windows((int)std::min<int64_t>(complete, G), 0, nullptr, 0);
         } else {
-            launch_windows_from_buf(1, next_batch == 0 ? 2 : 1);
+            launch_windows(1, next_batch == 0 ? 2 : 1, nullptr, 0);
         }
     }
     seg_active = false;
