@@ -45,8 +45,8 @@ __device__ __forceinline__ unsigned cluster_rank() {
     return r;
 }
 
-constexpr int kWarps = kMatchThreads / 32;
-constexpr int kMaxRounds = 64;   // slice <= 64 * 512 samples per CTA
+constexpr int kMaxRoundsGlobal = 64;   // slice <= 64 * threads samples per CTA (scores in L2)
+constexpr int kMaxRoundsSmem = 4;      // the shared-memory slice is at most a few hundred samples
 constexpr int kPerLane = 8;      // row elements each lane loads before it stores (256 per warp)
 
 // dynamic shared memory of one CTA: [score slice if SMEM_B][s_cf][s_t][s_amp][1/nm], floats/ints
@@ -56,11 +56,14 @@ __host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, 
     return (smem_b ? (size_t)span * T * 4 : 0) + halo * 12 + (size_t)T * 4;
 }
 
-template <int G, bool SMEM_B>
-__global__ void __launch_bounds__(kMatchThreads, 2)
+template <int G, bool SMEM_B, int NTHR>
+__global__ void __launch_bounds__(NTHR, SMEM_B ? 1 : 2)
 match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __restrict__ ctcP,
              const float* __restrict__ pre_wf, const float* __restrict__ nm, float th2, int W, int T, int C,
              int nt, int max_iters, MatchScratch sc, MatchOut out) {
+    constexpr int kMatchThreads = NTHR;
+    constexpr int kWarps = NTHR / 32;
+    constexpr int kMaxRounds = SMEM_B ? kMaxRoundsSmem : kMaxRoundsGlobal;
     extern __shared__ float smem[];
     const int b = blockIdx.x / G;
     const int rank = (G == 1) ? 0 : (int)cluster_rank();
@@ -383,12 +386,12 @@ residual_kernel(float* __restrict__ Xres, const float* __restrict__ pre_wf, Matc
     }
 }
 
-template <int G, bool SMEM_B>
+template <int G, bool SMEM_B, int NTHR>
 static cudaError_t launch_match_cfg(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                                     float th2, int W, int T, int C, int nt, int max_iters, int nb,
                                     const MatchScratch& sc, const MatchOut& out, cudaStream_t s) {
     const size_t smem = match_smem_bytes(W, T, nt, G, SMEM_B);
-    auto kern = match_kernel<G, SMEM_B>;
+    auto kern = match_kernel<G, SMEM_B, NTHR>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (G > 8) {
@@ -397,7 +400,7 @@ static cudaError_t launch_match_cfg(float* Bt, float* Xres, const float* ctcP, c
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb * G, 1, 1);
-    cfg.blockDim = dim3(kMatchThreads, 1, 1);
+    cfg.blockDim = dim3(NTHR, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -412,12 +415,13 @@ static cudaError_t launch_match_cfg(float* Bt, float* Xres, const float* ctcP, c
 
 // Can a cluster of 16 CTAs with the whole score slice in shared memory run on this device?
 static int smem16_ok(int W, int T, int nt) {
+    if ((W + 15) / 16 > kMaxRoundsSmem * kMatchThreadsSmem) return 0;
     const size_t smem = match_smem_bytes(W, T, nt, 16, true);
     int dev = 0, maxopt = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
-    if (smem + 8192 > (size_t)maxopt) return 0;   // static shared memory and the driver reserve
-    auto kern = match_kernel<16, true>;
+    if (smem + 12288 > (size_t)maxopt) return 0;   // static shared memory and the driver reserve
+    auto kern = match_kernel<16, true, kMatchThreadsSmem>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
         cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
         cudaGetLastError();
@@ -425,7 +429,7 @@ static int smem16_ok(int W, int T, int nt) {
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(16, 1, 1);
-    cfg.blockDim = dim3(kMatchThreads, 1, 1);
+    cfg.blockDim = dim3(kMatchThreadsSmem, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -460,10 +464,10 @@ cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float*
     bool smem = false;
     if (variant == 2) smem = match_variant(W, T, nt) == 16;
     else if (variant == 0) smem = nb <= 8 && match_variant(W, T, nt) == 16;
-    cudaError_t e = smem ? launch_match_cfg<16, true>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc,
-                                                      out, s)
-                         : launch_match_cfg<8, false>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc,
-                                                      out, s);
+    cudaError_t e = smem ? launch_match_cfg<16, true, kMatchThreadsSmem>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt,
+                                                                          max_iters, nb, sc, out, s)
+                         : launch_match_cfg<8, false, kMatchThreads>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt,
+                                                                     max_iters, nb, sc, out, s);
     if (e != cudaSuccess) return e;
     dim3 grid((W + kResRows - 1) / kResRows, nb);
     residual_kernel<<<grid, 256, 0, s>>>(Xres, pre_wf, out, W, C, nt);

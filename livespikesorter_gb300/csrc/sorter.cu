@@ -603,6 +603,12 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
     const int nf = nC * K;
     std::vector<lss_spike> batch;
     for (int b = 0; b < s.nb; ++b) {
+        if (s.h_status[b] & 2) {
+            s.busy = false;
+            throw LoadError{LSS_ERR_ARG, "window too long for the matching kernel's slice bookkeeping"};
+        }
+    }
+    for (int b = 0; b < s.nb; ++b) {
         const int n = s.h_off[b + 1] - s.h_off[b];
         if (s.h_status[b] & 1) overflow_pending = true;
         batch.clear();
