@@ -222,6 +222,20 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             s_amp[i] = in ? __ldcg(at_amp + w) : 0.f;
         }
         __syncthreads();
+        // pull the ctc rows this CTA will read into L2 now: a spike at w touches the own samples
+        // [max(lo, w - nt), min(hi, w + nt + 1)), i.e. the contiguous rows l = wp - w + nt of ctcP[ts]
+        if (((T * 4) & 15) == 0) {
+            for (int i = tid; i < halo; i += kMatchThreads) {
+                const int ts = s_t[i];
+                if (ts < 0) continue;
+                const int w = lo - nt + i;
+                const int a = max(lo, w - nt), z = min(hi, w + nt + 1);
+                if (a >= z) continue;
+                const float* src = ctcP + ((int64_t)ts * L2 + (a - w + nt)) * T;
+                const uint32_t bytes = (uint32_t)(z - a) * (uint32_t)T * 4u;
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+            }
+        }
         for (int wp = lo + warp; wp < hi; wp += kWarps) {
             const int i0 = wp - lo;   // s_t[i0 + e] is the sample wp - nt + e
             int n_sp = 0;
@@ -243,6 +257,37 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                 const float* c0 = ctcP + ((int64_t)t0s * L2 + l0s) * T;
                 const float* c1 = ctcP + ((int64_t)t1s * L2 + l1s) * T;
                 const bool two = npend == 2;
+                if constexpr (SMEM_B) {
+                    // the score row is in shared memory: only the ctc rows make a round trip,
+                    // all of them issued at once (16 per lane = 512 templates per pass)
+                    constexpr int kP = 16;
+                    for (int tb = 0; tb < T; tb += 32 * kP) {
+                        float v0[kP], v1[kP];
+#pragma unroll
+                        for (int j = 0; j < kP; ++j) {
+                            const int t = tb + lane + 32 * j;
+                            const bool ok = t < T;
+                            v0[j] = ok ? __ldg(c0 + t) : 0.f;
+                            v1[j] = (ok && two) ? __ldg(c1 + t) : 0.f;
+                        }
+#pragma unroll
+                        for (int j = 0; j < kP; ++j) {
+                            const int t = tb + lane + 32 * j;
+                            if (t < T) {
+                                float x = fmaf(-a0s, v0[j], br[t]);
+                                if (two) x = fmaf(-a1s, v1[j], x);
+                                br[t] = x;
+                                if (last) {
+                                    const float r = fmaxf(x, 0.f);
+                                    const float v = r * r * s_inm[t];
+                                    if (v > best) { best = v; bi = t; }
+                                }
+                            }
+                        }
+                    }
+                    npend = 0;
+                    return;
+                }
                 for (int tb = 0; tb < T; tb += 32 * kPerLane) {
                     float v0[kPerLane], v1[kPerLane], bv[kPerLane];
 #pragma unroll
