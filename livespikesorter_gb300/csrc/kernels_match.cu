@@ -48,12 +48,16 @@ __device__ __forceinline__ unsigned cluster_rank() {
 constexpr int kMaxRoundsGlobal = 64;   // slice <= 64 * threads samples per CTA (scores in L2)
 constexpr int kMaxRoundsSmem = 4;      // the shared-memory slice is at most a few hundred samples
 constexpr int kPerLane = 8;      // row elements each lane loads before it stores (256 per warp)
+constexpr int kNearMax = 128;    // spikes near one CTA's slice in one iteration (more: scalar path)
+constexpr int kVecSmem = 4;      // float4 per lane per pass of the subtraction (512 templates)
+constexpr int kVecGlobal = 2;    // 256 templates: the global variant runs at 64 registers
 
 // dynamic shared memory of one CTA: [score slice if SMEM_B][s_cf][s_t][s_amp][1/nm], floats/ints
 __host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, bool smem_b) {
     const int span = (W + G - 1) / G;
     const size_t halo = (size_t)span + 2 * nt;
-    return (smem_b ? (size_t)span * T * 4 : 0) + halo * 12 + (size_t)T * 4;
+    // 1 / nm starts on a 16-byte boundary (read as float4)
+    return (smem_b ? (size_t)span * T * 4 : 0) + ((halo * 3 + 3) & ~(size_t)3) * 4 + (size_t)T * 4;
 }
 
 template <int G, bool SMEM_B, int NTHR>
@@ -64,6 +68,7 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     constexpr int kMatchThreads = NTHR;
     constexpr int kWarps = NTHR / 32;
     constexpr int kMaxRounds = SMEM_B ? kMaxRoundsSmem : kMaxRoundsGlobal;
+    constexpr int kVec = SMEM_B ? kVecSmem : kVecGlobal;
     extern __shared__ float smem[];
     const int b = blockIdx.x / G;
     const int rank = (G == 1) ? 0 : (int)cluster_rank();
@@ -74,10 +79,13 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     float* s_cf = smem + (SMEM_B ? (size_t)span * T : 0);            // [halo]
     int* s_t = reinterpret_cast<int*>(s_cf + halo);                    // [halo]
     float* s_amp = reinterpret_cast<float*>(s_t + halo);               // [halo]
-    float* s_inm = s_amp + halo;                                       // [T] 1 / nm
+    float* s_inm = s_cf + ((3 * halo + 3) & ~3);                      // [T] 1 / nm, 16-byte aligned
     __shared__ int s_cnt[G];
     __shared__ int s_woff[kMaxRounds * kWarps];
     __shared__ int s_total;
+    __shared__ int s_nw[kNearMax], s_nt[kNearMax];
+    __shared__ float s_na[kNearMax];
+    __shared__ int s_nn;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int L2 = 2 * nt + 1;
@@ -163,6 +171,14 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                     tt = imax[w];
                     amp = brow(w)[tt] / __ldg(nm + tt);
                     acc = true;
+                    // phase C of every CTA near w reads rows of ctcP[tt]: start pulling the whole
+                    // (2nt+1) x T slab into L2 now, a barrier and a few round trips ahead of use
+                    if (((T * 4) & 15) == 0) {
+                        const float* slab = ctcP + (int64_t)tt * L2 * T;
+                        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(slab),
+                                     "r"((uint32_t)(L2 * T * 4))
+                                     : "memory");
+                    }
                 }
                 at_t[w] = tt;
                 at_amp[w] = amp;
@@ -222,88 +238,114 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             s_amp[i] = in ? __ldcg(at_amp + w) : 0.f;
         }
         __syncthreads();
-        // pull the ctc rows this CTA will read into L2 now: a spike at w touches the own samples
-        // [max(lo, w - nt), min(hi, w + nt + 1)), i.e. the contiguous rows l = wp - w + nt of ctcP[ts]
-        if (((T * 4) & 15) == 0) {
-            for (int i = tid; i < halo; i += kMatchThreads) {
-                const int ts = s_t[i];
-                if (ts < 0) continue;
-                const int w = lo - nt + i;
-                const int a = max(lo, w - nt), z = min(hi, w + nt + 1);
-                if (a >= z) continue;
-                const float* src = ctcP + ((int64_t)ts * L2 + (a - w + nt)) * T;
-                const uint32_t bytes = (uint32_t)(z - a) * (uint32_t)T * 4u;
-                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+        // the spikes near the own slice, in sample order (typically a handful): one compaction per
+        // iteration instead of a scan of the 2nt+1 neighbours of every sample
+        if (warp == 0) {
+            int cnt = 0;
+            for (int i0 = 0; i0 < halo; i0 += 32) {
+                const int i = i0 + lane;
+                const bool hit = i < halo && s_t[i] >= 0;
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (hit) {
+                    const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                    if (pos < kNearMax) {
+                        s_nw[pos] = lo - nt + i;
+                        s_nt[pos] = s_t[i];
+                        s_na[pos] = s_amp[i];
+                    }
+                }
+                cnt += __popc(m);
             }
+            if (lane == 0) s_nn = cnt;
         }
+        __syncthreads();
+        const int n_near = s_nn;
+        const bool vec_ok = (T & 3) == 0 && n_near <= kNearMax && ((reinterpret_cast<uintptr_t>(ctcP) |
+                                                                      reinterpret_cast<uintptr_t>(Bt)) & 15) == 0;
         for (int wp = lo + warp; wp < hi; wp += kWarps) {
             const int i0 = wp - lo;   // s_t[i0 + e] is the sample wp - nt + e
-            int n_sp = 0;
-            for (int e0 = 0; e0 < L2; e0 += 32) {
-                const int e = e0 + lane;
-                n_sp += __popc(__ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0));
-            }
-            if (n_sp == 0) continue;   // scores unchanged: cfmax / imax stay valid
             float* br = brow(wp);
-            // spikes within +-nt of wp, in increasing sample order, two at a time: both rows of
-            // ctc are loaded before either is applied, and they are applied in order; the pass
-            // that applies the last spike also takes the new max / argmax of the sample
-            int t0s = 0, l0s = 0, t1s = 0, l1s = 0;
-            float a0s = 0.f, a1s = 0.f;
-            int npend = 0, done = 0;
             float best = -1.f;
             int bi = 0x7fffffff;
-            auto flush = [&](bool last) {
-                const float* c0 = ctcP + ((int64_t)t0s * L2 + l0s) * T;
-                const float* c1 = ctcP + ((int64_t)t1s * L2 + l1s) * T;
-                const bool two = npend == 2;
-                if constexpr (SMEM_B) {
-                    // the score row is in shared memory: only the ctc rows make a round trip,
-                    // all of them issued at once (16 per lane = 512 templates per pass)
-                    constexpr int kP = 16;
-                    for (int tb = 0; tb < T; tb += 32 * kP) {
-                        float v0[kP], v1[kP];
+            bool touched = false;
+            if (vec_ok) {
+                // spikes k with |w_k - wp| <= nt, two at a time, in sample order
+                int k = 0;
+                while (k < n_near) {
+                    while (k < n_near && (s_nw[k] < wp - nt || s_nw[k] > wp + nt)) ++k;
+                    if (k >= n_near) break;
+                    int k2 = k + 1;
+                    while (k2 < n_near && (s_nw[k2] < wp - nt || s_nw[k2] > wp + nt)) ++k2;
+                    const bool two = k2 < n_near;
+                    int k3 = two ? k2 + 1 : n_near;
+                    while (k3 < n_near && (s_nw[k3] < wp - nt || s_nw[k3] > wp + nt)) ++k3;
+                    const bool last = k3 >= n_near;   // no further spike for this sample
+                    const float a0 = s_na[k], a1 = two ? s_na[k2] : 0.f;
+                    const float4* c0 = reinterpret_cast<const float4*>(ctcP + ((int64_t)s_nt[k] * L2 + (wp - s_nw[k] + nt)) * T);
+                    const float4* c1 = two ? reinterpret_cast<const float4*>(ctcP + ((int64_t)s_nt[k2] * L2 + (wp - s_nw[k2] + nt)) * T)
+                                           : c0;
+                    float4* b4 = reinterpret_cast<float4*>(br);
+                    const int T4 = T >> 2;
+                    for (int fb = 0; fb < T4; fb += 32 * kVec) {
+                        float4 v0[kVec], v1[kVec];
 #pragma unroll
-                        for (int j = 0; j < kP; ++j) {
-                            const int t = tb + lane + 32 * j;
-                            const bool ok = t < T;
-                            v0[j] = ok ? __ldg(c0 + t) : 0.f;
-                            v1[j] = (ok && two) ? __ldg(c1 + t) : 0.f;
+                        for (int j = 0; j < kVec; ++j) {
+                            const int f = fb + lane + 32 * j;
+                            const bool ok = f < T4;
+                            v0[j] = ok ? __ldg(c0 + f) : make_float4(0.f, 0.f, 0.f, 0.f);
+                            v1[j] = (ok && two) ? __ldg(c1 + f) : make_float4(0.f, 0.f, 0.f, 0.f);
                         }
 #pragma unroll
-                        for (int j = 0; j < kP; ++j) {
-                            const int t = tb + lane + 32 * j;
-                            if (t < T) {
-                                float x = fmaf(-a0s, v0[j], br[t]);
-                                if (two) x = fmaf(-a1s, v1[j], x);
-                                br[t] = x;
+                        for (int j = 0; j < kVec; ++j) {
+                            const int f = fb + lane + 32 * j;
+                            if (f < T4) {
+                                float4 x = b4[f];
+                                x.x = fmaf(-a0, v0[j].x, x.x);
+                                x.y = fmaf(-a0, v0[j].y, x.y);
+                                x.z = fmaf(-a0, v0[j].z, x.z);
+                                x.w = fmaf(-a0, v0[j].w, x.w);
+                                if (two) {
+                                    x.x = fmaf(-a1, v1[j].x, x.x);
+                                    x.y = fmaf(-a1, v1[j].y, x.y);
+                                    x.z = fmaf(-a1, v1[j].z, x.z);
+                                    x.w = fmaf(-a1, v1[j].w, x.w);
+                                }
+                                b4[f] = x;
                                 if (last) {
-                                    const float r = fmaxf(x, 0.f);
-                                    const float v = r * r * s_inm[t];
-                                    if (v > best) { best = v; bi = t; }
+                                    const int t = 4 * f;
+                                    const float4 im = reinterpret_cast<const float4*>(s_inm)[f];
+                                    float r, v;
+                                    r = fmaxf(x.x, 0.f); v = r * r * im.x; if (v > best) { best = v; bi = t; }
+                                    r = fmaxf(x.y, 0.f); v = r * r * im.y; if (v > best) { best = v; bi = t + 1; }
+                                    r = fmaxf(x.z, 0.f); v = r * r * im.z; if (v > best) { best = v; bi = t + 2; }
+                                    r = fmaxf(x.w, 0.f); v = r * r * im.w; if (v > best) { best = v; bi = t + 3; }
                                 }
                             }
                         }
                     }
-                    npend = 0;
-                    return;
+                    touched = true;
+                    k = two ? k2 + 1 : k + 1;
                 }
-                for (int tb = 0; tb < T; tb += 32 * kPerLane) {
-                    float v0[kPerLane], v1[kPerLane], bv[kPerLane];
-#pragma unroll
-                    for (int j = 0; j < kPerLane; ++j) {
-                        const int t = tb + lane + 32 * j;
-                        const bool ok = t < T;
-                        v0[j] = ok ? __ldg(c0 + t) : 0.f;
-                        v1[j] = (ok && two) ? __ldg(c1 + t) : 0.f;
-                        bv[j] = ok ? br[t] : 0.f;
-                    }
-#pragma unroll
-                    for (int j = 0; j < kPerLane; ++j) {
-                        const int t = tb + lane + 32 * j;
-                        if (t < T) {
-                            float x = fmaf(-a0s, v0[j], bv[j]);
-                            if (two) x = fmaf(-a1s, v1[j], x);
+            } else {
+                // general shapes: scan the 2nt+1 neighbours, scalar rows
+                int n_sp = 0;
+                for (int e0 = 0; e0 < L2; e0 += 32) {
+                    const int e = e0 + lane;
+                    n_sp += __popc(__ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0));
+                }
+                int done = 0;
+                for (int e0 = 0; e0 < L2 && n_sp > 0; e0 += 32) {
+                    const int e = e0 + lane;
+                    unsigned m = __ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0);
+                    while (m) {
+                        const int ee = e0 + __ffs(m) - 1;
+                        m &= m - 1;
+                        ++done;
+                        const bool last = done == n_sp;
+                        const float a = s_amp[i0 + ee];
+                        const float* c = ctcP + ((int64_t)s_t[i0 + ee] * L2 + (2 * nt - ee)) * T;
+                        for (int t = lane; t < T; t += 32) {
+                            const float x = fmaf(-a, __ldg(c + t), br[t]);
                             br[t] = x;
                             if (last) {
                                 const float r = fmaxf(x, 0.f);
@@ -311,32 +353,11 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                                 if (v > best) { best = v; bi = t; }
                             }
                         }
+                        touched = true;
                     }
-                }
-                npend = 0;
-            };
-            for (int e0 = 0; e0 < L2; e0 += 32) {
-                const int e = e0 + lane;
-                unsigned m = __ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0);
-                while (m) {
-                    const int ee = e0 + __ffs(m) - 1;
-                    m &= m - 1;
-                    ++done;
-                    if (npend == 0) {
-                        t0s = s_t[i0 + ee];
-                        a0s = s_amp[i0 + ee];
-                        l0s = 2 * nt - ee;                    // = wp - w + nt
-                        npend = 1;
-                    } else {
-                        t1s = s_t[i0 + ee];
-                        a1s = s_amp[i0 + ee];
-                        l1s = 2 * nt - ee;
-                        npend = 2;
-                    }
-                    if (npend == 2 || done == n_sp) flush(done == n_sp);
                 }
             }
-            finish_sample(wp, best, bi);
+            if (touched) finish_sample(wp, best, bi);
         }
         n_total += total;
         group_barrier<G>();   // cfmax of the changed samples is read by the neighbours in B1
