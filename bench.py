@@ -17,6 +17,11 @@ PC features.
 
 ``--impl reference`` times the CPU oracle port (the reference's Kilosort CPU path restated)
 on the same workload.
+
+``--path tc`` measures the reference's other sorter, threshold crossing, instead: 384 channels of
+raw int16 at 30 kHz, one step = one push of ``--tc-rows`` rows (20 s, 461 MB, larger than L2)
+tested against 3 x the per-channel median; same JSON keys, roofline of the count kernel (2 bytes
+read per channel-sample).
 """
 from __future__ import annotations
 
@@ -52,6 +57,9 @@ def args_():
     ap.add_argument("--cpu-sample", type=int, default=6, help="batches timed on the CPU oracle")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--match-variant", type=int, default=0, help="0 auto, 1 scores in L2, 2 scores in SMEM")
+    ap.add_argument("--path", default="sort", choices=["sort", "tc"],
+                    help="sort = template matching (default); tc = threshold crossing")
+    ap.add_argument("--tc-rows", type=int, default=600_000, help="rows per threshold-crossing push")
     return ap.parse_args()
 
 
@@ -376,8 +384,149 @@ def run_gpu(a):
     return 0
 
 
+# -------------------------------------------------------------------------------------------
+# threshold crossing
+# -------------------------------------------------------------------------------------------
+TC_METRIC = "ch*samples/s (threshold crossing, events identical to the reference's test)"
+TC_CHANNELS, TC_THRESHOLD = 384, 3.0
+
+
+def tc_dataset(rows: int):
+    from livespikesorter_gb300 import synth
+    data = synth.threshold_recording(2 * rows, TC_CHANNELS, seed=1)
+    from oracle import tc_oracle  # calibration of the constants the detector is built with
+    means, medians = tc_oracle.calibrate(data[:30000])
+    return data, means, medians
+
+
+def tc_config(a):
+    return {"workload": f"threshold crossing, {TC_CHANNELS} ch x 30 kHz raw int16, pushes of {a.tc_rows} rows "
+                        f"({a.tc_rows / 30000:.0f} s), threshold {TC_THRESHOLD} x per-channel median",
+            "channels": TC_CHANNELS, "rows_per_push": a.tc_rows, "threshold_std": TC_THRESHOLD,
+            "l2": "each push reads a fresh 461 MB slice (two slices alternate), larger than the 129 MB L2",
+            "parallelism": "single"}
+
+
+def tc_cpu_rate(data, means, medians, rows=30000, reps=3):
+    from oracle import tc_oracle
+    sample = data[:rows]
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        tc_oracle.threshold_crossings(sample, means, medians, TC_THRESHOLD)
+        times.append(time.perf_counter() - t0)
+    return rows * TC_CHANNELS / float(np.median(times)), times
+
+
+def run_tc_reference(a):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    data, means, medians = tc_dataset(a.tc_rows)
+    rows = min(a.tc_rows, 60000)
+    times = []
+    from oracle import tc_oracle
+    for i in range(a.warmup + a.steps):
+        t0 = time.perf_counter()
+        tc_oracle.threshold_crossings(data[:rows], means, medians, TC_THRESHOLD)
+        if i >= a.warmup:
+            times.append(time.perf_counter() - t0)
+    rate = rows * TC_CHANNELS / float(np.mean(times))
+    line = {"metric": TC_METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
+            "data": "synthetic (seeded generator)", "config": tc_config(a),
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"{rows} rows x {TC_CHANNELS} ch per step through the numpy oracle"},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_tc_gpu(a):
+    import torch
+    from livespikesorter_gb300 import threshold
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    n = a.tc_rows
+    C = TC_CHANNELS
+    data, means, medians = tc_dataset(n)
+    d_data = torch.from_numpy(data).to(f"cuda:{dev}")
+    base = d_data.data_ptr()
+    tc = threshold.ThresholdCrossing(means, medians, TC_THRESHOLD, device=dev, max_rows=n, profile=1)
+
+    def step(i):
+        tc.push_device(base + (i % 2) * n * C * 2, n, first_row_sample=(i % 2) * n)
+
+    for i in range(a.warmup):
+        step(i)
+    ev_warm = tc.poll_all()
+    t_base, k_base = tc.stage_times()
+    torch.cuda.synchronize(dev)
+    # each step: one push of device-resident rows, then its events read back through lss_tc_poll;
+    # value = rows x channels / the device time of the push's kernels (CUDA events on the
+    # detector's stream around count, offsets, emit and the copy to host memory); the wall time of
+    # the same loop, host event reads included, is reported beside it
+    n_events = 0
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        for i in range(a.steps):
+            step(a.warmup + i)
+            n_events += len(tc.poll(cap=n * C // 16))
+        wall = time.perf_counter() - t0
+    n_events += len(tc.poll_all())
+    t_all, k_all = tc.stage_times()
+    stage = {k: (t_all[k] - t_base[k]) / max(1, k_all - k_base) for k in t_all}
+    ms = sum(stage[k] for k in ("count", "offsets", "emit", "d2h")) * a.steps
+    launches = tc.kernel_launches() * a.steps
+    value = a.steps * n * C / (ms / 1e3)
+    hbm, _, src = peaks()
+    count_bytes = 2.0 * n * C
+    roof = {"kernel": "tc_count_kernel", "bound": "hbm", "achieved": count_bytes / 1e9 / (stage["count"] / 1e3),
+            "peak": hbm, "unit": "GB/s", "peak_source": src, "traffic": None, "ms_per_launch": stage["count"],
+            "stage_ms_per_launch": stage,
+            "algorithmic_bytes_per_launch": count_bytes}
+    roof["frac"] = roof["achieved"] / hbm
+    tc.close()
+    del d_data
+
+    # end to end: pinned host rows -> lss_tc_push -> lss_tc_poll
+    tc2 = threshold.ThresholdCrossing(means, medians, TC_THRESHOLD, device=dev, max_rows=n)
+    hdata = torch.from_numpy(data).pin_memory().numpy()
+    for i in range(a.warmup):
+        tc2.push(hdata[(i % 2) * n:(i % 2 + 1) * n], (i % 2) * n)
+    tc2.poll_all()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    n_ev2 = 0
+    for i in range(a.steps):
+        tc2.push(hdata[(i % 2) * n:(i % 2 + 1) * n], (i % 2) * n)
+        n_ev2 += len(tc2.poll_all())
+    e2e_s = time.perf_counter() - t0
+    tc2.close()
+    e2e = {"value": a.steps * n * C / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * C * 2,
+           "d2h_bytes_per_step": int(16 * n_ev2 / a.steps),
+           "path": "lss_tc_push + lss_tc_poll from pinned host int16 rows"}
+    cpu = None
+    if not a.no_cpu:
+        rate, times = tc_cpu_rate(data, means, medians)
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"30000 rows x {C} ch through the numpy oracle (float32 subtract, double compare, "
+                         f"channel-major order), median of {len(times)}"}
+    line = {"metric": TC_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int16", "data": "synthetic (seeded generator)", "config": tc_config(a), "e2e": e2e,
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": launches,
+            "events_per_push": n_events / a.steps, "warmup_events": len(ev_warm),
+            "value_basis": "device time of the four kernels per push (CUDA events on the detector's stream)",
+            "wall_ms_per_step_with_event_reads": 1e3 * wall / a.steps}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     a = args_()
+    if a.path == "tc":
+        return run_tc_reference(a) if a.impl == "reference" else run_tc_gpu(a)
     if a.impl == "reference":
         return run_reference(a)
     return run_gpu(a)

@@ -63,6 +63,10 @@ struct InputParameters {
     int iMaxIts = 50;
     int iGroupBatches = 1;
     int iChannelsIn = 0;             // row width delivered by the socket (0 = oss_input channels)
+    // ThresholdCrossing (iSorterType 1): channels per row (ThresholdCrossing.cpp:26 reads them
+    // from iNumTemplates) and the threshold in units of the per-channel median (fThresholdStd)
+    int iNumTemplates = 0;
+    float fThresholdStd = 3.f;
 };
 
 class SorterError : public std::runtime_error {

@@ -59,7 +59,7 @@ static T* dev_upload(const std::vector<T>& v, int64_t& tally, cudaStream_t s) {
 
 // memcpy split across threads for large host copies (pinned staging fills at several GB/s per
 // core; one thread alone is the bottleneck of the host path for multi-MB groups)
-static void par_memcpy(void* dst, const void* src, size_t bytes) {
+void par_memcpy(void* dst, const void* src, size_t bytes) {
     constexpr size_t kChunk = 4u << 20;
     const size_t nthr = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency() / 2), 16);
     if (bytes < 2 * kChunk || nthr < 2) {

@@ -1,4 +1,6 @@
-"""Python mirror of the sorter's C ABI (``include/lss_gb300.h``) over ctypes.
+"""Python mirror of the sorter's C ABI (``include/lss_gb300.h``) over ctypes.  The library's
+threshold-crossing functions (``include/lss_threshold.h``) are declared here too and wrapped in
+``threshold.py``.
 
 ``OnlineSorter`` follows the reference's sorter surface (src/SpikeSorter/OnlineSpikesV2.h:29-34):
 construct it on an ``oss_input/`` directory, push int16 samples, and poll the sorted spikes.
@@ -72,6 +74,23 @@ _SIGS = {
                                      ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p,
                                      ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_void_p]),
 }
+# include/lss_threshold.h (threshold-crossing detector; Python side in threshold.py)
+_SIGS.update({
+    "lss_tc_default_params": (ct.c_int, [ct.c_void_p]),
+    "lss_tc_int_thresholds": (ct.c_int, [ct.c_int32, ct.c_void_p, ct.c_void_p, ct.c_float, ct.c_void_p]),
+    "lss_tc_calibrate": (ct.c_int, [ct.c_void_p, ct.c_int64, ct.c_int32, ct.c_void_p, ct.c_void_p]),
+    "lss_tc_open": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, _P(ct.c_void_p)]),
+    "lss_tc_push": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int64]),
+    "lss_tc_push_device": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int64]),
+    "lss_tc_poll": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, _P(ct.c_int64)]),
+    "lss_tc_pending": (ct.c_int, [ct.c_void_p, _P(ct.c_int64)]),
+    "lss_tc_thresholds": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32]),
+    "lss_tc_cuda_stream": (ct.c_int, [ct.c_void_p, _P(ct.c_void_p)]),
+    "lss_tc_kernel_launches": (ct.c_int, [ct.c_void_p, _P(ct.c_int64)]),
+    "lss_tc_stage_times": (ct.c_int, [ct.c_void_p, _P(ct.c_double), ct.c_int32, _P(ct.c_int64)]),
+    "lss_tc_close": (ct.c_int, [ct.c_void_p]),
+    "lss_tc_last_error": (ct.c_char_p, [ct.c_void_p]),
+})
 STAGES = ("h2d", "colsum", "car", "highpass", "whiten", "basis_conv", "project", "match", "features", "d2h")
 
 _lib = None
@@ -239,8 +258,10 @@ class OnlineSorter:
 
 
 def header_functions(header=None):
-    """Names of the functions declared in include/lss_gb300.h."""
+    """Names of the functions declared in the C headers (include/*.h, or the one given)."""
     import re
-    h = Path(header) if header else _PKG.parent / "include" / "lss_gb300.h"
-    txt = h.read_text()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(lss_\w+)\s*\(", txt, re.M)))
+    hs = [Path(header)] if header else sorted((_PKG.parent / "include").glob("*.h"))
+    names = set()
+    for h in hs:
+        names |= set(re.findall(r"^\s*(?:int|const char\*)\s+(lss_\w+)\s*\(", h.read_text(), re.M))
+    return sorted(names)

@@ -469,3 +469,31 @@ def cached_dataset(cfg: SynthConfig, root=None):
         oss = build_oss_input(rec)
         write_oss_input(oss, d / "oss_input")
     return d / "oss_input", rec.data, rec
+
+
+def threshold_recording(n_rows: int, n_chan: int = 384, seed: int = 0, rate_hz: float = 40.0,
+                        fs: float = 30000.0, chunk: int = 65536) -> np.ndarray:
+    """Seeded raw int16 rows [n_rows][n_chan] for the threshold-crossing detector: a per-channel
+    DC offset (SD 20) and Gaussian noise (SD 5-12 counts, unfiltered like the reference's input),
+    plus negative biphasic spikes (peak lognormal around 90 counts) on five neighbouring channels,
+    rate_hz per group of 8 channels.  Generated chunk by chunk to bound host memory."""
+    rng = np.random.default_rng(seed)
+    dc = rng.normal(0, 20, n_chan)
+    sd = rng.uniform(5, 12, n_chan)
+    out = np.empty((n_rows, n_chan), np.int16)
+    L = 30
+    wave = (-np.exp(-0.5 * ((np.arange(L) - 10) / 2.5) ** 2)
+            + 0.35 * np.exp(-0.5 * ((np.arange(L) - 18) / 4.0) ** 2))
+    spread = np.exp(-0.5 * np.arange(-2, 3) ** 2)
+    for a in range(0, n_rows, chunk):
+        b = min(n_rows, a + chunk)
+        x = rng.standard_normal((b - a + L, n_chan), dtype=np.float32) * sd[None, :] + dc[None, :]
+        n_sp = rng.poisson(rate_hz * n_chan / 8 * (b - a) / fs)
+        t0 = rng.integers(0, b - a, n_sp)
+        c0 = rng.integers(0, n_chan, n_sp)
+        amp = rng.lognormal(np.log(90.0), 0.4, n_sp)
+        for t, c, am in zip(t0, c0, amp):
+            lo, hi = max(0, c - 2), min(n_chan, c + 3)
+            x[t:t + L, lo:hi] += (am * wave)[:, None] * spread[lo - c + 2:hi - c + 2][None, :]
+        out[a:b] = np.clip(np.rint(x[:b - a]), -32768, 32767).astype(np.int16)
+    return out
