@@ -41,9 +41,9 @@ extern thread_local std::string g_handleless_error;
 namespace lss {
 namespace tc {
 
-constexpr int kKeep = 64;            // crossings a unit keeps from the count pass
+constexpr int kKeep = 32;            // crossings a unit keeps from the count pass
 constexpr int kUnitsPerCta = 512;    // R x G <= this (threads per CTA)
-constexpr int kMinSlab = 16, kMaxSlab = 128;   // <= 1024 channel-samples per unit
+constexpr int kMinSlab = 16, kMaxSlab = 32;    // <= 256 channel-samples per unit
 constexpr int64_t kFillUnits = 152LL * 1024;   // units that fill the GPU (152 SMs x 1024 threads)
 constexpr int kSlots = 3;
 
@@ -92,61 +92,114 @@ __device__ __forceinline__ int unpack_r(uint32_t e) { return (int)(e >> 19); }
 __device__ __forceinline__ int unpack_k(uint32_t e) { return (int)((e >> 16) & 7u); }
 __device__ __forceinline__ int unpack_x(uint32_t e) { return (int)(int16_t)(uint16_t)(e & 0xffffu); }
 
-template <int V>
-__global__ void __launch_bounds__(kUnitsPerCta, 1)
-tc_count_kernel(const int16_t* __restrict__ rows, int64_t n_rows, int C, int G, int S, int R, int64_t nslabs,
-                const int* __restrict__ thr, uint32_t* __restrict__ ent, int* __restrict__ ucnt,
-                int* __restrict__ ctot) {
-    extern __shared__ int s_cnt[];   // [R][C]
+// bit k set when channel k of the 8 int16 in v is <= its threshold (t: thresholds clamped to
+// int16, en: 0xffff where a channel can cross at all, 0 where its threshold is below -32768)
+__device__ __forceinline__ unsigned cross_mask8(const uint4& v, const uint4& t, const uint4& en) {
+    const unsigned m0 = __vcmples2(v.x, t.x) & en.x, m1 = __vcmples2(v.y, t.y) & en.y;
+    const unsigned m2 = __vcmples2(v.z, t.z) & en.z, m3 = __vcmples2(v.w, t.w) & en.w;
+    return (m0 & 1u) | ((m0 >> 15) & 2u) | ((m1 & 1u) << 2) | ((m1 >> 13) & 8u) | ((m2 & 1u) << 4) |
+           ((m2 >> 11) & 32u) | ((m3 & 1u) << 6) | ((m3 >> 9) & 128u);
+}
+
+// count pass, 8 channels per thread: four packed compares per row, the rare crossings recorded on
+// a side path; per-channel CTA totals by shared-memory atomics
+__global__ void __launch_bounds__(kUnitsPerCta, 2)
+tc_count8_kernel(const int16_t* __restrict__ rows, int64_t n_rows, int C, int G, int S, int R, int64_t nslabs,
+                 const int16_t* __restrict__ thr16, const uint16_t* __restrict__ en16, uint32_t* __restrict__ ent,
+                 int* __restrict__ ucnt, int* __restrict__ ctot) {
+    extern __shared__ int s_tot[];   // [C]
     const int tid = threadIdx.x;
+    for (int c = tid; c < C; c += blockDim.x) s_tot[c] = 0;
+    __syncthreads();
     const int rl = tid / G, g = tid - rl * G;
     const int64_t slab = (int64_t)blockIdx.x * R + rl;
-    int cnt[V];
-#pragma unroll
-    for (int k = 0; k < V; ++k) cnt[k] = 0;
     if (slab < nslabs) {
-        int th[V];
-#pragma unroll
-        for (int k = 0; k < V; ++k) th[k] = __ldg(thr + g * V + k);
+        const uint4 t = __ldg(reinterpret_cast<const uint4*>(thr16) + g);
+        const uint4 en = __ldg(reinterpret_cast<const uint4*>(en16) + g);
         const int64_t r0 = slab * S;
         const int nr = (int)min((int64_t)S, n_rows - r0);
-        const int16_t* p = rows + r0 * C + g * V;
+        const uint4* p = reinterpret_cast<const uint4*>(rows + r0 * C) + g;
+        const int64_t stride = C / 8;   // uint4 per row
         const int64_t u = slab * G + g;
         uint32_t* e = ent + u * kKeep;
         int kept = 0;
-        auto test = [&](const Row<V>& row, int r) {
-#pragma unroll
-            for (int k = 0; k < V; ++k) {
-                const int x = row.at(k);
-                if (x <= th[k]) {
-                    if (kept < kKeep) e[kept] = pack(r, k, x);
-                    ++kept;
-                    ++cnt[k];
-                }
+        auto record = [&](const uint4& v, unsigned m, int r) {
+            while (m) {
+                const int k = __ffs(m) - 1;
+                m &= m - 1;
+                const unsigned w = k < 2 ? v.x : k < 4 ? v.y : k < 6 ? v.z : v.w;
+                const int x = (int)(int16_t)(uint16_t)((k & 1) ? (w >> 16) : (w & 0xffffu));
+                atomicAdd(&s_tot[g * 8 + k], 1);
+                if (kept < kKeep) e[kept] = pack(r, k, x);
+                ++kept;
             }
         };
         int r = 0;
         for (; r + 8 <= nr; r += 8) {
-            Row<V> v[8];
+            uint4 v[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) v[j].load(p + (int64_t)(r + j) * C);
+            for (int j = 0; j < 8; ++j) v[j] = __ldg(p + (int64_t)(r + j) * stride);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) test(v[j], r + j);
+            for (int j = 0; j < 8; ++j) {
+                const unsigned m = cross_mask8(v[j], t, en);
+                if (m) record(v[j], m, r + j);
+            }
         }
         for (; r < nr; ++r) {
-            Row<V> v;
-            v.load(p + (int64_t)r * C);
-            test(v, r);
+            const uint4 v = __ldg(p + (int64_t)r * stride);
+            const unsigned m = cross_mask8(v, t, en);
+            if (m) record(v, m, r);
         }
         ucnt[u] = kept;
     }
+    __syncthreads();
+    for (int c = tid; c < C; c += blockDim.x) ctot[(int64_t)blockIdx.x * C + c] = s_tot[c];
+}
+
+// count pass, one channel per thread (rows not 16-byte aligned or C not a multiple of 8)
+__global__ void __launch_bounds__(kUnitsPerCta, 2)
+tc_count1_kernel(const int16_t* __restrict__ rows, int64_t n_rows, int C, int G, int S, int R, int64_t nslabs,
+                 const int* __restrict__ thr, uint32_t* __restrict__ ent, int* __restrict__ ucnt,
+                 int* __restrict__ ctot) {
+    extern __shared__ int s_tot[];   // [C]
+    const int tid = threadIdx.x;
+    const int rl = tid / G, g = tid - rl * G;
+    const int64_t slab = (int64_t)blockIdx.x * R + rl;
+    int cnt = 0;
+    if (slab < nslabs) {
+        const int th = __ldg(thr + g);
+        const int64_t r0 = slab * S;
+        const int nr = (int)min((int64_t)S, n_rows - r0);
+        const int16_t* p = rows + r0 * C + g;
+        const int64_t u = slab * G + g;
+        uint32_t* e = ent + u * kKeep;
+        int r = 0;
+        for (; r + 8 <= nr; r += 8) {
+            int x[8];
 #pragma unroll
-    for (int k = 0; k < V; ++k) s_cnt[rl * C + g * V + k] = cnt[k];
+            for (int j = 0; j < 8; ++j) x[j] = __ldg(p + (int64_t)(r + j) * C);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (x[j] <= th) {
+                    if (cnt < kKeep) e[cnt] = pack(r + j, 0, x[j]);
+                    ++cnt;
+                }
+        }
+        for (; r < nr; ++r) {
+            const int x = __ldg(p + (int64_t)r * C);
+            if (x <= th) {
+                if (cnt < kKeep) e[cnt] = pack(r, 0, x);
+                ++cnt;
+            }
+        }
+        ucnt[u] = cnt;
+    }
+    s_tot[rl * C + g] = cnt;   // [R][C] here: one channel per thread
     __syncthreads();
     for (int c = tid; c < C; c += blockDim.x) {
-        int s = 0;
-        for (int i = 0; i < R; ++i) s += s_cnt[i * C + c];
-        ctot[(int64_t)blockIdx.x * C + c] = s;
+        int sum = 0;
+        for (int i = 0; i < R; ++i) sum += s_tot[i * C + c];
+        ctot[(int64_t)blockIdx.x * C + c] = sum;
     }
 }
 
@@ -309,8 +362,17 @@ __global__ void __launch_bounds__(256) tc_copy_kernel(const int4* __restrict__ s
     const long long t = *total;
     const int64_t n = min((int64_t)t, cap);
     if (blockIdx.x == 0 && threadIdx.x == 0) *total_host = t;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        dst[i] = __ldcs(src + i);
+    // four records per thread per round, loads ahead of the stores
+    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * step < n; i += 4 * step) {
+        int4 v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = __ldcs(src + i + j * step);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dst[i + j * step] = v[j];
+    }
+    for (; i < n; i += step) dst[i] = __ldcs(src + i);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -375,8 +437,12 @@ struct Handle {
     lss_tc_params prm{};
     cudaStream_t st = nullptr;
     std::vector<int32_t> ithr;
+    std::vector<int16_t> thr16;
+    std::vector<uint16_t> en16;
     std::vector<float> means;
     int* d_thr = nullptr;
+    int16_t* d_thr16 = nullptr;     // thresholds clamped to int16 and the channels that can cross
+    uint16_t* d_en16 = nullptr;
     float* d_means = nullptr;
     int64_t ucap = 0, ctacap = 0, cap = 0;
     Slot slots[kSlots];
@@ -422,9 +488,19 @@ struct Handle {
             ucap = std::max(ucap, units);
             ctacap = std::max<int64_t>(ctacap, (units / gm.G + gm.R - 1) / gm.R + 1);
         }
+        thr16.resize(C);
+        en16.resize(C);
+        for (int c = 0; c < C; ++c) {
+            thr16[c] = (int16_t)std::max(-32768, ithr[c]);
+            en16[c] = ithr[c] >= -32768 ? 0xffffu : 0u;
+        }
         TC_CUDA(cudaMalloc(&d_thr, sizeof(int) * C));
+        TC_CUDA(cudaMalloc(&d_thr16, sizeof(int16_t) * C));
+        TC_CUDA(cudaMalloc(&d_en16, sizeof(uint16_t) * C));
         TC_CUDA(cudaMalloc(&d_means, sizeof(float) * C));
         TC_CUDA(cudaMemcpyAsync(d_thr, ithr.data(), sizeof(int) * C, cudaMemcpyHostToDevice, st));
+        TC_CUDA(cudaMemcpyAsync(d_thr16, thr16.data(), sizeof(int16_t) * C, cudaMemcpyHostToDevice, st));
+        TC_CUDA(cudaMemcpyAsync(d_en16, en16.data(), sizeof(uint16_t) * C, cudaMemcpyHostToDevice, st));
         TC_CUDA(cudaMemcpyAsync(d_means, means.data(), sizeof(float) * C, cudaMemcpyHostToDevice, st));
         for (Slot& s : slots) {
             TC_CUDA(cudaMalloc(&s.d_ent, sizeof(uint32_t) * ucap * kKeep));
@@ -464,6 +540,8 @@ struct Handle {
                 if (e) cudaEventDestroy(e);
         }
         cudaFree(d_thr);
+        cudaFree(d_thr16);
+        cudaFree(d_en16);
         cudaFree(d_means);
         if (st) cudaStreamDestroy(st);
         st = nullptr;
@@ -528,14 +606,14 @@ struct Handle {
         int64_t got = 0;
         if (spill_head < spill.size()) {
             const int64_t k = std::min<int64_t>(cap_out, (int64_t)(spill.size() - spill_head));
-            std::memcpy(out, spill.data() + spill_head, sizeof(lss_tc_event) * (size_t)k);
+            par_memcpy(out, spill.data() + spill_head, sizeof(lss_tc_event) * (size_t)k);
             spill_head += (size_t)k;
             got += k;
         }
         while (got < cap_out && !ready.empty()) {
             Slot& s = slots[ready.front()];
             const int64_t k = std::min(cap_out - got, s.n - s.off);
-            if (k > 0) std::memcpy(out + got, s.h_ev + s.off, sizeof(lss_tc_event) * (size_t)k);
+            if (k > 0) par_memcpy(out + got, s.h_ev + s.off, sizeof(lss_tc_event) * (size_t)k);
             s.off += k;
             got += k;
             if (s.off == s.n) {
@@ -553,13 +631,13 @@ struct Handle {
         const Geometry gm = geometry(C, n_rows, V);
         if (gm.nslabs * gm.G > ucap || gm.nctas > ctacap) throw Error{LSS_ERR_INTERNAL, "scratch too small"};
         const int threads = gm.R * gm.G;
-        const size_t sm_count = sizeof(int) * (size_t)gm.R * C;
-        const size_t sm_emit = sm_count + sizeof(int) * C;
+        const size_t sm_slabs = sizeof(int) * (size_t)gm.R * C;
+        const size_t sm_emit = sm_slabs + sizeof(int) * C;
         if (V == 8) {
-            tc_count_kernel<8><<<(unsigned)gm.nctas, threads, sm_count, st>>>(
-                d_rows, n_rows, C, gm.G, gm.S, gm.R, gm.nslabs, d_thr, s.d_ent, s.d_ucnt, s.d_ctot);
+            tc_count8_kernel<<<(unsigned)gm.nctas, threads, sizeof(int) * C, st>>>(
+                d_rows, n_rows, C, gm.G, gm.S, gm.R, gm.nslabs, d_thr16, d_en16, s.d_ent, s.d_ucnt, s.d_ctot);
         } else {
-            tc_count_kernel<1><<<(unsigned)gm.nctas, threads, sm_count, st>>>(
+            tc_count1_kernel<<<(unsigned)gm.nctas, threads, sm_slabs, st>>>(
                 d_rows, n_rows, C, gm.G, gm.S, gm.R, gm.nslabs, d_thr, s.d_ent, s.d_ucnt, s.d_ctot);
         }
         TC_CUDA(cudaGetLastError());

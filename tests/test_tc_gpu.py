@@ -88,7 +88,7 @@ def test_long_recording_single_push():
 
 
 def test_dense_units_reread_rows():
-    """Channels below threshold for hundreds of consecutive rows: units keep 64 crossings and
+    """Channels below threshold for hundreds of consecutive rows: units keep 32 crossings and
     must read their rows again to place the rest."""
     C, n = 64, 5000
     rows = recording(n, C, seed=4)
