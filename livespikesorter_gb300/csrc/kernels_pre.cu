@@ -57,6 +57,39 @@ __device__ __forceinline__ void tf32_split_(float x, float& hi, float& lo) {
 
 constexpr int kCarWarps = 8;
 
+// The k-th smallest of the warp's 32 * NJ keys (all lanes hold NJ; padding keys are 0xffffffff),
+// MSB first, one bit per pass.  The count of keys still matching the prefix is tracked, and once
+// it is one that key is the answer: after about log2(32 * NJ) passes for distinct values instead
+// of 32.  Ties simply run to bit 0.
+template <int NJ>
+__device__ __forceinline__ uint32_t warp_kth_key(const uint32_t (&key)[NJ], int k) {
+    uint32_t prefix = 0;
+    int alive = 32 * NJ;
+    for (int bit = 31; bit >= 0; --bit) {
+        const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
+        int cnt = 0;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) cnt += ((key[j] & hi_mask) == prefix) && !((key[j] >> bit) & 1u);
+        cnt = __reduce_add_sync(0xffffffffu, cnt);
+        if (k >= cnt) {
+            k -= cnt;
+            prefix |= (1u << bit);
+            alive -= cnt;
+        } else {
+            alive = cnt;
+        }
+        if (alive == 1) {
+            const uint32_t m = 0xffffffffu << bit;
+            uint32_t got = 0;
+#pragma unroll
+            for (int j = 0; j < NJ; ++j)
+                if ((key[j] & m) == prefix) got = key[j];
+            return __reduce_or_sync(0xffffffffu, got);
+        }
+    }
+    return prefix;
+}
+
 // NJ = channels per lane (C <= 32 * NJ), so the selection loop runs over live registers only
 template <int NJ>
 __global__ void __launch_bounds__(kCarWarps * 32)
@@ -86,22 +119,7 @@ car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* _
         }
     }
     // k-th smallest by MSB-first bit selection over order-preserving keys
-    uint32_t prefix = 0;
-    int k = (C - 1) >> 1;
-    for (int bit = 31; bit >= 0; --bit) {
-        const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
-        int cnt = 0;
-#pragma unroll
-        for (int j = 0; j < kMaxChanPerLane; ++j) {
-            if (j < nj) cnt += ((key[j] & hi_mask) == prefix) && !((key[j] >> bit) & 1u);
-        }
-        cnt = __reduce_add_sync(0xffffffffu, cnt);
-        if (k >= cnt) {
-            k -= cnt;
-            prefix |= (1u << bit);
-        }
-    }
-    const float med = key2f(prefix);
+    const float med = key2f(warp_kth_key<kMaxChanPerLane>(key, (C - 1) >> 1));
     const int rows = W + L + R;
     float* xb = Xw + (int64_t)b * rows * C;
     const bool wrapL = (w >= W - L);   // also lands in the left pad
@@ -154,20 +172,7 @@ car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t*
                 key[j] = 0xffffffffu;
             }
         }
-        uint32_t prefix = 0;
-        int k = (C - 1) >> 1;
-        for (int bit = 31; bit >= 0; --bit) {
-            const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
-            int cnt = 0;
-#pragma unroll
-            for (int j = 0; j < NJ; ++j) cnt += ((key[j] & hi_mask) == prefix) && !((key[j] >> bit) & 1u);
-            cnt = __reduce_add_sync(0xffffffffu, cnt);
-            if (k >= cnt) {
-                k -= cnt;
-                prefix |= (1u << bit);
-            }
-        }
-        const float med = key2f(prefix);
+        const float med = key2f(warp_kth_key<NJ>(key, (C - 1) >> 1));
 #pragma unroll
         for (int j = 0; j < NJ; ++j) {
             const int c = lane + 32 * j;
@@ -316,57 +321,83 @@ void launch_highpass(const float* Xw, int C, int W, int L, int R, const float* t
 constexpr int kConvRows = 8;        // rows per thread
 constexpr int kConvMaxK = 8;
 
-template <int NT_, int K_>
-struct BasisParam {
-    float w[K_ * NT_];
-};
+// two fp32 fused multiply-adds per instruction: d.{x,y} = a.{x,y} * b.{x,y} + d.{x,y}, each
+// rounded like fmaf
+__device__ __forceinline__ void fma2(unsigned long long& d, unsigned long long a, unsigned long long b) {
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(d) : "l"(a), "l"(b));
+}
+__device__ __forceinline__ unsigned long long dup2(float x) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(x));
+    return r;
+}
 
-// Specialised for the common (nt, K): the basis lives in the kernel parameter bank so every
-// multiply-add takes it as an immediate constant operand.
+// Specialised for the common (nt, K) with K even: the basis sits in shared memory as [nt][K] (pairs
+// of components one 8-byte load apart), each thread owns one channel and kConvRows rows, and every
+// tap multiplies the kConvRows inputs it meets in packed pairs (fma.rn.f32x2, two fmaf per
+// instruction).  Taps are applied in ascending order, as in basis_conv_generic.
 template <int NT_, int K_>
 __global__ void __launch_bounds__(128)
-basis_conv_fixed(const float* __restrict__ Z, int C, int W, BasisParam<NT_, K_> bp, float* __restrict__ Bpc,
-                 float* __restrict__ Blo) {
+basis_conv_x2(const float* __restrict__ Z, int C, int W, const float* __restrict__ wPCA, float* __restrict__ Bpc,
+              float* __restrict__ Blo) {
+    static_assert(K_ % 2 == 0, "pairs of components");
+    constexpr int KP = K_ / 2;
+    constexpr int R = kConvRows;
+    constexpr int H = NT_ / 2;
+    __shared__ __align__(16) float s_w[NT_ * K_];   // [m][k]
+    for (int i = threadIdx.x; i < NT_ * K_; i += blockDim.x) {
+        const int m = i / K_, k = i - m * K_;
+        s_w[i] = __ldg(wPCA + k * NT_ + m);
+    }
+    __syncthreads();
     const int b = blockIdx.z;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const int w0 = blockIdx.y * kConvRows;
+    const int w0 = blockIdx.y * R;
     if (c >= C) return;
-    const float* zb = Z + (int64_t)b * W * C;
-    constexpr int H = NT_ / 2;
-    float acc[kConvRows][K_];
+    const float* zb = Z + (int64_t)b * W * C + c;
+    unsigned long long acc[R][KP];
 #pragma unroll
-    for (int r = 0; r < kConvRows; ++r)
+    for (int r = 0; r < R; ++r)
 #pragma unroll
-        for (int k = 0; k < K_; ++k) acc[r][k] = 0.f;
+        for (int j = 0; j < KP; ++j) acc[r][j] = 0ull;
+    unsigned long long xs[R + NT_ - 1];
 #pragma unroll
-    for (int u = 0; u < kConvRows + NT_ - 1; ++u) {
+    for (int u = 0; u < R + NT_ - 1; ++u) {
         const int row = w0 + u - H;
-        const float x = (row >= 0 && row < W) ? __ldg(zb + (int64_t)row * C + c) : 0.f;
+        xs[u] = dup2((row >= 0 && row < W) ? __ldg(zb + (int64_t)row * C) : 0.f);
+    }
+    const unsigned long long* wp = reinterpret_cast<const unsigned long long*>(s_w);
 #pragma unroll
-        for (int r = 0; r < kConvRows; ++r) {
-            const int m = u - r;
-            if (m >= 0 && m < NT_) {
+    for (int m = 0; m < NT_; ++m) {
+        unsigned long long wv[KP];
 #pragma unroll
-                for (int k = 0; k < K_; ++k) acc[r][k] = fmaf(x, bp.w[k * NT_ + m], acc[r][k]);
-            }
-        }
+        for (int j = 0; j < KP; ++j) wv[j] = wp[m * KP + j];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int j = 0; j < KP; ++j) fma2(acc[r][j], xs[m + r], wv[j]);
     }
     float* ob = Bpc + (int64_t)b * W * K_ * C;
     float* lb = Blo ? Blo + (int64_t)b * W * K_ * C : nullptr;
 #pragma unroll
-    for (int r = 0; r < kConvRows; ++r) {
+    for (int r = 0; r < R; ++r) {
         const int w = w0 + r;
         if (w < W) {
 #pragma unroll
-            for (int k = 0; k < K_; ++k) {
-                const int64_t o = ((int64_t)w * K_ + k) * C + c;
-                if (lb) {
-                    float h, l;
-                    tf32_split(acc[r][k], h, l);
-                    ob[o] = h;
-                    lb[o] = l;
-                } else {
-                    ob[o] = acc[r][k];
+            for (int j = 0; j < KP; ++j) {
+                const float2 v = *reinterpret_cast<const float2*>(&acc[r][j]);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float a = h ? v.y : v.x;
+                    const int64_t o = ((int64_t)w * K_ + 2 * j + h) * C + c;
+                    if (lb) {
+                        float hi, lo;
+                        tf32_split(a, hi, lo);
+                        ob[o] = hi;
+                        lb[o] = lo;
+                    } else {
+                        ob[o] = a;
+                    }
                 }
             }
         }
@@ -427,10 +458,9 @@ basis_conv_generic(const float* __restrict__ Z, int C, int W, const float* __res
 void launch_basis_conv_host(const float* Z, int C, int W, const float* wPCA_dev, const float* wPCA_host, int K,
                             int nt, int nb, float* Bpc, cudaStream_t s, float* Blo) {
     dim3 grid((C + 127) / 128, (W + kConvRows - 1) / kConvRows, nb);
-    if (nt == 61 && K == 6 && wPCA_host) {
-        BasisParam<61, 6> bp;
-        for (int i = 0; i < 6 * 61; ++i) bp.w[i] = wPCA_host[i];
-        basis_conv_fixed<61, 6><<<grid, 128, 0, s>>>(Z, C, W, bp, Bpc, Blo);
+    (void)wPCA_host;
+    if (nt == 61 && K == 6) {
+        basis_conv_x2<61, 6><<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, Bpc, Blo);
     } else {
         basis_conv_generic<<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, K, nt, Bpc, Blo);
     }
