@@ -18,6 +18,12 @@ PC features.
 ``--impl reference`` times the CPU oracle port (the reference's Kilosort CPU path restated)
 on the same workload.
 
+``--serving`` measures several probe streams on one GPU at once (one handle and one host thread
+per stream, each handle on its own CUDA stream): eight streams of uneven size (96/192/384
+channels, 64-1000 templates, 750-3000-sample batches) paced at 30 kHz with +/-20 % jitter
+(per-batch push-to-spikes latency p50/p99), the same streams unpaced (aggregate ch*samples/s),
+and eight 384-channel / 500-template streams unpaced (aggregate, as a multiple of real time).
+
 ``--path tc`` measures the reference's other sorter, threshold crossing, instead: 384 channels of
 raw int16 at 30 kHz, one step = one push of ``--tc-rows`` rows (20 s, 461 MB, larger than L2)
 tested against 3 x the per-channel median; same JSON keys, roofline of the count kernel (2 bytes
@@ -60,6 +66,8 @@ def args_():
     ap.add_argument("--path", default="sort", choices=["sort", "tc"],
                     help="sort = template matching (default); tc = threshold crossing")
     ap.add_argument("--tc-rows", type=int, default=600_000, help="rows per threshold-crossing push")
+    ap.add_argument("--serving", action="store_true", help="several concurrent probe streams")
+    ap.add_argument("--serving-seconds", type=float, default=8.0, help="signal per stream")
     return ap.parse_args()
 
 
@@ -523,8 +531,121 @@ def run_tc_gpu(a):
     return 0
 
 
+# -------------------------------------------------------------------------------------------
+# serving: concurrent probe streams
+# -------------------------------------------------------------------------------------------
+SERVING_STREAMS = [  # (channels, templates, batch samples)
+    (384, 1000, 3000), (384, 500, 1500), (384, 250, 750), (192, 300, 1500),
+    (192, 128, 3000), (96, 64, 750), (96, 100, 1500), (384, 700, 2250)]
+
+
+def _serving_data(streams, seconds, seed0):
+    from livespikesorter_gb300 import synth
+    out = []
+    for i, (C, T, NT) in enumerate(streams):
+        cfg = synth.SynthConfig(n_chan=C, n_units=T, n_samples=int(seconds * 30000), drift_um=20.0,
+                                seed=seed0 + i)
+        d, data, _ = synth.cached_dataset(cfg)
+        out.append((d, data, NT))
+    return out
+
+
+def _run_streams(sets, paced: bool, jitter: float = 0.2, seed: int = 0):
+    """One thread per stream: push each batch (paced at 30 kHz with +/-jitter, or back to back),
+    then poll its spikes; returns per-batch latencies (ms), wall seconds and new samples x channels."""
+    from livespikesorter_gb300 import sorter
+    handles = [sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=1) for d, _, NT in sets]
+    for (d, data, NT), h in zip(sets, handles):   # warm-up: one window each
+        h.push(data[:NT + 2 * 61], 0)
+        h.poll_all()
+    lat = [[] for _ in sets]
+    work = [0] * len(sets)
+    errors = []
+    barrier = threading.Barrier(len(sets) + 1)
+
+    def run(i):
+        try:
+            d, data, NT = sets[i]
+            h = handles[i]
+            rng = np.random.default_rng(seed + i)
+            out = np.zeros(1 << 16, sorter.SPIKE_DTYPE)
+            p = NT + 2 * 61
+            barrier.wait()
+            t_next = time.perf_counter()
+            while p + NT <= data.shape[0]:
+                if paced:
+                    t_next += NT / 30000.0 * (1.0 + rng.uniform(-jitter, jitter))
+                    dt = t_next - time.perf_counter()
+                    if dt > 0:
+                        time.sleep(dt)
+                t1 = time.perf_counter()
+                h.push(data[p:p + NT])
+                h.poll(out=out)
+                lat[i].append(1e3 * (time.perf_counter() - t1))
+                work[i] += NT * data.shape[1]
+                p += NT
+        except Exception as e:
+            errors.append(repr(e))
+
+    th = [threading.Thread(target=run, args=(i,)) for i in range(len(sets))]
+    for t in th:
+        t.start()
+    barrier.wait()
+    t0 = time.perf_counter()
+    for t in th:
+        t.join()
+    wall = time.perf_counter() - t0
+    for h in handles:
+        h.close()
+    if errors:
+        raise RuntimeError(errors[0])
+    return lat, wall, work
+
+
+def run_serving(a):
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    t_start = time.perf_counter()
+    sets = _serving_data(SERVING_STREAMS, a.serving_seconds, seed0=100)
+    with ClockSampler(dev) as clk:
+        lat, wall, work = _run_streams(sets, paced=True)
+    all_lat = np.concatenate([np.asarray(x) for x in lat])
+    per_stream = [{"channels": C, "templates": T, "batch_samples": NT, "batches": len(l),
+                   "p50_ms": float(np.percentile(l, 50)), "p99_ms": float(np.percentile(l, 99)),
+                   "batch_ms_of_signal": 1e3 * NT / 30000.0}
+                  for (C, T, NT), l in zip(SERVING_STREAMS, lat)]
+    paced = {"p50_ms": float(np.percentile(all_lat, 50)), "p99_ms": float(np.percentile(all_lat, 99)),
+             "max_ms": float(all_lat.max()), "batches": int(all_lat.size),
+             "ch_samples_per_s": sum(work) / wall, "wall_s": wall, "streams": per_stream}
+    lat_u, wall_u, work_u = _run_streams(sets, paced=False)
+    lu = np.concatenate([np.asarray(x) for x in lat_u])
+    unpaced = {"ch_samples_per_s": sum(work_u) / wall_u, "realtime_factor": (sum(work_u) / wall_u) /
+               (30000.0 * sum(C for C, _, _ in SERVING_STREAMS)), "p50_ms": float(np.percentile(lu, 50)),
+               "p99_ms": float(np.percentile(lu, 99)), "wall_s": wall_u}
+    sets8 = _serving_data([(384, 500, 1500)] * 8, a.serving_seconds, seed0=200)
+    lat8, wall8, work8 = _run_streams(sets8, paced=False)
+    l8 = np.concatenate([np.asarray(x) for x in lat8])
+    eight = {"ch_samples_per_s": sum(work8) / wall8, "realtime_factor": (sum(work8) / wall8) / (8 * 384 * 30000.0),
+             "p50_ms": float(np.percentile(l8, 50)), "p99_ms": float(np.percentile(l8, 99)), "wall_s": wall8}
+    line = {"metric": "serving: p99 push-to-spikes latency per batch, 8 concurrent streams at 30 kHz pacing",
+            "value": paced["p99_ms"], "unit": "ms", "n_gpus": 1, "steps": int(all_lat.size), "warmup": 1,
+            "ms_per_step": paced["p50_ms"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded generator, shapes of the serving config)",
+            "config": {"workload": "8 probe streams (96/192/384 ch, 64-1000 templates, 750-3000-sample "
+                                   "batches), 30 kHz pacing +/-20 % jitter, one handle + host thread each",
+                       "streams": [list(x) for x in SERVING_STREAMS], "seconds_per_stream": a.serving_seconds,
+                       "parallelism": "single GPU, 8 CUDA streams"},
+            "paced": paced, "unpaced": unpaced, "eight_384ch_unpaced": eight, "clocks": clk.summary(),
+            "wall_s": time.perf_counter() - t_start}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     a = args_()
+    if a.serving:
+        return run_serving(a)
     if a.path == "tc":
         return run_tc_reference(a) if a.impl == "reference" else run_tc_gpu(a)
     if a.impl == "reference":

@@ -52,7 +52,8 @@ typedef struct lss_params {
     int32_t spike_cap;      /* per-batch spike buffer; 0 = automatic */
     int64_t mem_budget;     /* device bytes this handle may hold; 0 = no limit (admission check) */
     int32_t profile;        /* 1 = time every stage with CUDA events (lss_stage_times) */
-    int32_t match_variant;  /* 0 = automatic; 1 = scores in L2, 8-CTA clusters; 2 = scores in shared memory */
+    int32_t match_variant;  /* 0 = automatic; 1 = scores in L2, 8-CTA clusters; 2 = scores in shared memory;
+                               3 = scores in L2, 16-CTA clusters of 1024 threads (one CTA per SM) */
     int32_t gemm_path;      /* 0 = tensor cores (tcgen05, 3xTF32 = FP32 accuracy) where shapes allow; 1 = FP32 SIMT */
     int32_t reserved[3];
 } lss_params;

@@ -61,7 +61,7 @@ __host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, 
 }
 
 template <int G, bool SMEM_B, int NTHR>
-__global__ void __launch_bounds__(NTHR, SMEM_B ? 1 : 2)
+__global__ void __launch_bounds__(NTHR, (SMEM_B || NTHR > 512) ? 1 : 2)
 match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __restrict__ ctcP,
              const float* __restrict__ pre_wf, const float* __restrict__ nm, float th2, int W, int T, int C,
              int nt, int max_iters, MatchScratch sc, MatchOut out) {
@@ -458,7 +458,7 @@ static cudaError_t launch_match_cfg(float* Bt, float* Xres, const float* ctcP, c
                                     const MatchScratch& sc, const MatchOut& out, cudaStream_t s) {
     const size_t smem = match_smem_bytes(W, T, nt, G, SMEM_B);
     auto kern = match_kernel<G, SMEM_B, NTHR>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_limit((const void*)kern, smem);
     if (e != cudaSuccess) return e;
     if (G > 8) {
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -488,7 +488,7 @@ static int smem16_ok(int W, int T, int nt) {
     if (cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
     if (smem + 12288 > (size_t)maxopt) return 0;   // static shared memory and the driver reserve
     auto kern = match_kernel<16, true, kMatchThreadsSmem>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+    if (raise_smem_limit((const void*)kern, smem) != cudaSuccess ||
         cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
         cudaGetLastError();
         return 0;
@@ -512,28 +512,72 @@ static int smem16_ok(int W, int T, int nt) {
     return n;
 }
 
-int match_variant(int W, int T, int nt) {
+// Can a cluster of 16 CTAs of 1024 threads (scores in L2, one CTA per SM) run on this device?
+static int wide16_ok(int W, int T, int nt) {
+    if ((W + 15) / 16 > kMaxRoundsGlobal * kMatchThreadsWide) return 0;
+    const size_t smem = match_smem_bytes(W, T, nt, 16, false);
+    auto kern = match_kernel<16, false, kMatchThreadsWide>;
+    if (raise_smem_limit((const void*)kern, smem) != cudaSuccess ||
+        cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16, 1, 1);
+    cfg.blockDim = dim3(kMatchThreadsWide, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+// 16 when the shared-memory variant fits, else 8; wide = the 16-CTA / 1024-thread global variant fits
+int match_variant(int W, int T, int nt, bool* wide) {
     static thread_local int cW = -1, cT = -1, cnt = -1, cres = 0;
+    static thread_local bool cwide = false;
     if (W != cW || T != cT || nt != cnt) {
         cres = smem16_ok(W, T, nt) > 0 ? 16 : 8;
+        cwide = wide16_ok(W, T, nt) > 0;
         cW = W, cT = T, cnt = nt;
     }
+    if (wide) *wide = cwide;
     return cres;
 }
 
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm, float th2,
                          int W, int T, int C, int nt, int max_iters, int nb, const MatchScratch& sc,
                          const MatchOut& out, cudaStream_t s, int variant) {
-    // variant: 0 = automatic (shared-memory scores when they fit and the group is small enough
-    // that 16-CTA clusters do not leave SMs idle), 1 = scores in global memory, 8-CTA clusters,
-    // 2 = scores in shared memory, 16-CTA clusters (falls back to 1 when it cannot launch)
-    bool smem = false;
-    if (variant == 2) smem = match_variant(W, T, nt) == 16;
-    else if (variant == 0) smem = nb <= 8 && match_variant(W, T, nt) == 16;
-    cudaError_t e = smem ? launch_match_cfg<16, true, kMatchThreadsSmem>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt,
-                                                                          max_iters, nb, sc, out, s)
-                         : launch_match_cfg<8, false, kMatchThreads>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt,
-                                                                     max_iters, nb, sc, out, s);
+    // variant: 0 = automatic -- for groups of at most 8 batches (latency), scores in shared memory
+    // when they fit, else in L2 with 16-CTA clusters of 1024 threads (one CTA per SM); larger
+    // groups (throughput) scores in L2 with 8-CTA clusters, two CTAs per SM.  1 = the 8-CTA L2
+    // variant, 2 = shared memory (falls back to 1 when it cannot launch), 3 = the 16-CTA L2
+    // variant (falls back to 1)
+    bool wide = false;
+    const int fit = match_variant(W, T, nt, &wide);
+    int kind = 1;
+    if (variant == 2) kind = fit == 16 ? 2 : 1;
+    else if (variant == 3) kind = wide ? 3 : 1;
+    else if (variant == 0 && nb <= 8) kind = fit == 16 ? 2 : (wide ? 3 : 1);
+    cudaError_t e;
+    if (kind == 2)
+        e = launch_match_cfg<16, true, kMatchThreadsSmem>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb,
+                                                          sc, out, s);
+    else if (kind == 3)
+        e = launch_match_cfg<16, false, kMatchThreadsWide>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters,
+                                                           nb, sc, out, s);
+    else
+        e = launch_match_cfg<8, false, kMatchThreads>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc,
+                                                      out, s);
     if (e != cudaSuccess) return e;
     dim3 grid((W + kResRows - 1) / kResRows, nb);
     residual_kernel<<<grid, 256, 0, s>>>(Xres, pre_wf, out, W, C, nt);

@@ -208,7 +208,7 @@ void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, i
     const size_t smem = (size_t)kCarTRows * (C + 1) * sizeof(float);
 #define LSS_CART(N)                                                                                        \
     do {                                                                                                   \
-        cudaFuncSetAttribute(car_t_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+        raise_smem_limit((const void*)car_t_kernel<N>, smem);                                              \
         car_t_kernel<N><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, L, R,  \
                                                            pitch, Xt_hi, Xt_lo);                           \
     } while (0)

@@ -363,7 +363,7 @@ cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int
     if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
     auto kern = umma_gemm_3xtf32<kPlainBN, kPlain>;
     constexpr int smem = smem_bytes<kPlainBN>();
-    const cudaError_t attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
     UmmaArgs a{};
     a.out = Cm;
@@ -383,7 +383,7 @@ cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo
     if (!u || nb * C > u->rows_a) return cudaErrorInvalidValue;
     auto kern = umma_gemm_3xtf32<kToepBN, kToeplitz>;
     constexpr int smem = smem_bytes<kToepBN>();
-    const cudaError_t attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
     UmmaArgs a{};
     a.out = Y_hi;

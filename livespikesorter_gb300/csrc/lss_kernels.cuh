@@ -49,6 +49,10 @@ struct SpikeRec {
 constexpr int kMatchCluster = 16;  // largest cluster (CTAs per batch) the matching loop launches
 constexpr int kMatchThreads = 512;       // matching loop, scores in L2 (two CTAs per SM)
 constexpr int kMatchThreadsSmem = 768;   // matching loop, scores in shared memory (one CTA per SM)
+constexpr int kMatchThreadsWide = 1024;  // matching loop, scores in L2, 16-CTA clusters, one CTA per SM
+
+// raise (never lower) a kernel's dynamic shared-memory limit on the current device
+cudaError_t raise_smem_limit(const void* kernel, size_t bytes);
 
 void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT,
                    int nb, long long* colsum, cudaStream_t s);

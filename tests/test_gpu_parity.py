@@ -272,6 +272,24 @@ def test_tensor_core_and_simt_gemms_agree(win_oss, win):
     assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
 
 
+def test_match_variants_agree(cfg_stream):
+    """The matching-loop variants -- scores in L2 with 8-CTA clusters (1) or 16-CTA clusters of 1024
+    threads (3), scores in shared memory (2) -- run the same arithmetic in the same order per sample:
+    bitwise-equal spikes for three windows at once and an equal residual."""
+    d, data, _ = cfg_stream
+    wins = np.stack([data[k * 1500: k * 1500 + 1622] for k in (1, 2, 3)])
+    outs = {}
+    for v in (1, 2, 3):
+        with sorter.OnlineSorter(d, match_variant=v, group_batches=3) as s:
+            outs[v] = (s.sort_windows(wins), s.debug_stage(wins[0], sorter.STAGE_RESIDUAL))
+    for v in (2, 3):
+        for a, b in zip(outs[1][0], outs[v][0]):
+            assert len(a) == len(b) > 0
+            for f in ("time", "tmpl", "amp", "iter", "x", "y", "pcfeat"):
+                np.testing.assert_array_equal(a[f], b[f], err_msg=f"variant {v} {f}")
+        np.testing.assert_array_equal(outs[1][1], outs[v][1])
+
+
 def test_tensor_core_gemm_384ch(cfg_stream):
     """The 384-channel / 500-template shapes (two N tiles, ragged last M tile) through both paths."""
     d, data, _ = cfg_stream
