@@ -49,7 +49,7 @@ typedef struct lss_params {
     int32_t hp_half_taps;   /* high-pass FIR half length (taps beyond are < 1e-8 of the centre); 0 = 640 */
     int32_t dedup;          /* 1 = drop same-cluster spikes within duplicate_spike_bins (default 1) */
     float th_override;      /* > 0 replaces Th_learned of misc.txt */
-    int32_t spike_cap;      /* per-batch spike buffer; 0 = automatic */
+    int32_t spike_cap;      /* per-batch spike buffer; 0 = automatic (2 * max_iters * ceil(W / (nt + 1))) */
     int64_t mem_budget;     /* device bytes this handle may hold; 0 = no limit (admission check) */
     int32_t profile;        /* 1 = time every stage with CUDA events (lss_stage_times) */
     int32_t match_variant;  /* 0 = automatic; 1 = scores in L2, 8-CTA clusters; 2 = scores in shared memory;

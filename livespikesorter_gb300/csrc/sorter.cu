@@ -388,7 +388,9 @@ void Handle::ensure_work(int Wn, int nb) {
     free_work();
     int64_t before = dev_bytes;
     const int LRmax = Wa;   // wrap rows never exceed the window length
-    cap = p.spike_cap > 0 ? p.spike_cap : std::max(2048, Wa);
+    // one iteration accepts at most one spike per nt + 1 samples (the (2nt+1) max pool), twice
+    // that with exact ties
+    cap = p.spike_cap > 0 ? p.spike_cap : std::max(2048, 2 * max_iters * ((Wa + nt) / (nt + 1)));
     raw_rows_cap = (size_t)nba * (size_t)std::max(Wa, NT) + 2 * (size_t)nt;
     const int64_t need = (int64_t)raw_rows_cap * Cin * 2 + (int64_t)nba * C * 8 +
                          (int64_t)nba * (Wa + LRmax) * C * 4 + 2LL * nba * Wa * C * 4 +
