@@ -90,9 +90,12 @@ struct TapSet {
     UmmaOperands* um = nullptr;
 };
 
+constexpr int kSlots = 4;   // groups in flight + the one collecting the stream's next rows
+
 struct Slot {
     int16_t* h_stage = nullptr;
     size_t stage_rows = 0;
+    size_t recs_n = 0;          // SpikeRec capacity of h_recs
     SpikeRec* h_recs = nullptr;
     SpikeRec* d_recs = nullptr;
     int* h_off = nullptr;
@@ -100,8 +103,10 @@ struct Slot {
     int* h_nsp = nullptr;     // [nbcap] spikes found (may exceed cap)
     int* h_status = nullptr;  // [nbcap]
     cudaEvent_t ev = nullptr;
+    cudaEvent_t ev_copy = nullptr;            // its rows are on the device (copy stream)
     cudaEvent_t tev[LSS_N_STAGES + 1] = {};   // stage boundaries (profile = 1)
     bool busy = false;
+    bool reserved = false;     // collecting the stream's next rows (the pending slot)
     int nb = 0, W = 0;
     bool windows_api = false;
     std::vector<int64_t> win_start;   // stream sample of each window's first row
@@ -114,6 +119,7 @@ struct Handle {
     OssModel m;
     int dev = 0;
     cudaStream_t st = nullptr;
+    cudaStream_t st_copy = nullptr;   // host-to-device copies, overlapped with the previous group's kernels
     int C = 0, T = 0, K = 0, nt = 0, nC = 0, Tf = 0, Cin = 0, NT = 0, W = 0, G = 1, cap = 0, max_iters = 50;
     float th = 8.f;
     int64_t dev_bytes = 0;
@@ -142,7 +148,7 @@ struct Handle {
     // work buffers
     int Wcap = 0, nbcap = 0;
     size_t raw_rows_cap = 0;
-    int16_t* d_raw = nullptr;
+    int16_t* d_raw = nullptr;   // [kSlots][raw_rows_cap][Cin]: each slot's rows on the device
     long long* d_colsum = nullptr;
     float *d_Xw = nullptr, *d_Y = nullptr, *d_Z = nullptr, *d_Bpc = nullptr, *d_Bt = nullptr;
     float *d_Y_lo = nullptr, *d_Bpc_lo = nullptr;   // tf32 remainders (tensor-core path)
@@ -159,7 +165,8 @@ struct Handle {
     // stream framing
     bool seg_active = false;
     int64_t seg_s0 = 0, next_batch = 0, expected_ct = 0, batch_counter = 0;
-    std::vector<int16_t> buf;   // rows from the next window's first row on
+    int pend = -1;              // slot whose pinned staging collects the next group's rows
+    int64_t pend_rows = 0;      // rows staged there, from the group's first window row on
     std::vector<int64_t> last_kept;     // per final cluster: last kept spike time (duplicate removal)
     std::vector<char> has_kept;
 
@@ -173,16 +180,19 @@ struct Handle {
                       const int16_t* dev_src = nullptr);
     void push_device(const int16_t* rows, int64_t n_batches, int64_t first_row_sample);
     void collect(int slot_idx, std::vector<lss_spike>* direct, std::vector<int64_t>* counts);
+    void alloc_slot(Slot& s);
     void drain_all();
     void push(const int16_t* x, int64_t n, int64_t ct);
     void flush();
-    int64_t launch_windows(int g, int pad_mode, const int16_t* x, int64_t xr);
+    Slot& pending_slot();
+    void launch_pending(int g, int pad_mode);
     void run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
                               const std::function<void()>& mark);
 };
 
 Handle::~Handle() {
     if (dev >= 0) cudaSetDevice(dev);
+    if (st_copy) cudaStreamSynchronize(st_copy);
     if (st) cudaStreamSynchronize(st);
     free_work();
     for (auto& kv : taps) {
@@ -202,9 +212,11 @@ Handle::~Handle() {
         if (s.h_nsp) cudaFreeHost(s.h_nsp);
         if (s.h_status) cudaFreeHost(s.h_status);
         if (s.ev) cudaEventDestroy(s.ev);
+        if (s.ev_copy) cudaEventDestroy(s.ev_copy);
         for (cudaEvent_t e : s.tev)
             if (e) cudaEventDestroy(e);
     }
+    if (st_copy) cudaStreamDestroy(st_copy);
     if (st) cudaStreamDestroy(st);
 }
 
@@ -270,6 +282,7 @@ void Handle::init(const char* dir, const lss_params* prm) {
     if (dev < 0 || dev >= ndev) throw LoadError{LSS_ERR_ARG, "device ordinal out of range"};
     LSS_CUDA(cudaSetDevice(dev));
     LSS_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    LSS_CUDA(cudaStreamCreateWithFlags(&st_copy, cudaStreamNonBlocking));
 
     // derived host arrays: (M @ Wrot) in float64, ctc permuted so the target template is
     // contiguous, squared template norms
@@ -340,14 +353,15 @@ void Handle::init(const char* dir, const lss_params* prm) {
 
     last_kept.assign(Tf, 0);
     has_kept.assign(Tf, 0);
-    taps_for(W);
-    ensure_work(W, G);
-    slots.resize(3);
+    slots.resize(kSlots);
     for (auto& s : slots) {
         LSS_CUDA(cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming));
+        LSS_CUDA(cudaEventCreateWithFlags(&s.ev_copy, cudaEventDisableTiming));
         if (p.profile)
             for (cudaEvent_t& e : s.tev) LSS_CUDA(cudaEventCreate(&e));
     }
+    taps_for(W);
+    ensure_work(W, G);
 }
 
 TapSet& Handle::taps_for(int Wn) {
@@ -384,6 +398,7 @@ TapSet& Handle::taps_for(int Wn) {
 void Handle::ensure_work(int Wn, int nb) {
     if (Wn <= Wcap && nb <= nbcap) return;
     if (st) LSS_CUDA(cudaStreamSynchronize(st));
+    if (st_copy) LSS_CUDA(cudaStreamSynchronize(st_copy));
     const int Wa = std::max(Wn, Wcap), nba = std::max(nb, nbcap);
     free_work();
     int64_t before = dev_bytes;
@@ -392,14 +407,14 @@ void Handle::ensure_work(int Wn, int nb) {
     // that with exact ties
     cap = p.spike_cap > 0 ? p.spike_cap : std::max(2048, 2 * max_iters * ((Wa + nt) / (nt + 1)));
     raw_rows_cap = (size_t)nba * (size_t)std::max(Wa, NT) + 2 * (size_t)nt;
-    const int64_t need = (int64_t)raw_rows_cap * Cin * 2 + (int64_t)nba * C * 8 +
+    const int64_t need = (int64_t)kSlots * raw_rows_cap * Cin * 2 + (int64_t)nba * C * 8 +
                          (int64_t)nba * (Wa + LRmax) * C * 4 + 2LL * nba * Wa * C * 4 +
                          (int64_t)nba * Wa * K * C * 4 * (tc_project ? 2 : 1) + (int64_t)nba * Wa * C * 4 * (tc_whiten ? 1 : 0) +
                          (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16;
     if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
         throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
                                            " device bytes, budget " + std::to_string(p.mem_budget)};
-    d_raw = dev_alloc<int16_t>(raw_rows_cap * Cin, dev_bytes);
+    d_raw = dev_alloc<int16_t>((size_t)kSlots * raw_rows_cap * Cin, dev_bytes);
     d_colsum = dev_alloc<long long>((size_t)nba * C, dev_bytes);
     if (tc_highpass) {
         // row pitch of any window length up to Wa: W + L + R <= 2W - 1, rounded up to 4
@@ -442,35 +457,40 @@ void Handle::ensure_work(int Wn, int nb) {
     work_bytes = dev_bytes - before;
     Wcap = Wa;
     nbcap = nba;
-    // pinned staging + mapped outputs of every slot follow the new capacity
-    for (auto& s : slots) {
-        if (s.busy) continue;
-        if (s.h_stage) cudaFreeHost(s.h_stage), s.h_stage = nullptr;
-        if (s.h_recs) cudaFreeHost(s.h_recs), s.h_recs = nullptr;
-        if (s.h_off) cudaFreeHost(s.h_off), s.h_off = nullptr;
-        if (s.h_nsp) cudaFreeHost(s.h_nsp), s.h_nsp = nullptr;
-        if (s.h_status) cudaFreeHost(s.h_status), s.h_status = nullptr;
-    }
+    // pinned staging + mapped outputs of every idle slot follow the new capacity now, so no
+    // later push pays for pinning memory; a slot still in flight is resized when it is reused
+    for (auto& s : slots)
+        if (!s.busy && !s.reserved) alloc_slot(s);
+}
+
+// (re)allocate a slot's pinned staging and host-mapped outputs at the current capacity
+void Handle::alloc_slot(Slot& s) {
+    if (s.h_stage) cudaFreeHost(s.h_stage), s.h_stage = nullptr;
+    if (s.h_recs) cudaFreeHost(s.h_recs), s.h_recs = nullptr;
+    if (s.h_off) cudaFreeHost(s.h_off), s.h_off = nullptr;
+    if (s.h_nsp) cudaFreeHost(s.h_nsp), s.h_nsp = nullptr;
+    if (s.h_status) cudaFreeHost(s.h_status), s.h_status = nullptr;
+    s.stage_rows = s.recs_n = 0;
+    LSS_CUDA(cudaHostAlloc((void**)&s.h_stage, raw_rows_cap * Cin * sizeof(int16_t), cudaHostAllocPortable));
+    LSS_CUDA(cudaHostAlloc((void**)&s.h_recs, (size_t)nbcap * cap * sizeof(SpikeRec),
+                           cudaHostAllocMapped | cudaHostAllocPortable));
+    LSS_CUDA(cudaHostGetDevicePointer((void**)&s.d_recs, s.h_recs, 0));
+    LSS_CUDA(cudaHostAlloc((void**)&s.h_off, (size_t)(nbcap + 1) * sizeof(int),
+                           cudaHostAllocMapped | cudaHostAllocPortable));
+    LSS_CUDA(cudaHostGetDevicePointer((void**)&s.d_off, s.h_off, 0));
+    LSS_CUDA(cudaHostAlloc((void**)&s.h_nsp, (size_t)nbcap * sizeof(int), cudaHostAllocPortable));
+    LSS_CUDA(cudaHostAlloc((void**)&s.h_status, (size_t)nbcap * sizeof(int), cudaHostAllocPortable));
+    s.stage_rows = raw_rows_cap;
+    s.recs_n = (size_t)nbcap * cap;
 }
 
 int Handle::acquire_slot() {
     // finish the oldest group if every slot is in flight
     for (;;) {
         for (size_t i = 0; i < slots.size(); ++i)
-            if (!slots[i].busy) {
+            if (!slots[i].busy && !slots[i].reserved) {
                 Slot& s = slots[i];
-                if (!s.h_stage) {
-                    s.stage_rows = raw_rows_cap;
-                    LSS_CUDA(cudaHostAlloc((void**)&s.h_stage, s.stage_rows * Cin * sizeof(int16_t), cudaHostAllocPortable));
-                    LSS_CUDA(cudaHostAlloc((void**)&s.h_recs, (size_t)nbcap * cap * sizeof(SpikeRec),
-                                           cudaHostAllocMapped | cudaHostAllocPortable));
-                    LSS_CUDA(cudaHostGetDevicePointer((void**)&s.d_recs, s.h_recs, 0));
-                    LSS_CUDA(cudaHostAlloc((void**)&s.h_off, (size_t)(nbcap + 1) * sizeof(int),
-                                           cudaHostAllocMapped | cudaHostAllocPortable));
-                    LSS_CUDA(cudaHostGetDevicePointer((void**)&s.d_off, s.h_off, 0));
-                    LSS_CUDA(cudaHostAlloc((void**)&s.h_nsp, (size_t)nbcap * sizeof(int), cudaHostAllocPortable));
-                    LSS_CUDA(cudaHostAlloc((void**)&s.h_status, (size_t)nbcap * sizeof(int), cudaHostAllocPortable));
-                }
+                if (!s.h_stage || s.stage_rows < raw_rows_cap || s.recs_n < (size_t)nbcap * cap) alloc_slot(s);
                 return (int)i;
             }
         collect(inflight.front(), nullptr, nullptr);
@@ -531,8 +551,14 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     mark();
     const int16_t* raw = dev_src;
     if (!raw) {
-        LSS_CUDA(cudaMemcpyAsync(d_raw, s.h_stage, (size_t)stage_rows * Cin * sizeof(int16_t), cudaMemcpyHostToDevice, st));
-        raw = d_raw;
+        // the slot's own device rows: the copy runs on the copy stream while the previous group's
+        // kernels run (a slot is reused only after its group was collected)
+        int16_t* sraw = d_raw + (size_t)(&s - slots.data()) * raw_rows_cap * Cin;
+        LSS_CUDA(cudaMemcpyAsync(sraw, s.h_stage, (size_t)stage_rows * Cin * sizeof(int16_t), cudaMemcpyHostToDevice,
+                                 st_copy));
+        LSS_CUDA(cudaEventRecord(s.ev_copy, st_copy));
+        LSS_CUDA(cudaStreamWaitEvent(st, s.ev_copy, 0));
+        raw = sraw;
     }
     mark();
     int64_t nl = 0;
@@ -603,24 +629,38 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
     }
     const int hw = nt / 2;
     const int nf = nC * K;
-    std::vector<lss_spike> batch;
     for (int b = 0; b < s.nb; ++b) {
         if (s.h_status[b] & 2) {
             s.busy = false;
             throw LoadError{LSS_ERR_ARG, "window too long for the matching kernel's slice bookkeeping"};
         }
     }
+    // per batch: order by (time, template), ties in record order, on small keys; every output
+    // record is then built once, in its final place
+    struct Key {
+        int64_t time;
+        int32_t tmpl, i;
+        bool operator<(const Key& o) const {
+            return time != o.time ? time < o.time : (tmpl != o.tmpl ? tmpl < o.tmpl : i < o.i);
+        }
+    };
+    std::vector<Key> keys;
     for (int b = 0; b < s.nb; ++b) {
         const int n = s.h_off[b + 1] - s.h_off[b];
         if (s.h_status[b] & 1) overflow_pending = true;
-        batch.clear();
-        batch.reserve(n);
+        const SpikeRec* recs = s.h_recs + s.h_off[b];
+        keys.clear();
+        keys.reserve(n);
         for (int i = 0; i < n; ++i) {
-            const SpikeRec& r = s.h_recs[s.h_off[b] + i];
-            lss_spike o;
+            const int64_t t = s.win_start[b] + recs[i].w - hw + m.nt0min;
+            if (t < s.drop_before[b]) continue;
+            keys.push_back({t, recs[i].t, i});
+        }
+        std::sort(keys.begin(), keys.end());
+        auto make = [&](const Key& k, lss_spike& o) {
+            const SpikeRec& r = recs[k.i];
             std::memset(&o, 0, sizeof(o));
-            o.time = s.win_start[b] + r.w - hw + m.nt0min;
-            if (o.time < s.drop_before[b]) continue;
+            o.time = k.time;
             o.tmpl = r.t;
             o.cluster = r.cluster;
             o.amp = r.amp;
@@ -630,26 +670,26 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
             o.n_feat = nf;
             o.iter = r.iter;
             std::memcpy(o.pcfeat, r.feat, sizeof(float) * nf);
-            batch.push_back(o);
-        }
-        std::stable_sort(batch.begin(), batch.end(), [](const lss_spike& a, const lss_spike& c) {
-            return a.time != c.time ? a.time < c.time : a.tmpl < c.tmpl;
-        });
+        };
         if (direct) {
-            direct->insert(direct->end(), batch.begin(), batch.end());
-            if (counts) counts->push_back((int64_t)batch.size());
+            const size_t at = direct->size();
+            direct->resize(at + keys.size());
+            for (size_t j = 0; j < keys.size(); ++j) make(keys[j], (*direct)[at + j]);
+            if (counts) counts->push_back((int64_t)keys.size());
         } else {
-            for (const lss_spike& o : batch) {
-                if (p.dedup && o.cluster >= 0 && o.cluster < Tf) {
+            for (const Key& k : keys) {
+                const int cl = recs[k.i].cluster;
+                if (p.dedup && cl >= 0 && cl < Tf) {
                     // Kilosort postprocessing.py:9-30: keep when t >= last kept + dt
-                    if (has_kept[o.cluster] && o.time < last_kept[o.cluster] + m.dup_bins) continue;
-                    last_kept[o.cluster] = o.time;
-                    has_kept[o.cluster] = 1;
+                    if (has_kept[cl] && k.time < last_kept[cl] + m.dup_bins) continue;
+                    last_kept[cl] = k.time;
+                    has_kept[cl] = 1;
                 }
-                ready.push_back(o);
+                ready.emplace_back();
+                make(k, ready.back());
             }
         }
-        spikes_done += (int64_t)batch.size();
+        spikes_done += (int64_t)keys.size();
     }
     batches_done += s.nb;
     s.busy = false;
@@ -659,30 +699,35 @@ void Handle::drain_all() {
     while (!inflight.empty()) collect(inflight.front(), nullptr, nullptr);
 }
 
-// Launch g windows whose rows are the concatenation of buf (rows not launched yet) and the
-// caller's rows x[0 .. xr): each row is copied once, straight into the pinned staging slot.  Rows
-// past the end (only at a flush, g = 1): pad_mode 1 repeats the last row (Kilosort's last batch,
-// io.py:626-629); pad_mode 2 leaves them zero, which is what Kilosort does when the first batch is
-// also the last one (its ibatch == 0 branch, io.py:621-625, runs first and never fills the right
-// side).  Returns the number of caller rows consumed (dropped from the front of the stream).
-int64_t Handle::launch_windows(int g, int pad_mode, const int16_t* x, int64_t xr) {
-    const int64_t brows = (int64_t)(buf.size() / Cin);
-    const int64_t rows_have = brows + xr;
-    const int64_t rows_need = (int64_t)g * NT + 2 * nt;
-    const int si = acquire_slot();
+// The slot whose pinned staging receives the stream's next rows; a caller's rows are copied once,
+// straight into it, and a group launches from it when its windows are complete.
+Slot& Handle::pending_slot() {
+    if (pend < 0) {
+        pend = acquire_slot();
+        slots[pend].reserved = true;
+        pend_rows = 0;
+    }
+    return slots[pend];
+}
+
+// Launch g windows from the pending staging (rows [0, g*NT + 2nt) from the first window's first
+// row).  Rows past the staged ones (only at a flush, g = 1): pad_mode 1 repeats the last row
+// (Kilosort's last batch, io.py:626-629); pad_mode 2 leaves them zero, which is what Kilosort does
+// when the first batch is also the last one (its ibatch == 0 branch, io.py:621-625, runs first and
+// never fills the right side).  The staged rows after the g*NT launched ones start the next
+// pending slot.
+void Handle::launch_pending(int g, int pad_mode) {
+    const int si = pend;
     Slot& s = slots[si];
-    const int64_t from_buf = std::min(brows, rows_need);
-    const int64_t from_x = std::min(xr, rows_need - from_buf);
-    par_memcpy(s.h_stage, buf.data(), (size_t)from_buf * Cin * sizeof(int16_t));
-    if (from_x > 0) par_memcpy(s.h_stage + from_buf * Cin, x, (size_t)from_x * Cin * sizeof(int16_t));
-    const int64_t copy_rows = from_buf + from_x;
-    if (copy_rows < rows_need) {
-        if (pad_mode == 0 || copy_rows == 0 || g != 1) throw LoadError{LSS_ERR_INTERNAL, "window underflow"};
-        for (int64_t r = copy_rows; r < rows_need; ++r) {
+    const int64_t rows_need = (int64_t)g * NT + 2 * nt;
+    const int64_t have = pend_rows;
+    if (have < rows_need) {
+        if (pad_mode == 0 || have == 0 || g != 1) throw LoadError{LSS_ERR_INTERNAL, "window underflow"};
+        for (int64_t r = have; r < rows_need; ++r) {
             if (pad_mode == 2)
                 std::memset(s.h_stage + r * Cin, 0, (size_t)Cin * sizeof(int16_t));
             else
-                std::memcpy(s.h_stage + r * Cin, s.h_stage + (copy_rows - 1) * Cin, (size_t)Cin * sizeof(int16_t));
+                std::memcpy(s.h_stage + r * Cin, s.h_stage + (have - 1) * Cin, (size_t)Cin * sizeof(int16_t));
         }
     }
     s.windows_api = false;
@@ -695,18 +740,21 @@ int64_t Handle::launch_windows(int g, int pad_mode, const int16_t* x, int64_t xr
         s.batch_id[b] = batch_counter + b;
         if (j == 0) s.drop_before[b] = seg_s0;   // Kilosort drops negative times of batch 0
     }
+    s.reserved = false;
+    pend = -1;
+    pend_rows = 0;
     launch_group(s, g, W, NT, taps_for(W), (int)rows_need);
     inflight.push_back(si);
     next_batch += g;
     batch_counter += g;
-    // advance the stream by g * NT rows
-    const int64_t adv = std::min<int64_t>((int64_t)g * NT, rows_have);
-    if (adv <= brows) {
-        buf.erase(buf.begin(), buf.begin() + (size_t)adv * Cin);
-        return 0;
+    const int64_t carry = have - (int64_t)g * NT;   // rows of the following windows staged already
+    if (carry > 0) {
+        // the launched slot's staging is host memory the GPU only reads; if collecting the oldest
+        // group hands the same slot back, the rows move down within it
+        Slot& ns = pending_slot();
+        std::memmove(ns.h_stage, s.h_stage + (size_t)g * NT * Cin, (size_t)carry * Cin * sizeof(int16_t));
+        pend_rows = carry;
     }
-    buf.clear();
-    return adv - brows;
 }
 
 void Handle::push(const int16_t* x, int64_t n, int64_t ct) {
@@ -717,36 +765,42 @@ void Handle::push(const int16_t* x, int64_t n, int64_t ct) {
         seg_active = true;
         seg_s0 = ct >= 0 ? ct : expected_ct;
         next_batch = 0;
-        buf.clear();
-        for (int r = 0; r < nt; ++r) buf.insert(buf.end(), x, x + Cin);   // left pad = first sample
+        Slot& s = pending_slot();
+        for (int r = 0; r < nt; ++r) std::memcpy(s.h_stage + (size_t)r * Cin, x, (size_t)Cin * sizeof(int16_t));
+        pend_rows = nt;                                        // left pad = first sample
         expected_ct = seg_s0;
     }
     expected_ct += n;
     const int64_t need = (int64_t)G * NT + 2 * nt;
-    while ((int64_t)(buf.size() / Cin) + n >= need) {
-        const int64_t used = launch_windows(G, 0, x, n);
-        x += used * Cin;
-        n -= used;
+    while (n > 0) {
+        Slot& s = pending_slot();
+        const int64_t take = std::min(n, need - pend_rows);
+        par_memcpy(s.h_stage + pend_rows * Cin, x, (size_t)take * Cin * sizeof(int16_t));
+        pend_rows += take;
+        x += take * Cin;
+        n -= take;
+        if (pend_rows == need) launch_pending(G, 0);
     }
-    buf.insert(buf.end(), x, x + (size_t)n * Cin);
 }
 
 void Handle::flush() {
     if (!seg_active) return;
-    // pending new samples: rows past the nt context rows at the front of buf.  Complete windows
+    // staged rows past the nt context rows at the front are pending new samples.  Complete windows
     // go out in groups; a window that runs past the data is padded and launched on its own.
     for (;;) {
-        const int64_t rows = (int64_t)(buf.size() / Cin);
+        const int64_t rows = pend_rows;
         if (rows - nt <= 0) break;
         const int64_t complete = rows >= W ? (rows - W) / NT + 1 : 0;
         if (complete > 0) {
-            launch_windows((int)std::min<int64_t>(complete, G), 0, nullptr, 0);
+            launch_pending((int)std::min<int64_t>(complete, G), 0);
         } else {
-            launch_windows(1, next_batch == 0 ? 2 : 1, nullptr, 0);
+            launch_pending(1, next_batch == 0 ? 2 : 1);
         }
     }
     seg_active = false;
-    buf.clear();
+    if (pend >= 0) slots[pend].reserved = false;
+    pend = -1;
+    pend_rows = 0;
 }
 
 }  // namespace lss
