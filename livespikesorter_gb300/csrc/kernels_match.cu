@@ -45,79 +45,108 @@ __device__ __forceinline__ unsigned cluster_rank() {
     return r;
 }
 
-constexpr int kMaxRoundsGlobal = 64;   // slice <= 64 * threads samples per CTA (scores in L2)
-constexpr int kMaxRoundsSmem = 4;      // the shared-memory slice is at most a few hundred samples
-constexpr int kPerLane = 8;      // row elements each lane loads before it stores (256 per warp)
-constexpr int kNearMax = 128;    // spikes near one CTA's slice in one iteration (more: scalar path)
 constexpr int kVecSmem = 4;      // float4 per lane per pass of the subtraction (512 templates)
 constexpr int kVecGlobal = 2;    // 256 templates: the global variant runs at 64 registers
 
-// dynamic shared memory of one CTA: [score slice if SMEM_B][s_cf][s_t][s_amp][1/nm], floats/ints
+// accepted spikes one iteration can hold in the shared list: the (2nt+1) max pool admits at most
+// one per nt + 1 samples, twice that with exact ties; more fall back to reading the spike maps
+__host__ __device__ inline int match_near_cap(int W, int nt) { return 2 * ((W + nt) / (nt + 1)) + 32; }
+
+constexpr int kStageChunk = 4096;   // samples of per-sample maxima staged at once in B1
+
+// dynamic shared memory of one CTA: [owned score rows if SMEM_B][cfmax of a window chunk + 2nt]
+// [1/nm][per-32-sample accepted masks and prefix][accepted-spike list (sample, template, amp)]
 __host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, bool smem_b) {
-    const int span = (W + G - 1) / G;
-    const size_t halo = (size_t)span + 2 * nt;
-    // 1 / nm starts on a 16-byte boundary (read as float4)
-    return (smem_b ? (size_t)span * T * 4 : 0) + ((halo * 3 + 3) & ~(size_t)3) * 4 + (size_t)T * 4;
+    const size_t span = (size_t)(W + G - 1) / G;
+    const size_t chunk = (size_t)(W < kStageChunk ? W : kStageChunk);
+    const size_t pad = (chunk + 2 * nt + 3) & ~(size_t)3;   // 1/nm starts 16-byte aligned
+    const size_t words = (size_t)(W + 31) / 32 + 1;
+    return (smem_b ? span * T * 4 : 0) + pad * 4 + (size_t)T * 4 + words * 8 + (size_t)match_near_cap(W, nt) * 12;
 }
 
+// ctc is read by every batch (about 30 times per group launch from a table the size of L2) while
+// the score rows stream through once per iteration: its lines are loaded, and prefetched, under an
+// L2 evict-last policy so the score traffic evicts them last
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ float4 ld_keep(const float4* p, uint64_t pol) {
+    float4 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p), "l"(pol));
+    return v;
+}
+
+// One thread-block cluster (G CTAs) runs the matching loop of one batch.  CTA r owns the samples
+// w = r, r + G, r + 2G, ... (interleaved, so the ~2nt+1 samples each spike touches spread evenly
+// over the cluster instead of loading the one or two CTAs whose contiguous slice holds them).
+// Per iteration:
+//   B1  every CTA stages the whole window's per-sample maxima, tests its own samples (window max
+//       over +-nt, threshold) and writes their accepted (template, amplitude) maps;
+//   --  cluster barrier;
+//   B2  every CTA reads the whole accepted map, ranks the spikes in sample order (the list is in
+//       (iteration, sample) order), keeps them in a shared list and records its own;
+//   C   each CTA subtracts amp * ctc from the score rows of its own samples within +-nt of a spike,
+//       in ascending spike order, and recomputes those samples' maxima;
+//   --  cluster barrier.
 template <int G, bool SMEM_B, int NTHR>
 __global__ void __launch_bounds__(NTHR, (SMEM_B || NTHR > 512) ? 1 : 2)
 match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __restrict__ ctcP,
              const float* __restrict__ pre_wf, const float* __restrict__ nm, float th2, int W, int T, int C,
              int nt, int max_iters, MatchScratch sc, MatchOut out) {
-    constexpr int kMatchThreads = NTHR;
     constexpr int kWarps = NTHR / 32;
-    constexpr int kMaxRounds = SMEM_B ? kMaxRoundsSmem : kMaxRoundsGlobal;
     constexpr int kVec = SMEM_B ? kVecSmem : kVecGlobal;
     extern __shared__ float smem[];
     const int b = blockIdx.x / G;
     const int rank = (G == 1) ? 0 : (int)cluster_rank();
     const int span = (W + G - 1) / G;
-    const int lo = min(W, rank * span), hi = min(W, lo + span);
-    const int halo = span + 2 * nt;
-    float* Bs = smem;                                                  // [span][T] when SMEM_B
-    float* s_cf = smem + (SMEM_B ? (size_t)span * T : 0);            // [halo]
-    int* s_t = reinterpret_cast<int*>(s_cf + halo);                    // [halo]
-    float* s_amp = reinterpret_cast<float*>(s_t + halo);               // [halo]
-    float* s_inm = s_cf + ((3 * halo + 3) & ~3);                      // [T] 1 / nm, 16-byte aligned
-    __shared__ int s_cnt[G];
-    __shared__ int s_woff[kMaxRounds * kWarps];
+    const int own = rank < W ? (W - rank + G - 1) / G : 0;   // samples rank + G*j < W
+    const int chunk = min(W, kStageChunk);
+    const int nwords = (W + 31) / 32;
+    const int near_cap = match_near_cap(W, nt);
+    float* Bs = smem;                                                   // [span][T]: row j = sample rank + G*j
+    float* s_cf = smem + (SMEM_B ? (size_t)span * T : 0);              // [chunk + 2nt]: cfmax of w at s_cf[w - c0 + nt]
+    float* s_inm = s_cf + ((chunk + 2 * nt + 3) & ~3);                  // [T] 1 / nm, 16-byte aligned
+    unsigned* s_mask = reinterpret_cast<unsigned*>(s_inm + T);          // [nwords + 1] accepted bits
+    int* s_woff = reinterpret_cast<int*>(s_mask + nwords + 1);          // [nwords + 1] exclusive prefix
+    int* s_nw = s_woff + nwords + 1;                                    // [near_cap] sample
+    int* s_nt = s_nw + near_cap;                                        // [near_cap] template
+    float* s_na = reinterpret_cast<float*>(s_nt + near_cap);            // [near_cap] amplitude
     __shared__ int s_total;
-    __shared__ int s_nw[kNearMax], s_nt[kNearMax];
-    __shared__ float s_na[kNearMax];
-    __shared__ int s_nn;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int L2 = 2 * nt + 1;
-    const int rounds = (hi - lo + kMatchThreads - 1) / kMatchThreads;
+    const uint64_t pol_keep = l2_keep_policy();
     float* Bg = Bt + (int64_t)b * W * T;
-    // row pointer of sample w (own slice only)
-    auto brow = [&](int w) -> float* { return SMEM_B ? Bs + (size_t)(w - lo) * T : Bg + (int64_t)w * T; };
+    // score row of an own sample w = rank + G*j
+    auto brow = [&](int w) -> float* { return SMEM_B ? Bs + (size_t)(w / G) * T : Bg + (int64_t)w * T; };
     float* cfmax = sc.cfmax + (int64_t)b * W;
     int* imax = sc.imax + (int64_t)b * W;
     int* at_t = sc.at_t + (int64_t)b * W;
     float* at_amp = sc.at_amp + (int64_t)b * W;
-    int* cta_cnt = sc.cta_cnt + (int64_t)b * 2 * G;
     int* sp_w = out.sp_w + (int64_t)b * out.cap;
     int* sp_t = out.sp_t + (int64_t)b * out.cap;
     float* sp_amp = out.sp_amp + (int64_t)b * out.cap;
     int* sp_iter = out.sp_iter + (int64_t)b * out.cap;
 
     if (G > 1 && rank != (int)(blockIdx.x % G) && tid == 0) atomicOr(out.status + b, 2);
-    if (rounds > kMaxRounds && tid == 0) atomicOr(out.status + b, 2);
     if constexpr (SMEM_B) {
-        // the slice [lo, hi) x T is contiguous in global memory
-        const int64_t n = (int64_t)(hi - lo) * T;
-        const float* src = Bg + (int64_t)lo * T;
-        if ((((uintptr_t)src) & 15) == 0 && (n & 3) == 0) {
-            const float4* s4 = reinterpret_cast<const float4*>(src);
-            float4* d4 = reinterpret_cast<float4*>(Bs);
-            for (int64_t i = tid; i < n / 4; i += kMatchThreads) d4[i] = __ldcs(s4 + i);
-        } else {
-            for (int64_t i = tid; i < n; i += kMatchThreads) Bs[i] = __ldcs(src + i);
+        // own rows, each contiguous in global memory
+        const bool v4 = ((T & 3) == 0) && ((reinterpret_cast<uintptr_t>(Bg) & 15) == 0);
+        const int per = v4 ? T / 4 : T;
+        for (int64_t i = tid; i < (int64_t)own * per; i += NTHR) {
+            const int j = (int)(i / per), e = (int)(i - (int64_t)j * per);
+            const int64_t src = (int64_t)(rank + G * j) * T;
+            if (v4)
+                reinterpret_cast<float4*>(Bs + (size_t)j * T)[e] = __ldcs(reinterpret_cast<const float4*>(Bg + src) + e);
+            else
+                Bs[(size_t)j * T + e] = __ldcs(Bg + src + e);
         }
     }
-    for (int t = tid; t < T; t += kMatchThreads) s_inm[t] = 1.f / nm[t];
+    for (int t = tid; t < T; t += NTHR) s_inm[t] = 1.f / nm[t];
     __syncthreads();
 
     // warp-wide max / argmax of relu(x)^2 / nm (first index on ties) into cfmax / imax of w
@@ -135,8 +164,9 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
         }
     };
 
-    // ---- A (once): per-sample max / argmax over templates of the whole slice ----
-    for (int w = lo + warp; w < hi; w += kWarps) {
+    // ---- A (once): per-sample max / argmax over templates of the own samples ----
+    for (int j = warp; j < own; j += kWarps) {
+        const int w = rank + G * j;
         const float* row = brow(w);
         float best = -1.f;
         int bi = 0x7fffffff;
@@ -149,137 +179,122 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     }
     group_barrier<G>();
 
+    const bool vec_ok = (T & 3) == 0 &&
+                        ((reinterpret_cast<uintptr_t>(ctcP) | reinterpret_cast<uintptr_t>(Bt)) & 15) == 0;
     int n_total = 0, iters = 0;
-    for (int it = 0; it < max_iters && rounds <= kMaxRounds; ++it) {
-        // ---- B1: pooled max and acceptance on the own slice; per-warp counts per round ----
-        for (int i = tid; i < halo; i += kMatchThreads) {
-            const int w = lo - nt + i;
-            s_cf[i] = (w >= 0 && w < W) ? __ldcg(cfmax + w) : -FLT_MAX;
-        }
-        __syncthreads();
-        for (int r = 0; r < rounds; ++r) {
-            const int w = lo + r * kMatchThreads + tid;
-            bool acc = false;
-            if (w < hi) {
-                const int i = w - lo + nt;
+    for (int it = 0; it < max_iters; ++it) {
+        // ---- B1: window max and acceptance on the own samples, chunk by chunk ----
+        for (int c0 = 0; c0 < W; c0 += chunk) {
+            const int c1 = min(W, c0 + chunk);
+            for (int i = tid; i < c1 - c0 + 2 * nt; i += NTHR) {
+                const int w = c0 - nt + i;
+                s_cf[i] = (w >= 0 && w < W) ? __ldcg(cfmax + w) : -FLT_MAX;
+            }
+            __syncthreads();
+            const int j0 = c0 > rank ? (c0 - rank + G - 1) / G : 0;
+            for (int j = j0 + tid; j < own && rank + G * j < c1; j += NTHR) {
+                const int w = rank + G * j;
+                const float* win = s_cf + (w - c0);   // cfmax of w - nt .. w + nt
                 float cm = -FLT_MAX;
-                for (int d = -nt; d <= nt; ++d) cm = fmaxf(cm, s_cf[i + d]);
-                const float cf = s_cf[i];
+                for (int d = 0; d < L2; ++d) cm = fmaxf(cm, win[d]);
+                const float cf = win[nt];
                 int tt = -1;
                 float amp = 0.f;
                 if (cm > th2 && cf == cm) {
                     tt = imax[w];
                     amp = brow(w)[tt] / __ldg(nm + tt);
-                    acc = true;
-                    // phase C of every CTA near w reads rows of ctcP[tt]: start pulling the whole
-                    // (2nt+1) x T slab into L2 now, a barrier and a few round trips ahead of use
+                    // phase C of every CTA reads rows of ctcP[tt]: start pulling the (2nt+1) x T slab
+                    // into L2 now, a barrier ahead of use
                     if (((T * 4) & 15) == 0) {
                         const float* slab = ctcP + (int64_t)tt * L2 * T;
-                        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(slab),
-                                     "r"((uint32_t)(L2 * T * 4))
+                        asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(slab),
+                                     "r"((uint32_t)(L2 * T * 4)), "l"(pol_keep)
                                      : "memory");
                     }
                 }
                 at_t[w] = tt;
                 at_amp[w] = amp;
             }
-            const unsigned m = __ballot_sync(0xffffffffu, acc);
-            if (lane == 0) s_woff[r * kWarps + warp] = __popc(m);
-        }
-        __syncthreads();
-        if (tid == 0) {
-            // exclusive prefix over (round, warp) = sample order within the slice
-            int acc = 0;
-            for (int i = 0; i < rounds * kWarps; ++i) {
-                const int c = s_woff[i];
-                s_woff[i] = acc;
-                acc += c;
-            }
-            cta_cnt[(it & 1) * G + rank] = acc;
+            __syncthreads();   // the next chunk overwrites s_cf
         }
         group_barrier<G>();
 
-        // ---- totals: the same numbers in every CTA of the cluster ----
-        if (tid < G) s_cnt[tid] = __ldcg(cta_cnt + (it & 1) * G + tid);
+        // ---- B2: the accepted spikes of the whole window, ranked in sample order ----
+        for (int q = warp; q < nwords; q += kWarps) {
+            const int w = 32 * q + lane;
+            const bool hit = w < W && __ldcg(at_t + w) >= 0;
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0) s_mask[q] = m;
+        }
         __syncthreads();
-        if (tid == 0) {
-            int total = 0;
-            for (int r = 0; r < G; ++r) total += s_cnt[r];
-            s_total = total;
+        if (warp == 0) {
+            // exclusive prefix of the per-word counts: each lane a run of words, then a warp scan
+            const int per = (nwords + 31) / 32;
+            const int q0 = min(nwords, lane * per), q1 = min(nwords, q0 + per);
+            int sum = 0;
+            for (int q = q0; q < q1; ++q) sum += __popc(s_mask[q]);
+            int inc = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            int run = inc - sum;
+            for (int q = q0; q < q1; ++q) {
+                s_woff[q] = run;
+                run += __popc(s_mask[q]);
+            }
+            if (lane == 31) s_total = inc;
         }
         __syncthreads();
         const int total = s_total;
         if (total == 0) break;
         ++iters;
-        int base = n_total;
-        for (int r = 0; r < rank; ++r) base += s_cnt[r];
-
-        // ---- B2: record the own slice's spikes in sample order (all threads) ----
-        for (int r = 0; r < rounds; ++r) {
-            const int w = lo + r * kMatchThreads + tid;
-            const int tt = (w < hi) ? at_t[w] : -1;
-            const unsigned m = __ballot_sync(0xffffffffu, tt >= 0);
-            if (tt >= 0) {
-                const int slot = base + s_woff[r * kWarps + warp] + __popc(m & ((1u << lane) - 1u));
-                if (slot < out.cap) {
+        for (int q = warp; q < nwords; q += kWarps) {
+            const unsigned m = s_mask[q];
+            const int w = 32 * q + lane;
+            if ((m >> lane) & 1u) {
+                const int pos = s_woff[q] + __popc(m & ((1u << lane) - 1u));
+                const int tt = __ldcg(at_t + w);
+                const float amp = __ldcg(at_amp + w);
+                if (pos < near_cap) {
+                    s_nw[pos] = w;
+                    s_nt[pos] = tt;
+                    s_na[pos] = amp;
+                }
+                const int slot = n_total + pos;
+                if (w % G == rank && slot < out.cap) {
                     sp_w[slot] = w;
                     sp_t[slot] = tt;
-                    sp_amp[slot] = at_amp[w];
+                    sp_amp[slot] = amp;
                     sp_iter[slot] = it;
                 }
             }
         }
+        __syncthreads();
 
-        // ---- C: subtract the accepted spikes from the own samples ----
-        for (int i = tid; i < halo; i += kMatchThreads) {
-            const int w = lo - nt + i;
-            const bool in = (w >= 0 && w < W);
-            s_t[i] = in ? __ldcg(at_t + w) : -1;
-            s_amp[i] = in ? __ldcg(at_amp + w) : 0.f;
-        }
-        __syncthreads();
-        // the spikes near the own slice, in sample order (typically a handful): one compaction per
-        // iteration instead of a scan of the 2nt+1 neighbours of every sample
-        if (warp == 0) {
-            int cnt = 0;
-            for (int i0 = 0; i0 < halo; i0 += 32) {
-                const int i = i0 + lane;
-                const bool hit = i < halo && s_t[i] >= 0;
-                const unsigned m = __ballot_sync(0xffffffffu, hit);
-                if (hit) {
-                    const int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                    if (pos < kNearMax) {
-                        s_nw[pos] = lo - nt + i;
-                        s_nt[pos] = s_t[i];
-                        s_na[pos] = s_amp[i];
-                    }
-                }
-                cnt += __popc(m);
-            }
-            if (lane == 0) s_nn = cnt;
-        }
-        __syncthreads();
-        const int n_near = s_nn;
-        const bool vec_ok = (T & 3) == 0 && n_near <= kNearMax && ((reinterpret_cast<uintptr_t>(ctcP) |
-                                                                      reinterpret_cast<uintptr_t>(Bt)) & 15) == 0;
-        for (int wp = lo + warp; wp < hi; wp += kWarps) {
-            const int i0 = wp - lo;   // s_t[i0 + e] is the sample wp - nt + e
+        // ---- C: subtract the accepted spikes from the own samples near them ----
+        const int n_near = total;
+        const bool use_list = vec_ok && n_near <= near_cap;
+        for (int j = warp; j < own; j += kWarps) {
+            const int wp = rank + G * j;
             float* br = brow(wp);
             float best = -1.f;
             int bi = 0x7fffffff;
             bool touched = false;
-            if (vec_ok) {
-                // spikes k with |w_k - wp| <= nt, two at a time, in sample order
-                int k = 0;
-                while (k < n_near) {
-                    while (k < n_near && (s_nw[k] < wp - nt || s_nw[k] > wp + nt)) ++k;
-                    if (k >= n_near) break;
-                    int k2 = k + 1;
-                    while (k2 < n_near && (s_nw[k2] < wp - nt || s_nw[k2] > wp + nt)) ++k2;
-                    const bool two = k2 < n_near;
-                    int k3 = two ? k2 + 1 : n_near;
-                    while (k3 < n_near && (s_nw[k3] < wp - nt || s_nw[k3] > wp + nt)) ++k3;
-                    const bool last = k3 >= n_near;   // no further spike for this sample
+            if (use_list) {
+                // spikes k with |w_k - wp| <= nt, two at a time, in sample order: the list is sorted
+                // by sample, so they are the run that starts at the first w_k >= wp - nt
+                int k = 0, hi_k = n_near;
+                while (k < hi_k) {
+                    const int mid = (k + hi_k) >> 1;
+                    if (s_nw[mid] < wp - nt) k = mid + 1; else hi_k = mid;
+                }
+                while (k < n_near && s_nw[k] <= wp + nt) {
+                    const int k2 = k + 1;
+                    const bool two = k2 < n_near && s_nw[k2] <= wp + nt;
+                    const int k3 = two ? k2 + 1 : k2;
+                    const bool last = k3 >= n_near || s_nw[k3] > wp + nt;   // no further spike for this sample
                     const float a0 = s_na[k], a1 = two ? s_na[k2] : 0.f;
                     const float4* c0 = reinterpret_cast<const float4*>(ctcP + ((int64_t)s_nt[k] * L2 + (wp - s_nw[k] + nt)) * T);
                     const float4* c1 = two ? reinterpret_cast<const float4*>(ctcP + ((int64_t)s_nt[k2] * L2 + (wp - s_nw[k2] + nt)) * T)
@@ -289,26 +304,26 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                     for (int fb = 0; fb < T4; fb += 32 * kVec) {
                         float4 v0[kVec], v1[kVec];
 #pragma unroll
-                        for (int j = 0; j < kVec; ++j) {
-                            const int f = fb + lane + 32 * j;
+                        for (int jj = 0; jj < kVec; ++jj) {
+                            const int f = fb + lane + 32 * jj;
                             const bool ok = f < T4;
-                            v0[j] = ok ? __ldg(c0 + f) : make_float4(0.f, 0.f, 0.f, 0.f);
-                            v1[j] = (ok && two) ? __ldg(c1 + f) : make_float4(0.f, 0.f, 0.f, 0.f);
+                            v0[jj] = ok ? ld_keep(c0 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
+                            v1[jj] = (ok && two) ? ld_keep(c1 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
                         }
 #pragma unroll
-                        for (int j = 0; j < kVec; ++j) {
-                            const int f = fb + lane + 32 * j;
+                        for (int jj = 0; jj < kVec; ++jj) {
+                            const int f = fb + lane + 32 * jj;
                             if (f < T4) {
                                 float4 x = b4[f];
-                                x.x = fmaf(-a0, v0[j].x, x.x);
-                                x.y = fmaf(-a0, v0[j].y, x.y);
-                                x.z = fmaf(-a0, v0[j].z, x.z);
-                                x.w = fmaf(-a0, v0[j].w, x.w);
+                                x.x = fmaf(-a0, v0[jj].x, x.x);
+                                x.y = fmaf(-a0, v0[jj].y, x.y);
+                                x.z = fmaf(-a0, v0[jj].z, x.z);
+                                x.w = fmaf(-a0, v0[jj].w, x.w);
                                 if (two) {
-                                    x.x = fmaf(-a1, v1[j].x, x.x);
-                                    x.y = fmaf(-a1, v1[j].y, x.y);
-                                    x.z = fmaf(-a1, v1[j].z, x.z);
-                                    x.w = fmaf(-a1, v1[j].w, x.w);
+                                    x.x = fmaf(-a1, v1[jj].x, x.x);
+                                    x.y = fmaf(-a1, v1[jj].y, x.y);
+                                    x.z = fmaf(-a1, v1[jj].z, x.z);
+                                    x.w = fmaf(-a1, v1[jj].w, x.w);
                                 }
                                 b4[f] = x;
                                 if (last) {
@@ -327,23 +342,27 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                     k = two ? k2 + 1 : k + 1;
                 }
             } else {
-                // general shapes: scan the 2nt+1 neighbours, scalar rows
+                // general shapes or an overfull list: the 2nt+1 neighbours from the spike maps,
+                // scalar rows
                 int n_sp = 0;
                 for (int e0 = 0; e0 < L2; e0 += 32) {
-                    const int e = e0 + lane;
-                    n_sp += __popc(__ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0));
+                    const int w2 = wp - nt + e0 + lane;
+                    const bool hit = e0 + lane < L2 && w2 >= 0 && w2 < W && __ldcg(at_t + w2) >= 0;
+                    n_sp += __popc(__ballot_sync(0xffffffffu, hit));
                 }
                 int done = 0;
                 for (int e0 = 0; e0 < L2 && n_sp > 0; e0 += 32) {
-                    const int e = e0 + lane;
-                    unsigned m = __ballot_sync(0xffffffffu, e < L2 && s_t[i0 + e] >= 0);
+                    const int w2l = wp - nt + e0 + lane;
+                    const bool hit = e0 + lane < L2 && w2l >= 0 && w2l < W && __ldcg(at_t + w2l) >= 0;
+                    unsigned m = __ballot_sync(0xffffffffu, hit);
                     while (m) {
                         const int ee = e0 + __ffs(m) - 1;
                         m &= m - 1;
                         ++done;
                         const bool last = done == n_sp;
-                        const float a = s_amp[i0 + ee];
-                        const float* c = ctcP + ((int64_t)s_t[i0 + ee] * L2 + (2 * nt - ee)) * T;
+                        const int w2 = wp - nt + ee;
+                        const float a = __ldcg(at_amp + w2);
+                        const float* c = ctcP + ((int64_t)__ldcg(at_t + w2) * L2 + (2 * nt - ee)) * T;
                         for (int t = lane; t < T; t += 32) {
                             const float x = fmaf(-a, __ldg(c + t), br[t]);
                             br[t] = x;
@@ -360,7 +379,7 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             if (touched) finish_sample(wp, best, bi);
         }
         n_total += total;
-        group_barrier<G>();   // cfmax of the changed samples is read by the neighbours in B1
+        group_barrier<G>();   // the changed samples' maxima are read by every CTA in B1
     }
     if (rank == 0 && tid == 0) {
         out.n_spikes[b] = n_total;
@@ -377,6 +396,7 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
 // ---------------------------------------------------------------------------------------------
 constexpr int kResRows = 64;
 constexpr int kResList = 1024;
+constexpr int kPerLane = 8;      // row elements each lane loads before it stores (256 per warp)
 
 __global__ void __launch_bounds__(256)
 residual_kernel(float* __restrict__ Xres, const float* __restrict__ pre_wf, MatchOut out, int W, int C, int nt) {
@@ -481,7 +501,6 @@ static cudaError_t launch_match_cfg(float* Bt, float* Xres, const float* ctcP, c
 
 // Can a cluster of 16 CTAs with the whole score slice in shared memory run on this device?
 static int smem16_ok(int W, int T, int nt) {
-    if ((W + 15) / 16 > kMaxRoundsSmem * kMatchThreadsSmem) return 0;
     const size_t smem = match_smem_bytes(W, T, nt, 16, true);
     int dev = 0, maxopt = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
@@ -514,7 +533,6 @@ static int smem16_ok(int W, int T, int nt) {
 
 // Can a cluster of 16 CTAs of 1024 threads (scores in L2, one CTA per SM) run on this device?
 static int wide16_ok(int W, int T, int nt) {
-    if ((W + 15) / 16 > kMaxRoundsGlobal * kMatchThreadsWide) return 0;
     const size_t smem = match_smem_bytes(W, T, nt, 16, false);
     auto kern = match_kernel<16, false, kMatchThreadsWide>;
     if (raise_smem_limit((const void*)kern, smem) != cudaSuccess ||
