@@ -25,6 +25,7 @@
 #include "lss_kernels.cuh"
 
 #include <cfloat>
+#include <climits>
 
 namespace lss {
 
@@ -55,13 +56,24 @@ __host__ __device__ inline int match_near_cap(int W, int nt) { return 2 * ((W + 
 constexpr int kStageChunk = 4096;   // samples of per-sample maxima staged at once in B1
 
 // dynamic shared memory of one CTA: [owned score rows if SMEM_B][cfmax of a window chunk + 2nt]
-// [1/nm][per-32-sample accepted masks and prefix][accepted-spike list (sample, template, amp)]
+// [1/nm][nm][own samples' argmax][per-32-sample accepted masks and prefix]
+// [two accepted-spike lists (sample, template, amp), by iteration parity]
 __host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, bool smem_b) {
     const size_t span = (size_t)(W + G - 1) / G;
     const size_t chunk = (size_t)(W < kStageChunk ? W : kStageChunk);
     const size_t pad = (chunk + 2 * nt + 3) & ~(size_t)3;   // 1/nm starts 16-byte aligned
     const size_t words = (size_t)(W + 31) / 32 + 1;
-    return (smem_b ? span * T * 4 : 0) + pad * 4 + (size_t)T * 4 + words * 8 + (size_t)match_near_cap(W, nt) * 12;
+    return (smem_b ? span * T * 4 : 0) + pad * 4 + (size_t)T * 8 + span * 4 + words * 8 +
+           2 * (size_t)match_near_cap(W, nt) * 12;
+}
+
+// shared::cluster address of the same shared variable in CTA `rank` of the cluster
+__device__ __forceinline__ unsigned dsmem_addr(const void* local, unsigned rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(r)
+                 : "r"((unsigned)__cvta_generic_to_shared(local)), "r"(rank));
+    return r;
 }
 
 // ctc is read by every batch (about 30 times per group launch from a table the size of L2) while
@@ -110,21 +122,29 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     float* Bs = smem;                                                   // [span][T]: row j = sample rank + G*j
     float* s_cf = smem + (SMEM_B ? (size_t)span * T : 0);              // [chunk + 2nt]: cfmax of w at s_cf[w - c0 + nt]
     float* s_inm = s_cf + ((chunk + 2 * nt + 3) & ~3);                  // [T] 1 / nm, 16-byte aligned
-    unsigned* s_mask = reinterpret_cast<unsigned*>(s_inm + T);          // [nwords + 1] accepted bits
+    float* s_nm = s_inm + T;                                            // [T] nm
+    int* s_imax = reinterpret_cast<int*>(s_nm + T);                     // [span] argmax of own sample j
+    unsigned* s_mask = reinterpret_cast<unsigned*>(s_imax + span);      // [nwords + 1] accepted bits
     int* s_woff = reinterpret_cast<int*>(s_mask + nwords + 1);          // [nwords + 1] exclusive prefix
-    int* s_nw = s_woff + nwords + 1;                                    // [near_cap] sample
-    int* s_nt = s_nw + near_cap;                                        // [near_cap] template
-    float* s_na = reinterpret_cast<float*>(s_nt + near_cap);            // [near_cap] amplitude
-    __shared__ int s_total;
+    // accepted-spike lists by iteration parity: the spikes of iteration it arrive unordered in
+    // list it & 1 (sent by their owners into every CTA); the other list then holds them in sample
+    // order for phase C
+    int* s_lw = s_woff + nwords + 1;                                    // [2][near_cap] sample
+    int* s_lt = s_lw + 2 * near_cap;                                    // [2][near_cap] template
+    float* s_la = reinterpret_cast<float*>(s_lt + 2 * near_cap);        // [2][near_cap] amplitude
+    __shared__ int s_wcnt[kWarps];
+    __shared__ int s_lcnt[2];                                           // spikes received, by parity
 
+    static_assert(G >= 2 && G <= 32, "one cluster of 2..32 CTAs per batch");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int L2 = 2 * nt + 1;
     const uint64_t pol_keep = l2_keep_policy();
     float* Bg = Bt + (int64_t)b * W * T;
+    if (tid < 2) s_lcnt[tid] = 0;
+    for (int q = tid; q <= nwords; q += NTHR) s_mask[q] = 0u;
     // score row of an own sample w = rank + G*j
     auto brow = [&](int w) -> float* { return SMEM_B ? Bs + (size_t)(w / G) * T : Bg + (int64_t)w * T; };
     float* cfmax = sc.cfmax + (int64_t)b * W;
-    int* imax = sc.imax + (int64_t)b * W;
     int* at_t = sc.at_t + (int64_t)b * W;
     float* at_amp = sc.at_amp + (int64_t)b * W;
     int* sp_w = out.sp_w + (int64_t)b * out.cap;
@@ -146,8 +166,19 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                 Bs[(size_t)j * T + e] = __ldcs(Bg + src + e);
         }
     }
-    for (int t = tid; t < T; t += NTHR) s_inm[t] = 1.f / nm[t];
-    __syncthreads();
+    for (int t = tid; t < T; t += NTHR) {
+        s_nm[t] = nm[t];
+        s_inm[t] = 1.f / nm[t];
+    }
+    // a window of at most kStageChunk samples keeps every sample's maximum in every CTA: owners
+    // push each new value into all CTAs, so phase B1 reads shared memory only
+    const bool resident = W <= kStageChunk;
+    if (resident)
+        for (int i = tid; i < W + 2 * nt; i += NTHR)
+            if (i < nt || i >= W + nt) s_cf[i] = -FLT_MAX;
+    // every CTA of the cluster has started (and initialised its lists) before any writes into
+    // another's shared memory
+    group_barrier<G>();
 
     // warp-wide max / argmax of relu(x)^2 / nm (first index on ties) into cfmax / imax of w
     auto finish_sample = [&](int w, float best, int bi) {
@@ -157,11 +188,15 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
             if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
         }
+        const bool inner = w >= nt && w < W - nt;
+        const float v = inner ? best : 0.f;
         if (lane == 0) {
-            const bool inner = w >= nt && w < W - nt;
-            cfmax[w] = inner ? best : 0.f;
-            imax[w] = inner ? bi : 0;
+            if (!resident) cfmax[w] = v;
+            s_imax[w / G] = inner ? bi : 0;
         }
+        if (resident && lane < G)
+            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(dsmem_addr(s_cf + w + nt, (unsigned)lane)), "f"(v)
+                         : "memory");
     };
 
     // ---- A (once): per-sample max / argmax over templates of the own samples ----
@@ -186,96 +221,165 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
         // ---- B1: window max and acceptance on the own samples, chunk by chunk ----
         for (int c0 = 0; c0 < W; c0 += chunk) {
             const int c1 = min(W, c0 + chunk);
-            for (int i = tid; i < c1 - c0 + 2 * nt; i += NTHR) {
-                const int w = c0 - nt + i;
-                s_cf[i] = (w >= 0 && w < W) ? __ldcg(cfmax + w) : -FLT_MAX;
+            if (!resident) {
+                for (int i = tid; i < c1 - c0 + 2 * nt; i += NTHR) {
+                    const int w = c0 - nt + i;
+                    s_cf[i] = (w >= 0 && w < W) ? __ldcg(cfmax + w) : -FLT_MAX;
+                }
+                __syncthreads();
             }
-            __syncthreads();
+            // one warp per own sample: the lanes read consecutive maxima of its window (own
+            // samples are G apart, so one thread per sample would hit the same banks)
             const int j0 = c0 > rank ? (c0 - rank + G - 1) / G : 0;
-            for (int j = j0 + tid; j < own && rank + G * j < c1; j += NTHR) {
+            for (int j = j0 + warp; j < own && rank + G * j < c1; j += kWarps) {
                 const int w = rank + G * j;
                 const float* win = s_cf + (w - c0);   // cfmax of w - nt .. w + nt
                 float cm = -FLT_MAX;
-                for (int d = 0; d < L2; ++d) cm = fmaxf(cm, win[d]);
-                const float cf = win[nt];
+                for (int d = lane; d < L2; d += 32) cm = fmaxf(cm, win[d]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) cm = fmaxf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
                 int tt = -1;
                 float amp = 0.f;
-                if (cm > th2 && cf == cm) {
-                    tt = imax[w];
-                    amp = brow(w)[tt] / __ldg(nm + tt);
-                    // phase C of every CTA reads rows of ctcP[tt]: start pulling the (2nt+1) x T slab
-                    // into L2 now, a barrier ahead of use
-                    if (((T * 4) & 15) == 0) {
-                        const float* slab = ctcP + (int64_t)tt * L2 * T;
-                        asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(slab),
-                                     "r"((uint32_t)(L2 * T * 4)), "l"(pol_keep)
+                if (lane == 0) {
+                    if (cm > th2 && win[nt] == cm) {
+                        tt = s_imax[j];
+                        amp = brow(w)[tt] / s_nm[tt];
+                        // phase C of every CTA reads rows of ctcP[tt]: start pulling the (2nt+1) x T
+                        // slab into L2 now, a barrier ahead of use
+                        if (((T * 4) & 15) == 0) {
+                            const float* slab = ctcP + (int64_t)tt * L2 * T;
+                            asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(slab),
+                                         "r"((uint32_t)(L2 * T * 4)), "l"(pol_keep)
+                                         : "memory");
+                        }
+                    }
+                    at_t[w] = tt;   // the maps serve the overflow path
+                    at_amp[w] = amp;
+                }
+                tt = __shfl_sync(0xffffffffu, tt, 0);
+                amp = __shfl_sync(0xffffffffu, amp, 0);
+                if (tt >= 0 && lane < G) {
+                    // into list p of CTA `lane`: claim a slot there, then write the entry
+                    const int p = it & 1;
+                    unsigned slot;
+                    asm volatile("atom.shared::cluster.add.u32 %0, [%1], 1;"
+                                 : "=r"(slot)
+                                 : "r"(dsmem_addr(&s_lcnt[p], (unsigned)lane))
+                                 : "memory");
+                    if ((int)slot < near_cap) {
+                        const int e = p * near_cap + (int)slot;
+                        asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(dsmem_addr(s_lw + e, (unsigned)lane)), "r"(w)
+                                     : "memory");
+                        asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(dsmem_addr(s_lt + e, (unsigned)lane)), "r"(tt)
+                                     : "memory");
+                        asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(dsmem_addr(s_la + e, (unsigned)lane)), "f"(amp)
                                      : "memory");
                     }
                 }
-                at_t[w] = tt;
-                at_amp[w] = amp;
             }
-            __syncthreads();   // the next chunk overwrites s_cf
+            if (!resident) __syncthreads();   // the next chunk overwrites s_cf
         }
         group_barrier<G>();
 
         // ---- B2: the accepted spikes of the whole window, ranked in sample order ----
-        for (int q = warp; q < nwords; q += kWarps) {
-            const int w = 32 * q + lane;
-            const bool hit = w < W && __ldcg(at_t + w) >= 0;
-            const unsigned m = __ballot_sync(0xffffffffu, hit);
-            if (lane == 0) s_mask[q] = m;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            // exclusive prefix of the per-word counts: each lane a run of words, then a warp scan
-            const int per = (nwords + 31) / 32;
-            const int q0 = min(nwords, lane * per), q1 = min(nwords, q0 + per);
-            int sum = 0;
-            for (int q = q0; q < q1; ++q) sum += __popc(s_mask[q]);
-            int inc = sum;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += v;
-            }
-            int run = inc - sum;
-            for (int q = q0; q < q1; ++q) {
-                s_woff[q] = run;
-                run += __popc(s_mask[q]);
-            }
-            if (lane == 31) s_total = inc;
-        }
-        __syncthreads();
-        const int total = s_total;
+        const int p = it & 1, q = p ^ 1;
+        const int total = s_lcnt[p];   // every CTA received every spike: the same count everywhere
         if (total == 0) break;
         ++iters;
-        for (int q = warp; q < nwords; q += kWarps) {
-            const unsigned m = s_mask[q];
-            const int w = 32 * q + lane;
-            if ((m >> lane) & 1u) {
-                const int pos = s_woff[q] + __popc(m & ((1u << lane) - 1u));
-                const int tt = __ldcg(at_t + w);
-                const float amp = __ldcg(at_amp + w);
-                if (pos < near_cap) {
-                    s_nw[pos] = w;
-                    s_nt[pos] = tt;
-                    s_na[pos] = amp;
+        const bool listed = total <= near_cap;
+        auto place = [&](int w, int tt, float amp, int r) {
+            s_lw[q * near_cap + r] = w;
+            s_lt[q * near_cap + r] = tt;
+            s_la[q * near_cap + r] = amp;
+            const int slot = n_total + r;
+            if (w % G == rank && slot < out.cap) {
+                sp_w[slot] = w;
+                sp_t[slot] = tt;
+                sp_amp[slot] = amp;
+                sp_iter[slot] = it;
+            }
+        };
+        if (listed && total <= 32) {
+            // a handful of spikes: one warp ranks them by sample with shuffles
+            if (warp == 0) {
+                const bool have = lane < total;
+                const int w = have ? s_lw[p * near_cap + lane] : INT_MAX;
+                int r = 0;
+                for (int k = 0; k < total; ++k) r += __shfl_sync(0xffffffffu, w, k) < w;
+                if (have) place(w, s_lt[p * near_cap + lane], s_la[p * near_cap + lane], r);
+            }
+        } else if (listed) {
+            // rank = accepted samples before w: a bitmap of the received samples and its word prefix
+            for (int i = tid; i < total; i += NTHR) {
+                const int w = s_lw[p * near_cap + i];
+                atomicOr(&s_mask[w >> 5], 1u << (w & 31));
+            }
+            __syncthreads();
+            const int wpw = (nwords + kWarps - 1) / kWarps;
+            const int qa = min(nwords, warp * wpw), qb = min(nwords, qa + wpw);
+            int wcnt = 0;
+            for (int qq = qa + lane; qq < qb; qq += 32) wcnt += __popc(s_mask[qq]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) wcnt += __shfl_xor_sync(0xffffffffu, wcnt, o);
+            if (lane == 0) s_wcnt[warp] = wcnt;
+            __syncthreads();
+            if (lane == 0) {
+                int off = 0;
+                for (int i = 0; i < warp; ++i) off += s_wcnt[i];
+                for (int qq = qa; qq < qb; ++qq) {
+                    s_woff[qq] = off;
+                    off += __popc(s_mask[qq]);
                 }
-                const int slot = n_total + pos;
-                if (w % G == rank && slot < out.cap) {
+            }
+            __syncthreads();
+            for (int i = tid; i < total; i += NTHR) {
+                const int w = s_lw[p * near_cap + i];
+                const int r = s_woff[w >> 5] + __popc(s_mask[w >> 5] & ((1u << (w & 31)) - 1u));
+                place(w, s_lt[p * near_cap + i], s_la[p * near_cap + i], r);
+            }
+        } else {
+            // more spikes than the lists hold: rank them from the global maps
+            const int wpw = (nwords + kWarps - 1) / kWarps;
+            const int qa = min(nwords, warp * wpw), qb = min(nwords, qa + wpw);
+            int wcnt = 0;
+            for (int qq = qa; qq < qb; ++qq) {
+                const int w = 32 * qq + lane;
+                const unsigned m = __ballot_sync(0xffffffffu, w < W && __ldcg(at_t + w) >= 0);
+                if (lane == 0) s_mask[qq] = m;
+                wcnt += __popc(m);
+            }
+            if (lane == 0) s_wcnt[warp] = wcnt;
+            __syncthreads();
+            int off = 0;
+            for (int i = lane; i < warp; i += 32) off += s_wcnt[i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
+            for (int qq = qa; qq < qb; ++qq) {
+                const unsigned m = s_mask[qq];
+                const int w = 32 * qq + lane;
+                const int slot = n_total + off + __popc(m & ((1u << lane) - 1u));
+                if (((m >> lane) & 1u) && w % G == rank && slot < out.cap) {
                     sp_w[slot] = w;
-                    sp_t[slot] = tt;
-                    sp_amp[slot] = amp;
+                    sp_t[slot] = __ldcg(at_t + w);
+                    sp_amp[slot] = __ldcg(at_amp + w);
                     sp_iter[slot] = it;
                 }
+                off += __popc(m);
             }
         }
         __syncthreads();
+        // the bitmap starts empty next iteration; so does the list the next iteration's spikes
+        // arrive in (nobody sends before the barrier that ends this iteration)
+        if (!(listed && total <= 32))
+            for (int qq = tid; qq <= nwords; qq += NTHR) s_mask[qq] = 0u;
+        if (tid == 0) s_lcnt[q] = 0;
+        const int* s_nw = s_lw + q * near_cap;
+        const int* s_nt = s_lt + q * near_cap;
+        const float* s_na = s_la + q * near_cap;
 
         // ---- C: subtract the accepted spikes from the own samples near them ----
         const int n_near = total;
-        const bool use_list = vec_ok && n_near <= near_cap;
+        const bool use_list = vec_ok && listed;
         for (int j = warp; j < own; j += kWarps) {
             const int wp = rank + G * j;
             float* br = brow(wp);
