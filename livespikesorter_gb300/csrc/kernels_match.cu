@@ -380,72 +380,127 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
         // ---- C: subtract the accepted spikes from the own samples near them ----
         const int n_near = total;
         const bool use_list = vec_ok && listed;
-        for (int j = warp; j < own; j += kWarps) {
-            const int wp = rank + G * j;
-            float* br = brow(wp);
-            float best = -1.f;
-            int bi = 0x7fffffff;
-            bool touched = false;
-            if (use_list) {
-                // spikes k with |w_k - wp| <= nt, two at a time, in sample order: the list is sorted
-                // by sample, so they are the run that starts at the first w_k >= wp - nt
-                int k = 0, hi_k = n_near;
-                while (k < hi_k) {
-                    const int mid = (k + hi_k) >> 1;
-                    if (s_nw[mid] < wp - nt) k = mid + 1; else hi_k = mid;
+        if (use_list) {
+            // The warp's own samples j = warp, warp + kWarps, ... with their nearby spikes (runs of
+            // the list in sample order) are consumed as (sample, spike) items, two per pass: two
+            // spikes of one sample (applied in order on its row) or the last spike of one sample
+            // and the next sample's first.  A row's maximum is taken in the pass of its last spike.
+            int j = warp, k = 0, kend = 0;
+            auto seek = [&]() {   // from sample j on, the next own sample with nearby spikes
+                for (; j < own; j += kWarps) {
+                    const int w = rank + G * j;
+                    int lo = 0, hi = n_near;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (s_nw[mid] < w - nt) lo = mid + 1; else hi = mid;
+                    }
+                    int e = lo;
+                    while (e < n_near && s_nw[e] <= w + nt) ++e;
+                    if (e > lo) {
+                        k = lo;
+                        kend = e;
+                        return;
+                    }
                 }
-                while (k < n_near && s_nw[k] <= wp + nt) {
-                    const int k2 = k + 1;
-                    const bool two = k2 < n_near && s_nw[k2] <= wp + nt;
-                    const int k3 = two ? k2 + 1 : k2;
-                    const bool last = k3 >= n_near || s_nw[k3] > wp + nt;   // no further spike for this sample
-                    const float a0 = s_na[k], a1 = two ? s_na[k2] : 0.f;
-                    const float4* c0 = reinterpret_cast<const float4*>(ctcP + ((int64_t)s_nt[k] * L2 + (wp - s_nw[k] + nt)) * T);
-                    const float4* c1 = two ? reinterpret_cast<const float4*>(ctcP + ((int64_t)s_nt[k2] * L2 + (wp - s_nw[k2] + nt)) * T)
-                                           : c0;
-                    float4* b4 = reinterpret_cast<float4*>(br);
-                    const int T4 = T >> 2;
-                    for (int fb = 0; fb < T4; fb += 32 * kVec) {
-                        float4 v0[kVec], v1[kVec];
+            };
+            seek();
+            const int T4 = T >> 2;
+            auto ctc_row = [&](int kk, int w) {
+                return reinterpret_cast<const float4*>(ctcP + ((int64_t)s_nt[kk] * L2 + (w - s_nw[kk] + nt)) * T);
+            };
+            while (j < own) {
+                const int wA = rank + G * j;
+                const int kA = k;
+                const bool twoA = k + 1 < kend;
+                k += twoA ? 2 : 1;
+                const bool lastA = k >= kend;
+                if (lastA) {
+                    j += kWarps;
+                    seek();
+                }
+                int wB = -1, kB = -1;
+                bool lastB = false;
+                if (!twoA && j < own) {   // one spike of A: pair it with the next item
+                    wB = rank + G * j;
+                    kB = k;
+                    k += 1;
+                    lastB = k >= kend;
+                    if (lastB) {
+                        j += kWarps;
+                        seek();
+                    }
+                }
+                const bool hasB = kB >= 0;
+                const float aA0 = s_na[kA], a1 = twoA ? s_na[kA + 1] : (hasB ? s_na[kB] : 0.f);
+                const float4* c0 = ctc_row(kA, wA);
+                const float4* c1 = twoA ? ctc_row(kA + 1, wA) : (hasB ? ctc_row(kB, wB) : c0);
+                const bool has1 = twoA || hasB;
+                float4* bA = reinterpret_cast<float4*>(brow(wA));
+                float4* bB = reinterpret_cast<float4*>(hasB ? brow(wB) : brow(wA));
+                float bestA = -1.f, bestB = -1.f;
+                int biA = 0x7fffffff, biB = 0x7fffffff;
+                for (int fb = 0; fb < T4; fb += 32 * kVec) {
+                    float4 v0[kVec], v1[kVec];
 #pragma unroll
-                        for (int jj = 0; jj < kVec; ++jj) {
-                            const int f = fb + lane + 32 * jj;
-                            const bool ok = f < T4;
-                            v0[jj] = ok ? ld_keep(c0 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
-                            v1[jj] = (ok && two) ? ld_keep(c1 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
-                        }
+                    for (int jj = 0; jj < kVec; ++jj) {
+                        const int f = fb + lane + 32 * jj;
+                        const bool ok = f < T4;
+                        v0[jj] = ok ? ld_keep(c0 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        v1[jj] = (ok && has1) ? ld_keep(c1 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
 #pragma unroll
-                        for (int jj = 0; jj < kVec; ++jj) {
-                            const int f = fb + lane + 32 * jj;
-                            if (f < T4) {
-                                float4 x = b4[f];
-                                x.x = fmaf(-a0, v0[jj].x, x.x);
-                                x.y = fmaf(-a0, v0[jj].y, x.y);
-                                x.z = fmaf(-a0, v0[jj].z, x.z);
-                                x.w = fmaf(-a0, v0[jj].w, x.w);
-                                if (two) {
-                                    x.x = fmaf(-a1, v1[jj].x, x.x);
-                                    x.y = fmaf(-a1, v1[jj].y, x.y);
-                                    x.z = fmaf(-a1, v1[jj].z, x.z);
-                                    x.w = fmaf(-a1, v1[jj].w, x.w);
-                                }
-                                b4[f] = x;
-                                if (last) {
-                                    const int t = 4 * f;
-                                    const float4 im = reinterpret_cast<const float4*>(s_inm)[f];
+                    for (int jj = 0; jj < kVec; ++jj) {
+                        const int f = fb + lane + 32 * jj;
+                        if (f < T4) {
+                            const int t = 4 * f;
+                            float4 x = bA[f];
+                            x.x = fmaf(-aA0, v0[jj].x, x.x);
+                            x.y = fmaf(-aA0, v0[jj].y, x.y);
+                            x.z = fmaf(-aA0, v0[jj].z, x.z);
+                            x.w = fmaf(-aA0, v0[jj].w, x.w);
+                            if (twoA) {
+                                x.x = fmaf(-a1, v1[jj].x, x.x);
+                                x.y = fmaf(-a1, v1[jj].y, x.y);
+                                x.z = fmaf(-a1, v1[jj].z, x.z);
+                                x.w = fmaf(-a1, v1[jj].w, x.w);
+                            }
+                            bA[f] = x;
+                            const float4 im = reinterpret_cast<const float4*>(s_inm)[f];
+                            if (lastA) {
+                                float r, v;
+                                r = fmaxf(x.x, 0.f); v = r * r * im.x; if (v > bestA) { bestA = v; biA = t; }
+                                r = fmaxf(x.y, 0.f); v = r * r * im.y; if (v > bestA) { bestA = v; biA = t + 1; }
+                                r = fmaxf(x.z, 0.f); v = r * r * im.z; if (v > bestA) { bestA = v; biA = t + 2; }
+                                r = fmaxf(x.w, 0.f); v = r * r * im.w; if (v > bestA) { bestA = v; biA = t + 3; }
+                            }
+                            if (hasB) {
+                                float4 y = bB[f];
+                                y.x = fmaf(-a1, v1[jj].x, y.x);
+                                y.y = fmaf(-a1, v1[jj].y, y.y);
+                                y.z = fmaf(-a1, v1[jj].z, y.z);
+                                y.w = fmaf(-a1, v1[jj].w, y.w);
+                                bB[f] = y;
+                                if (lastB) {
                                     float r, v;
-                                    r = fmaxf(x.x, 0.f); v = r * r * im.x; if (v > best) { best = v; bi = t; }
-                                    r = fmaxf(x.y, 0.f); v = r * r * im.y; if (v > best) { best = v; bi = t + 1; }
-                                    r = fmaxf(x.z, 0.f); v = r * r * im.z; if (v > best) { best = v; bi = t + 2; }
-                                    r = fmaxf(x.w, 0.f); v = r * r * im.w; if (v > best) { best = v; bi = t + 3; }
+                                    r = fmaxf(y.x, 0.f); v = r * r * im.x; if (v > bestB) { bestB = v; biB = t; }
+                                    r = fmaxf(y.y, 0.f); v = r * r * im.y; if (v > bestB) { bestB = v; biB = t + 1; }
+                                    r = fmaxf(y.z, 0.f); v = r * r * im.z; if (v > bestB) { bestB = v; biB = t + 2; }
+                                    r = fmaxf(y.w, 0.f); v = r * r * im.w; if (v > bestB) { bestB = v; biB = t + 3; }
                                 }
                             }
                         }
                     }
-                    touched = true;
-                    k = two ? k2 + 1 : k + 1;
                 }
-            } else {
+                if (lastA) finish_sample(wA, bestA, biA);
+                if (hasB && lastB) finish_sample(wB, bestB, biB);
+            }
+        } else {
+            for (int j = warp; j < own; j += kWarps) {
+                const int wp = rank + G * j;
+                float* br = brow(wp);
+                float best = -1.f;
+                int bi = 0x7fffffff;
+                bool touched = false;
                 // general shapes or an overfull list: the 2nt+1 neighbours from the spike maps,
                 // scalar rows
                 int n_sp = 0;
@@ -479,8 +534,8 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                         touched = true;
                     }
                 }
+                if (touched) finish_sample(wp, best, bi);
             }
-            if (touched) finish_sample(wp, best, bi);
         }
         n_total += total;
         group_barrier<G>();   // the changed samples' maxima are read by every CTA in B1
