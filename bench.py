@@ -63,6 +63,8 @@ def args_():
     ap.add_argument("--cpu-sample", type=int, default=6, help="batches timed on the CPU oracle")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--match-variant", type=int, default=0, help="0 auto, 1 scores in L2, 2 scores in SMEM")
+    ap.add_argument("--gemm-path", type=int, default=0,
+                    help="0 tcgen05 FP32 (3xTF32), 1 FP32 SIMT, 2 tcgen05 with TF32 data (two products)")
     ap.add_argument("--path", default="sort", choices=["sort", "tc"],
                     help="sort = template matching (default); tc = threshold crossing")
     ap.add_argument("--tc-rows", type=int, default=600_000, help="rows per threshold-crossing push")
@@ -262,7 +264,7 @@ def run_gpu(a):
     base_ptr = d_data.data_ptr()
     row_bytes = C * 2
     s = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1,
-                           match_variant=a.match_variant)
+                           match_variant=a.match_variant, gemm_path=a.gemm_path)
     ext = torch.cuda.ExternalStream(s.cuda_stream(), device=f"cuda:{dev}")
     spikes_seen = [0]
 
@@ -313,7 +315,7 @@ def run_gpu(a):
 
     # ---- end to end through the host API ---------------------------------------------------
     s2 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
-                             match_variant=a.match_variant)
+                             match_variant=a.match_variant, gemm_path=a.gemm_path)
     chunk = G * NT
     pos = [0]
     obuf = np.zeros(1 << 16, sorter.SPIKE_DTYPE)
@@ -365,7 +367,7 @@ def run_gpu(a):
 
     # ---- per-batch latency (one batch per launch) --------------------------------------------
     s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1, profile=1,
-                             match_variant=a.match_variant)
+                             match_variant=a.match_variant, gemm_path=a.gemm_path)
     lat = []
     s3.push(data[:NT + 2 * nt], 0)
     drain(s3)

@@ -54,7 +54,9 @@ typedef struct lss_params {
     int32_t profile;        /* 1 = time every stage with CUDA events (lss_stage_times) */
     int32_t match_variant;  /* 0 = automatic; 1 = scores in L2, 8-CTA clusters; 2 = scores in shared memory;
                                3 = scores in L2, 16-CTA clusters of 1024 threads (one CTA per SM) */
-    int32_t gemm_path;      /* 0 = tensor cores (tcgen05, 3xTF32 = FP32 accuracy) where shapes allow; 1 = FP32 SIMT */
+    int32_t gemm_path;      /* 0 = tensor cores (tcgen05, 3xTF32 = FP32 accuracy) where shapes allow; 1 = FP32 SIMT;
+                               2 = tensor cores with the data operands stored once as TF32 (two products; the
+                               fixed matrices keep FP32 accuracy): faster, spike agreement with 0 measured */
     int32_t reserved[3];
 } lss_params;
 

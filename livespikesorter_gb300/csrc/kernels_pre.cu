@@ -142,7 +142,7 @@ car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* _
 // channel, tf32-split into (Xt_hi, Xt_lo); columns past W + L + R up to the row pitch are zeroed.
 constexpr int kCarTRows = 32;
 
-template <int NJ>
+template <int NJ, bool LO>
 __global__ void __launch_bounds__(kCarWarps * 32)
 car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C, int W,
              int NT, const long long* __restrict__ colsum, int L, int R, int pitch, float* __restrict__ Xt_hi,
@@ -189,14 +189,21 @@ car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t*
             const int w = w0 + rr;
             float h, l;
             tf32_split_(s_y[rr * ld + c], h, l);
+            // (the remainder is absent on the tier that feeds TF32 data to the tensor cores)
             Xt_hi[rbase + w + L] = h;
-            Xt_lo[rbase + w + L] = l;
-            if (w >= W - L) { Xt_hi[rbase + w + L - W] = h; Xt_lo[rbase + w + L - W] = l; }
-            if (w < R) { Xt_hi[rbase + w + L + W] = h; Xt_lo[rbase + w + L + W] = l; }
+            if constexpr (LO) Xt_lo[rbase + w + L] = l;
+            if (w >= W - L) {
+                Xt_hi[rbase + w + L - W] = h;
+                if constexpr (LO) Xt_lo[rbase + w + L - W] = l;
+            }
+            if (w < R) {
+                Xt_hi[rbase + w + L + W] = h;
+                if constexpr (LO) Xt_lo[rbase + w + L + W] = l;
+            }
         }
         if (blockIdx.x == 0 && rr < pitch - total) {   // row padding read by the last tiles' band
             Xt_hi[rbase + total + rr] = 0.f;
-            Xt_lo[rbase + total + rr] = 0.f;
+            if constexpr (LO) Xt_lo[rbase + total + rr] = 0.f;
         }
     }
 }
@@ -208,9 +215,15 @@ void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, i
     const size_t smem = (size_t)kCarTRows * (C + 1) * sizeof(float);
 #define LSS_CART(N)                                                                                        \
     do {                                                                                                   \
-        raise_smem_limit((const void*)car_t_kernel<N>, smem);                                              \
-        car_t_kernel<N><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, L, R,  \
-                                                           pitch, Xt_hi, Xt_lo);                           \
+        if (Xt_lo) {                                                                                       \
+            raise_smem_limit((const void*)car_t_kernel<N, true>, smem);                                    \
+            car_t_kernel<N, true><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
+                                                                     L, R, pitch, Xt_hi, Xt_lo);           \
+        } else {                                                                                           \
+            raise_smem_limit((const void*)car_t_kernel<N, false>, smem);                                   \
+            car_t_kernel<N, false><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
+                                                                      L, R, pitch, Xt_hi, nullptr);        \
+        }                                                                                                  \
     } while (0)
     if (nj <= 4) LSS_CART(4);
     else if (nj <= 8) LSS_CART(8);
@@ -336,7 +349,9 @@ __device__ __forceinline__ unsigned long long dup2(float x) {
 // of components one 8-byte load apart), each thread owns one channel and kConvRows rows, and every
 // tap multiplies the kConvRows inputs it meets in packed pairs (fma.rn.f32x2, two fmaf per
 // instruction).  Taps are applied in ascending order, as in basis_conv_generic.
-template <int NT_, int K_>
+// HI_ONLY: store tf32(x) alone (the tier that feeds TF32 data to the tensor cores); otherwise the
+// tf32 split when Blo is given, else the fp32 values
+template <int NT_, int K_, bool HI_ONLY>
 __global__ void __launch_bounds__(128)
 basis_conv_x2(const float* __restrict__ Z, int C, int W, const float* __restrict__ wPCA, float* __restrict__ Bpc,
               float* __restrict__ Blo) {
@@ -390,7 +405,11 @@ basis_conv_x2(const float* __restrict__ Z, int C, int W, const float* __restrict
                 for (int h = 0; h < 2; ++h) {
                     const float a = h ? v.y : v.x;
                     const int64_t o = ((int64_t)w * K_ + 2 * j + h) * C + c;
-                    if (lb) {
+                    if constexpr (HI_ONLY) {
+                        float hi, lo;
+                        tf32_split(a, hi, lo);
+                        ob[o] = hi;
+                    } else if (lb) {
                         float hi, lo;
                         tf32_split(a, hi, lo);
                         ob[o] = hi;
@@ -407,7 +426,7 @@ basis_conv_x2(const float* __restrict__ Z, int C, int W, const float* __restrict
 // Any (nt, K <= 8): basis read from global memory (cached).
 __global__ void __launch_bounds__(128)
 basis_conv_generic(const float* __restrict__ Z, int C, int W, const float* __restrict__ wPCA, int K, int nt,
-                   float* __restrict__ Bpc, float* __restrict__ Blo) {
+                   float* __restrict__ Bpc, float* __restrict__ Blo, bool round_tf32) {
     const int b = blockIdx.z;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int w0 = blockIdx.y * kConvRows;
@@ -440,11 +459,11 @@ basis_conv_generic(const float* __restrict__ Z, int C, int W, const float* __res
         if (w < W)
             for (int k = 0; k < K; ++k) {
                 const int64_t o = ((int64_t)w * K + k) * C + c;
-                if (lb) {
+                if (lb || round_tf32) {
                     float h, l;
                     tf32_split(acc[r][k], h, l);
                     ob[o] = h;
-                    lb[o] = l;
+                    if (lb) lb[o] = l;
                 } else {
                     ob[o] = acc[r][k];
                 }
@@ -456,13 +475,16 @@ basis_conv_generic(const float* __restrict__ Z, int C, int W, const float* __res
 
 // Host-side basis (needed for the parameter-bank specialisation).
 void launch_basis_conv_host(const float* Z, int C, int W, const float* wPCA_dev, const float* wPCA_host, int K,
-                            int nt, int nb, float* Bpc, cudaStream_t s, float* Blo) {
+                            int nt, int nb, float* Bpc, cudaStream_t s, float* Blo, bool round_tf32) {
     dim3 grid((C + 127) / 128, (W + kConvRows - 1) / kConvRows, nb);
     (void)wPCA_host;
     if (nt == 61 && K == 6) {
-        basis_conv_x2<61, 6><<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, Bpc, Blo);
+        if (round_tf32 && !Blo)
+            basis_conv_x2<61, 6, true><<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, Bpc, nullptr);
+        else
+            basis_conv_x2<61, 6, false><<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, Bpc, Blo);
     } else {
-        basis_conv_generic<<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, K, nt, Bpc, Blo);
+        basis_conv_generic<<<grid, 128, 0, s>>>(Z, C, W, wPCA_dev, K, nt, Bpc, Blo, round_tf32);
     }
 }
 

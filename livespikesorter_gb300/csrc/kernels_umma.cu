@@ -112,13 +112,16 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                  : "memory");
 }
 
-template <int BN, int MODE>
+// ALO = false: A is TF32 data without a remainder (the two products hi_a*hi_b + hi_a*lo_b; the
+// fixed B operand keeps its split), for the tensor-core tier whose activations are stored once
+template <int BN, int MODE, bool ALO>
 __global__ void __launch_bounds__(128, 1)
 umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
                  const __grid_constant__ CUtensorMap tB_hi, const __grid_constant__ CUtensorMap tB_lo, UmmaArgs args) {
     constexpr int kBN = BN;
     constexpr int kTileB = kBN * kBK * 4;
     constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;
+    constexpr int kLoadBytes = ALO ? kStageBytes : kTileA + 2 * kTileB;   // bytes the TMA lands per stage
     constexpr int kStages = kSmemBudget / kStageBytes;
     const int M = args.M, N = args.N, K = args.K;
     int* err = args.err;
@@ -169,14 +172,14 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
                 break;
             }
             const uint32_t fb = smem_u32(&full_bar[s]);
-            mbar_expect_tx(fb, kStageBytes);
+            mbar_expect_tx(fb, kLoadBytes);
             const int k0 = kt * kBK;   // a multiple of 16 fp32 = 64 bytes
             // Toeplitz: A columns start at the tile's output time n0 (a multiple of 128), B is the
             // same band matrix for every tile
             const int ax = (MODE == kToeplitz) ? n0 + k0 : k0;
             const int by = (MODE == kToeplitz) ? 0 : n0;
             tma_load_2d(sA_hi(s), &tA_hi, fb, ax, m0);
-            tma_load_2d(sA_lo(s), &tA_lo, fb, ax, m0);
+            if constexpr (ALO) tma_load_2d(sA_lo(s), &tA_lo, fb, ax, m0);
             tma_load_2d(sB_hi(s), &tB_hi, fb, k0, by);
             tma_load_2d(sB_lo(s), &tB_lo, fb, k0, by);
             ++issued;
@@ -202,7 +205,7 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
                 const uint64_t bh = smem_desc(sB_hi(s) + off), bl = smem_desc(sB_lo(s) + off);
                 mma_tf32<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
                 mma_tf32<BN>(tmem, ah, bl, 1u);
-                mma_tf32<BN>(tmem, al, bh, 1u);
+                if constexpr (ALO) mma_tf32<BN>(tmem, al, bh, 1u);
             }
             mma_commit(smem_u32(&empty_bar[s]));        // frees the stage once these MMAs finish
         }
@@ -239,7 +242,7 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
                         asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
                         const int64_t o = ((int64_t)b * args.wlen + w) * args.chans + c;
                         args.out[o] = __uint_as_float(h);
-                        args.out_lo[o] = v - __uint_as_float(h);
+                        if (args.out_lo) args.out_lo[o] = v - __uint_as_float(h);
                     }
                 }
             }
@@ -316,6 +319,7 @@ bool make_map(CUtensorMap* m, const float* ptr, uint64_t rows, uint64_t cols, ui
 
 struct UmmaOperands {
     CUtensorMap a_hi, a_lo, b_hi, b_lo;
+    bool has_a_lo = true;     // false: A is TF32 data alone (two products)
     int rows_a = 0, rows_b = 0, K = 0;
     int cols_a = 0;           // Toeplitz: columns of A (wrapped window length, padded)
 };
@@ -333,6 +337,8 @@ UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, co
     u->rows_a = (int)rows_a;
     u->rows_b = (int)rows_b;
     u->K = K;
+    u->has_a_lo = a_lo != nullptr;
+    if (!a_lo) a_lo = a_hi;   // the map is never used
     if (!make_map(&u->a_hi, a_hi, rows_a, K, kBM) || !make_map(&u->a_lo, a_lo, rows_a, K, kBM) ||
         !make_map(&u->b_hi, b_hi, rows_b, K, kPlainBN) || !make_map(&u->b_lo, b_lo, rows_b, K, kPlainBN)) {
         delete u;
@@ -349,6 +355,8 @@ UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t r
     u->cols_a = (int)cols;
     u->rows_b = kToepBN;
     u->K = K;
+    u->has_a_lo = x_lo != nullptr;
+    if (!x_lo) x_lo = x_hi;   // the map is never used
     if (!make_map(&u->a_hi, x_hi, rows, cols, kBM) || !make_map(&u->a_lo, x_lo, rows, cols, kBM) ||
         !make_map(&u->b_hi, g_hi, kToepBN, K, kToepBN) || !make_map(&u->b_lo, g_lo, kToepBN, K, kToepBN)) {
         delete u;
@@ -361,7 +369,7 @@ void umma_free(UmmaOperands* u) { delete u; }
 
 cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, int* err, cudaStream_t s) {
     if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
-    auto kern = umma_gemm_3xtf32<kPlainBN, kPlain>;
+    auto kern = u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true> : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
     constexpr int smem = smem_bytes<kPlainBN>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
@@ -381,7 +389,7 @@ cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int
 cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W, int* err,
                                  cudaStream_t s) {
     if (!u || nb * C > u->rows_a) return cudaErrorInvalidValue;
-    auto kern = umma_gemm_3xtf32<kToepBN, kToeplitz>;
+    auto kern = u->has_a_lo ? umma_gemm_3xtf32<kToepBN, kToeplitz, true> : umma_gemm_3xtf32<kToepBN, kToeplitz, false>;
     constexpr int smem = smem_bytes<kToepBN>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;

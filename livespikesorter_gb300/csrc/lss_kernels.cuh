@@ -69,7 +69,8 @@ void launch_sgemm_nt(const float* A, int64_t lda, int64_t strideA, const float* 
 // wPCA_host (K*nt floats) enables the specialisation with the basis in the parameter bank;
 // Blo != nullptr writes the tf32 split like launch_highpass.
 void launch_basis_conv_host(const float* Z, int C, int W, const float* wPCA_dev, const float* wPCA_host, int K,
-                            int nt, int nb, float* Bpc, cudaStream_t s, float* Blo = nullptr);
+                            int nt, int nb, float* Bpc, cudaStream_t s, float* Blo = nullptr,
+                            bool round_tf32 = false);
 
 // tensor-core (tcgen05) FP32-accurate GEMM C[m][n] = sum_k A[m][k] B[n][k] from tf32-split operands
 struct UmmaOperands;

@@ -137,6 +137,7 @@ struct Handle {
     float *d_WD_hi = nullptr, *d_WD_lo = nullptr, *d_Wall3_hi = nullptr, *d_Wall3_lo = nullptr;
     bool tc_whiten = false, tc_project = false;   // GEMMs on the tensor cores
     bool tc_highpass = false;                     // circular high-pass as a tensor-core band GEMM
+    bool tf32_data = false;   // gemm_path 2: activations stored once as TF32, two products per GEMM
     UmmaOperands* um_whiten = nullptr;
     UmmaOperands* um_project = nullptr;
     int* h_gemm_err = nullptr;                    // mapped: device-side wait timeouts
@@ -326,7 +327,9 @@ void Handle::init(const char* dir, const lss_params* prm) {
     d_iU = dev_upload(m.iU, dev_bytes, st);
     d_chan = (Cin > C) ? dev_upload(chan, dev_bytes, st) : nullptr;
     // tensor-core GEMMs need K % 16 == 0 and N <= 512 (C for the whitening, T for the projection)
-    const bool want_tc = p.gemm_path == 0;
+    if (p.gemm_path < 0 || p.gemm_path > 2) throw LoadError{LSS_ERR_ARG, "lss_params.gemm_path must be 0, 1 or 2"};
+    const bool want_tc = p.gemm_path == 0 || p.gemm_path == 2;
+    tf32_data = p.gemm_path == 2;
     tc_whiten = want_tc && C % 16 == 0 && C <= 512;
     tc_project = want_tc && (K * C) % 16 == 0 && T <= 512;
     tc_highpass = tc_whiten;
@@ -409,7 +412,8 @@ void Handle::ensure_work(int Wn, int nb) {
     raw_rows_cap = (size_t)nba * (size_t)std::max(Wa, NT) + 2 * (size_t)nt;
     const int64_t need = (int64_t)kSlots * raw_rows_cap * Cin * 2 + (int64_t)nba * C * 8 +
                          (int64_t)nba * (Wa + LRmax) * C * 4 + 2LL * nba * Wa * C * 4 +
-                         (int64_t)nba * Wa * K * C * 4 * (tc_project ? 2 : 1) + (int64_t)nba * Wa * C * 4 * (tc_whiten ? 1 : 0) +
+                         (int64_t)nba * Wa * K * C * 4 * (tc_project && !tf32_data ? 2 : 1) +
+                         (int64_t)nba * Wa * C * 4 * (tc_whiten && !tf32_data ? 1 : 0) +
                          (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16;
     if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
         throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
@@ -420,9 +424,11 @@ void Handle::ensure_work(int Wn, int nb) {
         // row pitch of any window length up to Wa: W + L + R <= 2W - 1, rounded up to 4
         const size_t n = (size_t)nba * C * (size_t)((2 * Wa + 3) / 4 * 4);
         d_Xt_hi = dev_alloc<float>(n, dev_bytes);
-        d_Xt_lo = dev_alloc<float>(n, dev_bytes);
         LSS_CUDA(cudaMemsetAsync(d_Xt_hi, 0, n * sizeof(float), st));
-        LSS_CUDA(cudaMemsetAsync(d_Xt_lo, 0, n * sizeof(float), st));
+        if (!tf32_data) {
+            d_Xt_lo = dev_alloc<float>(n, dev_bytes);
+            LSS_CUDA(cudaMemsetAsync(d_Xt_lo, 0, n * sizeof(float), st));
+        }
     } else {
         d_Xw = dev_alloc<float>((size_t)nba * (Wa + LRmax) * C, dev_bytes);
     }
@@ -430,8 +436,8 @@ void Handle::ensure_work(int Wn, int nb) {
     d_Z = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     d_Bpc = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
     d_Bt = dev_alloc<float>((size_t)nba * Wa * T, dev_bytes);
-    if (tc_whiten) d_Y_lo = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
-    if (tc_project) d_Bpc_lo = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
+    if (tc_whiten && !tf32_data) d_Y_lo = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
+    if (tc_project && !tf32_data) d_Bpc_lo = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
     sc.cfmax = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
     sc.imax = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
     sc.at_t = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
@@ -526,7 +532,7 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
         launch_sgemm_nt(d_Y, C, (int64_t)Wn * C, d_WD, C, d_Z, C, (int64_t)Wn * C, Wn, C, C, nb, st);
     ++nl;
     mark();
-    launch_basis_conv_host(d_Z, C, Wn, d_wPCA, m.wPCA.data(), K, nt, nb, d_Bpc, st, tc_project ? d_Bpc_lo : nullptr),
+    launch_basis_conv_host(d_Z, C, Wn, d_wPCA, m.wPCA.data(), K, nt, nb, d_Bpc, st, d_Bpc_lo, tc_project && tf32_data),
         ++nl;
     mark();
     if (tc_project)
