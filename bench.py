@@ -65,6 +65,7 @@ def args_():
     ap.add_argument("--match-variant", type=int, default=0, help="0 auto, 1 scores in L2, 2 scores in SMEM")
     ap.add_argument("--gemm-path", type=int, default=0,
                     help="0 tcgen05 FP32 (3xTF32), 1 FP32 SIMT, 2 tcgen05 with TF32 data (two products)")
+    ap.add_argument("--no-tier", action="store_true", help="skip the chosen-tier measurement")
     ap.add_argument("--path", default="sort", choices=["sort", "tc"],
                     help="sort = template matching (default); tc = threshold crossing")
     ap.add_argument("--tc-rows", type=int, default=600_000, help="rows per threshold-crossing push")
@@ -235,6 +236,29 @@ def roofline(stage_ms, n_groups, group, C, T, K, nt, W, ntaps, spikes_per_batch)
             "ms_per_launch": ms, "stage_ms_per_launch": per}
 
 
+def spike_agreement(ref, got, tol=1):
+    """Fraction of ref spikes with a got spike of the same template within tol samples, and the
+    fraction of those whose amplitudes agree within 1e-3 relative (each got spike used once)."""
+    if len(ref) == 0:
+        return 1.0, 1.0
+    order = np.lexsort((got["time"], got["tmpl"]))
+    gt, gk, ga = got["time"][order], got["tmpl"][order], got["amp"][order]
+    used = np.zeros(len(gt), bool)
+    matched = amp_ok = 0
+    for t, k, amp in zip(ref["time"], ref["tmpl"], ref["amp"]):
+        lo = np.searchsorted(gk, k, "left")
+        hi = np.searchsorted(gk, k, "right")
+        i0 = lo + np.searchsorted(gt[lo:hi], t - tol, "left")
+        i1 = lo + np.searchsorted(gt[lo:hi], t + tol, "right")
+        for i in range(i0, i1):
+            if not used[i]:
+                used[i] = True
+                matched += 1
+                amp_ok += abs(ga[i] - amp) <= 1e-3 * max(abs(amp), 1e-12)
+                break
+    return matched / len(ref), amp_ok / max(1, matched)
+
+
 def run_gpu(a):
     import torch
     rank = int(os.environ.get("RANK", "0"))
@@ -311,6 +335,50 @@ def run_gpu(a):
     ntaps = 1281
     roof = roofline(stage, n_timed, G, C, T, K, nt, W, ntaps, spikes_per_batch)
     s.close()
+
+    # ---- the faster tier (gemm_path 2) beside the plain FP32 path ---------------------------
+    tier = None
+    if a.gemm_path == 0 and not a.no_tier:
+        st = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1,
+                                 match_variant=a.match_variant, gemm_path=2)
+        ext2 = torch.cuda.ExternalStream(st.cuda_stream(), device=f"cuda:{dev}")
+
+        def step2(i):
+            g0 = (i % n_groups) * G
+            st.push_device_span(base_ptr + g0 * NT * row_bytes, G, i * G * NT)
+
+        for i in range(a.warmup):
+            step2(i)
+        drain(st)
+        tb, nb0 = st.stage_times()
+        torch.cuda.synchronize(dev)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext2):
+            f0.record(ext2)
+        for i in range(a.steps):
+            step2(a.warmup + i)
+        with torch.cuda.stream(ext2):
+            f1.record(ext2)
+        f1.synchronize()
+        ms2 = f0.elapsed_time(f1)
+        drain(st)
+        ta, na = st.stage_times()
+        st.close()
+        # spike agreement with the FP32 path on the same 256 batches, streamed
+        n_rows = min(data.shape[0], 256 * NT + 2 * nt)
+        got = {}
+        for path in (0, 2):
+            with sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
+                                     match_variant=a.match_variant, gemm_path=path) as sa:
+                got[path] = sa.sort_stream(data[:n_rows])
+        frac, amp_ok = spike_agreement(got[0], got[2])
+        tier = {"gemm_path": 2, "value": a.steps * G * NT * C / (ms2 / 1e3), "unit": UNIT,
+                "ms_per_step": ms2 / a.steps, "dtype": "tf32 activations x fp32-split fixed matrices, fp32 accumulate",
+                "stage_ms_per_launch": {k: (ta[k] - tb[k]) / max(1, na - nb0) for k in ta},
+                "agreement_vs_fp32": {"batches": (n_rows - 2 * nt) // NT, "spikes_fp32": int(len(got[0])),
+                                      "spikes_tier": int(len(got[2])), "matched": frac, "amp_within_1e-3": amp_ok,
+                                      "rule": "same template, |dt| <= 1 sample, amplitude within 1e-3 relative"}}
     del d_data
 
     # ---- end to end through the host API ---------------------------------------------------
@@ -403,7 +471,7 @@ def run_gpu(a):
                 "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded generator, shapes of the named config)",
                 "config": workload_config(a, cfg, G), "e2e": e2e, "latency": latency, "roofline": roof,
-                "cpu_baseline": cpu, "clocks": clk.summary(),
+                "cpu_baseline": cpu, "clocks": clk.summary(), "chosen_tier": tier,
                 "gpu_launches": launches_per_step * a.steps,
                 "spikes_per_batch": spikes_per_batch,
                 "realtime_factor": value / (C * 30000.0)}
