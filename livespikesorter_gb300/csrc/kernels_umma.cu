@@ -4,12 +4,14 @@
 //
 // FP32 accuracy from TF32 units: every operand x is stored as hi = tf32(x) and lo = tf32(x - hi)
 // (split_tf32_kernel), and the tile accumulates hi*hi + hi*lo + lo*hi in FP32.  The dropped lo*lo
-// term and the truncation of lo are below 2^-21 of |x*y|, i.e. at FP32 rounding level.
+// term and the truncation of lo are below 2^-21 of |x*y|, i.e. at FP32 rounding level.  The faster
+// tier stores the data operand A once as tf32(x) and accumulates hi*hi + hi*lo (the fixed B keeps
+// its split), an error of about 2^-12 of |x*y| per product.
 //
-// One CTA (4 warps) computes a 128 x 256 tile: warp 0 / lane 0 streams A and B tiles into shared
+// One CTA (4 warps) computes a 128 x N tile: warp 0 / lane 0 streams A and B tiles into shared
 // memory with TMA (cp.async.bulk.tensor, 64-byte swizzle) through a 4-stage mbarrier pipeline;
-// warp 1 / lane 0 issues tcgen05.mma.kind::tf32 (M = 128, N = 256, K = 8) into a 256-column TMEM
-// accumulator and releases each stage with tcgen05.commit; all four warps then read the
+// warp 1 / lane 0 issues tcgen05.mma.kind::tf32 (M = 128, N = 128 or 256, K = 8) into an N-column
+// TMEM accumulator and releases each stage with tcgen05.commit; all four warps then read the
 // accumulator back with tcgen05.ld (each warp its 32 TMEM lanes = tile rows) and store it.
 // Every wait is bounded (globaltimer); on a timeout the kernel sets an error word, waits (bounded)
 // for the copies it issued, frees its TMEM and returns.
@@ -31,8 +33,9 @@ constexpr uint64_t kWaitNs = 2000000000ull;             // 2 s
 // Two uses of one kernel:
 //   kPlain     C[m][n] = sum_k A[m][k] B[n][k]; tile N = 256; B rows = n
 //   kToeplitz  the circular high-pass: A = channel-major wrapped windows [(b, c)][time], B = a fixed
-//              128 x K band matrix G[j][k] = taps[k - j]; the tile at output time w0 reads A columns
-//              w0 + k, and the epilogue stores Y[b][w0 + j][c] as its tf32 split (hi, lo)
+//              N x K band matrix G[j][k] = taps[k - j] (N = 256 output times per tile for groups of
+//              batches, 128 for a few); the tile at output time w0 reads A columns w0 + k, and the
+//              epilogue stores Y[b][w0 + j][c] as its tf32 split (hi, lo) or as tf32 alone
 enum UmmaMode { kPlain = 0, kToeplitz = 1 };
 
 struct UmmaArgs {
@@ -324,7 +327,7 @@ struct UmmaOperands {
     int cols_a = 0;           // Toeplitz: columns of A (wrapped window length, padded)
 };
 
-constexpr int kPlainBN = 256, kToepBN = 128;
+constexpr int kPlainBN = 256;
 template <int BN>
 constexpr int smem_bytes() {
     return (kSmemBudget / (2 * kTileA + 2 * BN * kBK * 4)) * (2 * kTileA + 2 * BN * kBK * 4) + 1024;
@@ -347,18 +350,18 @@ UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, co
     return u;
 }
 
-UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t rows, int64_t cols, const float* g_hi,
-                                 const float* g_lo, int K) {
-    if (K % kBK != 0 || cols % 4 != 0) return nullptr;
+UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t rows, int64_t cols, int tile,
+                                 const float* g_hi, const float* g_lo, int K) {
+    if (K % kBK != 0 || cols % 4 != 0 || (tile != kHighpassTileSmall && tile != kHighpassTileLarge)) return nullptr;
     auto* u = new UmmaOperands();
     u->rows_a = (int)rows;
     u->cols_a = (int)cols;
-    u->rows_b = kToepBN;
+    u->rows_b = tile;
     u->K = K;
     u->has_a_lo = x_lo != nullptr;
     if (!x_lo) x_lo = x_hi;   // the map is never used
     if (!make_map(&u->a_hi, x_hi, rows, cols, kBM) || !make_map(&u->a_lo, x_lo, rows, cols, kBM) ||
-        !make_map(&u->b_hi, g_hi, kToepBN, K, kToepBN) || !make_map(&u->b_lo, g_lo, kToepBN, K, kToepBN)) {
+        !make_map(&u->b_hi, g_hi, tile, K, tile) || !make_map(&u->b_lo, g_lo, tile, K, tile)) {
         delete u;
         return nullptr;
     }
@@ -386,11 +389,11 @@ cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int
 }
 
 // Y[b][w][c] (tf32 split) = circular high-pass of nb windows held channel-major in the operands
-cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W, int* err,
-                                 cudaStream_t s) {
-    if (!u || nb * C > u->rows_a) return cudaErrorInvalidValue;
-    auto kern = u->has_a_lo ? umma_gemm_3xtf32<kToepBN, kToeplitz, true> : umma_gemm_3xtf32<kToepBN, kToeplitz, false>;
-    constexpr int smem = smem_bytes<kToepBN>();
+template <int TILE>
+static cudaError_t launch_highpass_tile(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W,
+                                        int* err, cudaStream_t s) {
+    auto kern = u->has_a_lo ? umma_gemm_3xtf32<TILE, kToeplitz, true> : umma_gemm_3xtf32<TILE, kToeplitz, false>;
+    constexpr int smem = smem_bytes<TILE>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
     UmmaArgs a{};
@@ -402,9 +405,17 @@ cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo
     a.chans = C;
     a.wlen = W;
     a.err = err;
-    dim3 grid((W + kToepBN - 1) / kToepBN, (nb * C + kBM - 1) / kBM);
+    dim3 grid((W + TILE - 1) / TILE, (nb * C + kBM - 1) / kBM);
     kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     return cudaGetLastError();
+}
+
+cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W, int* err,
+                                 cudaStream_t s) {
+    if (!u || nb * C > u->rows_a) return cudaErrorInvalidValue;
+    if (u->rows_b == kHighpassTileLarge)
+        return launch_highpass_tile<kHighpassTileLarge>(u, Y_hi, Y_lo, nb, C, W, err, s);
+    return launch_highpass_tile<kHighpassTileSmall>(u, Y_hi, Y_lo, nb, C, W, err, s);
 }
 
 }  // namespace lss

@@ -51,6 +51,11 @@ constexpr int kMatchThreads = 512;       // matching loop, scores in L2 (two CTA
 constexpr int kMatchThreadsSmem = 768;   // matching loop, scores in shared memory (one CTA per SM)
 constexpr int kMatchThreadsWide = 1024;  // matching loop, scores in L2, 16-CTA clusters, one CTA per SM
 
+// output times per tile of the tensor-core high-pass (the band matrix is tile x Kt): 256 for
+// groups of batches (the window tiles are re-read half as often), 128 for a few batches (twice
+// the CTAs for one window)
+constexpr int kHighpassTileSmall = 128, kHighpassTileLarge = 256, kHighpassSmallGroup = 8;
+
 // raise (never lower) a kernel's dynamic shared-memory limit on the current device
 cudaError_t raise_smem_limit(const void* kernel, size_t bytes);
 
@@ -80,7 +85,7 @@ void umma_free(UmmaOperands* u);
 cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, int* err, cudaStream_t s);
 // circular high-pass on the tensor cores: x = channel-major windows [rows][cols] (tf32 split),
 // g = the 128 x K band matrix of the taps (tf32 split)
-UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t rows, int64_t cols, const float* g_hi,
+UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t rows, int64_t cols, int tile, const float* g_hi,
                                  const float* g_lo, int K);
 cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W, int* err,
                                  cudaStream_t s);

@@ -83,12 +83,15 @@ void par_memcpy(void* dst, const void* src, size_t bytes) {
 struct TapSet {
     float* d = nullptr;          // taps, zero-padded to a multiple of 32 (SIMT FIR)
     int L = 0, R = 0;
-    // tensor-core high-pass: the 128 x Kt band matrix G[j][k] = taps[k - j] (tf32 split), the row
-    // pitch of the channel-major window buffer and the tensor maps over it
-    float *g_hi = nullptr, *g_lo = nullptr;
-    int Kt = 0, pitch = 0;
-    UmmaOperands* um = nullptr;
+    // tensor-core high-pass, for the small [0] and large [1] output tiles: the tile x Kt band
+    // matrix G[j][k] = taps[k - j] (tf32 split) and the tensor maps over the channel-major window
+    // buffer, whose row pitch is `pitch`
+    float *g_hi[2] = {}, *g_lo[2] = {};
+    int Kt[2] = {};
+    int pitch = 0;
+    UmmaOperands* um[2] = {};
 };
+constexpr int kHighpassTile[2] = {kHighpassTileSmall, kHighpassTileLarge};
 
 constexpr int kSlots = 4;   // groups in flight + the one collecting the stream's next rows
 
@@ -198,8 +201,10 @@ Handle::~Handle() {
     free_work();
     for (auto& kv : taps) {
         cudaFree(kv.second.d);
-        if (kv.second.g_hi) cudaFree(kv.second.g_hi);
-        if (kv.second.g_lo) cudaFree(kv.second.g_lo);
+        for (int v = 0; v < 2; ++v) {
+            if (kv.second.g_hi[v]) cudaFree(kv.second.g_hi[v]);
+            if (kv.second.g_lo[v]) cudaFree(kv.second.g_lo[v]);
+        }
     }
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
@@ -225,10 +230,11 @@ void Handle::free_work() {
     umma_free(um_whiten);
     umma_free(um_project);
     um_whiten = um_project = nullptr;
-    for (auto& kv : taps) {
-        umma_free(kv.second.um);
-        kv.second.um = nullptr;
-    }
+    for (auto& kv : taps)
+        for (int v = 0; v < 2; ++v) {
+            umma_free(kv.second.um[v]);
+            kv.second.um[v] = nullptr;
+        }
     for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
                     (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo,
                     (void*)sc.cfmax, (void*)sc.imax, (void*)sc.at_t, (void*)sc.at_amp, (void*)sc.dirty,
@@ -379,20 +385,24 @@ TapSet& Handle::taps_for(int Wn) {
     ts.R = (int)R;
     ts.d = dev_upload(tv, dev_bytes, st);
     if (tc_highpass) {
-        const int ntaps = (int)(L + R + 1), TB = 128;
-        ts.Kt = ((TB + ntaps - 1) + 15) / 16 * 16;
+        const int ntaps = (int)(L + R + 1);
         ts.pitch = (int)(((Wn + L + R) + 3) / 4 * 4);
-        std::vector<float> G((size_t)TB * ts.Kt, 0.f);
-        for (int j = 0; j < TB; ++j)
-            for (int d = 0; d < ntaps; ++d) G[(size_t)j * ts.Kt + j + d] = tv[(size_t)d];
-        float* g = dev_upload(G, dev_bytes, st);
-        ts.g_hi = dev_alloc<float>(G.size(), dev_bytes);
-        ts.g_lo = dev_alloc<float>(G.size(), dev_bytes);
-        launch_split_tf32(g, ts.g_hi, ts.g_lo, (int64_t)G.size(), st);
-        LSS_CUDA(cudaGetLastError());
-        LSS_CUDA(cudaStreamSynchronize(st));
-        cudaFree(g);
-        dev_bytes -= (int64_t)G.size() * 4;
+        for (int v = 0; v < 2; ++v) {
+            const int TB = kHighpassTile[v];
+            const int Kt = ((TB + ntaps - 1) + 15) / 16 * 16;
+            ts.Kt[v] = Kt;
+            std::vector<float> G((size_t)TB * Kt, 0.f);
+            for (int j = 0; j < TB; ++j)
+                for (int d = 0; d < ntaps; ++d) G[(size_t)j * Kt + j + d] = tv[(size_t)d];
+            float* g = dev_upload(G, dev_bytes, st);
+            ts.g_hi[v] = dev_alloc<float>(G.size(), dev_bytes);
+            ts.g_lo[v] = dev_alloc<float>(G.size(), dev_bytes);
+            launch_split_tf32(g, ts.g_hi[v], ts.g_lo[v], (int64_t)G.size(), st);
+            LSS_CUDA(cudaGetLastError());
+            LSS_CUDA(cudaStreamSynchronize(st));
+            cudaFree(g);
+            dev_bytes -= (int64_t)G.size() * 4;
+        }
     }
     LSS_CUDA(cudaStreamSynchronize(st));
     return taps.emplace(Wn, ts).first->second;
@@ -511,13 +521,15 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
     mark();
     if (tc_highpass) {
         TapSet& tw = const_cast<TapSet&>(ts);
-        if (!tw.um) {
-            tw.um = umma_make_toeplitz(d_Xt_hi, d_Xt_lo, (int64_t)nbcap * C, tw.pitch, tw.g_hi, tw.g_lo, tw.Kt);
-            if (!tw.um) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (high-pass band GEMM)"};
+        const int v = nb <= kHighpassSmallGroup ? 0 : 1;
+        if (!tw.um[v]) {
+            tw.um[v] = umma_make_toeplitz(d_Xt_hi, d_Xt_lo, (int64_t)nbcap * C, tw.pitch, kHighpassTile[v], tw.g_hi[v],
+                                          tw.g_lo[v], tw.Kt[v]);
+            if (!tw.um[v]) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (high-pass band GEMM)"};
         }
         launch_car_t(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, tw.pitch, d_Xt_hi, d_Xt_lo, st), ++nl;
         mark();
-        LSS_CUDA(launch_umma_highpass(tw.um, d_Y, d_Y_lo, nb, C, Wn, d_gemm_err, st));
+        LSS_CUDA(launch_umma_highpass(tw.um[v], d_Y, d_Y_lo, nb, C, Wn, d_gemm_err, st));
         ++nl;
         mark();
     } else {
