@@ -440,20 +440,26 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                 float bestA = -1.f, bestB = -1.f;
                 int biA = 0x7fffffff, biB = 0x7fffffff;
                 for (int fb = 0; fb < T4; fb += 32 * kVec) {
-                    float4 v0[kVec], v1[kVec];
+                    float4 v0[kVec], v1[kVec], xa[kVec], xb[kVec];
+                    // the ctc rows and, when the scores live in L2, the score rows in one batch of
+                    // loads: one round trip per step instead of two
 #pragma unroll
                     for (int jj = 0; jj < kVec; ++jj) {
                         const int f = fb + lane + 32 * jj;
                         const bool ok = f < T4;
                         v0[jj] = ok ? ld_keep(c0 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
                         v1[jj] = (ok && has1) ? ld_keep(c1 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        if constexpr (!SMEM_B) {
+                            xa[jj] = ok ? bA[f] : make_float4(0.f, 0.f, 0.f, 0.f);
+                            xb[jj] = (ok && hasB) ? bB[f] : make_float4(0.f, 0.f, 0.f, 0.f);
+                        }
                     }
 #pragma unroll
                     for (int jj = 0; jj < kVec; ++jj) {
                         const int f = fb + lane + 32 * jj;
                         if (f < T4) {
                             const int t = 4 * f;
-                            float4 x = bA[f];
+                            float4 x = SMEM_B ? bA[f] : xa[jj];
                             x.x = fmaf(-aA0, v0[jj].x, x.x);
                             x.y = fmaf(-aA0, v0[jj].y, x.y);
                             x.z = fmaf(-aA0, v0[jj].z, x.z);
@@ -474,7 +480,7 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                                 r = fmaxf(x.w, 0.f); v = r * r * im.w; if (v > bestA) { bestA = v; biA = t + 3; }
                             }
                             if (hasB) {
-                                float4 y = bB[f];
+                                float4 y = SMEM_B ? bB[f] : xb[jj];
                                 y.x = fmaf(-a1, v1[jj].x, y.x);
                                 y.y = fmaf(-a1, v1[jj].y, y.y);
                                 y.z = fmaf(-a1, v1[jj].z, y.z);
