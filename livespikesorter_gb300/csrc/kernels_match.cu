@@ -217,6 +217,11 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     const bool vec_ok = (T & 3) == 0 &&
                         ((reinterpret_cast<uintptr_t>(ctcP) | reinterpret_cast<uintptr_t>(Bt)) & 15) == 0;
     int n_total = 0, iters = 0;
+    // The spike maps at_t / at_amp (read only when an iteration overflows the shared lists or the
+    // rows are not float4-aligned) hold -1 at every sample not accepted in the current iteration.
+    // A full pass writes every own sample's entry; otherwise only accepted samples are written and
+    // their owners clear them again once the sorted list has replaced the maps.
+    bool full = true;
     for (int it = 0; it < max_iters; ++it) {
         // ---- B1: window max and acceptance on the own samples, chunk by chunk ----
         for (int c0 = 0; c0 < W; c0 += chunk) {
@@ -228,52 +233,66 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                 }
                 __syncthreads();
             }
-            // one warp per own sample: the lanes read consecutive maxima of its window (own
-            // samples are G apart, so one thread per sample would hit the same banks)
+            // An accepted sample's own maximum is its window's maximum and above Th^2, so only
+            // samples whose own maximum exceeds Th^2 are tested: the lanes screen 32 of the warp's
+            // own samples (j = j0 + warp + kWarps*m) at once, then the whole warp takes each
+            // candidate's window, lanes on consecutive maxima (own samples are G apart, so one
+            // thread per window would hit the same banks).
             const int j0 = c0 > rank ? (c0 - rank + G - 1) / G : 0;
-            for (int j = j0 + warp; j < own && rank + G * j < c1; j += kWarps) {
-                const int w = rank + G * j;
-                const float* win = s_cf + (w - c0);   // cfmax of w - nt .. w + nt
-                float cm = -FLT_MAX;
-                for (int d = lane; d < L2; d += 32) cm = fmaxf(cm, win[d]);
+            const int j1 = c1 > rank ? min(own, (c1 - rank + G - 1) / G) : 0;   // own samples in [c0, c1)
+            for (int m0 = 0; j0 + warp + kWarps * m0 < j1; m0 += 32) {
+                const int js = j0 + warp + kWarps * (m0 + lane);
+                const bool cand = js < j1 && s_cf[rank + G * js - c0 + nt] > th2;
+                if (full && js < j1 && !cand) at_t[rank + G * js] = -1;
+                unsigned cbits = __ballot_sync(0xffffffffu, cand);
+                while (cbits) {
+                    const int j = j0 + warp + kWarps * (m0 + __ffs(cbits) - 1);
+                    cbits &= cbits - 1;
+                    const int w = rank + G * j;
+                    const float* win = s_cf + (w - c0);   // cfmax of w - nt .. w + nt
+                    float cm = -FLT_MAX;
+                    for (int d = lane; d < L2; d += 32) cm = fmaxf(cm, win[d]);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) cm = fmaxf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
-                int tt = -1;
-                float amp = 0.f;
-                if (lane == 0) {
-                    if (cm > th2 && win[nt] == cm) {
-                        tt = s_imax[j];
-                        amp = brow(w)[tt] / s_nm[tt];
-                        // phase C of every CTA reads rows of ctcP[tt]: start pulling the (2nt+1) x T
-                        // slab into L2 now, a barrier ahead of use
-                        if (((T * 4) & 15) == 0) {
-                            const float* slab = ctcP + (int64_t)tt * L2 * T;
-                            asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(slab),
-                                         "r"((uint32_t)(L2 * T * 4)), "l"(pol_keep)
-                                         : "memory");
+                    for (int o = 16; o > 0; o >>= 1) cm = fmaxf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
+                    int tt = -1;
+                    float amp = 0.f;
+                    if (lane == 0) {
+                        if (cm > th2 && win[nt] == cm) {
+                            tt = s_imax[j];
+                            amp = brow(w)[tt] / s_nm[tt];
+                            // phase C of every CTA reads rows of ctcP[tt]: start pulling the (2nt+1) x T
+                            // slab into L2 now, a barrier ahead of use
+                            if (((T * 4) & 15) == 0) {
+                                const float* slab = ctcP + (int64_t)tt * L2 * T;
+                                asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(slab),
+                                             "r"((uint32_t)(L2 * T * 4)), "l"(pol_keep)
+                                             : "memory");
+                            }
+                            at_t[w] = tt;   // the maps serve the overflow paths
+                            at_amp[w] = amp;
+                        } else if (full) {
+                            at_t[w] = -1;
                         }
                     }
-                    at_t[w] = tt;   // the maps serve the overflow path
-                    at_amp[w] = amp;
-                }
-                tt = __shfl_sync(0xffffffffu, tt, 0);
-                amp = __shfl_sync(0xffffffffu, amp, 0);
-                if (tt >= 0 && lane < G) {
-                    // into list p of CTA `lane`: claim a slot there, then write the entry
-                    const int p = it & 1;
-                    unsigned slot;
-                    asm volatile("atom.shared::cluster.add.u32 %0, [%1], 1;"
-                                 : "=r"(slot)
-                                 : "r"(dsmem_addr(&s_lcnt[p], (unsigned)lane))
-                                 : "memory");
-                    if ((int)slot < near_cap) {
-                        const int e = p * near_cap + (int)slot;
-                        asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(dsmem_addr(s_lw + e, (unsigned)lane)), "r"(w)
+                    tt = __shfl_sync(0xffffffffu, tt, 0);
+                    amp = __shfl_sync(0xffffffffu, amp, 0);
+                    if (tt >= 0 && lane < G) {
+                        // into list p of CTA `lane`: claim a slot there, then write the entry
+                        const int p = it & 1;
+                        unsigned slot;
+                        asm volatile("atom.shared::cluster.add.u32 %0, [%1], 1;"
+                                     : "=r"(slot)
+                                     : "r"(dsmem_addr(&s_lcnt[p], (unsigned)lane))
                                      : "memory");
-                        asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(dsmem_addr(s_lt + e, (unsigned)lane)), "r"(tt)
-                                     : "memory");
-                        asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(dsmem_addr(s_la + e, (unsigned)lane)), "f"(amp)
-                                     : "memory");
+                        if ((int)slot < near_cap) {
+                            const int e = p * near_cap + (int)slot;
+                            asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(dsmem_addr(s_lw + e, (unsigned)lane)), "r"(w)
+                                         : "memory");
+                            asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(dsmem_addr(s_lt + e, (unsigned)lane)), "r"(tt)
+                                         : "memory");
+                            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(dsmem_addr(s_la + e, (unsigned)lane)), "f"(amp)
+                                         : "memory");
+                        }
                     }
                 }
             }
@@ -287,16 +306,22 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
         if (total == 0) break;
         ++iters;
         const bool listed = total <= near_cap;
+        // with the sorted list and float4 rows nothing reads the maps this iteration: owners clear
+        // their accepted samples' entries as they place them
+        const bool use_list = vec_ok && listed;
         auto place = [&](int w, int tt, float amp, int r) {
             s_lw[q * near_cap + r] = w;
             s_lt[q * near_cap + r] = tt;
             s_la[q * near_cap + r] = amp;
             const int slot = n_total + r;
-            if (w % G == rank && slot < out.cap) {
-                sp_w[slot] = w;
-                sp_t[slot] = tt;
-                sp_amp[slot] = amp;
-                sp_iter[slot] = it;
+            if (w % G == rank) {
+                if (slot < out.cap) {
+                    sp_w[slot] = w;
+                    sp_t[slot] = tt;
+                    sp_amp[slot] = amp;
+                    sp_iter[slot] = it;
+                }
+                if (use_list) at_t[w] = -1;
             }
         };
         if (listed && total <= 32) {
@@ -379,28 +404,35 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
 
         // ---- C: subtract the accepted spikes from the own samples near them ----
         const int n_near = total;
-        const bool use_list = vec_ok && listed;
         if (use_list) {
             // The warp's own samples j = warp, warp + kWarps, ... with their nearby spikes (runs of
             // the list in sample order) are consumed as (sample, spike) items, two per pass: two
             // spikes of one sample (applied in order on its row) or the last spike of one sample
             // and the next sample's first.  A row's maximum is taken in the pass of its last spike.
             int j = warp, k = 0, kend = 0;
+            // lo = first spike at or after w - nt of the current sample w; samples only grow, so
+            // it only moves forward
+            int lo = 0;
             auto seek = [&]() {   // from sample j on, the next own sample with nearby spikes
-                for (; j < own; j += kWarps) {
+                while (j < own) {
                     const int w = rank + G * j;
-                    int lo = 0, hi = n_near;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (s_nw[mid] < w - nt) lo = mid + 1; else hi = mid;
+                    while (lo < n_near && s_nw[lo] < w - nt) ++lo;
+                    if (lo == n_near) {
+                        j = own;
+                        return;
                     }
-                    int e = lo;
-                    while (e < n_near && s_nw[e] <= w + nt) ++e;
-                    if (e > lo) {
+                    const int ws = s_nw[lo];
+                    if (ws <= w + nt) {
+                        int e = lo + 1;
+                        while (e < n_near && s_nw[e] <= w + nt) ++e;
                         k = lo;
                         kend = e;
                         return;
                     }
+                    // nothing within nt of w: on to the warp's first own sample at or after
+                    // ws - nt (> w), the next j = warp (mod kWarps) from jt
+                    const int jt = (ws - nt - rank + G - 1) / G;
+                    j = jt + ((warp - jt) % kWarps + kWarps) % kWarps;
                 }
             };
             seek();
@@ -544,6 +576,7 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             }
         }
         n_total += total;
+        full = !use_list;     // the maps still hold this iteration's spikes: rewrite them all
         group_barrier<G>();   // the changed samples' maxima are read by every CTA in B1
     }
     if (rank == 0 && tid == 0) {
