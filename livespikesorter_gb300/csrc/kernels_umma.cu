@@ -45,6 +45,11 @@ struct UmmaArgs {
     int64_t ldc;      // kPlain
     int chans, wlen;  // kToeplitz: C and W of a window (rows of A are (b, c) = (r / chans, r % chans))
     int* err;
+    // kPlain, optional: C also stored channel-major, zt[(row / wlen) * N + n][row % wlen] at row
+    // pitch zpitch, as its tf32 split (zt_lo null: tf32 alone)
+    float* zt_hi;
+    float* zt_lo;
+    int zpitch;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -254,6 +259,21 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
         if (ok && row < M) {
             float* crow = args.out + (int64_t)row * args.ldc + n0 + c0;
             const int ncol = min(32, N - (n0 + c0));
+            if (args.zt_hi) {
+                // lanes hold consecutive rows = consecutive times of one channel row of zt
+                const int b = row / args.wlen, w = row - b * args.wlen;
+                const int64_t o = ((int64_t)b * N + n0 + c0) * args.zpitch + w;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    if (j < ncol) {
+                        const float v = __uint_as_float(r[j]);
+                        uint32_t h;
+                        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+                        args.zt_hi[o + (int64_t)j * args.zpitch] = __uint_as_float(h);
+                        if (args.zt_lo) args.zt_lo[o + (int64_t)j * args.zpitch] = v - __uint_as_float(h);
+                    }
+                }
+            }
             if (ncol == 32 && ((((uintptr_t)crow) & 15) == 0)) {
 #pragma unroll
                 for (int j = 0; j < 32; j += 4)
@@ -283,6 +303,240 @@ __global__ void split_tf32_kernel(const float* __restrict__ x, float* __restrict
         hi[i] = hf;
         lo[i] = v - hf;
     }
+}
+
+// ------------------------------------------------------------------------------------------
+// temporal basis convolution as a band GEMM per component:
+//   Bpc[b][w][k][c] = sum_m wPCA[k][m] * Z[b][w + m - nt/2][c]
+// A = the channel-major whitened windows Zt[(b, c)][time] (M = 128 (b, c) rows per tile), B_k =
+// the band matrix of component k over the tile's input times.  A tile covers 32 output times
+// w0..w0+31 and the K = 16 ks input times from x0 = w0 - hr on, so B_k[j][u] = wPCA[k][u - j - d]
+// (d = hr - nt/2).  Every K-step's band is the previous one 16 rows further down one resident
+// strip S_k[r][i] = wPCA[k][i - r + 16 (ks - 1) - d] (16 (ks + 1) rows): the B descriptor of K-step
+// s starts at strip row 16 (ks - 1 - s), a multiple of 1024 bytes, so no band tile is ever
+// loaded twice.  Out-of-window input times (< 0 or >= W) come from the TMA zero fill.
+//
+// Persistent CTAs (one per SM), warp-specialised: warp E / lane 0 loads the strips once, then A
+// tiles through a kConvStages mbarrier ring; warp E + 1 / lane 0 issues tcgen05.mma (M = 128,
+// N = 32, K = 8) into one of two TMEM accumulators of K x 32 columns; the E = kConvEpiWarps warps
+// 0..E-1 drain the other accumulator into Bpc while the next tile accumulates -- warp e reads TMEM
+// lanes 32 (e % 4) .. + 31 (its (b, c) rows) for the components k = e / 4, e / 4 + E / 4, ...
+// (several warps per lane quadrant keep more stores in flight).  Bounded waits as in the GEMM
+// above.
+// ------------------------------------------------------------------------------------------
+constexpr int kConvStages = 4;
+constexpr int kConvEpiWarps = 8;                        // a multiple of 4
+constexpr int kConvThreads = (kConvEpiWarps + 2) * 32;
+constexpr int kConvMaxK = 8;       // 2 x 8 x 32 TMEM columns
+
+struct ConvArgs {
+    float* out_hi;
+    float* out_lo;
+    int nrows;      // nb * C
+    int chans, wlen;
+    int kc;         // components
+    int ks, hr;     // ConvGeometry
+    int ntiles_w;
+    int hi_only;
+    int* err;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+template <bool ALO>
+__global__ void __launch_bounds__(kConvThreads, 1)
+umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
+                const __grid_constant__ CUtensorMap tS_hi, const __grid_constant__ CUtensorMap tS_lo, ConvArgs args) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full_bar[kConvStages], empty_bar[kConvStages], tfull_bar[2], tempty_bar[2];
+    __shared__ __align__(8) uint64_t strip_bar, drain_bar;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int abort_raw;
+    volatile int& abort_s = abort_raw;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int KC = args.kc, KS = args.ks;
+    const uint32_t sbytes = (uint32_t)(16 * (KS + 1)) * 64u;   // one component's strip
+    const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    const uint32_t s_hi = base, s_lo = base + (uint32_t)KC * sbytes;
+    const uint32_t stage0 = base + 2u * (uint32_t)KC * sbytes;
+    auto sA_hi = [&](int s) { return stage0 + (uint32_t)s * 2u * kTileA; };
+    auto sA_lo = [&](int s) { return stage0 + (uint32_t)s * 2u * kTileA + kTileA; };
+    const int ntiles = ((args.nrows + kBM - 1) / kBM) * args.ntiles_w;
+    int* err = args.err;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kConvStages; ++s) {
+            mbar_init(smem_u32(&full_bar[s]), 1);
+            mbar_init(smem_u32(&empty_bar[s]), 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(smem_u32(&tfull_bar[a]), 1);
+            mbar_init(smem_u32(&tempty_bar[a]), kConvEpiWarps);   // one arrival per epilogue warp
+        }
+        mbar_init(smem_u32(&strip_bar), 1);
+        mbar_init(smem_u32(&drain_bar), 1);
+        abort_s = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                     "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base_s;
+
+    if (warp == kConvEpiWarps && lane == 0) {
+        // ---- producer: the strips once, then the A tiles of every tile of this CTA ----
+        const uint32_t sb = smem_u32(&strip_bar);
+        mbar_expect_tx(sb, 2u * (uint32_t)KC * sbytes);
+        for (int c = 0; c < KC; ++c) {
+            tma_load_2d(s_hi + (uint32_t)c * sbytes, &tS_hi, sb, 0, c * 16 * (KS + 1));
+            tma_load_2d(s_lo + (uint32_t)c * sbytes, &tS_lo, sb, 0, c * 16 * (KS + 1));
+        }
+        int q = 0;
+        for (int tile = blockIdx.x; tile < ntiles && !abort_s; tile += gridDim.x) {
+            const int mt = tile / args.ntiles_w, wt = tile - mt * args.ntiles_w;
+            const int m0 = mt * kBM, x0 = wt * kConvTileW - args.hr;   // x0 % 4 == 0: 16-byte aligned
+            bool stop = false;
+            for (int ks = 0; ks < KS; ++ks, ++q) {
+                const int s = q % kConvStages;
+                const uint32_t round = (uint32_t)(q / kConvStages);
+                if (!mbar_wait(smem_u32(&empty_bar[s]), (round & 1u) ^ 1u) || abort_s) {
+                    atomicOr(err, 1);
+                    abort_s = 1;
+                    stop = true;
+                    break;
+                }
+                const uint32_t fb = smem_u32(&full_bar[s]);
+                mbar_expect_tx(fb, ALO ? 2u * kTileA : (uint32_t)kTileA);
+                tma_load_2d(sA_hi(s), &tA_hi, fb, x0 + 16 * ks, m0);
+                if constexpr (ALO) tma_load_2d(sA_lo(s), &tA_lo, fb, x0 + 16 * ks, m0);
+            }
+            if (stop) break;
+        }
+        // the copies of the last rounds and the strips land before the CTA may exit
+        for (int kt = (q > kConvStages ? q - kConvStages : 0); kt < q; ++kt)
+            if (!mbar_wait(smem_u32(&full_bar[kt % kConvStages]), (uint32_t)(kt / kConvStages) & 1u)) atomicOr(err, 4);
+        if (!mbar_wait(sb, 0u)) atomicOr(err, 4);
+    } else if (warp == kConvEpiWarps + 1 && lane == 0) {
+        // ---- MMA issuer ----
+        if (!mbar_wait(smem_u32(&strip_bar), 0u)) {
+            atomicOr(err, 2);
+            abort_s = 1;
+        }
+        int q = 0, i = 0;
+        for (int tile = blockIdx.x; tile < ntiles && !abort_s; tile += gridDim.x, ++i) {
+            const int ab = i & 1;
+            if (!mbar_wait(smem_u32(&tempty_bar[ab]), ((uint32_t)(i >> 1) & 1u) ^ 1u) || abort_s) {
+                atomicOr(err, 2);
+                abort_s = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t dcol = tmem + (uint32_t)(ab * KC * 32);
+            bool stop = false;
+            for (int ks = 0; ks < KS; ++ks, ++q) {
+                const int s = q % kConvStages;
+                const uint32_t round = (uint32_t)(q / kConvStages);
+                if (!mbar_wait(smem_u32(&full_bar[s]), round & 1u) || abort_s) {
+                    atomicOr(err, 2);
+                    abort_s = 1;
+                    stop = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t band = (uint32_t)(KS - 1 - ks) * 1024u;   // strip row 16 (ks - 1 - s)
+#pragma unroll
+                for (int kk = 0; kk < kBK / 8; ++kk) {          // K = 8 tf32 (32 bytes) per MMA
+                    const uint32_t off = (uint32_t)kk * 32u;
+                    const uint64_t ah = smem_desc(sA_hi(s) + off), al = smem_desc(sA_lo(s) + off);
+                    for (int c = 0; c < KC; ++c) {
+                        const uint32_t boff = (uint32_t)c * sbytes + band + off;
+                        const uint64_t bh = smem_desc(s_hi + boff), bl = smem_desc(s_lo + boff);
+                        const uint32_t d = dcol + (uint32_t)(c * 32);
+                        mma_tf32<32>(d, ah, bh, (ks > 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32<32>(d, ah, bl, 1u);
+                        if constexpr (ALO) mma_tf32<32>(d, al, bh, 1u);
+                    }
+                }
+                mma_commit(smem_u32(&empty_bar[s]));
+            }
+            if (stop) break;
+            mma_commit(smem_u32(&tfull_bar[ab]));
+        }
+        // every MMA issued has finished before the TMEM is released
+        mma_commit(smem_u32(&drain_bar));
+        if (!mbar_wait(smem_u32(&drain_bar), 0u)) atomicOr(err, 2);
+    } else if (warp < kConvEpiWarps) {
+        // ---- epilogue: accumulator -> Bpc (tf32 split) ----
+        const int quad = warp & 3, c_first = warp >> 2;
+        int i = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+            const int ab = i & 1;
+            // one decision per warp: the tcgen05.ld below is .sync.aligned
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[ab]), (uint32_t)(i >> 1) & 1u) && !abort_s);
+            if (!ok) {
+                if (lane == 0) atomicOr(err, 8);
+                abort_s = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int mt = tile / args.ntiles_w, wt = tile - mt * args.ntiles_w;
+            const int row = mt * kBM + quad * 32 + lane, w0 = wt * kConvTileW;
+            const int b = row / args.chans, ch = row - b * args.chans;
+            const int nj = min(kConvTileW, args.wlen - w0);
+            for (int c = c_first; c < KC; c += kConvEpiWarps / 4) {
+                uint32_t r[32];
+                const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)((ab * KC + c) * 32);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+                    "[%32];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                      "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                      "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (row < args.nrows) {
+                    // lanes = consecutive channels of one (w, k): 128-byte stores
+                    const int64_t o0 = (((int64_t)b * args.wlen + w0) * KC + c) * args.chans + ch;
+                    const int64_t step = (int64_t)KC * args.chans;
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        if (j < nj) {
+                            const float v = __uint_as_float(r[j]);
+                            const int64_t o = o0 + (int64_t)j * step;
+                            if (args.out_lo || args.hi_only) {
+                                uint32_t h;
+                                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+                                args.out_hi[o] = __uint_as_float(h);
+                                if (args.out_lo) args.out_lo[o] = v - __uint_as_float(h);
+                            } else {
+                                args.out_hi[o] = v;
+                            }
+                        }
+                    }
+                }
+            }
+            // the accumulator may be overwritten once every epilogue warp has read it
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&tempty_bar[ab]));
+        }
+    }
+    __syncwarp();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
 }
 
 void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s) {
@@ -371,7 +625,13 @@ UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t r
 void umma_free(UmmaOperands* u) { delete u; }
 
 cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, int* err, cudaStream_t s) {
+    return launch_umma_gemm_zt(u, Cm, M, N, ldc, nullptr, nullptr, 1, 0, err, s);
+}
+
+cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* zt_hi,
+                                float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s) {
     if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
+    if (zt_hi && (wlen <= 0 || zpitch < wlen)) return cudaErrorInvalidValue;
     auto kern = u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true> : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
     constexpr int smem = smem_bytes<kPlainBN>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
@@ -383,6 +643,10 @@ cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int
     a.K = u->K;
     a.ldc = ldc;
     a.err = err;
+    a.zt_hi = zt_hi;
+    a.zt_lo = zt_lo;
+    a.wlen = wlen;
+    a.zpitch = zpitch;
     dim3 grid((N + kPlainBN - 1) / kPlainBN, (M + kBM - 1) / kBM);
     kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     return cudaGetLastError();
@@ -416,6 +680,103 @@ cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo
     if (u->rows_b == kHighpassTileLarge)
         return launch_highpass_tile<kHighpassTileLarge>(u, Y_hi, Y_lo, nb, C, W, err, s);
     return launch_highpass_tile<kHighpassTileSmall>(u, Y_hi, Y_lo, nb, C, W, err, s);
+}
+
+// ---- tensor-core basis convolution: geometry, strips, maps, launch ----
+bool conv_tc_geometry(int nt, int K, ConvGeometry& g) {
+    if (K < 1 || K > kConvMaxK || nt < 1) return false;
+    const int H = nt / 2;
+    g.hr = (H + 3) / 4 * 4;                            // tile inputs start 16-byte aligned
+    const int need = kConvTileW + nt - 1 + (g.hr - H);  // input times one tile reads
+    g.ks = (need + kBK - 1) / kBK;
+    g.rows = 16 * (g.ks + 1);
+    if (g.rows > 256) return false;                     // one TMA box per strip
+    const size_t smem = 1024 + 2 * (size_t)K * g.rows * 64 + (size_t)kConvStages * 2 * kTileA;
+    return smem <= 220 * 1024;
+}
+
+void conv_tc_strips(const float* wPCA, int K, int nt, const ConvGeometry& g, float* strips) {
+    const int d = g.hr - nt / 2;
+    for (int k = 0; k < K; ++k)
+        for (int r = 0; r < g.rows; ++r)
+            for (int i = 0; i < 16; ++i) {
+                const int m = i - r + 16 * (g.ks - 1) - d;
+                strips[((size_t)k * g.rows + r) * 16 + i] = (m >= 0 && m < nt) ? wPCA[(size_t)k * nt + m] : 0.f;
+            }
+}
+
+struct ConvOperands {
+    CUtensorMap a_hi, a_lo, s_hi, s_lo;
+    bool has_a_lo = true;
+    int K = 0;
+    ConvGeometry g;
+    int64_t rows = 0;
+    int wlen = 0;
+};
+
+// rows x cols fp32 at a row pitch of `pitch` floats: TMA fills columns >= cols (and < 0) with zeros
+static bool make_map_pitched(CUtensorMap* m, const float* ptr, uint64_t rows, uint64_t cols, uint64_t pitch,
+                             uint32_t box_rows) {
+    auto fn = encode_fn();
+    if (!fn || ((uintptr_t)ptr & 15) || (pitch * 4) % 16 || pitch < cols) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {pitch * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)kBK, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
+ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows, int wlen, int zpitch,
+                           const float* s_hi, const float* s_lo, int K, const ConvGeometry& g) {
+    auto* u = new ConvOperands();
+    u->has_a_lo = zt_lo != nullptr;
+    u->K = K;
+    u->g = g;
+    u->rows = rows;
+    u->wlen = wlen;
+    if (!zt_lo) zt_lo = zt_hi;   // the map is never used
+    if (!make_map_pitched(&u->a_hi, zt_hi, rows, wlen, zpitch, kBM) ||
+        !make_map_pitched(&u->a_lo, zt_lo, rows, wlen, zpitch, kBM) ||
+        !make_map(&u->s_hi, s_hi, (uint64_t)K * g.rows, 16, g.rows) ||
+        !make_map(&u->s_lo, s_lo, (uint64_t)K * g.rows, 16, g.rows)) {
+        delete u;
+        return nullptr;
+    }
+    return u;
+}
+
+void conv_tc_free(ConvOperands* u) { delete u; }
+
+cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* out_lo, bool hi_only, int nb, int C,
+                                   int W, int* err, cudaStream_t s) {
+    if (!u || (int64_t)nb * C > u->rows || W != u->wlen || nb <= 0) return cudaErrorInvalidValue;
+    auto kern = u->has_a_lo ? umma_basis_conv<true> : umma_basis_conv<false>;
+    // at least 120 KB, so that one CTA (holding all 512 TMEM columns) runs per SM
+    const int smem = std::max<int>(120 * 1024, 1024 + 2 * u->K * u->g.rows * 64 + kConvStages * 2 * kTileA);
+    const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
+    if (attr_err != cudaSuccess) return attr_err;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    ConvArgs a{};
+    a.out_hi = out_hi;
+    a.out_lo = out_lo;
+    a.nrows = nb * C;
+    a.chans = C;
+    a.wlen = W;
+    a.kc = u->K;
+    a.ks = u->g.ks;
+    a.hr = u->g.hr;
+    a.ntiles_w = (W + kConvTileW - 1) / kConvTileW;
+    a.hi_only = hi_only ? 1 : 0;
+    a.err = err;
+    const int64_t ntiles = (int64_t)((nb * C + kBM - 1) / kBM) * a.ntiles_w;
+    const int grid = (int)std::min<int64_t>(ntiles, std::max(sms, 1));
+    kern<<<grid, kConvThreads, smem, s>>>(u->a_hi, u->a_lo, u->s_hi, u->s_lo, a);
+    return cudaGetLastError();
 }
 
 }  // namespace lss

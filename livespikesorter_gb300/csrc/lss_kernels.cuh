@@ -90,6 +90,29 @@ UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t r
 cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W, int* err,
                                  cudaStream_t s);
 void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
+// the same GEMM, whose epilogue also writes the result channel-major, Zt[(row / wlen) * N + n][row %
+// wlen] at row pitch zpitch, as its tf32 split (zt_lo may be null: tf32 alone)
+cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* zt_hi,
+                                float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s);
+
+// temporal basis convolution on the tensor cores (kernels_umma.cu): Bpc[b][w][k][c] from the
+// channel-major whitened windows Zt[(b, c)][time] and one band strip per component
+struct ConvGeometry {
+    int ks = 0;    // K-steps of 16 input times per 32-output tile
+    int hr = 0;    // a tile's first input time is its first output time - hr (hr % 4 == 0)
+    int rows = 0;  // strip rows per component, 16 * (ks + 1)
+};
+constexpr int kConvTileW = 32;   // output times per tile
+bool conv_tc_geometry(int nt, int K, ConvGeometry& g);
+// strip[k][r][i] = wPCA[k][i - r + 16 (ks - 1) - (hr - nt / 2)] (zero outside 0..nt-1), [K][rows][16]
+void conv_tc_strips(const float* wPCA, int K, int nt, const ConvGeometry& g, float* strips);
+struct ConvOperands;
+ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows, int wlen, int zpitch,
+                           const float* s_hi, const float* s_lo, int K, const ConvGeometry& g);
+void conv_tc_free(ConvOperands* u);
+// out_lo == nullptr: store tf32(x) when hi_only, else fp32 x
+cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* out_lo, bool hi_only, int nb, int C,
+                                   int W, int* err, cudaStream_t s);
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                          float th2, int W, int T, int C, int nt, int max_iters, int nb,
                          const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0);

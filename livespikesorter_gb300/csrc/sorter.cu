@@ -90,6 +90,10 @@ struct TapSet {
     int Kt[2] = {};
     int pitch = 0;
     UmmaOperands* um[2] = {};
+    // tensor-core basis convolution: maps over the channel-major whitened windows (row pitch
+    // zpitch = W rounded up to 4) and the component strips
+    int zpitch = 0;
+    ConvOperands* conv = nullptr;
 };
 constexpr int kHighpassTile[2] = {kHighpassTileSmall, kHighpassTileLarge};
 
@@ -141,6 +145,9 @@ struct Handle {
     bool tc_whiten = false, tc_project = false;   // GEMMs on the tensor cores
     bool tc_highpass = false;                     // circular high-pass as a tensor-core band GEMM
     bool tf32_data = false;   // gemm_path 2: activations stored once as TF32, two products per GEMM
+    bool tc_conv = false;     // basis convolution as per-component band GEMMs on the tensor cores
+    ConvGeometry conv_g;
+    float *d_S_hi = nullptr, *d_S_lo = nullptr;   // its band strips (tf32 split)
     UmmaOperands* um_whiten = nullptr;
     UmmaOperands* um_project = nullptr;
     int* h_gemm_err = nullptr;                    // mapped: device-side wait timeouts
@@ -157,6 +164,7 @@ struct Handle {
     float *d_Xw = nullptr, *d_Y = nullptr, *d_Z = nullptr, *d_Bpc = nullptr, *d_Bt = nullptr;
     float *d_Y_lo = nullptr, *d_Bpc_lo = nullptr;   // tf32 remainders (tensor-core path)
     float *d_Xt_hi = nullptr, *d_Xt_lo = nullptr;   // channel-major wrapped windows (tensor-core high-pass)
+    float *d_Zt_hi = nullptr, *d_Zt_lo = nullptr;   // channel-major whitened windows (tensor-core convolution)
     MatchScratch sc{};
     MatchOut mo{};
     int64_t work_bytes = 0;
@@ -208,7 +216,8 @@ Handle::~Handle() {
     }
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
-                    (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo})
+                    (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo,
+                    (void*)d_S_hi, (void*)d_S_lo})
         if (p) cudaFree(p);
     if (h_gemm_err) cudaFreeHost(h_gemm_err);
     for (auto& s : slots) {
@@ -230,13 +239,16 @@ void Handle::free_work() {
     umma_free(um_whiten);
     umma_free(um_project);
     um_whiten = um_project = nullptr;
-    for (auto& kv : taps)
+    for (auto& kv : taps) {
         for (int v = 0; v < 2; ++v) {
             umma_free(kv.second.um[v]);
             kv.second.um[v] = nullptr;
         }
+        conv_tc_free(kv.second.conv);
+        kv.second.conv = nullptr;
+    }
     for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
-                    (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo,
+                    (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo, (void*)d_Zt_hi, (void*)d_Zt_lo,
                     (void*)sc.cfmax, (void*)sc.imax, (void*)sc.at_t, (void*)sc.at_amp, (void*)sc.dirty,
                     (void*)sc.cta_cnt, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
                     (void*)mo.sp_t, (void*)mo.sp_amp, (void*)mo.sp_iter})
@@ -246,6 +258,7 @@ void Handle::free_work() {
     d_Xw = d_Y = d_Z = d_Bpc = d_Bt = nullptr;
     d_Y_lo = d_Bpc_lo = nullptr;
     d_Xt_hi = d_Xt_lo = nullptr;
+    d_Zt_hi = d_Zt_lo = nullptr;
     sc = MatchScratch{};
     mo = MatchOut{};
     dev_bytes -= work_bytes;
@@ -339,6 +352,20 @@ void Handle::init(const char* dir, const lss_params* prm) {
     tc_whiten = want_tc && C % 16 == 0 && C <= 512;
     tc_project = want_tc && (K * C) % 16 == 0 && T <= 512;
     tc_highpass = tc_whiten;
+    // the convolution reads the whitened windows the whitening GEMM also writes channel-major
+    tc_conv = tc_whiten && tc_project && conv_tc_geometry(nt, K, conv_g);
+    if (tc_conv) {
+        std::vector<float> S((size_t)K * conv_g.rows * 16);
+        conv_tc_strips(m.wPCA.data(), K, nt, conv_g, S.data());
+        float* d = dev_upload(S, dev_bytes, st);
+        d_S_hi = dev_alloc<float>(S.size(), dev_bytes);
+        d_S_lo = dev_alloc<float>(S.size(), dev_bytes);
+        launch_split_tf32(d, d_S_hi, d_S_lo, (int64_t)S.size(), st);
+        LSS_CUDA(cudaGetLastError());
+        LSS_CUDA(cudaStreamSynchronize(st));
+        cudaFree(d);
+        dev_bytes -= (int64_t)S.size() * 4;
+    }
     if (tc_whiten || tc_project) {
         if (tc_whiten) {
             d_WD_hi = dev_alloc<float>((size_t)C * C, dev_bytes);
@@ -384,6 +411,7 @@ TapSet& Handle::taps_for(int Wn) {
     ts.L = (int)L;
     ts.R = (int)R;
     ts.d = dev_upload(tv, dev_bytes, st);
+    ts.zpitch = (Wn + 3) / 4 * 4;
     if (tc_highpass) {
         const int ntaps = (int)(L + R + 1);
         ts.pitch = (int)(((Wn + L + R) + 3) / 4 * 4);
@@ -424,6 +452,7 @@ void Handle::ensure_work(int Wn, int nb) {
                          (int64_t)nba * (Wa + LRmax) * C * 4 + 2LL * nba * Wa * C * 4 +
                          (int64_t)nba * Wa * K * C * 4 * (tc_project && !tf32_data ? 2 : 1) +
                          (int64_t)nba * Wa * C * 4 * (tc_whiten && !tf32_data ? 1 : 0) +
+                         (int64_t)nba * ((Wa + 3) / 4 * 4) * C * 4 * (tc_conv ? (tf32_data ? 1 : 2) : 0) +
                          (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16;
     if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
         throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
@@ -444,6 +473,12 @@ void Handle::ensure_work(int Wn, int nb) {
     }
     d_Y = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     d_Z = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
+    if (tc_conv) {
+        // any window length up to Wa: rows of W rounded up to 4; the pad columns are never read
+        const size_t n = (size_t)nba * C * (size_t)((Wa + 3) / 4 * 4);
+        d_Zt_hi = dev_alloc<float>(n, dev_bytes);
+        if (!tf32_data) d_Zt_lo = dev_alloc<float>(n, dev_bytes);
+    }
     d_Bpc = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
     d_Bt = dev_alloc<float>((size_t)nba * Wa * T, dev_bytes);
     if (tc_whiten && !tf32_data) d_Y_lo = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
@@ -539,13 +574,24 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
         mark();
     }
     if (tc_whiten)
-        LSS_CUDA(launch_umma_gemm(um_whiten, d_Z, nb * Wn, C, C, d_gemm_err, st));
+        LSS_CUDA(launch_umma_gemm_zt(um_whiten, d_Z, nb * Wn, C, C, tc_conv ? d_Zt_hi : nullptr,
+                                     tc_conv ? d_Zt_lo : nullptr, Wn, ts.zpitch, d_gemm_err, st));
     else
         launch_sgemm_nt(d_Y, C, (int64_t)Wn * C, d_WD, C, d_Z, C, (int64_t)Wn * C, Wn, C, C, nb, st);
     ++nl;
     mark();
-    launch_basis_conv_host(d_Z, C, Wn, d_wPCA, m.wPCA.data(), K, nt, nb, d_Bpc, st, d_Bpc_lo, tc_project && tf32_data),
-        ++nl;
+    if (tc_conv) {
+        TapSet& tw = const_cast<TapSet&>(ts);
+        if (!tw.conv) {
+            tw.conv = conv_tc_make(d_Zt_hi, d_Zt_lo, (int64_t)nbcap * C, Wn, tw.zpitch, d_S_hi, d_S_lo, K, conv_g);
+            if (!tw.conv) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (basis convolution)"};
+        }
+        LSS_CUDA(launch_umma_basis_conv(tw.conv, d_Bpc, d_Bpc_lo, tf32_data, nb, C, Wn, d_gemm_err, st));
+    } else {
+        launch_basis_conv_host(d_Z, C, Wn, d_wPCA, m.wPCA.data(), K, nt, nb, d_Bpc, st, d_Bpc_lo,
+                               tc_project && tf32_data);
+    }
+    ++nl;
     mark();
     if (tc_project)
         LSS_CUDA(launch_umma_gemm(um_project, d_Bt, nb * Wn, T, T, d_gemm_err, st));

@@ -133,6 +133,37 @@ def test_config_small_one_batch(cfg_small):
     assert a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax, len(sp), len(r.match.st))
 
 
+def test_tensor_core_conv_tiles_span_windows(cfg_small):
+    """96 channels in a group of five windows: the 128-row (window, channel) tiles of the
+    tensor-core basis convolution span two windows each.  The group's spikes agree with each window
+    sorted by the float64 oracle, and equal those of the FP32-SIMT path (gemm_path 1)."""
+    d, data, _ = cfg_small
+    oss = ko.load_oss_input(d)
+    nt, nt0 = oss.wPCA.shape[1], oss.nt0min
+    W = 1500 + 2 * nt
+    wins = np.stack([data[k * 1500: k * 1500 + W] for k in range(5)])
+    outs = {}
+    for path in (0, 1):
+        with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=5, gemm_path=path) as s:
+            outs[path] = s.sort_windows(wins)
+    ref, got = [], {0: [], 1: []}
+    for k in range(5):
+        r = ko.sort_window(wins[k].T, oss, max_iters=50)
+        off = k * 100_000   # keep the windows apart in one agreement count
+        ref.append((r.match.st[:, 0] - nt // 2 + nt0 + off, r.match.st[:, 1], r.match.amps))
+        for path in (0, 1):
+            sp = outs[path][k]
+            got[path].append((sp["time"].astype(np.int64) + off, sp["tmpl"], sp["amp"]))
+    cat = lambda parts: [np.concatenate([p[i] for p in parts]) for i in range(3)]
+    t_r, k_r, a_r = cat(ref)
+    assert len(t_r) > 30
+    for path in (0, 1):
+        a, amp_ok, amax = agreement(t_r, k_r, a_r, *cat(got[path]))
+        assert a >= AGREE and amp_ok >= AGREE, (path, a, amp_ok, amax, len(t_r))
+    a, amp_ok, amax = agreement(*cat(got[1]), *cat(got[0]))
+    assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
+
+
 @pytest.fixture(scope="module")
 def cfg_stream(tmp_path_factory):
     """384 channels, 500 templates, 6 batches of 1500 new samples with a rigid drift."""
