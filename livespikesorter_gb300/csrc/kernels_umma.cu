@@ -309,20 +309,22 @@ __global__ void split_tf32_kernel(const float* __restrict__ x, float* __restrict
 // temporal basis convolution as a band GEMM per component:
 //   Bpc[b][w][k][c] = sum_m wPCA[k][m] * Z[b][w + m - nt/2][c]
 // A = the channel-major whitened windows Zt[(b, c)][time] (M = 128 (b, c) rows per tile), B_k =
-// the band matrix of component k over the tile's input times.  A tile covers 32 output times
-// w0..w0+31 and the K = 16 ks input times from x0 = w0 - hr on, so B_k[j][u] = wPCA[k][u - j - d]
-// (d = hr - nt/2).  Every K-step's band is the previous one 16 rows further down one resident
-// strip S_k[r][i] = wPCA[k][i - r + 16 (ks - 1) - d] (16 (ks + 1) rows): the B descriptor of K-step
-// s starts at strip row 16 (ks - 1 - s), a multiple of 1024 bytes, so no band tile is ever
-// loaded twice.  Out-of-window input times (< 0 or >= W) come from the TMA zero fill.
+// the band matrix of component k over the tile's input times.  A tile covers TW = kConvTileW output
+// times w0..w0+TW-1 of kg components and the K = 16 ks input times from x0 = w0 - hr on, so
+// B_k[j][u] = wPCA[k][u - j - d] (d = hr - nt/2).  Every K-step's band is the previous one 16 rows
+// further down one resident strip S_k[r][i] = wPCA[k][i - r + 16 (ks - 1) - d] (TW + 16 (ks - 1)
+// rows): the B descriptor of K-step s starts at strip row 16 (ks - 1 - s), a multiple of 1024
+// bytes, so no band tile is ever loaded twice.  Out-of-window input times (< 0 or >= W) come from
+// the TMA zero fill.
 //
 // Persistent CTAs (one per SM), warp-specialised: warp E / lane 0 loads the strips once, then A
 // tiles through a kConvStages mbarrier ring; warp E + 1 / lane 0 issues tcgen05.mma (M = 128,
-// N = 32, K = 8) into one of two TMEM accumulators of K x 32 columns; the E = kConvEpiWarps warps
-// 0..E-1 drain the other accumulator into Bpc while the next tile accumulates -- warp e reads TMEM
-// lanes 32 (e % 4) .. + 31 (its (b, c) rows) for the components k = e / 4, e / 4 + E / 4, ...
-// (several warps per lane quadrant keep more stores in flight).  Bounded waits as in the GEMM
-// above.
+// N = TW, K = 8; the per-instruction cost of narrower MMAs dominated) into one of two TMEM
+// accumulators of kg x TW columns; the E = kConvEpiWarps warps 0..E-1 drain the other accumulator
+// into Bpc while the next tile accumulates -- warp e reads TMEM lanes 32 (e % 4) .. + 31 (its
+// (b, c) rows) for the tile's components e / 4, e / 4 + E / 4, ...  The K components are split
+// into groups of kg (tiles of one (rows, times) block, one group each, run on neighbouring CTAs
+// and share its A tiles through L2).  Bounded waits as in the GEMM above.
 // ------------------------------------------------------------------------------------------
 constexpr int kConvStages = 4;
 constexpr int kConvEpiWarps = 8;                        // a multiple of 4
@@ -336,6 +338,8 @@ struct ConvArgs {
     int chans, wlen;
     int kc;         // components
     int ks, hr;     // ConvGeometry
+    int rows, kg;   // strip rows, components per tile
+    int ncg;        // component groups
     int ntiles_w;
     int hi_only;
     int* err;
@@ -356,14 +360,15 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
     __shared__ int abort_raw;
     volatile int& abort_s = abort_raw;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int KC = args.kc, KS = args.ks;
-    const uint32_t sbytes = (uint32_t)(16 * (KS + 1)) * 64u;   // one component's strip
+    constexpr int TW = kConvTileW;
+    const int KC = args.kc, KS = args.ks, KG = args.kg, NCG = args.ncg;
+    const uint32_t sbytes = (uint32_t)args.rows * 64u;   // one component's strip (a multiple of 1024)
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
     const uint32_t s_hi = base, s_lo = base + (uint32_t)KC * sbytes;
     const uint32_t stage0 = base + 2u * (uint32_t)KC * sbytes;
     auto sA_hi = [&](int s) { return stage0 + (uint32_t)s * 2u * kTileA; };
     auto sA_lo = [&](int s) { return stage0 + (uint32_t)s * 2u * kTileA + kTileA; };
-    const int ntiles = ((args.nrows + kBM - 1) / kBM) * args.ntiles_w;
+    const int ntiles = ((args.nrows + kBM - 1) / kBM) * args.ntiles_w * NCG;
     int* err = args.err;
 
     if (threadIdx.x == 0) {
@@ -396,13 +401,13 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
         const uint32_t sb = smem_u32(&strip_bar);
         mbar_expect_tx(sb, 2u * (uint32_t)KC * sbytes);
         for (int c = 0; c < KC; ++c) {
-            tma_load_2d(s_hi + (uint32_t)c * sbytes, &tS_hi, sb, 0, c * 16 * (KS + 1));
-            tma_load_2d(s_lo + (uint32_t)c * sbytes, &tS_lo, sb, 0, c * 16 * (KS + 1));
+            tma_load_2d(s_hi + (uint32_t)c * sbytes, &tS_hi, sb, 0, c * args.rows);
+            tma_load_2d(s_lo + (uint32_t)c * sbytes, &tS_lo, sb, 0, c * args.rows);
         }
         int q = 0;
         for (int tile = blockIdx.x; tile < ntiles && !abort_s; tile += gridDim.x) {
-            const int mt = tile / args.ntiles_w, wt = tile - mt * args.ntiles_w;
-            const int m0 = mt * kBM, x0 = wt * kConvTileW - args.hr;   // x0 % 4 == 0: 16-byte aligned
+            const int blk = tile / NCG, mt = blk / args.ntiles_w, wt = blk - mt * args.ntiles_w;
+            const int m0 = mt * kBM, x0 = wt * TW - args.hr;   // x0 % 4 == 0: 16-byte aligned
             bool stop = false;
             for (int ks = 0; ks < KS; ++ks, ++q) {
                 const int s = q % kConvStages;
@@ -439,7 +444,8 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t dcol = tmem + (uint32_t)(ab * KC * 32);
+            const uint32_t dcol = tmem + (uint32_t)(ab * KG * TW);
+            const int cg0 = (tile % NCG) * KG, ng = min(KG, KC - cg0);
             bool stop = false;
             for (int ks = 0; ks < KS; ++ks, ++q) {
                 const int s = q % kConvStages;
@@ -456,13 +462,13 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                 for (int kk = 0; kk < kBK / 8; ++kk) {          // K = 8 tf32 (32 bytes) per MMA
                     const uint32_t off = (uint32_t)kk * 32u;
                     const uint64_t ah = smem_desc(sA_hi(s) + off), al = smem_desc(sA_lo(s) + off);
-                    for (int c = 0; c < KC; ++c) {
-                        const uint32_t boff = (uint32_t)c * sbytes + band + off;
+                    for (int g = 0; g < ng; ++g) {
+                        const uint32_t boff = (uint32_t)(cg0 + g) * sbytes + band + off;
                         const uint64_t bh = smem_desc(s_hi + boff), bl = smem_desc(s_lo + boff);
-                        const uint32_t d = dcol + (uint32_t)(c * 32);
-                        mma_tf32<32>(d, ah, bh, (ks > 0 || kk > 0) ? 1u : 0u);
-                        mma_tf32<32>(d, ah, bl, 1u);
-                        if constexpr (ALO) mma_tf32<32>(d, al, bh, 1u);
+                        const uint32_t d = dcol + (uint32_t)(g * TW);
+                        mma_tf32<TW>(d, ah, bh, (ks > 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32<TW>(d, ah, bl, 1u);
+                        if constexpr (ALO) mma_tf32<TW>(d, al, bh, 1u);
                     }
                 }
                 mma_commit(smem_u32(&empty_bar[s]));
@@ -487,13 +493,17 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int mt = tile / args.ntiles_w, wt = tile - mt * args.ntiles_w;
-            const int row = mt * kBM + quad * 32 + lane, w0 = wt * kConvTileW;
+            const int blk = tile / NCG, mt = blk / args.ntiles_w, wt = blk - mt * args.ntiles_w;
+            const int cg0 = (tile % NCG) * KG, ng = min(KG, KC - cg0);
+            const int row = mt * kBM + quad * 32 + lane, w0 = wt * TW;
             const int b = row / args.chans, ch = row - b * args.chans;
-            const int nj = min(kConvTileW, args.wlen - w0);
-            for (int c = c_first; c < KC; c += kConvEpiWarps / 4) {
+            for (int cc = c_first; cc < 2 * ng; cc += kConvEpiWarps / 4) {
+                // 32 output times of one component per pass: (g, half) = (cc / 2, cc % 2)
+                const int g = cc >> 1, c = cg0 + g, wh = w0 + 32 * (cc & 1);
+                const int nj = min(32, args.wlen - wh);
                 uint32_t r[32];
-                const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)((ab * KC + c) * 32);
+                const uint32_t taddr =
+                    tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)((ab * KG + g) * TW + 32 * (cc & 1));
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
                     "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
@@ -507,7 +517,7 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 if (row < args.nrows) {
                     // lanes = consecutive channels of one (w, k): 128-byte stores
-                    const int64_t o0 = (((int64_t)b * args.wlen + w0) * KC + c) * args.chans + ch;
+                    const int64_t o0 = (((int64_t)b * args.wlen + wh) * KC + c) * args.chans + ch;
                     const int64_t step = (int64_t)KC * args.chans;
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
@@ -689,8 +699,10 @@ bool conv_tc_geometry(int nt, int K, ConvGeometry& g) {
     g.hr = (H + 3) / 4 * 4;                            // tile inputs start 16-byte aligned
     const int need = kConvTileW + nt - 1 + (g.hr - H);  // input times one tile reads
     g.ks = (need + kBK - 1) / kBK;
-    g.rows = 16 * (g.ks + 1);
+    g.rows = kConvTileW + 16 * (g.ks - 1);
     if (g.rows > 256) return false;                     // one TMA box per strip
+    const int ncg = (K * kConvTileW * 2 + 511) / 512;   // component groups that fit two accumulators
+    g.kg = (K + ncg - 1) / ncg;
     const size_t smem = 1024 + 2 * (size_t)K * g.rows * 64 + (size_t)kConvStages * 2 * kTileA;
     return smem <= 220 * 1024;
 }
@@ -769,11 +781,14 @@ cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* 
     a.wlen = W;
     a.kc = u->K;
     a.ks = u->g.ks;
+    a.rows = u->g.rows;
+    a.kg = u->g.kg;
+    a.ncg = (u->K + u->g.kg - 1) / u->g.kg;
     a.hr = u->g.hr;
     a.ntiles_w = (W + kConvTileW - 1) / kConvTileW;
     a.hi_only = hi_only ? 1 : 0;
     a.err = err;
-    const int64_t ntiles = (int64_t)((nb * C + kBM - 1) / kBM) * a.ntiles_w;
+    const int64_t ntiles = (int64_t)((nb * C + kBM - 1) / kBM) * a.ntiles_w * a.ncg;
     const int grid = (int)std::min<int64_t>(ntiles, std::max(sms, 1));
     kern<<<grid, kConvThreads, smem, s>>>(u->a_hi, u->a_lo, u->s_hi, u->s_lo, a);
     return cudaGetLastError();

@@ -98,11 +98,12 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
 // temporal basis convolution on the tensor cores (kernels_umma.cu): Bpc[b][w][k][c] from the
 // channel-major whitened windows Zt[(b, c)][time] and one band strip per component
 struct ConvGeometry {
-    int ks = 0;    // K-steps of 16 input times per 32-output tile
+    int ks = 0;    // K-steps of 16 input times per tile of kConvTileW output times
     int hr = 0;    // a tile's first input time is its first output time - hr (hr % 4 == 0)
-    int rows = 0;  // strip rows per component, 16 * (ks + 1)
+    int rows = 0;  // strip rows per component, kConvTileW + 16 * (ks - 1)
+    int kg = 0;    // components per tile (two accumulators of kg x kConvTileW TMEM columns)
 };
-constexpr int kConvTileW = 32;   // output times per tile
+constexpr int kConvTileW = 64;   // output times per tile
 bool conv_tc_geometry(int nt, int K, ConvGeometry& g);
 // strip[k][r][i] = wPCA[k][i - r + 16 (ks - 1) - (hr - nt / 2)] (zero outside 0..nt-1), [K][rows][16]
 void conv_tc_strips(const float* wPCA, int K, int nt, const ConvGeometry& g, float* strips);
