@@ -590,12 +590,16 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
 // residual: Xres[w][:] -= amp * waveform[t][w - w_s + nt/2][:] for every accepted spike with
 // |w - w_s| <= nt/2, applied in list order = (iteration, sample) -- the order the reference's
 // loop subtracts in.  A CTA owns kResRows rows; it first copies the spikes that can touch them
-// (in list order) into shared memory, then each warp applies them to its rows.
+// (in list order) into shared memory.  Then a warp holds one row (up to 512 channels per pass) in
+// registers, finds the spikes that touch it in list order (32 list entries per ballot), applies
+// them -- loading the next spike's waveform row while it applies the current one -- and stores
+// the row once: each element sees the same fmaf sequence as a per-spike read-modify-write.
 // ---------------------------------------------------------------------------------------------
 constexpr int kResRows = 64;
 constexpr int kResList = 1024;
-constexpr int kPerLane = 8;      // row elements each lane loads before it stores (256 per warp)
+constexpr int kResElems = 16;    // floats each lane holds per pass: 512 channels per warp
 
+template <bool VEC>
 __global__ void __launch_bounds__(256)
 residual_kernel(float* __restrict__ Xres, const float* __restrict__ pre_wf, MatchOut out, int W, int C, int nt) {
     __shared__ int s_w[kResList], s_t[kResList];
@@ -639,32 +643,89 @@ residual_kernel(float* __restrict__ Xres, const float* __restrict__ pre_wf, Matc
         }
         __syncthreads();
     }
+    // more spikes near these rows than the shared list holds: walk the whole list in global memory
     const bool over = s_over != 0;
-    const int ns = min(s_n, kResList);
+    const int cnt = over ? n : min(s_n, kResList);
+    const int* lw = over ? sw : s_w;
+    const int* lt = over ? st : s_t;
+    const float* la = over ? sa : s_a;
     float* X = Xres + (int64_t)b * W * C;
+    constexpr int kSpan = 32 * kResElems;
+    // element e of a lane: channel c0 + 4 (lane + 32 (e / 4)) + e % 4 (float4 rows), else c0 + lane + 32 e
+    auto chan = [&](int c0, int e) { return VEC ? c0 + 4 * (lane + 32 * (e >> 2)) + (e & 3) : c0 + lane + 32 * e; };
+    auto load = [&](const float* row, int c0, float (&v)[kResElems]) {
+        if constexpr (VEC) {
+#pragma unroll
+            for (int q = 0; q < kResElems / 4; ++q) {
+                const int c = c0 + 4 * (lane + 32 * q);
+                const float4 f = c < C ? *reinterpret_cast<const float4*>(row + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+                v[4 * q] = f.x;
+                v[4 * q + 1] = f.y;
+                v[4 * q + 2] = f.z;
+                v[4 * q + 3] = f.w;
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < kResElems; ++e) v[e] = chan(c0, e) < C ? row[chan(c0, e)] : 0.f;
+        }
+    };
     for (int w = r0 + warp; w < r1; w += 8) {
         float* xrow = X + (int64_t)w * C;
-        const int cnt = over ? n : ns;
-        for (int k = 0; k < cnt; ++k) {
-            const int ws = over ? sw[k] : s_w[k];
-            const int dw = w - ws;
-            if (dw < -hw || dw > hw) continue;
-            const int ts = over ? st[k] : s_t[k];
-            const float a = over ? sa[k] : s_a[k];
-            const float* wrow = pre_wf + ((int64_t)ts * nt + (dw + hw)) * C;
-            for (int c0 = 0; c0 < C; c0 += 32 * kPerLane) {
-                float wv[kPerLane], xv[kPerLane];
-#pragma unroll
-                for (int j = 0; j < kPerLane; ++j) {
-                    const int c = c0 + lane + 32 * j;
-                    wv[j] = (c < C) ? __ldg(wrow + c) : 0.f;
-                    xv[j] = (c < C) ? xrow[c] : 0.f;
+        for (int c0 = 0; c0 < C; c0 += kSpan) {
+            // the next list entry (in list order) whose spike touches row w, or -1
+            int k0 = -32;
+            unsigned m = 0u;
+            auto next_spike = [&]() -> int {
+                for (;;) {
+                    if (m) {
+                        const int k = k0 + __ffs(m) - 1;
+                        m &= m - 1u;
+                        return k;
+                    }
+                    k0 += 32;
+                    if (k0 >= cnt) return -1;
+                    const int k = k0 + lane;
+                    bool t = false;
+                    if (k < cnt) {
+                        const int dw = w - lw[k];
+                        t = dw >= -hw && dw <= hw;
+                    }
+                    m = __ballot_sync(0xffffffffu, t);
+                }
+            };
+            auto wrow = [&](int k) { return pre_wf + ((int64_t)lt[k] * nt + (w - lw[k] + hw)) * C; };
+            int kc = next_spike();
+            if (kc < 0) continue;   // no spike touches this row
+            float xv[kResElems], wa[kResElems], wb[kResElems];
+            load(xrow, c0, xv);
+            load(wrow(kc), c0, wa);
+            float aa = la[kc];
+            while (kc >= 0) {
+                const int kn = next_spike();
+                float an = 0.f;
+                if (kn >= 0) {
+                    load(wrow(kn), c0, wb);
+                    an = la[kn];
                 }
 #pragma unroll
-                for (int j = 0; j < kPerLane; ++j) {
-                    const int c = c0 + lane + 32 * j;
-                    if (c < C) xrow[c] = fmaf(-a, wv[j], xv[j]);
+                for (int e = 0; e < kResElems; ++e) xv[e] = fmaf(-aa, wa[e], xv[e]);
+#pragma unroll
+                for (int e = 0; e < kResElems; ++e) wa[e] = wb[e];
+                aa = an;
+                kc = kn;
+            }
+            if constexpr (VEC) {
+#pragma unroll
+                for (int q = 0; q < kResElems / 4; ++q) {
+                    const int c = c0 + 4 * (lane + 32 * q);
+                    if (c < C)
+                        *reinterpret_cast<float4*>(xrow + c) =
+                            make_float4(xv[4 * q], xv[4 * q + 1], xv[4 * q + 2], xv[4 * q + 3]);
                 }
+            } else {
+#pragma unroll
+                for (int e = 0; e < kResElems; ++e)
+                    if (chan(c0, e) < C) xrow[chan(c0, e)] = xv[e];
             }
         }
     }
@@ -796,7 +857,11 @@ cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float*
                                                       out, s);
     if (e != cudaSuccess) return e;
     dim3 grid((W + kResRows - 1) / kResRows, nb);
-    residual_kernel<<<grid, 256, 0, s>>>(Xres, pre_wf, out, W, C, nt);
+    const bool vec = (C & 3) == 0 && ((reinterpret_cast<uintptr_t>(Xres) | reinterpret_cast<uintptr_t>(pre_wf)) & 15) == 0;
+    if (vec)
+        residual_kernel<true><<<grid, 256, 0, s>>>(Xres, pre_wf, out, W, C, nt);
+    else
+        residual_kernel<false><<<grid, 256, 0, s>>>(Xres, pre_wf, out, W, C, nt);
     return cudaGetLastError();
 }
 

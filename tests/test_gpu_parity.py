@@ -164,6 +164,26 @@ def test_tensor_core_conv_tiles_span_windows(cfg_small):
     assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
 
 
+def test_ragged_shapes_scalar_paths(tmp_path):
+    """30 channels and 45 templates -- neither a multiple of 4 nor of 16: the FP32-SIMT GEMMs and
+    convolution, the matching loop's map-based subtraction (score rows not float4-aligned) and the
+    scalar residual, against the float64 oracle: the stream's spikes and one window's residual."""
+    cfg = synth.SynthConfig(n_chan=30, n_units=45, n_samples=3 * 1500 + 300, rate_hz=20.0, whiten_batch=1500,
+                            whiten_batches=2, seed=31)
+    d, data, _ = make_dataset(cfg, tmp_path)
+    oss = ko.load_oss_input(d)
+    ref = ko.sort_stream(data, oss, 1500, max_iters=50)
+    with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=2) as s:
+        sp = s.sort_stream(data)
+        xres = s.debug_stage(data[:1622], sorter.STAGE_RESIDUAL)
+    k = ref["keep"]
+    a, amp_ok, amax = agreement(ref["time"][k], ref["template"][k], ref["amp"][k], sp["time"], sp["tmpl"], sp["amp"])
+    assert k.sum() > 40
+    assert a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax, len(sp), int(k.sum()))
+    r = ko.sort_window(data[:1622].T, oss, max_iters=50)
+    _rel_close(xres.T.astype(np.float64), r.match.Xres, 5e-5)
+
+
 @pytest.fixture(scope="module")
 def cfg_stream(tmp_path_factory):
     """384 channels, 500 templates, 6 batches of 1500 new samples with a rigid drift."""
