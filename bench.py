@@ -387,8 +387,8 @@ def run_gpu(a):
     chunk = G * NT
     pos = [0]
     obuf = np.zeros(1 << 16, sorter.SPIKE_DTYPE)
-    # the caller's rows live in pinned host memory (the e2e contract); the API copies them once
-    # into its own pinned staging and launches the H2D copy asynchronously
+    # the caller's rows live in pinned host memory (the e2e contract); the API copies page-locked
+    # rows straight into the pending group's device rows on its copy stream
     pinned = torch.from_numpy(data).pin_memory()
     hdata = pinned.numpy()
 

@@ -172,13 +172,32 @@ struct Handle {
     // output slots (in flight groups) and the finished-spike queue
     std::vector<Slot> slots;
     std::deque<int> inflight;   // slot indices in launch order
-    std::deque<lss_spike> ready;
+    // finished spikes waiting for lss_poll: records [ready_head, ready_tail) of ready_buf, which
+    // only grows (its entries are rebuilt in place, never zero-filled again)
+    std::vector<lss_spike> ready_buf;
+    size_t ready_head = 0, ready_tail = 0;
+    size_t ready_count() const { return ready_tail - ready_head; }
+    lss_spike* ready_append(size_t n) {
+        if (ready_head == ready_tail) ready_head = ready_tail = 0;
+        if (ready_head > 0 && ready_tail + n > ready_buf.size()) {
+            std::memmove(ready_buf.data(), ready_buf.data() + ready_head, ready_count() * sizeof(lss_spike));
+            ready_tail -= ready_head;
+            ready_head = 0;
+        }
+        if (ready_tail + n > ready_buf.size()) ready_buf.resize(ready_tail + n);
+        lss_spike* p = ready_buf.data() + ready_tail;
+        ready_tail += n;
+        return p;
+    }
 
     // stream framing
     bool seg_active = false;
     int64_t seg_s0 = 0, next_batch = 0, expected_ct = 0, batch_counter = 0;
     int pend = -1;              // slot whose pinned staging collects the next group's rows
     int64_t pend_rows = 0;      // rows staged there, from the group's first window row on
+    int64_t pend_dev = 0;       // of those, rows [0, pend_dev) are in the slot's device rows already
+    std::vector<int16_t> last_row;   // the stream's newest row (right pad of a flushed window)
+    cudaEvent_t ev_push = nullptr;   // a caller's page-locked rows have reached the device
     std::vector<int64_t> last_kept;     // per final cluster: last kept spike time (duplicate removal)
     std::vector<char> has_kept;
 
@@ -189,7 +208,7 @@ struct Handle {
     void free_work();
     int acquire_slot();
     void launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, int stage_rows,
-                      const int16_t* dev_src = nullptr);
+                      const int16_t* dev_src = nullptr, bool rows_on_copy_stream = false);
     void push_device(const int16_t* rows, int64_t n_batches, int64_t first_row_sample);
     void collect(int slot_idx, std::vector<lss_spike>* direct, std::vector<int64_t>* counts);
     void alloc_slot(Slot& s);
@@ -198,6 +217,8 @@ struct Handle {
     void flush();
     Slot& pending_slot();
     void launch_pending(int g, int pad_mode);
+    int16_t* slot_raw(const Slot& s) { return d_raw + (size_t)(&s - slots.data()) * raw_rows_cap * Cin; }
+    void stage_to_device(Slot& s, int64_t upto);
     void run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
                               const std::function<void()>& mark);
 };
@@ -231,6 +252,7 @@ Handle::~Handle() {
         for (cudaEvent_t e : s.tev)
             if (e) cudaEventDestroy(e);
     }
+    if (ev_push) cudaEventDestroy(ev_push);
     if (st_copy) cudaStreamDestroy(st_copy);
     if (st) cudaStreamDestroy(st);
 }
@@ -396,6 +418,7 @@ void Handle::init(const char* dir, const lss_params* prm) {
         if (p.profile)
             for (cudaEvent_t& e : s.tev) LSS_CUDA(cudaEventCreate(&e));
     }
+    LSS_CUDA(cudaEventCreateWithFlags(&ev_push, cudaEventDisableTiming));
     taps_for(W);
     ensure_work(W, G);
 }
@@ -440,6 +463,13 @@ void Handle::ensure_work(int Wn, int nb) {
     if (Wn <= Wcap && nb <= nbcap) return;
     if (st) LSS_CUDA(cudaStreamSynchronize(st));
     if (st_copy) LSS_CUDA(cudaStreamSynchronize(st_copy));
+    if (pend >= 0 && pend_dev > 0) {
+        // the stream's pending rows on the device go back to the slot's staging before the
+        // device buffers are replaced
+        LSS_CUDA(cudaMemcpy(slots[pend].h_stage, slot_raw(slots[pend]), (size_t)pend_dev * Cin * sizeof(int16_t),
+                            cudaMemcpyDeviceToHost));
+        pend_dev = 0;
+    }
     const int Wa = std::max(Wn, Wcap), nba = std::max(nb, nbcap);
     free_work();
     int64_t before = dev_bytes;
@@ -604,8 +634,10 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
 }
 
 // Enqueue the kernels of one group: windows b = 0..nb-1 start at row b*NTs of the staging copy
-// (or of dev_src, rows already on the device).
-void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, int stage_rows, const int16_t* dev_src) {
+// (or of dev_src, rows already on the device, or arriving there through the copy stream when
+// rows_on_copy_stream).
+void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, int stage_rows, const int16_t* dev_src,
+                          bool rows_on_copy_stream) {
     const bool prof = p.profile != 0;
     int stage = 0;
     auto mark = [&]() {
@@ -623,6 +655,9 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
         LSS_CUDA(cudaEventRecord(s.ev_copy, st_copy));
         LSS_CUDA(cudaStreamWaitEvent(st, s.ev_copy, 0));
         raw = sraw;
+    } else if (rows_on_copy_stream) {
+        LSS_CUDA(cudaEventRecord(s.ev_copy, st_copy));
+        LSS_CUDA(cudaStreamWaitEvent(st, s.ev_copy, 0));
     }
     mark();
     int64_t nl = 0;
@@ -723,7 +758,6 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
         std::sort(keys.begin(), keys.end());
         auto make = [&](const Key& k, lss_spike& o) {
             const SpikeRec& r = recs[k.i];
-            std::memset(&o, 0, sizeof(o));
             o.time = k.time;
             o.tmpl = r.t;
             o.cluster = r.cluster;
@@ -734,6 +768,7 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
             o.n_feat = nf;
             o.iter = r.iter;
             std::memcpy(o.pcfeat, r.feat, sizeof(float) * nf);
+            std::memset(o.pcfeat + nf, 0, sizeof(float) * (LSS_MAX_PCFEAT - nf));
         };
         if (direct) {
             const size_t at = direct->size();
@@ -741,6 +776,7 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
             for (size_t j = 0; j < keys.size(); ++j) make(keys[j], (*direct)[at + j]);
             if (counts) counts->push_back((int64_t)keys.size());
         } else {
+            size_t kept = 0;
             for (const Key& k : keys) {
                 const int cl = recs[k.i].cluster;
                 if (p.dedup && cl >= 0 && cl < Tf) {
@@ -749,9 +785,10 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
                     last_kept[cl] = k.time;
                     has_kept[cl] = 1;
                 }
-                ready.emplace_back();
-                make(k, ready.back());
+                keys[kept++] = k;
             }
+            lss_spike* o = ready_append(kept);
+            for (size_t j = 0; j < kept; ++j) make(keys[j], o[j]);
         }
         spikes_done += (int64_t)keys.size();
     }
@@ -763,15 +800,25 @@ void Handle::drain_all() {
     while (!inflight.empty()) collect(inflight.front(), nullptr, nullptr);
 }
 
-// The slot whose pinned staging receives the stream's next rows; a caller's rows are copied once,
-// straight into it, and a group launches from it when its windows are complete.
+// The slot that collects the stream's next rows and launches a group when its windows are
+// complete.  Its rows gather in its device rows: a caller's page-locked rows are copied there
+// directly; pageable rows (and pads) wait in the slot's pinned staging and follow in one copy.
 Slot& Handle::pending_slot() {
     if (pend < 0) {
         pend = acquire_slot();
         slots[pend].reserved = true;
         pend_rows = 0;
+        pend_dev = 0;
     }
     return slots[pend];
+}
+
+// staged rows [pend_dev, upto) of the pending slot to its device rows (copy stream)
+void Handle::stage_to_device(Slot& s, int64_t upto) {
+    if (upto <= pend_dev) return;
+    LSS_CUDA(cudaMemcpyAsync(slot_raw(s) + (size_t)pend_dev * Cin, s.h_stage + (size_t)pend_dev * Cin,
+                             (size_t)(upto - pend_dev) * Cin * sizeof(int16_t), cudaMemcpyHostToDevice, st_copy));
+    pend_dev = upto;
 }
 
 // Launch g windows from the pending staging (rows [0, g*NT + 2nt) from the first window's first
@@ -791,9 +838,10 @@ void Handle::launch_pending(int g, int pad_mode) {
             if (pad_mode == 2)
                 std::memset(s.h_stage + r * Cin, 0, (size_t)Cin * sizeof(int16_t));
             else
-                std::memcpy(s.h_stage + r * Cin, s.h_stage + (have - 1) * Cin, (size_t)Cin * sizeof(int16_t));
+                std::memcpy(s.h_stage + r * Cin, last_row.data(), (size_t)Cin * sizeof(int16_t));
         }
     }
+    stage_to_device(s, std::max(have, rows_need));
     s.windows_api = false;
     s.win_start.assign(g, 0);
     s.batch_id.assign(g, 0);
@@ -807,17 +855,21 @@ void Handle::launch_pending(int g, int pad_mode) {
     s.reserved = false;
     pend = -1;
     pend_rows = 0;
-    launch_group(s, g, W, NT, taps_for(W), (int)rows_need);
+    pend_dev = 0;
+    launch_group(s, g, W, NT, taps_for(W), (int)rows_need, slot_raw(s), true);
     inflight.push_back(si);
     next_batch += g;
     batch_counter += g;
     const int64_t carry = have - (int64_t)g * NT;   // rows of the following windows staged already
     if (carry > 0) {
-        // the launched slot's staging is host memory the GPU only reads; if collecting the oldest
-        // group hands the same slot back, the rows move down within it
+        // they start the next pending slot: a device copy on the copy stream (the launched group
+        // only reads its rows; the new slot is idle, so it is never the launched one)
         Slot& ns = pending_slot();
-        std::memmove(ns.h_stage, s.h_stage + (size_t)g * NT * Cin, (size_t)carry * Cin * sizeof(int16_t));
+        if (&ns == &s) throw LoadError{LSS_ERR_INTERNAL, "pending rows carried into a busy slot"};
+        LSS_CUDA(cudaMemcpyAsync(slot_raw(ns), slot_raw(s) + (size_t)g * NT * Cin, (size_t)carry * Cin * sizeof(int16_t),
+                                 cudaMemcpyDeviceToDevice, st_copy));
         pend_rows = carry;
+        pend_dev = carry;
     }
 }
 
@@ -835,15 +887,34 @@ void Handle::push(const int16_t* x, int64_t n, int64_t ct) {
         expected_ct = seg_s0;
     }
     expected_ct += n;
+    last_row.assign(x + (size_t)(n - 1) * Cin, x + (size_t)n * Cin);
+    // page-locked rows go straight to the device on the copy stream, and the call returns once
+    // they are there; pageable rows are copied into the slot's pinned staging
+    cudaPointerAttributes pa{};
+    const bool pinned = cudaPointerGetAttributes(&pa, x) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    bool sync = false;
     const int64_t need = (int64_t)G * NT + 2 * nt;
     while (n > 0) {
         Slot& s = pending_slot();
         const int64_t take = std::min(n, need - pend_rows);
-        par_memcpy(s.h_stage + pend_rows * Cin, x, (size_t)take * Cin * sizeof(int16_t));
+        const size_t bytes = (size_t)take * Cin * sizeof(int16_t);
+        if (pinned) {
+            stage_to_device(s, pend_rows);   // staged rows ahead of these (pads, pageable pushes)
+            LSS_CUDA(cudaMemcpyAsync(slot_raw(s) + (size_t)pend_rows * Cin, x, bytes, cudaMemcpyHostToDevice, st_copy));
+            pend_dev = pend_rows + take;
+            sync = true;
+        } else {
+            par_memcpy(s.h_stage + pend_rows * Cin, x, bytes);
+        }
         pend_rows += take;
         x += take * Cin;
         n -= take;
         if (pend_rows == need) launch_pending(G, 0);
+    }
+    if (sync) {
+        LSS_CUDA(cudaEventRecord(ev_push, st_copy));
+        LSS_CUDA(cudaEventSynchronize(ev_push));
     }
 }
 
@@ -865,6 +936,7 @@ void Handle::flush() {
     if (pend >= 0) slots[pend].reserved = false;
     pend = -1;
     pend_rows = 0;
+    pend_dev = 0;
 }
 
 }  // namespace lss
@@ -996,12 +1068,10 @@ int lss_poll(lss_handle* hp, lss_spike* out, int64_t cap, int64_t* n_out) {
         // everything already finished, plus the oldest group if nothing is ready yet
         while (!h.inflight.empty() && cudaEventQuery(h.slots[h.inflight.front()].ev) == cudaSuccess)
             h.collect(h.inflight.front(), nullptr, nullptr);
-        if (h.ready.empty() && !h.inflight.empty()) h.collect(h.inflight.front(), nullptr, nullptr);
-        int64_t n = std::min<int64_t>(cap, (int64_t)h.ready.size());
-        for (int64_t i = 0; i < n; ++i) {
-            out[i] = h.ready.front();
-            h.ready.pop_front();
-        }
+        if (h.ready_count() == 0 && !h.inflight.empty()) h.collect(h.inflight.front(), nullptr, nullptr);
+        const int64_t n = std::min<int64_t>(cap, (int64_t)h.ready_count());
+        if (n > 0) std::memcpy(out, h.ready_buf.data() + h.ready_head, (size_t)n * sizeof(lss_spike));
+        h.ready_head += (size_t)n;
         *n_out = n;
         if (h.overflow_pending) {
             h.overflow_pending = false;
@@ -1023,7 +1093,7 @@ int lss_pending(lss_handle* hp, int64_t* n) {
     LSS_TRY(hp, {
         cudaSetDevice(hp->h.dev);
         hp->h.drain_all();
-        *n = (int64_t)hp->h.ready.size();
+        *n = (int64_t)hp->h.ready_count();
     })
 }
 
@@ -1096,9 +1166,10 @@ int lss_debug_stage(lss_handle* hp, const int16_t* window, int32_t W, int32_t st
         std::memcpy(s.h_stage, window, (size_t)W * h.Cin * sizeof(int16_t));
         lss::TapSet& ts = h.taps_for(W);
         cudaStream_t st = h.st;
-        LSS_CUDA(cudaMemcpyAsync(h.d_raw, s.h_stage, (size_t)W * h.Cin * 2, cudaMemcpyHostToDevice, st));
+        int16_t* sraw = h.slot_raw(s);   // not the stream's pending slot (reserved)
+        LSS_CUDA(cudaMemcpyAsync(sraw, s.h_stage, (size_t)W * h.Cin * 2, cudaMemcpyHostToDevice, st));
         int64_t nl = 0;
-        h.run_stages_to_scores(h.d_raw, 1, W, W, ts, nl, [] {});
+        h.run_stages_to_scores(sraw, 1, W, W, ts, nl, [] {});
         if (stage == LSS_STAGE_PREPROCESSED) {
             LSS_CUDA(cudaMemcpyAsync(out, h.d_Z, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
         } else {

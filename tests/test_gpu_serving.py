@@ -82,3 +82,35 @@ def test_concurrent_streams_equal_alone(datasets):
         assert len(got) == len(ref)
         for f in ("time", "tmpl", "cluster", "amp", "x", "y", "pcfeat"):
             np.testing.assert_array_equal(got[f], ref[f], err_msg=f)
+
+
+def test_pinned_and_pageable_pushes_agree(datasets):
+    """Page-locked rows go straight to the device (lss_push_batch returns once they are there, so
+    the caller may reuse the buffer at once); pageable rows go through the pinned staging.  Uneven
+    pushes alternating between the two -- the page-locked buffer overwritten right after each push
+    -- give the spikes of the pageable stream, bit for bit."""
+    torch = pytest.importorskip("torch")
+    d, data, NT = datasets[0]
+    ref = _sort_alone(d, data, NT)
+    buf = torch.empty((3 * NT, data.shape[1]), dtype=torch.int16).pin_memory().numpy()
+    rng = np.random.default_rng(7)
+    got = []
+    with sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=2) as s:
+        pos, i = 0, 0
+        while pos < data.shape[0]:
+            k = min(int(rng.integers(NT // 4, 3 * NT)), data.shape[0] - pos)
+            if i % 2 == 0:
+                buf[:k] = data[pos:pos + k]
+                s.push(buf[:k])
+                buf[:k] = -12345
+            else:
+                s.push(data[pos:pos + k])
+            pos += k
+            i += 1
+            got.append(s.poll())
+        s.flush()
+        got.append(s.poll_all())
+    got = np.concatenate(got)
+    assert len(got) == len(ref) > 50
+    for f in ("time", "tmpl", "cluster", "amp", "x", "y", "pcfeat"):
+        np.testing.assert_array_equal(got[f], ref[f], err_msg=f)
