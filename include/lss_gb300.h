@@ -108,9 +108,11 @@ int lss_get_info(const lss_handle* h, lss_info* info);
 /* Push n_samples rows of int16 [n_samples][n_chan_in] (channel fastest, SpikeGLX order).
  * stream_sample_ct = stream index of row 0, or -1 for "continues the previous push"; a
  * discontinuity flushes the current segment and starts a new one (the skip / behind policy
- * of OnlineSpikesV2::runSpikeSorting, OnlineSpikesV2.cu:698-761).  The rows are copied into
- * pinned staging before the call returns; every batch whose window is complete is launched
- * asynchronously on the handle's stream.  Replaces DataSocket::fetchLatest / fetchFromPlace +
+ * of OnlineSpikesV2::runSpikeSorting, OnlineSpikesV2.cu:698-761).  The caller may reuse the
+ * rows when the call returns: rows in page-locked memory (cudaHostAlloc / cudaHostRegister) are
+ * copied straight to the device and the call waits for that copy; pageable rows are copied into
+ * the handle's pinned staging.  Every batch whose window is complete is launched asynchronously
+ * on the handle's stream.  Replaces DataSocket::fetchLatest / fetchFromPlace +
  * the H2D copy + the per-batch body of runSpikeSorting (dataSocket.cpp:103-171,
  * OnlineSpikesV2.cu:747-822). */
 int lss_push_batch(lss_handle* h, const int16_t* samples, int64_t n_samples, int64_t stream_sample_ct);
