@@ -57,7 +57,11 @@ typedef struct lss_params {
     int32_t gemm_path;      /* 0 = tensor cores (tcgen05, 3xTF32 = FP32 accuracy) where shapes allow; 1 = FP32 SIMT;
                                2 = tensor cores with the data operands stored once as TF32 (two products; the
                                fixed matrices keep FP32 accuracy): faster, spike agreement with 0 measured */
-    int32_t reserved[3];
+    int32_t cluster_rule;   /* final cluster of a spike: 0 = nearest centroid in (x, y) (OnlineSpikesV2.cu:1058-1074);
+                               1 = best PC score 2 tF.mu - |mu|^2 among the clusters within cluster_radius_um of the
+                               spike (OnlineKilosort.py:233-284; cluster_centroids_pca.npy [T_final, nC*K]), -1 if none */
+    float cluster_radius_um;  /* radius of rule 1; 0 = 80 um (OnlineKilosort.py:449) */
+    int32_t reserved[1];
 } lss_params;
 
 /* One sorted spike.  time is the stream sample (Kilosort template_matching.py:68). */

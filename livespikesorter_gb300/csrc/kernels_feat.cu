@@ -5,7 +5,9 @@
 //   (x, y)   = sum_n (mass_n / sum mass) * (xc, yc)[iCC[n][iU[t]]],  mass_n = sum_k tF[n][k]^2
 //              (Kilosort postprocessing.py:33-46)
 //   cluster  = nearest final-cluster centroid in (x, y), first on ties
-//              (OnlineSpikesV2::closestCluster, OnlineSpikesV2.cu:1058-1074)
+//              (OnlineSpikesV2::closestCluster, OnlineSpikesV2.cu:1058-1074); or, with the PC-score
+//              rule, argmax_k 2 tF.mu_k - |mu_k|^2 over the clusters whose centroid lies within R
+//              of (x, y) (first on ties), -1 when none does (OnlineKilosort.py:233-284)
 //
 // One warp per spike; records are written straight into host-mapped memory.
 #include "lss_kernels.cuh"
@@ -35,7 +37,8 @@ __global__ void __launch_bounds__(kFeatWarps * 32)
 features_kernel(const float* __restrict__ Xres, MatchOut out, int nb, int W, int C, int T, int K, int nt, int nC,
                 const float* __restrict__ wPCA, const int64_t* __restrict__ iCC, const int64_t* __restrict__ iU,
                 const float* __restrict__ Ucc, const float* __restrict__ xc, const float* __restrict__ yc,
-                const float* __restrict__ centroids, int n_final, const int* __restrict__ rec_offset,
+                const float* __restrict__ centroids, int n_final, const float* __restrict__ cpca,
+                const float* __restrict__ cpca_nm, float r2, const int* __restrict__ rec_offset,
                 SpikeRec* __restrict__ recs, int batch_base) {
     const int lane = threadIdx.x & 31;
     const int total = rec_offset[nb];
@@ -88,21 +91,46 @@ features_kernel(const float* __restrict__ Xres, MatchOut out, int nb, int W, int
         ms += __shfl_xor_sync(0xffffffffu, ms, o);
     }
     const float x = mx / ms, y = my / ms;
-    // nearest centroid
-    float bd = FLT_MAX;
     int bi = 0x7fffffff;
-    for (int j = lane; j < n_final; j += 32) {
-        const float dx = x - centroids[2 * j], dy = y - centroids[2 * j + 1];
-        const float d = dx * dx + dy * dy;
-        if (d < bd) { bd = d; bi = j; }
-    }
+    if (cpca) {
+        // PC score among the clusters within R: squares and sums rounded separately, as
+        // elementwise float32 tensor arithmetic does (no fused multiply-add on the distance)
+        float bs = -FLT_MAX;
+        bool any = false;
+        for (int j = lane; j < n_final; j += 32) {
+            const float dx = __fsub_rn(x, centroids[2 * j]), dy = __fsub_rn(y, centroids[2 * j + 1]);
+            if (!(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) <= r2)) continue;
+            any = true;
+            const float* mu = cpca + (int64_t)j * nf;
+            float dot = 0.f;
+            for (int p = 0; p < nf; ++p) dot = fmaf(sf[p], mu[p], dot);
+            const float sc = __fsub_rn(__fmul_rn(2.f, dot), cpca_nm[j]);
+            if (sc > bs || bi == 0x7fffffff) { bs = sc; bi = j; }
+        }
+        any = __any_sync(0xffffffffu, any);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const float od = __shfl_xor_sync(0xffffffffu, bd, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (od < bd || (od == bd && oi < bi)) { bd = od; bi = oi; }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float os = __shfl_xor_sync(0xffffffffu, bs, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (oi != 0x7fffffff && (bi == 0x7fffffff || os > bs || (os == bs && oi < bi))) { bs = os; bi = oi; }
+        }
+        if (!any) bi = -1;
+    } else {
+        // nearest centroid
+        float bd = FLT_MAX;
+        for (int j = lane; j < n_final; j += 32) {
+            const float dx = x - centroids[2 * j], dy = y - centroids[2 * j + 1];
+            const float d = dx * dx + dy * dy;
+            if (d < bd) { bd = d; bi = j; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (od < bd || (od == bd && oi < bi)) { bd = od; bi = oi; }
+        }
+        if (bi == 0x7fffffff) bi = 0;   // NaN position (zero feature energy): first cluster
     }
-    if (bi == 0x7fffffff) bi = 0;   // NaN position (zero feature energy): first cluster
     SpikeRec* rec = recs + gw;
     rec->feat[lane] = f[0];
     rec->feat[lane + 32] = f[1];
@@ -121,12 +149,13 @@ features_kernel(const float* __restrict__ Xres, MatchOut out, int nb, int W, int
 
 void launch_features(const float* Xres, const MatchOut& out, int nb, int W, int C, int T, int K, int nt, int nC,
                      const float* wPCA, const int64_t* iCC, const int64_t* iU, const float* Ucc, const float* xc,
-                     const float* yc, const float* centroids, int n_final, const int* rec_offset, SpikeRec* recs,
-                     int batch_base, cudaStream_t s) {
+                     const float* yc, const float* centroids, int n_final, const float* cpca, const float* cpca_nm,
+                     float r2, const int* rec_offset, SpikeRec* recs, int batch_base, cudaStream_t s) {
     const int max_recs = nb * out.cap;
     const int blocks = std::min((max_recs + kFeatWarps - 1) / kFeatWarps, 2048);
     features_kernel<<<blocks, kFeatWarps * 32, 0, s>>>(Xres, out, nb, W, C, T, K, nt, nC, wPCA, iCC, iU, Ucc, xc,
-                                                       yc, centroids, n_final, rec_offset, recs, batch_base);
+                                                       yc, centroids, n_final, cpca, cpca_nm, r2, rec_offset, recs,
+                                                       batch_base);
 }
 
 }  // namespace lss

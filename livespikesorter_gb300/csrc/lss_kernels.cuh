@@ -119,8 +119,8 @@ cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float*
                          const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0);
 void launch_features(const float* Xres, const MatchOut& out, int nb, int W, int C, int T, int K, int nt, int nC,
                      const float* wPCA, const int64_t* iCC, const int64_t* iU, const float* Ucc, const float* xc,
-                     const float* yc, const float* centroids, int n_final, const int* rec_offset, SpikeRec* recs,
-                     int batch_base, cudaStream_t s);
+                     const float* yc, const float* centroids, int n_final, const float* cpca, const float* cpca_nm,
+                     float r2, const int* rec_offset, SpikeRec* recs, int batch_base, cudaStream_t s);
 void launch_rec_offsets(const MatchOut& out, int nb, int* rec_offset, cudaStream_t s);
 
 }  // namespace lss

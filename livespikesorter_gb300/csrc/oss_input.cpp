@@ -211,6 +211,15 @@ OssModel load_oss_input(const std::string& dir) {
     return m;
 }
 
+std::vector<float> load_centroids_pca(const std::string& dir, const OssModel& m) {
+    auto a = npy_load(join(dir, "cluster_centroids_pca.npy"));
+    const size_t nf = (size_t)(m.nC * m.K);
+    if (a.shape.size() != 2 || a.shape[0] != (size_t)m.T_final || a.shape[1] != nf)
+        throw err(LSS_ERR_FORMAT, "cluster_centroids_pca.npy: the PC-score cluster rule needs float32 [T_final, nC*K] "
+                                  "(each cluster's template features on its nearest channels, flattened)");
+    return a.as_f32("cluster_centroids_pca.npy");
+}
+
 void highpass_taps(const std::vector<float>& hp, int64_t W, int64_t half_taps,
                    std::vector<float>& taps, int64_t& left, int64_t& right) {
     // Kernel of length W after crop/pad (preprocessing.py:138-154): hfull[j].  The output is

@@ -55,6 +55,12 @@ struct OssModel {
 // SorterHelpers.cpp:24-115); throws LoadError instead of calling exit().
 OssModel load_oss_input(const std::string& dir);
 
+// cluster_centroids_pca.npy for the PC-score cluster rule: [T_final][nC * K] float32, each final
+// cluster's template PC features on its nearest channels, flattened channel-major
+// (OnlineKilosort.py:211-230).  The exporter's per-cluster channel average ([T_final][K],
+// run_online_spikes.py:523-573) does not fit the rule's scores and is refused.
+std::vector<float> load_centroids_pca(const std::string& dir, const OssModel& m);
+
 // Taps of the circular high-pass for window length W (Kilosort preprocessing.py:138-154
 // crop/pad, io.py:771-774 correlation + fftshift): out[j] multiplies x[(w + j - left) mod W];
 // left/right are clipped to the cropped kernel's support and to half_taps.

@@ -148,6 +148,9 @@ struct Handle {
     bool tc_conv = false;     // basis convolution as per-component band GEMMs on the tensor cores
     ConvGeometry conv_g;
     float *d_S_hi = nullptr, *d_S_lo = nullptr;   // its band strips (tf32 split)
+    // PC-score cluster rule: centroid features [T_final][nC*K], their squared norms, radius^2
+    float *d_cpca = nullptr, *d_cpca_nm = nullptr;
+    float cl_r2 = 0.f;
     UmmaOperands* um_whiten = nullptr;
     UmmaOperands* um_project = nullptr;
     int* h_gemm_err = nullptr;                    // mapped: device-side wait timeouts
@@ -238,7 +241,7 @@ Handle::~Handle() {
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
                     (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo,
-                    (void*)d_S_hi, (void*)d_S_lo})
+                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm})
         if (p) cudaFree(p);
     if (h_gemm_err) cudaFreeHost(h_gemm_err);
     for (auto& s : slots) {
@@ -369,6 +372,22 @@ void Handle::init(const char* dir, const lss_params* prm) {
     d_chan = (Cin > C) ? dev_upload(chan, dev_bytes, st) : nullptr;
     // tensor-core GEMMs need K % 16 == 0 and N <= 512 (C for the whitening, T for the projection)
     if (p.gemm_path < 0 || p.gemm_path > 2) throw LoadError{LSS_ERR_ARG, "lss_params.gemm_path must be 0, 1 or 2"};
+    if (p.cluster_rule < 0 || p.cluster_rule > 1 || !(p.cluster_radius_um >= 0.f))
+        throw LoadError{LSS_ERR_ARG, "lss_params.cluster_rule must be 0 or 1, cluster_radius_um >= 0"};
+    if (p.cluster_rule == 1) {
+        std::vector<float> cp = load_centroids_pca(dir ? dir : "", m);
+        const size_t nf = (size_t)(nC * K);
+        std::vector<float> nrm((size_t)Tf);
+        for (int j = 0; j < Tf; ++j) {
+            double a = 0.0;
+            for (size_t q = 0; q < nf; ++q) a += (double)cp[j * nf + q] * cp[j * nf + q];
+            nrm[(size_t)j] = (float)a;
+        }
+        d_cpca = dev_upload(cp, dev_bytes, st);
+        d_cpca_nm = dev_upload(nrm, dev_bytes, st);
+        const float R = p.cluster_radius_um > 0.f ? p.cluster_radius_um : 80.f;
+        cl_r2 = R * R;
+    }
     const bool want_tc = p.gemm_path == 0 || p.gemm_path == 2;
     tf32_data = p.gemm_path == 2;
     tc_whiten = want_tc && C % 16 == 0 && C <= 512;
@@ -668,8 +687,8 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     nl += 2;   // the loop and the residual
     mark();
     launch_rec_offsets(mo, nb, s.d_off, st), ++nl;
-    launch_features(d_Z, mo, nb, Wn, C, T, K, nt, nC, d_wPCA, d_iCC, d_iU, d_Ucc, d_xc, d_yc, d_cent, Tf, s.d_off,
-                    s.d_recs, 0, st), ++nl;
+    launch_features(d_Z, mo, nb, Wn, C, T, K, nt, nC, d_wPCA, d_iCC, d_iU, d_Ucc, d_xc, d_yc, d_cent, Tf, d_cpca,
+                    d_cpca_nm, cl_r2, s.d_off, s.d_recs, 0, st), ++nl;
     LSS_CUDA(cudaGetLastError());
     mark();
     LSS_CUDA(cudaMemcpyAsync(s.h_nsp, mo.n_spikes, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
@@ -993,6 +1012,8 @@ int lss_default_params(lss_params* p) {
     p->profile = 0;
     p->match_variant = 0;
     p->gemm_path = 0;
+    p->cluster_rule = 0;
+    p->cluster_radius_um = 0.f;
     return LSS_OK;
 }
 

@@ -30,7 +30,8 @@ class Params(ct.Structure):
                 ("max_iters", ct.c_int32), ("group_batches", ct.c_int32), ("n_chan_in", ct.c_int32),
                 ("hp_half_taps", ct.c_int32), ("dedup", ct.c_int32), ("th_override", ct.c_float),
                 ("spike_cap", ct.c_int32), ("mem_budget", ct.c_int64), ("profile", ct.c_int32),
-                ("match_variant", ct.c_int32), ("gemm_path", ct.c_int32), ("reserved", ct.c_int32 * 3)]
+                ("match_variant", ct.c_int32), ("gemm_path", ct.c_int32), ("cluster_rule", ct.c_int32),
+                ("cluster_radius_um", ct.c_float), ("reserved", ct.c_int32 * 1)]
 
 
 class Spike(ct.Structure):

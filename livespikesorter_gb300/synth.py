@@ -422,6 +422,16 @@ def build_oss_input(rec: Recording) -> OssInput:
                     centroids_pca=centroids_pca, spike_templates=rec.train.units[:n_keep].copy(), misc=misc)
 
 
+def centroids_pca_flat(oss: OssInput) -> np.ndarray:
+    """[T_final, nC*K] centroid features of the PC-score cluster rule: each final cluster's
+    template PC features on its template's nearest channels, flattened channel-major (the
+    layout OnlineKilosort.py:211-230 builds from Wall and pc_feature_ind).  Here the final
+    clusters are the units, so their templates are the rows of Wall3."""
+    T = oss.Wall3.shape[0]
+    chans = oss.iCC[:, oss.iU]                                   # [nC, T]
+    return np.stack([oss.Wall3[t][:, chans[:, t]].T.reshape(-1) for t in range(T)]).astype(np.float32)
+
+
 def write_oss_input(oss: OssInput, out_dir) -> Path:
     """Write every file the sorter loads, with the reference exporter's dtypes and orders
     (run_online_spikes.py:641-672, crop_methods.py:171-175)."""

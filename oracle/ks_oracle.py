@@ -333,13 +333,35 @@ def nearest_centroid(x: np.ndarray, y: np.ndarray, centroids: np.ndarray) -> np.
     return np.argmin(d, 1).astype(np.int64)
 
 
+def pc_score_cluster(tF: np.ndarray, xs: np.ndarray, ys: np.ndarray, centroids: np.ndarray,
+                     centroids_pca: np.ndarray, radius: float) -> np.ndarray:
+    """Final cluster by PC score (OnlineKilosort.py:233-284): among the clusters whose (x, y)
+    centroid lies within ``radius`` of the spike, argmax (first on ties) of 2 tF.mu - |mu|^2 with
+    tF flattened to [nC*K] and mu a row of ``centroids_pca``; -1 when no centroid is that close."""
+    if len(xs) == 0:
+        return np.zeros(0, np.int64)
+    X = tF.reshape(len(tF), -1).astype(np.float64)
+    mu = np.asarray(centroids_pca, np.float64)
+    sc = 2.0 * X @ mu.T - (mu ** 2).sum(1)[None, :]
+    c = np.asarray(centroids, np.float64)
+    d2 = (xs[:, None] - c[None, :, 0]) ** 2 + (ys[:, None] - c[None, :, 1]) ** 2
+    near = d2 <= radius ** 2
+    best = np.argmax(np.where(near, sc, -np.inf), 1).astype(np.int64)
+    best[~near.any(1)] = -1
+    return best
+
+
 def remove_duplicates(times: np.ndarray, clusters: np.ndarray, dt: int, last=None):
     """KS/postprocessing.py:9-30 over time-sorted spikes; ``last`` carries each cluster's last
-    kept time across calls (streaming).  Returns the keep mask."""
+    kept time across calls (streaming).  Spikes without a cluster (-1) are all kept.  Returns the
+    keep mask."""
     last = {} if last is None else last
     keep = np.zeros(len(times), bool)
     for i in range(len(times)):
         t, c = int(times[i]), int(clusters[i])
+        if c < 0:
+            keep[i] = True
+            continue
         t0 = last.get(c, t - dt)
         if t >= t0 + dt:
             last[c] = t
@@ -372,9 +394,10 @@ def sort_window(window_CW: np.ndarray, oss: OssArrays, max_iters: int = 50,
 
 
 def sort_stream(data_NC: np.ndarray, oss: OssArrays, NT: int, max_iters: int = 50,
-                dtype=np.float64, batches=None):
+                dtype=np.float64, batches=None, centroids_pca=None, radius: float = 80.0):
     """Kilosort ``extract`` over a whole recording (KS/template_matching.py:28-85) plus the
-    final-cluster assignment and duplicate removal.  Returns per-spike arrays sorted by time:
+    final-cluster assignment (nearest centroid, or the PC-score rule when ``centroids_pca`` is
+    given) and duplicate removal.  Returns per-spike arrays sorted by time:
     ``time, template, cluster, amp, x, y, tF`` and the keep mask of the duplicate pass."""
     nt = oss.wPCA.shape[1]
     nb = n_batches(data_NC.shape[0], NT)
@@ -392,6 +415,9 @@ def sort_stream(data_NC: np.ndarray, oss: OssArrays, NT: int, max_iters: int = 5
     res = {k: (np.concatenate(v) if len(v) else np.zeros(0)) for k, v in out.items()}
     order = np.lexsort((res["template"], res["time"]))
     res = {k: v[order] for k, v in res.items()}
-    res["cluster"] = nearest_centroid(res["x"], res["y"], oss.centroids)
+    if centroids_pca is None:
+        res["cluster"] = nearest_centroid(res["x"], res["y"], oss.centroids)
+    else:
+        res["cluster"] = pc_score_cluster(res["tF"], res["x"], res["y"], oss.centroids, centroids_pca, radius)
     res["keep"] = remove_duplicates(res["time"], res["cluster"], oss.dup_bins)
     return res

@@ -8,7 +8,7 @@ import pytest
 from livespikesorter_gb300 import sorter, synth
 from oracle import ks_oracle as ko
 
-from lss_testutil import agreement, make_dataset, write_oss_from_arrays
+from lss_testutil import agreement, make_dataset, match_spikes, write_oss_from_arrays
 
 pytestmark = pytest.mark.gpu
 
@@ -369,6 +369,38 @@ def test_tensor_core_and_simt_gemms_agree(win_oss, win):
     a, amp_ok, amax = agreement(outs[1][2]["time"], outs[1][2]["tmpl"], outs[1][2]["amp"],
                                 outs[0][2]["time"], outs[0][2]["tmpl"], outs[0][2]["amp"])
     assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
+
+
+def test_pc_score_cluster_rule(cfg_stream, tmp_path):
+    """cluster_rule 1 -- the final cluster with the best PC score 2 tF.mu - |mu|^2 among the
+    clusters within 80 um (OnlineKilosort.py:233-284) -- against the oracle's restatement on the
+    384-channel stream: the spikes agree as on the default rule and their cluster ids agree for
+    >= 99.5 % of the matched spikes; a radius no cluster is within gives -1 throughout; and the
+    exporter's channel-averaged [T, K] centroid file is refused."""
+    import shutil
+    d0, data, oss_in = cfg_stream
+    d = tmp_path / "oss_input"
+    shutil.copytree(d0, d)
+    flat = synth.centroids_pca_flat(oss_in)
+    np.save(d / "cluster_centroids_pca.npy", flat)
+    oss = ko.load_oss_input(d)
+    ref = ko.sort_stream(data, oss, 1500, max_iters=50, centroids_pca=flat, radius=80.0)
+    with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=4, cluster_rule=1) as s:
+        sp = s.sort_stream(data)
+    k = ref["keep"]
+    a, amp_ok, amax = agreement(ref["time"][k], ref["template"][k], ref["amp"][k], sp["time"], sp["tmpl"], sp["amp"])
+    assert k.sum() > 300 and a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax)
+    ri, gi = match_spikes(ref["time"][k], ref["template"][k], sp["time"], sp["tmpl"], 1)
+    same = (ref["cluster"][k][ri] == sp["cluster"][gi]).mean()
+    assert same >= AGREE, same
+    assert (sp["cluster"] >= 0).mean() > 0.5
+    with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, cluster_rule=1, cluster_radius_um=1e-3) as s:
+        far = s.sort_stream(data[:4000])
+    assert len(far) > 0 and np.all(far["cluster"] == -1)
+    np.save(d / "cluster_centroids_pca.npy", oss_in.centroids_pca)
+    with pytest.raises(sorter.SorterError) as e:
+        sorter.OnlineSorter(d, cluster_rule=1)
+    assert e.value.status == 3
 
 
 def test_match_variants_agree(cfg_stream):

@@ -96,3 +96,34 @@ def test_cnpy_semantics_ignore_fortran_order(tmp_path):
     got = ko.read_npy_cnpy(tmp_path / "m.npy")
     assert got.shape == (4, 3)
     np.testing.assert_array_equal(got.ravel(), M.ravel())
+
+
+def test_pc_score_cluster_rule_restated():
+    """The oracle's PC-score rule against a line-by-line transcription of
+    OnlineKilosort.py:233-284 (scores 2 X mu^T - |mu|^2, clusters beyond R masked to -inf, torch
+    argmax = first maximum, -1 when no cluster is within R), on features with exact ties, spikes
+    with no cluster in range and a NaN position."""
+    rng = np.random.default_rng(5)
+    N, nC, K, Tf, R = 200, 4, 3, 12, 30.0
+    tF = rng.integers(-3, 4, (N, nC, K)).astype(np.float64)
+    mu = rng.integers(-2, 3, (Tf, nC * K)).astype(np.float64)
+    mu[7] = mu[2]                                  # duplicate centroid features: exact score ties
+    cent = rng.uniform(0, 100, (Tf, 2))
+    cent[7] = cent[2]
+    xs, ys = rng.uniform(-20, 120, N), rng.uniform(-20, 120, N)
+    xs[0] = np.nan
+    got = ko.pc_score_cluster(tF, xs, ys, cent, mu, R)
+    want = []
+    for i in range(N):
+        X = tF[i].reshape(-1)
+        best, bs, any_in = 0, -np.inf, False
+        for k in range(Tf):
+            d2 = (xs[i] - cent[k, 0]) ** 2 + (ys[i] - cent[k, 1]) ** 2
+            s = 2 * X @ mu[k] - (mu[k] ** 2).sum() if d2 <= R * R else -np.inf
+            any_in |= bool(d2 <= R * R)
+            if s > bs:
+                best, bs = k, s
+        want.append(best if any_in else -1)
+    np.testing.assert_array_equal(got, np.array(want))
+    assert got[0] == -1 and (got == -1).sum() > 5 and (got >= 0).sum() > 50
+    assert not np.any(got == 7)                    # the tie always resolves to the first cluster
