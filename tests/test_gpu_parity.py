@@ -133,6 +133,26 @@ def test_config_small_one_batch(cfg_small):
     assert a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax, len(sp), len(r.match.st))
 
 
+def test_template_subset_directory(cfg_small, tmp_path):
+    """A directory cut to the 40 most active of 64 preclustered templates (livespikesorter_gb300.subset,
+    the reference's subset_templates.py) sorts like the float64 oracle on that same directory."""
+    from livespikesorter_gb300 import subset
+    d0, data, _ = cfg_small
+    d = tmp_path / "sub"
+    m = subset.subset_oss_input(d0, d, n=40)
+    assert m["new_unclu_T"] == 40
+    oss = ko.load_oss_input(d)
+    assert oss.Wall3.shape[0] == 40
+    with sorter.OnlineSorter(d, max_iters=50) as s:
+        (sp,) = s.sort_windows(data[: 60000 + 122])
+    r = ko.sort_window(data[: 60000 + 122].T, oss, max_iters=50)
+    nt, nt0 = oss.wPCA.shape[1], oss.nt0min
+    a, amp_ok, amax = agreement(r.match.st[:, 0] - nt // 2 + nt0, r.match.st[:, 1], r.match.amps,
+                                sp["time"], sp["tmpl"], sp["amp"])
+    assert len(r.match.st) > 300 and sp["tmpl"].max() < 40
+    assert a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax)
+
+
 def test_tensor_core_conv_tiles_span_windows(cfg_small):
     """96 channels in a group of five windows: the 128-row (window, channel) tiles of the
     tensor-core basis convolution span two windows each.  The group's spikes agree with each window
