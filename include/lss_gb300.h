@@ -46,7 +46,8 @@ typedef struct lss_params {
     int32_t max_iters;      /* matching-pursuit iterations per batch, default 50 (OnlineSpikesV2.cu:933) */
     int32_t group_batches;  /* batches launched together, default 1 (lowest latency); larger = throughput */
     int32_t n_chan_in;      /* channels per input row; 0 = C of the oss_input; > C selects channelMap */
-    int32_t hp_half_taps;   /* high-pass FIR half length (taps beyond are < 1e-8 of the centre); 0 = 640 */
+    int32_t hp_half_taps;   /* high-pass FIR half length; 0 = automatic: the shortest one beyond which every tap
+                               of the window's filter is < 1e-8 of its centre tap (442 for Kilosort's 300 Hz filter at 30 kHz) */
     int32_t dedup;          /* 1 = drop same-cluster spikes within duplicate_spike_bins (default 1) */
     float th_override;      /* > 0 replaces Th_learned of misc.txt */
     int32_t spike_cap;      /* per-batch spike buffer; 0 = automatic (2 * max_iters * ceil(W / (nt + 1))) */

@@ -3,6 +3,7 @@
 #include "../../include/lss_gb300.h"
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -238,6 +239,13 @@ void highpass_taps(const std::vector<float>& hp, int64_t W, int64_t half_taps,
         return hp[(size_t)j];
     };
     const int64_t half = W / 2;
+    if (half_taps <= 0) {
+        // the farthest offset whose tap still reaches kTapTail of the centre tap
+        const double c = std::fabs((double)hfull(half));
+        half_taps = 1;
+        for (int64_t j = 0; j < W; ++j)
+            if (std::fabs((double)hfull(j)) >= kTapTail * c) half_taps = std::max<int64_t>(half_taps, std::llabs(j - half));
+    }
     left = std::min<int64_t>(half, half_taps);
     right = std::min<int64_t>(W - 1 - half, half_taps);
     taps.resize((size_t)(left + right + 1));

@@ -63,7 +63,9 @@ std::vector<float> load_centroids_pca(const std::string& dir, const OssModel& m)
 
 // Taps of the circular high-pass for window length W (Kilosort preprocessing.py:138-154
 // crop/pad, io.py:771-774 correlation + fftshift): out[j] multiplies x[(w + j - left) mod W];
-// left/right are clipped to the cropped kernel's support and to half_taps.
+// left/right are clipped to the cropped kernel's support and to half_taps (half_taps <= 0: the
+// shortest half length beyond which every tap is below kTapTail of the centre tap).
+constexpr double kTapTail = 1e-8;
 void highpass_taps(const std::vector<float>& hp, int64_t W, int64_t half_taps,
                    std::vector<float>& taps, int64_t& left, int64_t& right);
 

@@ -447,7 +447,7 @@ TapSet& Handle::taps_for(int Wn) {
     if (it != taps.end()) return it->second;
     std::vector<float> tv;
     int64_t L = 0, R = 0;
-    highpass_taps(m.hp_filter, Wn, p.hp_half_taps > 0 ? p.hp_half_taps : 640, tv, L, R);
+    highpass_taps(m.hp_filter, Wn, p.hp_half_taps, tv, L, R);
     tv.resize(((tv.size() + 31) / 32) * 32, 0.f);   // the FIR kernel reads taps in chunks of 32
     TapSet ts;
     ts.L = (int)L;
@@ -1004,7 +1004,7 @@ int lss_default_params(lss_params* p) {
     p->max_iters = 50;
     p->group_batches = 1;
     p->n_chan_in = 0;
-    p->hp_half_taps = 640;
+    p->hp_half_taps = 0;
     p->dedup = 1;
     p->th_override = 0.f;
     p->spike_cap = 0;
