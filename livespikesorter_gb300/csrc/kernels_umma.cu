@@ -18,6 +18,7 @@
 #include "lss_kernels.cuh"
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -107,6 +108,22 @@ struct IdescTf32 {
         (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
 };
 
+// the same for A = B = BF16 (kind::f16, K = 16 per instruction = the same 32 bytes)
+template <int BN>
+struct IdescBf16 {
+    static constexpr uint32_t value =
+        (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+};
+
+template <int BN>
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(IdescBf16<BN>::value), "r"(accumulate)
+        : "memory");
+}
+
 template <int BN>
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
     asm volatile(
@@ -121,12 +138,15 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 }
 
 // ALO = false: A is TF32 data without a remainder (the two products hi_a*hi_b + hi_a*lo_b; the
-// fixed B operand keeps its split), for the tensor-core tier whose activations are stored once
-template <int BN, int MODE, bool ALO>
+// fixed B operand keeps its split), for the tensor-core tier whose activations are stored once.
+// BF16: the operands are BF16 splits (hi = bf16(x), lo = bf16(x - hi)) multiplied by kind::f16
+// MMAs: a K-step is 32 elements, still 64-byte rows, so tiles, swizzle and pipeline are unchanged.
+template <int BN, int MODE, bool ALO, bool BF16 = false>
 __global__ void __launch_bounds__(128, 1)
 umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
                  const __grid_constant__ CUtensorMap tB_hi, const __grid_constant__ CUtensorMap tB_lo, UmmaArgs args) {
     constexpr int kBN = BN;
+    constexpr int kKE = BF16 ? 2 * kBK : kBK;   // elements per K-step (64 bytes of each row)
     constexpr int kTileB = kBN * kBK * 4;
     constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;
     constexpr int kLoadBytes = ALO ? kStageBytes : kTileA + 2 * kTileB;   // bytes the TMA lands per stage
@@ -140,7 +160,7 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
     volatile int& abort_s = abort_raw;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n0 = blockIdx.x * kBN, m0 = blockIdx.y * kBM;
-    const int nk = K / kBK;
+    const int nk = K / kKE;
     // 1024-byte aligned stage buffers: [A_hi][A_lo][B_hi][B_lo] per stage
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
     auto sA_hi = [&](int s) { return base + (uint32_t)(s * kStageBytes); };
@@ -181,7 +201,7 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
             }
             const uint32_t fb = smem_u32(&full_bar[s]);
             mbar_expect_tx(fb, kLoadBytes);
-            const int k0 = kt * kBK;   // a multiple of 16 fp32 = 64 bytes
+            const int k0 = kt * kKE;   // a multiple of 64 bytes
             // Toeplitz: A columns start at the tile's output time n0 (a multiple of 128), B is the
             // same band matrix for every tile
             const int ax = (MODE == kToeplitz) ? n0 + k0 : k0;
@@ -207,13 +227,19 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-            for (int kk = 0; kk < kBK / 8; ++kk) {          // K = 8 tf32 (32 bytes) per MMA
+            for (int kk = 0; kk < 2; ++kk) {          // 32 bytes (8 tf32 / 16 bf16) per MMA
                 const uint32_t off = (uint32_t)kk * 32u;
                 const uint64_t ah = smem_desc(sA_hi(s) + off), al = smem_desc(sA_lo(s) + off);
                 const uint64_t bh = smem_desc(sB_hi(s) + off), bl = smem_desc(sB_lo(s) + off);
-                mma_tf32<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
-                mma_tf32<BN>(tmem, ah, bl, 1u);
-                if constexpr (ALO) mma_tf32<BN>(tmem, al, bh, 1u);
+                if constexpr (BF16) {
+                    mma_bf16<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
+                    mma_bf16<BN>(tmem, ah, bl, 1u);
+                    if constexpr (ALO) mma_bf16<BN>(tmem, al, bh, 1u);
+                } else {
+                    mma_tf32<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
+                    mma_tf32<BN>(tmem, ah, bl, 1u);
+                    if constexpr (ALO) mma_tf32<BN>(tmem, al, bh, 1u);
+                }
             }
             mma_commit(smem_u32(&empty_bar[s]));        // frees the stage once these MMAs finish
         }
@@ -342,6 +368,7 @@ struct ConvArgs {
     int ncg;        // component groups
     int ntiles_w;
     int hi_only;
+    int out_bf16;   // store the BF16 split (two bf16 arrays) instead of fp32 / tf32
     int* err;
 };
 
@@ -524,7 +551,12 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                         if (j < nj) {
                             const float v = __uint_as_float(r[j]);
                             const int64_t o = o0 + (int64_t)j * step;
-                            if (args.out_lo || args.hi_only) {
+                            if (args.out_bf16) {
+                                const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                                reinterpret_cast<__nv_bfloat16*>(args.out_hi)[o] = h;
+                                reinterpret_cast<__nv_bfloat16*>(args.out_lo)[o] =
+                                    __float2bfloat16_rn(v - __bfloat162float(h));
+                            } else if (args.out_lo || args.hi_only) {
                                 uint32_t h;
                                 asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
                                 args.out_hi[o] = __uint_as_float(h);
@@ -547,6 +579,22 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+}
+
+// hi = bf16(x) (round to nearest even), lo = bf16(x - hi)
+__global__ void split_bf16_kernel(const float* __restrict__ x, __nv_bfloat16* __restrict__ hi,
+                                  __nv_bfloat16* __restrict__ lo, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = x[i];
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[i] = h;
+        lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+}
+
+void launch_split_bf16(const float* x, void* hi, void* lo, int64_t n, cudaStream_t s) {
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+    split_bf16_kernel<<<blocks, 256, 0, s>>>(x, static_cast<__nv_bfloat16*>(hi), static_cast<__nv_bfloat16*>(lo), n);
 }
 
 void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s) {
@@ -584,8 +632,22 @@ bool make_map(CUtensorMap* m, const float* ptr, uint64_t rows, uint64_t cols, ui
            CUDA_SUCCESS;
 }
 
+// rows x cols bf16 row-major, boxes of 32 columns (64 B) x box_rows rows, 64-byte swizzle
+static bool make_map_bf16(CUtensorMap* m, const void* ptr, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+    auto fn = encode_fn();
+    if (!fn || ((uintptr_t)ptr & 15) || (cols * 2) % 16) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * kBK), box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)ptr, dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 struct UmmaOperands {
     CUtensorMap a_hi, a_lo, b_hi, b_lo;
+    bool bf16 = false;        // BF16 splits (kind::f16) instead of TF32 splits
     bool has_a_lo = true;     // false: A is TF32 data alone (two products)
     int rows_a = 0, rows_b = 0, K = 0;
     int cols_a = 0;           // Toeplitz: columns of A (wrapped window length, padded)
@@ -608,6 +670,22 @@ UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, co
     if (!a_lo) a_lo = a_hi;   // the map is never used
     if (!make_map(&u->a_hi, a_hi, rows_a, K, kBM) || !make_map(&u->a_lo, a_lo, rows_a, K, kBM) ||
         !make_map(&u->b_hi, b_hi, rows_b, K, kPlainBN) || !make_map(&u->b_lo, b_lo, rows_b, K, kPlainBN)) {
+        delete u;
+        return nullptr;
+    }
+    return u;
+}
+
+UmmaOperands* umma_make_bf16(const void* a_hi, const void* a_lo, int64_t rows_a, const void* b_hi, const void* b_lo,
+                             int64_t rows_b, int K) {
+    if (K % (2 * kBK) != 0 || rows_b > 2 * kPlainBN || !a_lo || !b_lo) return nullptr;
+    auto* u = new UmmaOperands();
+    u->bf16 = true;
+    u->rows_a = (int)rows_a;
+    u->rows_b = (int)rows_b;
+    u->K = K;
+    if (!make_map_bf16(&u->a_hi, a_hi, rows_a, K, kBM) || !make_map_bf16(&u->a_lo, a_lo, rows_a, K, kBM) ||
+        !make_map_bf16(&u->b_hi, b_hi, rows_b, K, kPlainBN) || !make_map_bf16(&u->b_lo, b_lo, rows_b, K, kPlainBN)) {
         delete u;
         return nullptr;
     }
@@ -642,7 +720,9 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
                                 float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s) {
     if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
     if (zt_hi && (wlen <= 0 || zpitch < wlen)) return cudaErrorInvalidValue;
-    auto kern = u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true> : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
+    auto kern = u->bf16       ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
+                : u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true>
+                              : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
     constexpr int smem = smem_bytes<kPlainBN>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
@@ -762,8 +842,9 @@ ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows,
 void conv_tc_free(ConvOperands* u) { delete u; }
 
 cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* out_lo, bool hi_only, int nb, int C,
-                                   int W, int* err, cudaStream_t s) {
-    if (!u || (int64_t)nb * C > u->rows || W != u->wlen || nb <= 0) return cudaErrorInvalidValue;
+                                   int W, int* err, cudaStream_t s, bool out_bf16) {
+    if (!u || (int64_t)nb * C > u->rows || W != u->wlen || nb <= 0 || (out_bf16 && !out_lo))
+        return cudaErrorInvalidValue;
     auto kern = u->has_a_lo ? umma_basis_conv<true> : umma_basis_conv<false>;
     // at least 120 KB, so that one CTA (holding all 512 TMEM columns) runs per SM
     const int smem = std::max<int>(120 * 1024, 1024 + 2 * u->K * u->g.rows * 64 + kConvStages * 2 * kTileA);
@@ -787,6 +868,7 @@ cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* 
     a.hr = u->g.hr;
     a.ntiles_w = (W + kConvTileW - 1) / kConvTileW;
     a.hi_only = hi_only ? 1 : 0;
+    a.out_bf16 = out_bf16 ? 1 : 0;
     a.err = err;
     const int64_t ntiles = (int64_t)((nb * C + kBM - 1) / kBM) * a.ntiles_w * a.ncg;
     const int grid = (int)std::min<int64_t>(ntiles, std::max(sms, 1));

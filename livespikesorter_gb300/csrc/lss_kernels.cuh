@@ -90,6 +90,11 @@ UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t r
 cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W, int* err,
                                  cudaStream_t s);
 void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
+// BF16 split: hi = bf16(x), lo = bf16(x - hi) (bf16 arrays of n elements)
+void launch_split_bf16(const float* x, void* hi, void* lo, int64_t n, cudaStream_t s);
+// the GEMM on BF16-split operands (kind::f16, hi*hi + hi*lo + lo*hi; K % 32 == 0)
+UmmaOperands* umma_make_bf16(const void* a_hi, const void* a_lo, int64_t rows_a, const void* b_hi, const void* b_lo,
+                             int64_t rows_b, int K);
 // the same GEMM, whose epilogue also writes the result channel-major, Zt[(row / wlen) * N + n][row %
 // wlen] at row pitch zpitch, as its tf32 split (zt_lo may be null: tf32 alone)
 cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* zt_hi,
@@ -111,9 +116,10 @@ struct ConvOperands;
 ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows, int wlen, int zpitch,
                            const float* s_hi, const float* s_lo, int K, const ConvGeometry& g);
 void conv_tc_free(ConvOperands* u);
-// out_lo == nullptr: store tf32(x) when hi_only, else fp32 x
+// out_lo == nullptr: store tf32(x) when hi_only, else fp32 x; out_bf16: the BF16 split of x into
+// out_hi / out_lo viewed as bf16 arrays
 cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* out_lo, bool hi_only, int nb, int C,
-                                   int W, int* err, cudaStream_t s);
+                                   int W, int* err, cudaStream_t s, bool out_bf16 = false);
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                          float th2, int W, int T, int C, int nt, int max_iters, int nb,
                          const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0);

@@ -145,6 +145,7 @@ struct Handle {
     bool tc_whiten = false, tc_project = false;   // GEMMs on the tensor cores
     bool tc_highpass = false;                     // circular high-pass as a tensor-core band GEMM
     bool tf32_data = false;   // gemm_path 2: activations stored once as TF32, two products per GEMM
+    bool bf16_proj = false;   // gemm_path 3: projection on BF16 splits (kind::f16, three products)
     bool tc_conv = false;     // basis convolution as per-component band GEMMs on the tensor cores
     ConvGeometry conv_g;
     float *d_S_hi = nullptr, *d_S_lo = nullptr;   // its band strips (tf32 split)
@@ -371,7 +372,8 @@ void Handle::init(const char* dir, const lss_params* prm) {
     d_iU = dev_upload(m.iU, dev_bytes, st);
     d_chan = (Cin > C) ? dev_upload(chan, dev_bytes, st) : nullptr;
     // tensor-core GEMMs need K % 16 == 0 and N <= 512 (C for the whitening, T for the projection)
-    if (p.gemm_path < 0 || p.gemm_path > 2) throw LoadError{LSS_ERR_ARG, "lss_params.gemm_path must be 0, 1 or 2"};
+    if (p.gemm_path < 0 || p.gemm_path > 3)
+        throw LoadError{LSS_ERR_ARG, "lss_params.gemm_path must be 0, 1, 2 or 3"};
     if (p.cluster_rule < 0 || p.cluster_rule > 1 || !(p.cluster_radius_um >= 0.f))
         throw LoadError{LSS_ERR_ARG, "lss_params.cluster_rule must be 0 or 1, cluster_radius_um >= 0"};
     if (p.cluster_rule == 1) {
@@ -388,7 +390,7 @@ void Handle::init(const char* dir, const lss_params* prm) {
         const float R = p.cluster_radius_um > 0.f ? p.cluster_radius_um : 80.f;
         cl_r2 = R * R;
     }
-    const bool want_tc = p.gemm_path == 0 || p.gemm_path == 2;
+    const bool want_tc = p.gemm_path != 1;
     tf32_data = p.gemm_path == 2;
     tc_whiten = want_tc && C % 16 == 0 && C <= 512;
     tc_project = want_tc && (K * C) % 16 == 0 && T <= 512;
@@ -407,6 +409,8 @@ void Handle::init(const char* dir, const lss_params* prm) {
         cudaFree(d);
         dev_bytes -= (int64_t)S.size() * 4;
     }
+    // the BF16 projection reads Bpc as the tensor-core convolution writes it (BF16 split)
+    bf16_proj = p.gemm_path == 3 && tc_conv && (K * C) % 32 == 0;
     if (tc_whiten || tc_project) {
         if (tc_whiten) {
             d_WD_hi = dev_alloc<float>((size_t)C * C, dev_bytes);
@@ -414,9 +418,13 @@ void Handle::init(const char* dir, const lss_params* prm) {
             launch_split_tf32(d_WD, d_WD_hi, d_WD_lo, (int64_t)C * C, st);
         }
         if (tc_project) {
+            // two bf16 arrays fit in the halves of the tf32 ones
             d_Wall3_hi = dev_alloc<float>((size_t)T * K * C, dev_bytes);
             d_Wall3_lo = dev_alloc<float>((size_t)T * K * C, dev_bytes);
-            launch_split_tf32(d_Wall3, d_Wall3_hi, d_Wall3_lo, (int64_t)T * K * C, st);
+            if (bf16_proj)
+                launch_split_bf16(d_Wall3, d_Wall3_hi, d_Wall3_lo, (int64_t)T * K * C, st);
+            else
+                launch_split_tf32(d_Wall3, d_Wall3_hi, d_Wall3_lo, (int64_t)T * K * C, st);
         }
         LSS_CUDA(cudaGetLastError());
         LSS_CUDA(cudaStreamSynchronize(st));
@@ -551,7 +559,9 @@ void Handle::ensure_work(int Wn, int nb) {
         if (!um_whiten) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (whitening GEMM)"};
     }
     if (tc_project) {
-        um_project = umma_make(d_Bpc, d_Bpc_lo, (int64_t)nba * Wa, d_Wall3_hi, d_Wall3_lo, T, K * C);
+        um_project = bf16_proj
+                         ? umma_make_bf16(d_Bpc, d_Bpc_lo, (int64_t)nba * Wa, d_Wall3_hi, d_Wall3_lo, T, K * C)
+                         : umma_make(d_Bpc, d_Bpc_lo, (int64_t)nba * Wa, d_Wall3_hi, d_Wall3_lo, T, K * C);
         if (!um_project) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (projection GEMM)"};
     }
     work_bytes = dev_bytes - before;
@@ -635,7 +645,7 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
             tw.conv = conv_tc_make(d_Zt_hi, d_Zt_lo, (int64_t)nbcap * C, Wn, tw.zpitch, d_S_hi, d_S_lo, K, conv_g);
             if (!tw.conv) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (basis convolution)"};
         }
-        LSS_CUDA(launch_umma_basis_conv(tw.conv, d_Bpc, d_Bpc_lo, tf32_data, nb, C, Wn, d_gemm_err, st));
+        LSS_CUDA(launch_umma_basis_conv(tw.conv, d_Bpc, d_Bpc_lo, tf32_data, nb, C, Wn, d_gemm_err, st, bf16_proj));
     } else {
         launch_basis_conv_host(d_Z, C, Wn, d_wPCA, m.wPCA.data(), K, nt, nb, d_Bpc, st, d_Bpc_lo,
                                tc_project && tf32_data);
