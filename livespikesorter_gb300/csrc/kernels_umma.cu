@@ -51,6 +51,7 @@ struct UmmaArgs {
     float* zt_hi;
     float* zt_lo;
     int zpitch;
+    int zt_bf16;      // zt as its BF16 split (bf16 arrays)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -293,10 +294,17 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
                 for (int j = 0; j < 32; ++j) {
                     if (j < ncol) {
                         const float v = __uint_as_float(r[j]);
-                        uint32_t h;
-                        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-                        args.zt_hi[o + (int64_t)j * args.zpitch] = __uint_as_float(h);
-                        if (args.zt_lo) args.zt_lo[o + (int64_t)j * args.zpitch] = v - __uint_as_float(h);
+                        const int64_t oj = o + (int64_t)j * args.zpitch;
+                        if (args.zt_bf16) {
+                            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                            reinterpret_cast<__nv_bfloat16*>(args.zt_hi)[oj] = h;
+                            reinterpret_cast<__nv_bfloat16*>(args.zt_lo)[oj] = __float2bfloat16_rn(v - __bfloat162float(h));
+                        } else {
+                            uint32_t h;
+                            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+                            args.zt_hi[oj] = __uint_as_float(h);
+                            if (args.zt_lo) args.zt_lo[oj] = v - __uint_as_float(h);
+                        }
                     }
                 }
             }
@@ -376,7 +384,7 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-template <bool ALO>
+template <bool ALO, bool BF16>
 __global__ void __launch_bounds__(kConvThreads, 1)
 umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
                 const __grid_constant__ CUtensorMap tS_hi, const __grid_constant__ CUtensorMap tS_lo, ConvArgs args) {
@@ -434,7 +442,8 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
         int q = 0;
         for (int tile = blockIdx.x; tile < ntiles && !abort_s; tile += gridDim.x) {
             const int blk = tile / NCG, mt = blk / args.ntiles_w, wt = blk - mt * args.ntiles_w;
-            const int m0 = mt * kBM, x0 = wt * TW - args.hr;   // x0 % 4 == 0: 16-byte aligned
+            const int m0 = mt * kBM, x0 = wt * TW - args.hr;   // 16-byte aligned (hr is)
+            constexpr int kStep = BF16 ? 2 * kBK : kBK;         // input times per K-step
             bool stop = false;
             for (int ks = 0; ks < KS; ++ks, ++q) {
                 const int s = q % kConvStages;
@@ -447,8 +456,8 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                 }
                 const uint32_t fb = smem_u32(&full_bar[s]);
                 mbar_expect_tx(fb, ALO ? 2u * kTileA : (uint32_t)kTileA);
-                tma_load_2d(sA_hi(s), &tA_hi, fb, x0 + 16 * ks, m0);
-                if constexpr (ALO) tma_load_2d(sA_lo(s), &tA_lo, fb, x0 + 16 * ks, m0);
+                tma_load_2d(sA_hi(s), &tA_hi, fb, x0 + kStep * ks, m0);
+                if constexpr (ALO) tma_load_2d(sA_lo(s), &tA_lo, fb, x0 + kStep * ks, m0);
             }
             if (stop) break;
         }
@@ -484,7 +493,8 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t band = (uint32_t)(KS - 1 - ks) * 1024u;   // strip row 16 (ks - 1 - s)
+                // strip row step (ks - 1 - s): 16 or 32 rows of 64 bytes per K-step
+                const uint32_t band = (uint32_t)(KS - 1 - ks) * (BF16 ? 2048u : 1024u);
 #pragma unroll
                 for (int kk = 0; kk < kBK / 8; ++kk) {          // K = 8 tf32 (32 bytes) per MMA
                     const uint32_t off = (uint32_t)kk * 32u;
@@ -493,9 +503,15 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                         const uint32_t boff = (uint32_t)(cg0 + g) * sbytes + band + off;
                         const uint64_t bh = smem_desc(s_hi + boff), bl = smem_desc(s_lo + boff);
                         const uint32_t d = dcol + (uint32_t)(g * TW);
-                        mma_tf32<TW>(d, ah, bh, (ks > 0 || kk > 0) ? 1u : 0u);
-                        mma_tf32<TW>(d, ah, bl, 1u);
-                        if constexpr (ALO) mma_tf32<TW>(d, al, bh, 1u);
+                        if constexpr (BF16) {
+                            mma_bf16<TW>(d, ah, bh, (ks > 0 || kk > 0) ? 1u : 0u);
+                            mma_bf16<TW>(d, ah, bl, 1u);
+                            if constexpr (ALO) mma_bf16<TW>(d, al, bh, 1u);
+                        } else {
+                            mma_tf32<TW>(d, ah, bh, (ks > 0 || kk > 0) ? 1u : 0u);
+                            mma_tf32<TW>(d, ah, bl, 1u);
+                            if constexpr (ALO) mma_tf32<TW>(d, al, bh, 1u);
+                        }
                     }
                 }
                 mma_commit(smem_u32(&empty_bar[s]));
@@ -717,9 +733,9 @@ cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int
 }
 
 cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* zt_hi,
-                                float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s) {
+                                float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s, bool zt_bf16) {
     if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
-    if (zt_hi && (wlen <= 0 || zpitch < wlen)) return cudaErrorInvalidValue;
+    if (zt_hi && (wlen <= 0 || zpitch < wlen || (zt_bf16 && !zt_lo))) return cudaErrorInvalidValue;
     auto kern = u->bf16       ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
                 : u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true>
                               : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
@@ -737,6 +753,7 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
     a.zt_lo = zt_lo;
     a.wlen = wlen;
     a.zpitch = zpitch;
+    a.zt_bf16 = zt_bf16 ? 1 : 0;
     dim3 grid((N + kPlainBN - 1) / kPlainBN, (M + kBM - 1) / kBM);
     kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     return cudaGetLastError();
@@ -773,13 +790,16 @@ cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo
 }
 
 // ---- tensor-core basis convolution: geometry, strips, maps, launch ----
-bool conv_tc_geometry(int nt, int K, ConvGeometry& g) {
+bool conv_tc_geometry(int nt, int K, ConvGeometry& g, bool bf16) {
     if (K < 1 || K > kConvMaxK || nt < 1) return false;
     const int H = nt / 2;
-    g.hr = (H + 3) / 4 * 4;                            // tile inputs start 16-byte aligned
+    g.bf16 = bf16;
+    g.step = bf16 ? 2 * kBK : kBK;
+    const int al = bf16 ? 8 : 4;                       // elements in 16 bytes
+    g.hr = (H + al - 1) / al * al;                     // tile inputs start 16-byte aligned
     const int need = kConvTileW + nt - 1 + (g.hr - H);  // input times one tile reads
-    g.ks = (need + kBK - 1) / kBK;
-    g.rows = kConvTileW + 16 * (g.ks - 1);
+    g.ks = (need + g.step - 1) / g.step;
+    g.rows = kConvTileW + g.step * (g.ks - 1);
     if (g.rows > 256) return false;                     // one TMA box per strip
     const int ncg = (K * kConvTileW * 2 + 511) / 512;   // component groups that fit two accumulators
     g.kg = (K + ncg - 1) / ncg;
@@ -791,9 +811,9 @@ void conv_tc_strips(const float* wPCA, int K, int nt, const ConvGeometry& g, flo
     const int d = g.hr - nt / 2;
     for (int k = 0; k < K; ++k)
         for (int r = 0; r < g.rows; ++r)
-            for (int i = 0; i < 16; ++i) {
-                const int m = i - r + 16 * (g.ks - 1) - d;
-                strips[((size_t)k * g.rows + r) * 16 + i] = (m >= 0 && m < nt) ? wPCA[(size_t)k * nt + m] : 0.f;
+            for (int i = 0; i < g.step; ++i) {
+                const int m = i - r + g.step * (g.ks - 1) - d;
+                strips[((size_t)k * g.rows + r) * g.step + i] = (m >= 0 && m < nt) ? wPCA[(size_t)k * nt + m] : 0.f;
             }
 }
 
@@ -820,8 +840,39 @@ static bool make_map_pitched(CUtensorMap* m, const float* ptr, uint64_t rows, ui
            CUDA_SUCCESS;
 }
 
+// the same for bf16 elements
+static bool make_map_pitched_bf16(CUtensorMap* m, const void* ptr, uint64_t rows, uint64_t cols, uint64_t pitch,
+                                  uint32_t box_rows) {
+    auto fn = encode_fn();
+    if (!fn || ((uintptr_t)ptr & 15) || (pitch * 2) % 16 || pitch < cols) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {pitch * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * kBK), box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)ptr, dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows, int wlen, int zpitch,
                            const float* s_hi, const float* s_lo, int K, const ConvGeometry& g) {
+    if (g.bf16) {
+        // BF16 splits: A and the strips are bf16 arrays (the three products need both lo parts)
+        if (!zt_lo) return nullptr;
+        auto* u = new ConvOperands();
+        u->K = K;
+        u->g = g;
+        u->rows = rows;
+        u->wlen = wlen;
+        if (!make_map_pitched_bf16(&u->a_hi, zt_hi, rows, wlen, zpitch, kBM) ||
+            !make_map_pitched_bf16(&u->a_lo, zt_lo, rows, wlen, zpitch, kBM) ||
+            !make_map_bf16(&u->s_hi, s_hi, (uint64_t)K * g.rows, g.step, g.rows) ||
+            !make_map_bf16(&u->s_lo, s_lo, (uint64_t)K * g.rows, g.step, g.rows)) {
+            delete u;
+            return nullptr;
+        }
+        return u;
+    }
     auto* u = new ConvOperands();
     u->has_a_lo = zt_lo != nullptr;
     u->K = K;
@@ -845,7 +896,8 @@ cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* 
                                    int W, int* err, cudaStream_t s, bool out_bf16) {
     if (!u || (int64_t)nb * C > u->rows || W != u->wlen || nb <= 0 || (out_bf16 && !out_lo))
         return cudaErrorInvalidValue;
-    auto kern = u->has_a_lo ? umma_basis_conv<true> : umma_basis_conv<false>;
+    auto kern = u->g.bf16 ? umma_basis_conv<true, true>
+                : u->has_a_lo ? umma_basis_conv<true, false> : umma_basis_conv<false, false>;
     // at least 120 KB, so that one CTA (holding all 512 TMEM columns) runs per SM
     const int smem = std::max<int>(120 * 1024, 1024 + 2 * u->K * u->g.rows * 64 + kConvStages * 2 * kTileA);
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);

@@ -96,21 +96,24 @@ void launch_split_bf16(const float* x, void* hi, void* lo, int64_t n, cudaStream
 UmmaOperands* umma_make_bf16(const void* a_hi, const void* a_lo, int64_t rows_a, const void* b_hi, const void* b_lo,
                              int64_t rows_b, int K);
 // the same GEMM, whose epilogue also writes the result channel-major, Zt[(row / wlen) * N + n][row %
-// wlen] at row pitch zpitch, as its tf32 split (zt_lo may be null: tf32 alone)
+// wlen] at row pitch zpitch, as its tf32 split (zt_lo may be null: tf32 alone), or as its BF16
+// split into zt_hi / zt_lo viewed as bf16 arrays when zt_bf16
 cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* zt_hi,
-                                float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s);
+                                float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s, bool zt_bf16 = false);
 
 // temporal basis convolution on the tensor cores (kernels_umma.cu): Bpc[b][w][k][c] from the
 // channel-major whitened windows Zt[(b, c)][time] and one band strip per component
 struct ConvGeometry {
-    int ks = 0;    // K-steps of 16 input times per tile of kConvTileW output times
-    int hr = 0;    // a tile's first input time is its first output time - hr (hr % 4 == 0)
-    int rows = 0;  // strip rows per component, kConvTileW + 16 * (ks - 1)
-    int kg = 0;    // components per tile (two accumulators of kg x kConvTileW TMEM columns)
+    bool bf16 = false;  // operands are BF16 splits (kind::f16) instead of TF32 splits
+    int step = 16;      // input times per K-step: 64-byte rows, 16 fp32 or 32 bf16
+    int ks = 0;         // K-steps per tile of kConvTileW output times
+    int hr = 0;         // a tile's first input time is its first output time - hr (16-byte aligned)
+    int rows = 0;       // strip rows per component, kConvTileW + step * (ks - 1)
+    int kg = 0;         // components per tile (two accumulators of kg x kConvTileW TMEM columns)
 };
 constexpr int kConvTileW = 64;   // output times per tile
-bool conv_tc_geometry(int nt, int K, ConvGeometry& g);
-// strip[k][r][i] = wPCA[k][i - r + 16 (ks - 1) - (hr - nt / 2)] (zero outside 0..nt-1), [K][rows][16]
+bool conv_tc_geometry(int nt, int K, ConvGeometry& g, bool bf16 = false);
+// strip[k][r][i] = wPCA[k][i - r + step (ks - 1) - (hr - nt / 2)] (zero outside 0..nt-1), [K][rows][step]
 void conv_tc_strips(const float* wPCA, int K, int nt, const ConvGeometry& g, float* strips);
 struct ConvOperands;
 ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows, int wlen, int zpitch,

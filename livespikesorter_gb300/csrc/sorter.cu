@@ -395,22 +395,27 @@ void Handle::init(const char* dir, const lss_params* prm) {
     tc_whiten = want_tc && C % 16 == 0 && C <= 512;
     tc_project = want_tc && (K * C) % 16 == 0 && T <= 512;
     tc_highpass = tc_whiten;
-    // the convolution reads the whitened windows the whitening GEMM also writes channel-major
-    tc_conv = tc_whiten && tc_project && conv_tc_geometry(nt, K, conv_g);
+    // the convolution reads the whitened windows the whitening GEMM also writes channel-major;
+    // gemm_path 3 runs it and the projection on BF16 splits
+    const bool bf16_tier = p.gemm_path == 3 && (K * C) % 32 == 0;
+    tc_conv = tc_whiten && tc_project && conv_tc_geometry(nt, K, conv_g, bf16_tier);
     if (tc_conv) {
-        std::vector<float> S((size_t)K * conv_g.rows * 16);
+        std::vector<float> S((size_t)K * conv_g.rows * conv_g.step);
         conv_tc_strips(m.wPCA.data(), K, nt, conv_g, S.data());
         float* d = dev_upload(S, dev_bytes, st);
         d_S_hi = dev_alloc<float>(S.size(), dev_bytes);
         d_S_lo = dev_alloc<float>(S.size(), dev_bytes);
-        launch_split_tf32(d, d_S_hi, d_S_lo, (int64_t)S.size(), st);
+        if (conv_g.bf16)
+            launch_split_bf16(d, d_S_hi, d_S_lo, (int64_t)S.size(), st);
+        else
+            launch_split_tf32(d, d_S_hi, d_S_lo, (int64_t)S.size(), st);
         LSS_CUDA(cudaGetLastError());
         LSS_CUDA(cudaStreamSynchronize(st));
         cudaFree(d);
         dev_bytes -= (int64_t)S.size() * 4;
     }
     // the BF16 projection reads Bpc as the tensor-core convolution writes it (BF16 split)
-    bf16_proj = p.gemm_path == 3 && tc_conv && (K * C) % 32 == 0;
+    bf16_proj = bf16_tier && tc_conv;
     if (tc_whiten || tc_project) {
         if (tc_whiten) {
             d_WD_hi = dev_alloc<float>((size_t)C * C, dev_bytes);
@@ -461,7 +466,7 @@ TapSet& Handle::taps_for(int Wn) {
     ts.L = (int)L;
     ts.R = (int)R;
     ts.d = dev_upload(tv, dev_bytes, st);
-    ts.zpitch = (Wn + 3) / 4 * 4;
+    ts.zpitch = (Wn + 7) / 8 * 8;   // 16-byte rows for fp32 and bf16
     if (tc_highpass) {
         const int ntaps = (int)(L + R + 1);
         ts.pitch = (int)(((Wn + L + R) + 3) / 4 * 4);
@@ -509,7 +514,7 @@ void Handle::ensure_work(int Wn, int nb) {
                          (int64_t)nba * (Wa + LRmax) * C * 4 + 2LL * nba * Wa * C * 4 +
                          (int64_t)nba * Wa * K * C * 4 * (tc_project && !tf32_data ? 2 : 1) +
                          (int64_t)nba * Wa * C * 4 * (tc_whiten && !tf32_data ? 1 : 0) +
-                         (int64_t)nba * ((Wa + 3) / 4 * 4) * C * 4 * (tc_conv ? (tf32_data ? 1 : 2) : 0) +
+                         (int64_t)nba * ((Wa + 7) / 8 * 8) * C * 4 * (tc_conv ? (tf32_data ? 1 : 2) : 0) +
                          (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16;
     if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
         throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
@@ -531,8 +536,8 @@ void Handle::ensure_work(int Wn, int nb) {
     d_Y = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     d_Z = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     if (tc_conv) {
-        // any window length up to Wa: rows of W rounded up to 4; the pad columns are never read
-        const size_t n = (size_t)nba * C * (size_t)((Wa + 3) / 4 * 4);
+        // any window length up to Wa: rows of W rounded up to 8; the pad columns are never read
+        const size_t n = (size_t)nba * C * (size_t)((Wa + 7) / 8 * 8);
         d_Zt_hi = dev_alloc<float>(n, dev_bytes);
         if (!tf32_data) d_Zt_lo = dev_alloc<float>(n, dev_bytes);
     }
@@ -634,7 +639,8 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
     }
     if (tc_whiten)
         LSS_CUDA(launch_umma_gemm_zt(um_whiten, d_Z, nb * Wn, C, C, tc_conv ? d_Zt_hi : nullptr,
-                                     tc_conv ? d_Zt_lo : nullptr, Wn, ts.zpitch, d_gemm_err, st));
+                                     tc_conv ? d_Zt_lo : nullptr, Wn, ts.zpitch, d_gemm_err, st,
+                                     tc_conv && conv_g.bf16));
     else
         launch_sgemm_nt(d_Y, C, (int64_t)Wn * C, d_WD, C, d_Z, C, (int64_t)Wn * C, Wn, C, C, nb, st);
     ++nl;
