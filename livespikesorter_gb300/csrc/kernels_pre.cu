@@ -4,6 +4,8 @@
 // (Kilosort template_matching.py:145, conv1d with padding nt//2).
 #include "lss_kernels.cuh"
 
+#include <cuda_bf16.h>
+
 #include <cstdio>
 
 namespace lss {
@@ -140,13 +142,15 @@ car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* _
 // warp four of them (the same median selection as car_kernel), stages the results in shared
 // memory and writes Xt[(b, c)][w + L] (+ the wrap copies) as coalesced runs of 32 samples per
 // channel, tf32-split into (Xt_hi, Xt_lo); columns past W + L + R up to the row pitch are zeroed.
+// OUT: 0 = tf32(x) alone, 1 = the tf32 split, 2 = the BF16 split (Xt_hi / Xt_lo viewed as bf16)
 constexpr int kCarTRows = 32;
 
-template <int NJ, bool LO>
+template <int NJ, int OUT>
 __global__ void __launch_bounds__(kCarWarps * 32)
 car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C, int W,
              int NT, const long long* __restrict__ colsum, int L, int R, int pitch, float* __restrict__ Xt_hi,
              float* __restrict__ Xt_lo) {
+    constexpr bool LO = OUT != 0;
     extern __shared__ float s_y[];   // [kCarTRows][C + 1]
     const int b = blockIdx.y;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -185,6 +189,31 @@ car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t*
     for (int idx = threadIdx.x; idx < kCarTRows * C; idx += blockDim.x) {
         const int c = idx / kCarTRows, rr = idx - c * kCarTRows;
         const int64_t rbase = ((int64_t)b * C + c) * pitch;
+        if constexpr (OUT == 2) {
+            __nv_bfloat16* bh = reinterpret_cast<__nv_bfloat16*>(Xt_hi);
+            __nv_bfloat16* bl = reinterpret_cast<__nv_bfloat16*>(Xt_lo);
+            if (rr < nrows) {
+                const int w = w0 + rr;
+                const float x = s_y[rr * ld + c];
+                const __nv_bfloat16 h = __float2bfloat16_rn(x);
+                const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+                bh[rbase + w + L] = h;
+                bl[rbase + w + L] = l;
+                if (w >= W - L) {
+                    bh[rbase + w + L - W] = h;
+                    bl[rbase + w + L - W] = l;
+                }
+                if (w < R) {
+                    bh[rbase + w + L + W] = h;
+                    bl[rbase + w + L + W] = l;
+                }
+            }
+            if (blockIdx.x == 0 && rr < pitch - total) {
+                bh[rbase + total + rr] = __float2bfloat16_rn(0.f);
+                bl[rbase + total + rr] = __float2bfloat16_rn(0.f);
+            }
+            continue;
+        }
         if (rr < nrows) {
             const int w = w0 + rr;
             float h, l;
@@ -209,20 +238,25 @@ car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t*
 }
 
 void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
-                  const long long* colsum, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s) {
+                  const long long* colsum, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s,
+                  bool bf16) {
     dim3 grid((W + kCarTRows - 1) / kCarTRows, nb);
     const int nj = (C + 31) / 32;
     const size_t smem = (size_t)kCarTRows * (C + 1) * sizeof(float);
 #define LSS_CART(N)                                                                                        \
     do {                                                                                                   \
-        if (Xt_lo) {                                                                                       \
-            raise_smem_limit((const void*)car_t_kernel<N, true>, smem);                                    \
-            car_t_kernel<N, true><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
-                                                                     L, R, pitch, Xt_hi, Xt_lo);           \
+        if (bf16 && Xt_lo) {                                                                               \
+            raise_smem_limit((const void*)car_t_kernel<N, 2>, smem);                                       \
+            car_t_kernel<N, 2><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
+                                                                  L, R, pitch, Xt_hi, Xt_lo);              \
+        } else if (Xt_lo) {                                                                                \
+            raise_smem_limit((const void*)car_t_kernel<N, 1>, smem);                                       \
+            car_t_kernel<N, 1><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
+                                                                  L, R, pitch, Xt_hi, Xt_lo);              \
         } else {                                                                                           \
-            raise_smem_limit((const void*)car_t_kernel<N, false>, smem);                                   \
-            car_t_kernel<N, false><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
-                                                                      L, R, pitch, Xt_hi, nullptr);        \
+            raise_smem_limit((const void*)car_t_kernel<N, 0>, smem);                                       \
+            car_t_kernel<N, 0><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
+                                                                  L, R, pitch, Xt_hi, nullptr);            \
         }                                                                                                  \
     } while (0)
     if (nj <= 4) LSS_CART(4);

@@ -273,11 +273,18 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
                     const int w = n0 + c0 + j;
                     if (w < args.wlen) {
                         const float v = __uint_as_float(r[j]);
-                        uint32_t h;
-                        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
                         const int64_t o = ((int64_t)b * args.wlen + w) * args.chans + c;
-                        args.out[o] = __uint_as_float(h);
-                        if (args.out_lo) args.out_lo[o] = v - __uint_as_float(h);
+                        if constexpr (BF16) {
+                            // the BF16 split, for the next GEMM on the BF16 tier
+                            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                            reinterpret_cast<__nv_bfloat16*>(args.out)[o] = h;
+                            reinterpret_cast<__nv_bfloat16*>(args.out_lo)[o] = __float2bfloat16_rn(v - __bfloat162float(h));
+                        } else {
+                            uint32_t h;
+                            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+                            args.out[o] = __uint_as_float(h);
+                            if (args.out_lo) args.out_lo[o] = v - __uint_as_float(h);
+                        }
                     }
                 }
             }
@@ -708,6 +715,25 @@ UmmaOperands* umma_make_bf16(const void* a_hi, const void* a_lo, int64_t rows_a,
     return u;
 }
 
+UmmaOperands* umma_make_toeplitz_bf16(const void* x_hi, const void* x_lo, int64_t rows, int64_t cols, int tile,
+                                      const void* g_hi, const void* g_lo, int K) {
+    if (K % (2 * kBK) != 0 || cols % 8 != 0 || !x_lo || !g_lo ||
+        (tile != kHighpassTileSmall && tile != kHighpassTileLarge))
+        return nullptr;
+    auto* u = new UmmaOperands();
+    u->bf16 = true;
+    u->rows_a = (int)rows;
+    u->cols_a = (int)cols;
+    u->rows_b = tile;
+    u->K = K;
+    if (!make_map_bf16(&u->a_hi, x_hi, rows, cols, kBM) || !make_map_bf16(&u->a_lo, x_lo, rows, cols, kBM) ||
+        !make_map_bf16(&u->b_hi, g_hi, tile, K, tile) || !make_map_bf16(&u->b_lo, g_lo, tile, K, tile)) {
+        delete u;
+        return nullptr;
+    }
+    return u;
+}
+
 UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t rows, int64_t cols, int tile,
                                  const float* g_hi, const float* g_lo, int K) {
     if (K % kBK != 0 || cols % 4 != 0 || (tile != kHighpassTileSmall && tile != kHighpassTileLarge)) return nullptr;
@@ -763,7 +789,9 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
 template <int TILE>
 static cudaError_t launch_highpass_tile(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W,
                                         int* err, cudaStream_t s) {
-    auto kern = u->has_a_lo ? umma_gemm_3xtf32<TILE, kToeplitz, true> : umma_gemm_3xtf32<TILE, kToeplitz, false>;
+    auto kern = u->bf16       ? umma_gemm_3xtf32<TILE, kToeplitz, true, true>
+                : u->has_a_lo ? umma_gemm_3xtf32<TILE, kToeplitz, true>
+                              : umma_gemm_3xtf32<TILE, kToeplitz, false>;
     constexpr int smem = smem_bytes<TILE>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;

@@ -64,8 +64,10 @@ void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, 
 void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
                 const long long* colsum, int L, int R, float* Xw, cudaStream_t s);
 // channel-major, tf32-split variant feeding the tensor-core high-pass: Xt[(b, c)][pitch]
+// bf16: Xt_hi / Xt_lo receive the BF16 split (viewed as bf16 arrays)
 void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
-                  const long long* colsum, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s);
+                  const long long* colsum, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s,
+                  bool bf16 = false);
 // Ylo != nullptr: Y receives tf32(y) and Ylo the remainder (operands of the tensor-core GEMM)
 void launch_highpass(const float* Xw, int C, int W, int L, int R, const float* taps, int nb, float* Y,
                      cudaStream_t s, float* Ylo = nullptr);
@@ -89,6 +91,10 @@ UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t r
                                  const float* g_lo, int K);
 cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo, int nb, int C, int W, int* err,
                                  cudaStream_t s);
+// the same on BF16 splits (x: bf16 [rows][cols], cols % 8 == 0; g: bf16 [tile][K], K % 32 == 0); its
+// epilogue writes Y as the BF16 split (Y_hi / Y_lo viewed as bf16)
+UmmaOperands* umma_make_toeplitz_bf16(const void* x_hi, const void* x_lo, int64_t rows, int64_t cols, int tile,
+                                      const void* g_hi, const void* g_lo, int K);
 void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
 // BF16 split: hi = bf16(x), lo = bf16(x - hi) (bf16 arrays of n elements)
 void launch_split_bf16(const float* x, void* hi, void* lo, int64_t n, cudaStream_t s);

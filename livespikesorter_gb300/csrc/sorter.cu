@@ -146,6 +146,7 @@ struct Handle {
     bool tc_highpass = false;                     // circular high-pass as a tensor-core band GEMM
     bool tf32_data = false;   // gemm_path 2: activations stored once as TF32, two products per GEMM
     bool bf16_proj = false;   // gemm_path 3: projection on BF16 splits (kind::f16, three products)
+    bool bf16_pre = false;    // gemm_path 3: high-pass and whitening on BF16 splits as well
     bool tc_conv = false;     // basis convolution as per-component band GEMMs on the tensor cores
     ConvGeometry conv_g;
     float *d_S_hi = nullptr, *d_S_lo = nullptr;   // its band strips (tf32 split)
@@ -398,6 +399,7 @@ void Handle::init(const char* dir, const lss_params* prm) {
     // the convolution reads the whitened windows the whitening GEMM also writes channel-major;
     // gemm_path 3 runs it and the projection on BF16 splits
     const bool bf16_tier = p.gemm_path == 3 && (K * C) % 32 == 0;
+    bf16_pre = bf16_tier && tc_whiten && C % 32 == 0;
     tc_conv = tc_whiten && tc_project && conv_tc_geometry(nt, K, conv_g, bf16_tier);
     if (tc_conv) {
         std::vector<float> S((size_t)K * conv_g.rows * conv_g.step);
@@ -420,7 +422,10 @@ void Handle::init(const char* dir, const lss_params* prm) {
         if (tc_whiten) {
             d_WD_hi = dev_alloc<float>((size_t)C * C, dev_bytes);
             d_WD_lo = dev_alloc<float>((size_t)C * C, dev_bytes);
-            launch_split_tf32(d_WD, d_WD_hi, d_WD_lo, (int64_t)C * C, st);
+            if (bf16_pre)
+                launch_split_bf16(d_WD, d_WD_hi, d_WD_lo, (int64_t)C * C, st);
+            else
+                launch_split_tf32(d_WD, d_WD_hi, d_WD_lo, (int64_t)C * C, st);
         }
         if (tc_project) {
             // two bf16 arrays fit in the halves of the tf32 ones
@@ -469,10 +474,12 @@ TapSet& Handle::taps_for(int Wn) {
     ts.zpitch = (Wn + 7) / 8 * 8;   // 16-byte rows for fp32 and bf16
     if (tc_highpass) {
         const int ntaps = (int)(L + R + 1);
-        ts.pitch = (int)(((Wn + L + R) + 3) / 4 * 4);
+        // rows of 16 bytes; K in whole K-steps (16 fp32 or 32 bf16)
+        ts.pitch = (int)(((Wn + L + R) + 7) / 8 * 8);
+        const int kstep = bf16_pre ? 32 : 16;
         for (int v = 0; v < 2; ++v) {
             const int TB = kHighpassTile[v];
-            const int Kt = ((TB + ntaps - 1) + 15) / 16 * 16;
+            const int Kt = ((TB + ntaps - 1) + kstep - 1) / kstep * kstep;
             ts.Kt[v] = Kt;
             std::vector<float> G((size_t)TB * Kt, 0.f);
             for (int j = 0; j < TB; ++j)
@@ -480,7 +487,10 @@ TapSet& Handle::taps_for(int Wn) {
             float* g = dev_upload(G, dev_bytes, st);
             ts.g_hi[v] = dev_alloc<float>(G.size(), dev_bytes);
             ts.g_lo[v] = dev_alloc<float>(G.size(), dev_bytes);
-            launch_split_tf32(g, ts.g_hi[v], ts.g_lo[v], (int64_t)G.size(), st);
+            if (bf16_pre)
+                launch_split_bf16(g, ts.g_hi[v], ts.g_lo[v], (int64_t)G.size(), st);
+            else
+                launch_split_tf32(g, ts.g_hi[v], ts.g_lo[v], (int64_t)G.size(), st);
             LSS_CUDA(cudaGetLastError());
             LSS_CUDA(cudaStreamSynchronize(st));
             cudaFree(g);
@@ -522,8 +532,8 @@ void Handle::ensure_work(int Wn, int nb) {
     d_raw = dev_alloc<int16_t>((size_t)kSlots * raw_rows_cap * Cin, dev_bytes);
     d_colsum = dev_alloc<long long>((size_t)nba * C, dev_bytes);
     if (tc_highpass) {
-        // row pitch of any window length up to Wa: W + L + R <= 2W - 1, rounded up to 4
-        const size_t n = (size_t)nba * C * (size_t)((2 * Wa + 3) / 4 * 4);
+        // row pitch of any window length up to Wa: W + L + R <= 2W - 1, rounded up to 8
+        const size_t n = (size_t)nba * C * (size_t)((2 * Wa + 7) / 8 * 8);
         d_Xt_hi = dev_alloc<float>(n, dev_bytes);
         LSS_CUDA(cudaMemsetAsync(d_Xt_hi, 0, n * sizeof(float), st));
         if (!tf32_data) {
@@ -560,7 +570,8 @@ void Handle::ensure_work(int Wn, int nb) {
     mo.sp_iter = dev_alloc<int>((size_t)nba * cap, dev_bytes);
     mo.cap = cap;
     if (tc_whiten) {
-        um_whiten = umma_make(d_Y, d_Y_lo, (int64_t)nba * Wa, d_WD_hi, d_WD_lo, C, C);
+        um_whiten = bf16_pre ? umma_make_bf16(d_Y, d_Y_lo, (int64_t)nba * Wa, d_WD_hi, d_WD_lo, C, C)
+                             : umma_make(d_Y, d_Y_lo, (int64_t)nba * Wa, d_WD_hi, d_WD_lo, C, C);
         if (!um_whiten) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (whitening GEMM)"};
     }
     if (tc_project) {
@@ -622,11 +633,14 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
         TapSet& tw = const_cast<TapSet&>(ts);
         const int v = nb <= kHighpassSmallGroup ? 0 : 1;
         if (!tw.um[v]) {
-            tw.um[v] = umma_make_toeplitz(d_Xt_hi, d_Xt_lo, (int64_t)nbcap * C, tw.pitch, kHighpassTile[v], tw.g_hi[v],
-                                          tw.g_lo[v], tw.Kt[v]);
+            tw.um[v] = bf16_pre ? umma_make_toeplitz_bf16(d_Xt_hi, d_Xt_lo, (int64_t)nbcap * C, tw.pitch,
+                                                          kHighpassTile[v], tw.g_hi[v], tw.g_lo[v], tw.Kt[v])
+                                : umma_make_toeplitz(d_Xt_hi, d_Xt_lo, (int64_t)nbcap * C, tw.pitch, kHighpassTile[v],
+                                                     tw.g_hi[v], tw.g_lo[v], tw.Kt[v]);
             if (!tw.um[v]) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (high-pass band GEMM)"};
         }
-        launch_car_t(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, tw.pitch, d_Xt_hi, d_Xt_lo, st), ++nl;
+        launch_car_t(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, tw.pitch, d_Xt_hi, d_Xt_lo, st, bf16_pre),
+            ++nl;
         mark();
         LSS_CUDA(launch_umma_highpass(tw.um[v], d_Y, d_Y_lo, nb, C, Wn, d_gemm_err, st));
         ++nl;
