@@ -66,6 +66,8 @@ def args_():
     ap.add_argument("--gemm-path", type=int, default=0,
                     help="0 tcgen05 FP32 (3xTF32), 1 FP32 SIMT, 2 tcgen05 with TF32 data (two products)")
     ap.add_argument("--no-tier", action="store_true", help="skip the chosen-tier measurement")
+    ap.add_argument("--tier-path", type=int, default=3,
+                    help="gemm_path of the chosen tier reported beside FP32: 3 BF16 splits, 2 TF32 activations")
     ap.add_argument("--path", default="sort", choices=["sort", "tc"],
                     help="sort = template matching (default); tc = threshold crossing")
     ap.add_argument("--tc-rows", type=int, default=600_000, help="rows per threshold-crossing push")
@@ -224,9 +226,9 @@ def roofline(stage_ms, n_groups, group, C, T, K, nt, W, ntaps, spikes_per_batch)
         unit, bound, peak = "GB/s", "hbm", hbm
     achieved = work / (ms / 1e3)
     # DRAM bytes (read + write) per batch of each stage's kernels (match: loop + residual) from ncu captures of the
-    # 64-batch group (profiles/match_kernel_interleaved_64batches.md,
+    # 64-batch group (profiles/match_kernel_interleaved_64batches.md, profiles/residual_and_features_64batches.md,
     # profiles/preprocess_and_gemm_kernels_64batches.md), scaled to this launch's batches
-    traffic_per_batch = {"match": (8.476e9 + 0.394e9) / 64, "project": 2.214e9 / 64, "basis_conv": 2.171e9 / 64,
+    traffic_per_batch = {"match": (8.476e9 + 0.371e9) / 64, "project": 2.214e9 / 64, "basis_conv": 2.171e9 / 64,
                          "highpass": 0.891e9 / 64, "whiten": 0.743e9 / 64, "car": 0.588e9 / 64}
     traffic = traffic_per_batch.get(kern)
     out = {"kernel": kern, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
@@ -340,15 +342,42 @@ def run_gpu(a):
     stage = {k: t_all[k] - t_base[k] for k in t_all}
     n_timed = n_all - n_base
     spikes_per_batch = spikes_seen[0] / max(1, a.steps * G)
-    ntaps = 1281
+    ntaps = 885   # the FIR the library cuts from this filter: taps beyond are < 1e-8 of the centre tap
     roof = roofline(stage, n_timed, G, C, T, K, nt, W, ntaps, spikes_per_batch)
     s.close()
 
-    # ---- the faster tier (gemm_path 2) beside the plain FP32 path ---------------------------
+    obuf = np.zeros(1 << 16, sorter.SPIKE_DTYPE)
+
+    def batch_latency(path, n):
+        """push-to-spikes wall time of single 1500-sample batches (one batch per launch)"""
+        s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1, profile=1,
+                                 match_variant=a.match_variant, gemm_path=path)
+        lat = []
+        s3.push(data[:NT + 2 * nt], 0)
+        drain(s3)
+        p = NT + 2 * nt
+        for i in range(n + 5):
+            if p + NT > data.shape[0]:
+                break
+            t1 = time.perf_counter()
+            s3.push(data[p: p + NT])
+            s3.poll(out=obuf)
+            if i >= 5:
+                lat.append(1e3 * (time.perf_counter() - t1))
+            p += NT
+        st3, ng3 = s3.stage_times()
+        s3.close()
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "batches": len(lat), "batch_ms_of_signal": 1e3 * NT / 30000.0,
+                "path": "lss_push_batch of 1500 new samples -> lss_poll, group_batches=1",
+                "stage_ms_per_batch": {k: v / max(ng3, 1) for k, v in st3.items()}}
+
+    # ---- the faster tier beside the plain FP32 path ----------------------------------------------
     tier = None
     if a.gemm_path == 0 and not a.no_tier:
+        tp = a.tier_path
         st = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1,
-                                 match_variant=a.match_variant, gemm_path=2)
+                                 match_variant=a.match_variant, gemm_path=tp)
         ext2 = torch.cuda.ExternalStream(st.cuda_stream(), device=f"cuda:{dev}")
 
         def step2(i):
@@ -376,16 +405,20 @@ def run_gpu(a):
         # spike agreement with the FP32 path on the same 256 batches, streamed
         n_rows = min(data.shape[0], 256 * NT + 2 * nt)
         got = {}
-        for path in (0, 2):
+        for path in (0, tp):
             with sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
                                      match_variant=a.match_variant, gemm_path=path) as sa:
                 got[path] = sa.sort_stream(data[:n_rows])
-        frac, amp_ok = spike_agreement(got[0], got[2])
-        tier = {"gemm_path": 2, "value": a.steps * G * NT * C / (ms2 / 1e3), "unit": UNIT,
-                "ms_per_step": ms2 / a.steps, "dtype": "tf32 activations x fp32-split fixed matrices, fp32 accumulate",
+        frac, amp_ok = spike_agreement(got[0], got[tp])
+        dt = {3: "bf16 splits (hi*hi + hi*lo + lo*hi on kind::f16), fp32 accumulate",
+              2: "tf32 activations x fp32-split fixed matrices, fp32 accumulate"}.get(tp, f"gemm_path {tp}")
+        tier = {"gemm_path": tp, "value": a.steps * G * NT * C / (ms2 / 1e3), "unit": UNIT,
+                "ms_per_step": ms2 / a.steps, "dtype": dt,
                 "stage_ms_per_launch": {k: (ta[k] - tb[k]) / max(1, na - nb0) for k in ta},
+                "latency": {k: v for k, v in batch_latency(tp, min(a.latency_batches, 100)).items()
+                            if k in ("p50_ms", "p99_ms", "batches")},
                 "agreement_vs_fp32": {"batches": (n_rows - 2 * nt) // NT, "spikes_fp32": int(len(got[0])),
-                                      "spikes_tier": int(len(got[2])), "matched": frac, "amp_within_1e-3": amp_ok,
+                                      "spikes_tier": int(len(got[tp])), "matched": frac, "amp_within_1e-3": amp_ok,
                                       "rule": "same template, |dt| <= 1 sample, amplitude within 1e-3 relative"}}
     del d_data
 
@@ -394,7 +427,6 @@ def run_gpu(a):
                              match_variant=a.match_variant, gemm_path=a.gemm_path)
     chunk = G * NT
     pos = [0]
-    obuf = np.zeros(1 << 16, sorter.SPIKE_DTYPE)
     # the caller's rows live in pinned host memory (the e2e contract); the API copies page-locked
     # rows straight into the pending group's device rows on its copy stream
     pinned = torch.from_numpy(data).pin_memory()
@@ -443,27 +475,7 @@ def run_gpu(a):
     s2.close()
 
     # ---- per-batch latency (one batch per launch) --------------------------------------------
-    s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1, profile=1,
-                             match_variant=a.match_variant, gemm_path=a.gemm_path)
-    lat = []
-    s3.push(data[:NT + 2 * nt], 0)
-    drain(s3)
-    p = NT + 2 * nt
-    for i in range(a.latency_batches + 5):
-        if p + NT > data.shape[0]:
-            break
-        t1 = time.perf_counter()
-        s3.push(data[p: p + NT])
-        s3.poll(out=obuf)
-        if i >= 5:
-            lat.append(1e3 * (time.perf_counter() - t1))
-        p += NT
-    st3, ng3 = s3.stage_times()
-    s3.close()
-    latency = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-               "batches": len(lat), "batch_ms_of_signal": 1e3 * NT / 30000.0,
-               "path": "lss_push_batch of 1500 new samples -> lss_poll, group_batches=1",
-               "stage_ms_per_batch": {k: v / max(ng3, 1) for k, v in st3.items()}}
+    latency = batch_latency(a.gemm_path, a.latency_batches)
 
     # ---- CPU baseline (rank 0) ----------------------------------------------------------------
     cpu = None
