@@ -156,28 +156,29 @@ def test_template_subset_directory(cfg_small, tmp_path):
 def test_tensor_core_conv_tiles_span_windows(cfg_small):
     """96 channels in a group of five windows: the 128-row (window, channel) tiles of the
     tensor-core basis convolution span two windows each.  The group's spikes agree with each window
-    sorted by the float64 oracle, and equal those of the FP32-SIMT path (gemm_path 1)."""
+    sorted by the float64 oracle -- on the FP32 tensor-core path, the FP32-SIMT path (gemm_path 1)
+    and the BF16-split path (3) -- and paths 0 and 1 give the same spikes."""
     d, data, _ = cfg_small
     oss = ko.load_oss_input(d)
     nt, nt0 = oss.wPCA.shape[1], oss.nt0min
     W = 1500 + 2 * nt
     wins = np.stack([data[k * 1500: k * 1500 + W] for k in range(5)])
     outs = {}
-    for path in (0, 1):
+    for path in (0, 1, 3):
         with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=5, gemm_path=path) as s:
             outs[path] = s.sort_windows(wins)
-    ref, got = [], {0: [], 1: []}
+    ref, got = [], {0: [], 1: [], 3: []}
     for k in range(5):
         r = ko.sort_window(wins[k].T, oss, max_iters=50)
         off = k * 100_000   # keep the windows apart in one agreement count
         ref.append((r.match.st[:, 0] - nt // 2 + nt0 + off, r.match.st[:, 1], r.match.amps))
-        for path in (0, 1):
+        for path in (0, 1, 3):
             sp = outs[path][k]
             got[path].append((sp["time"].astype(np.int64) + off, sp["tmpl"], sp["amp"]))
     cat = lambda parts: [np.concatenate([p[i] for p in parts]) for i in range(3)]
     t_r, k_r, a_r = cat(ref)
     assert len(t_r) > 30
-    for path in (0, 1):
+    for path in (0, 1, 3):
         a, amp_ok, amax = agreement(t_r, k_r, a_r, *cat(got[path]))
         assert a >= AGREE and amp_ok >= AGREE, (path, a, amp_ok, amax, len(t_r))
     a, amp_ok, amax = agreement(*cat(got[1]), *cat(got[0]))
@@ -376,11 +377,12 @@ def test_cpp_dropin_replay(golden_dir, tmp_path):
 
 
 def test_tensor_core_and_simt_gemms_agree(win_oss, win):
-    """gemm_path 0 (tcgen05, 3xTF32: high-pass band GEMM, whitening, projection) and 1 (FP32 SIMT)
-    agree within 1e-5 (preprocessed) / 2e-5 (scores) of the largest magnitude -- inside the
-    oracle tolerances -- and give the same spikes."""
+    """gemm_path 0 (tcgen05, 3xTF32: high-pass band GEMM, whitening, convolution, projection) and 1
+    (FP32 SIMT) agree within 1e-5 (preprocessed) / 2e-5 (scores) of the largest magnitude -- inside
+    the oracle tolerances -- and give the same spikes; the BF16-split path 3 (32 channels: every
+    stage on kind::f16) within 5e-5 / 1e-4, with the same spikes."""
     outs = {}
-    for path in (0, 1):
+    for path in (0, 1, 3):
         with sorter.OnlineSorter(win_oss, max_iters=int(win["max_iters"]), gemm_path=path) as s:
             outs[path] = (s.debug_stage(win["window"], sorter.STAGE_PREPROCESSED),
                           s.debug_stage(win["window"], sorter.STAGE_SCORES), s.sort_windows(win["window"])[0])
@@ -388,6 +390,11 @@ def test_tensor_core_and_simt_gemms_agree(win_oss, win):
     _rel_close(outs[0][1].astype(np.float64), outs[1][1].astype(np.float64), 2e-5)
     a, amp_ok, amax = agreement(outs[1][2]["time"], outs[1][2]["tmpl"], outs[1][2]["amp"],
                                 outs[0][2]["time"], outs[0][2]["tmpl"], outs[0][2]["amp"])
+    assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
+    _rel_close(outs[3][0].astype(np.float64), outs[1][0].astype(np.float64), 5e-5)
+    _rel_close(outs[3][1].astype(np.float64), outs[1][1].astype(np.float64), 1e-4)
+    a, amp_ok, amax = agreement(outs[1][2]["time"], outs[1][2]["tmpl"], outs[1][2]["amp"],
+                                outs[3][2]["time"], outs[3][2]["tmpl"], outs[3][2]["amp"])
     assert a == 1.0 and amp_ok == 1.0, (a, amp_ok, amax)
 
 
