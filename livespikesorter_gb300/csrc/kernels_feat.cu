@@ -32,6 +32,7 @@ void launch_rec_offsets(const MatchOut& out, int nb, int* rec_offset, cudaStream
 }
 
 constexpr int kFeatWarps = 8;
+constexpr int kFeatMaxK = 8;   // PCs (the loader refuses more)
 
 __global__ void __launch_bounds__(kFeatWarps * 32)
 features_kernel(const float* __restrict__ Xres, MatchOut out, int nb, int W, int C, int T, int K, int nt, int nC,
@@ -57,23 +58,39 @@ features_kernel(const float* __restrict__ Xres, MatchOut out, int nb, int W, int
     const int64_t peak = iU[t];
     const int nf = nC * K;
 
-    // two (n, k) pairs per lane (nC * K <= 64)
-    float f[2] = {0.f, 0.f};
+    // lpc lanes per nearest channel, each over a contiguous run of the nt taps for all K components
+    // (every residual sample loaded once); the channel's first lane adds the others' partial sums
+    // in lane order, then the amplitude term
+    __syncwarp();
+    sf[lane] = 0.f;
+    sf[lane + 32] = 0.f;
+    __syncwarp();
+    const int lpc = nC >= 32 ? 1 : 32 / nC;
+    const int part = lane % lpc, chunk = (nt + lpc - 1) / lpc;
+    const int r0 = part * chunk, r1 = min(nt, r0 + chunk);
+    for (int n0 = 0; n0 < nC; n0 += 32 / lpc) {
+        const int n = n0 + lane / lpc;
+        const bool have = lane / lpc < 32 / lpc && n < nC;
+        float acc[kFeatMaxK];
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int p = lane + 32 * q;
-        if (p < nf) {
-            const int n = p / K, k = p % K;
-            const int64_t ch = iCC[(int64_t)n * C + peak];
-            float acc = 0.f;
-            for (int r = 0; r < nt; ++r) acc = fmaf(X[(int64_t)(w + r - hw) * C + ch], wPCA[k * nt + r], acc);
-            f[q] = acc + amp * Ucc[((int64_t)n * T + t) * K + k];
+        for (int k = 0; k < kFeatMaxK; ++k) acc[k] = 0.f;
+        if (have) {
+            const float* xc_ = X + (int64_t)(w - hw) * C + iCC[(int64_t)n * C + peak];
+            for (int r = r0; r < r1; ++r) {
+                const float x = xc_[(int64_t)r * C];
+#pragma unroll
+                for (int k = 0; k < kFeatMaxK; ++k)
+                    if (k < K) acc[k] = fmaf(x, wPCA[k * nt + r], acc[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kFeatMaxK; ++k) {
+            float tot = acc[k];
+            for (int q = 1; q < lpc; ++q) tot += __shfl_sync(0xffffffffu, acc[k], (lane + q) & 31);
+            if (have && part == 0 && k < K) sf[n * K + k] = tot + amp * Ucc[((int64_t)n * T + t) * K + k];
         }
     }
     // mass per nearest channel, then the weighted position
-    __syncwarp();
-    sf[lane] = f[0];
-    sf[lane + 32] = f[1];
     __syncwarp();
     float mx = 0.f, my = 0.f, ms = 0.f;
     if (lane < nC) {
@@ -132,8 +149,8 @@ features_kernel(const float* __restrict__ Xres, MatchOut out, int nb, int W, int
         if (bi == 0x7fffffff) bi = 0;   // NaN position (zero feature energy): first cluster
     }
     SpikeRec* rec = recs + gw;
-    rec->feat[lane] = f[0];
-    rec->feat[lane + 32] = f[1];
+    rec->feat[lane] = sf[lane];
+    rec->feat[lane + 32] = sf[lane + 32];
     if (lane == 0) {
         rec->batch = batch_base + b;
         rec->w = w;
