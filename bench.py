@@ -229,7 +229,7 @@ def roofline(stage_ms, n_groups, group, C, T, K, nt, W, ntaps, spikes_per_batch)
     # 64-batch group (profiles/match_kernel_interleaved_64batches.md, profiles/residual_and_features_64batches.md,
     # profiles/preprocess_and_gemm_kernels_64batches.md), scaled to this launch's batches
     traffic_per_batch = {"match": (8.476e9 + 0.371e9) / 64, "project": 2.214e9 / 64, "basis_conv": 2.171e9 / 64,
-                         "highpass": 0.891e9 / 64, "whiten": 0.743e9 / 64, "car": 0.588e9 / 64}
+                         "highpass": 0.798e9 / 64, "whiten": 0.742e9 / 64, "car": 0.514e9 / 64}
     traffic = traffic_per_batch.get(kern)
     out = {"kernel": kern, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
            "frac": achieved / peak, "peak_source": src,
