@@ -474,6 +474,7 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
         if (!mbar_wait(sb, 0u)) atomicOr(err, 4);
     } else if (warp == kConvEpiWarps + 1 && lane == 0) {
         // ---- MMA issuer ----
+        const uint64_t dsh = smem_desc(s_hi), dsl = smem_desc(s_lo);   // the strips' base descriptors
         if (!mbar_wait(smem_u32(&strip_bar), 0u)) {
             atomicOr(err, 2);
             abort_s = 1;
@@ -500,24 +501,32 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                // strip row step (ks - 1 - s): 16 or 32 rows of 64 bytes per K-step
-                const uint32_t band = (uint32_t)(KS - 1 - ks) * (BF16 ? 2048u : 1024u);
+                // strip row step (ks - 1 - s): 16 or 32 rows of 64 bytes per K-step.  The start
+                // address sits in the descriptors' low bits (address >> 4, every shared address here
+                // is below 256 KB), so offsets are added to descriptors built once: the single
+                // issuing thread spends its instructions on the 18 MMAs of the K-step, not on
+                // rebuilding their operands
+                const uint64_t ah0 = smem_desc(sA_hi(s)), al0 = smem_desc(sA_lo(s));
+                const uint64_t band = ((uint64_t)(KS - 1 - ks) * (BF16 ? 2048u : 1024u) + cg0 * sbytes) >> 4;
 #pragma unroll
-                for (int kk = 0; kk < kBK / 8; ++kk) {          // K = 8 tf32 (32 bytes) per MMA
-                    const uint32_t off = (uint32_t)kk * 32u;
-                    const uint64_t ah = smem_desc(sA_hi(s) + off), al = smem_desc(sA_lo(s) + off);
-                    for (int g = 0; g < ng; ++g) {
-                        const uint32_t boff = (uint32_t)(cg0 + g) * sbytes + band + off;
-                        const uint64_t bh = smem_desc(s_hi + boff), bl = smem_desc(s_lo + boff);
-                        const uint32_t d = dcol + (uint32_t)(g * TW);
-                        if constexpr (BF16) {
-                            mma_bf16<TW>(d, ah, bh, (ks > 0 || kk > 0) ? 1u : 0u);
-                            mma_bf16<TW>(d, ah, bl, 1u);
-                            if constexpr (ALO) mma_bf16<TW>(d, al, bh, 1u);
-                        } else {
-                            mma_tf32<TW>(d, ah, bh, (ks > 0 || kk > 0) ? 1u : 0u);
-                            mma_tf32<TW>(d, ah, bl, 1u);
-                            if constexpr (ALO) mma_tf32<TW>(d, al, bh, 1u);
+                for (int kk = 0; kk < 2; ++kk) {          // 32 bytes (8 tf32 / 16 bf16) per MMA
+                    const uint64_t ah = ah0 + 2u * kk, al = al0 + 2u * kk;
+                    const uint32_t acc = (ks > 0 || kk > 0) ? 1u : 0u;
+#pragma unroll
+                    for (int g = 0; g < kConvMaxK / 2; ++g) {
+                        if (g < ng) {
+                            const uint64_t boff = band + (uint64_t)g * (sbytes >> 4) + 2u * kk;
+                            const uint64_t bh = dsh + boff, bl = dsl + boff;
+                            const uint32_t d = dcol + (uint32_t)(g * TW);
+                            if constexpr (BF16) {
+                                mma_bf16<TW>(d, ah, bh, acc);
+                                mma_bf16<TW>(d, ah, bl, 1u);
+                                if constexpr (ALO) mma_bf16<TW>(d, al, bh, 1u);
+                            } else {
+                                mma_tf32<TW>(d, ah, bh, acc);
+                                mma_tf32<TW>(d, ah, bl, 1u);
+                                if constexpr (ALO) mma_tf32<TW>(d, al, bh, 1u);
+                            }
                         }
                     }
                 }
