@@ -58,8 +58,11 @@ typedef struct lss_params {
     int32_t gemm_path;      /* 0 = tensor cores (tcgen05, 3xTF32 = FP32 accuracy) where shapes allow; 1 = FP32 SIMT;
                                2 = tensor cores with the data operands stored once as TF32 (two products; the
                                fixed matrices keep FP32 accuracy): faster, spike agreement with 0 measured;
-                               3 = as 0, with the projection on BF16 splits (hi = bf16(x), lo = bf16(x - hi),
-                               hi*hi + hi*lo + lo*hi in FP32: ~1e-5 relative per product) at the BF16 rate */
+                               3 = the high-pass, whitening, convolution and projection on BF16 splits
+                               (hi = bf16(x), lo = bf16(x - hi), hi*hi + hi*lo + lo*hi in FP32: ~1e-5 relative
+                               per product) at the BF16 rate, where C and K*C are multiples of 32 (the
+                               high-pass and whitening need C, the convolution and projection K*C); a stage
+                               whose shape does not allow it runs as on 0 */
     int32_t cluster_rule;   /* final cluster of a spike: 0 = nearest centroid in (x, y) (OnlineSpikesV2.cu:1058-1074);
                                1 = best PC score 2 tF.mu - |mu|^2 among the clusters within cluster_radius_um of the
                                spike (OnlineKilosort.py:233-284; cluster_centroids_pca.npy [T_final, nC*K]), -1 if none */
