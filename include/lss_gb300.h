@@ -208,7 +208,7 @@ int lss_stage_times(lss_handle* h, double* ms, int32_t n, int64_t* n_groups);
  * the array: calls whose work overlaps on the GPU race, so serialise them (one stream, or events).
  * Errors: LSS_ERR_ARG / LSS_ERR_CUDA, message via lss_last_error(NULL). */
 #define LSS_NOALLOC_MAX_SAMPLES 16384
-#define LSS_NOALLOC_SCRATCH_BYTES 279040
+#define LSS_NOALLOC_SCRATCH_BYTES 196864
 int lss_match_noalloc(float* scores, float* residual, const float* ctc_perm, const float* waveforms,
                       const float* template_norms, float th, int32_t W, int32_t T, int32_t C, int32_t nt,
                       int32_t max_iters, int32_t* n_spikes, int32_t* spike_sample, int32_t* spike_template,

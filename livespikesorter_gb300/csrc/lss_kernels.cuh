@@ -30,12 +30,9 @@ struct MatchOut {
 
 // Scratch of the matching loop (device), per batch.
 struct MatchScratch {
-    float* cfmax;      // [nb][W]
-    int* imax;         // [nb][W]
+    float* cfmax;      // [nb][W]   per-sample maximum (windows longer than the staged chunk)
     int* at_t;         // [nb][W]   template of the spike accepted at w this iteration, -1 if none
     float* at_amp;     // [nb][W]
-    unsigned char* dirty;  // [nb][W]
-    int* cta_cnt;      // [nb][2][G]
 };
 
 // One spike record as written by the feature kernel (host-mapped memory).
@@ -46,7 +43,6 @@ struct SpikeRec {
     float feat[64];
 };
 
-constexpr int kMatchCluster = 16;  // largest cluster (CTAs per batch) the matching loop launches
 constexpr int kMatchThreads = 512;       // matching loop, scores in L2 (two CTAs per SM)
 constexpr int kMatchThreadsSmem = 768;   // matching loop, scores in shared memory (one CTA per SM)
 constexpr int kMatchThreadsWide = 1024;  // matching loop, scores in L2, 16-CTA clusters, one CTA per SM

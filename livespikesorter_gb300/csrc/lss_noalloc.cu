@@ -4,9 +4,9 @@
 // acquisition thread that must not block on the allocator, code that runs inside a fixed
 // memory pool owned by another framework, or an application that already holds the scores
 // and residual in its own buffers.  lss_match_noalloc runs the same matching-pursuit kernel as
-// the rest of the library, but its working memory (per-sample maxima and argmaxima, the
-// accepted-spike maps, the changed-sample flags and the cluster counters) lives in the
-// statically sized device array below instead of buffers obtained from cudaMalloc.
+// the rest of the library, but its working memory (the per-sample maxima of long windows and the
+// accepted-spike maps) lives in the statically sized device array below instead of buffers
+// obtained from cudaMalloc.
 //
 // The array is a file-scope __device__ variable: every GPU that loads this library holds it
 // (LSS_NOALLOC_SCRATCH_BYTES) until the process exits.  Host code cannot use its name as a
@@ -32,12 +32,9 @@ constexpr size_t kAlign = 256;
 constexpr size_t align_up(size_t n) { return (n + kAlign - 1) / kAlign * kAlign; }
 // layout of the scratch array (byte offsets)
 constexpr size_t kOffCfmax = 0;
-constexpr size_t kOffImax = align_up(kOffCfmax + sizeof(float) * kMaxW);
-constexpr size_t kOffAtT = align_up(kOffImax + sizeof(int) * kMaxW);
+constexpr size_t kOffAtT = align_up(kOffCfmax + sizeof(float) * kMaxW);
 constexpr size_t kOffAtAmp = align_up(kOffAtT + sizeof(int) * kMaxW);
-constexpr size_t kOffDirty = align_up(kOffAtAmp + sizeof(float) * kMaxW);
-constexpr size_t kOffCta = align_up(kOffDirty + kMaxW);
-constexpr size_t kOffStatus = align_up(kOffCta + sizeof(int) * 2 * lss::kMatchCluster);
+constexpr size_t kOffStatus = align_up(kOffAtAmp + sizeof(float) * kMaxW);
 constexpr size_t kOffIters = kOffStatus + sizeof(int);
 constexpr size_t kScratchBytes = align_up(kOffIters + sizeof(int));
 static_assert(kScratchBytes == LSS_NOALLOC_SCRATCH_BYTES, "scratch size in lss_gb300.h is out of date");
@@ -93,11 +90,8 @@ extern "C" int lss_match_noalloc(float* scores, float* residual, const float* ct
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     lss::MatchScratch sc;
     sc.cfmax = reinterpret_cast<float*>(base + kOffCfmax);
-    sc.imax = reinterpret_cast<int*>(base + kOffImax);
     sc.at_t = reinterpret_cast<int*>(base + kOffAtT);
     sc.at_amp = reinterpret_cast<float*>(base + kOffAtAmp);
-    sc.dirty = base + kOffDirty;
-    sc.cta_cnt = reinterpret_cast<int*>(base + kOffCta);
     lss::MatchOut out;
     out.n_spikes = n_spikes;
     out.n_iters = reinterpret_cast<int*>(base + kOffIters);

@@ -276,8 +276,7 @@ void Handle::free_work() {
     }
     for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
                     (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo, (void*)d_Zt_hi, (void*)d_Zt_lo,
-                    (void*)sc.cfmax, (void*)sc.imax, (void*)sc.at_t, (void*)sc.at_amp, (void*)sc.dirty,
-                    (void*)sc.cta_cnt, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
+                    (void*)sc.cfmax, (void*)sc.at_t, (void*)sc.at_amp, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
                     (void*)mo.sp_t, (void*)mo.sp_amp, (void*)mo.sp_iter})
         if (p) cudaFree(p);
     d_raw = nullptr;
@@ -556,11 +555,8 @@ void Handle::ensure_work(int Wn, int nb) {
     if (tc_whiten && !tf32_data) d_Y_lo = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     if (tc_project && !tf32_data) d_Bpc_lo = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
     sc.cfmax = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
-    sc.imax = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
     sc.at_t = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
     sc.at_amp = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
-    sc.dirty = dev_alloc<unsigned char>((size_t)nba * Wa, dev_bytes);
-    sc.cta_cnt = dev_alloc<int>((size_t)nba * 2 * kMatchCluster, dev_bytes);
     mo.n_spikes = dev_alloc<int>(nba, dev_bytes);
     mo.n_iters = dev_alloc<int>(nba, dev_bytes);
     mo.status = dev_alloc<int>(nba, dev_bytes);
