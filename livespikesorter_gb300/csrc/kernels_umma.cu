@@ -162,6 +162,10 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n0 = blockIdx.x * kBN, m0 = blockIdx.y * kBM;
     const int nk = K / kKE;
+    // split K (plain mode, gridDim.z > 1): this CTA multiplies K-steps [kt0, kt0 + nkl) and writes its
+    // partial tile to output slice blockIdx.z (the caller sums the slices)
+    const int kt0 = (int)((int64_t)nk * blockIdx.z / gridDim.z);
+    const int nkl = (int)((int64_t)nk * (blockIdx.z + 1) / gridDim.z) - kt0;
     // 1024-byte aligned stage buffers: [A_hi][A_lo][B_hi][B_lo] per stage
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
     auto sA_hi = [&](int s) { return base + (uint32_t)(s * kStageBytes); };
@@ -192,7 +196,7 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
     if (warp == 0 && lane == 0) {
         // ---- producer: TMA ----
         int issued = 0;
-        for (int kt = 0; kt < nk; ++kt) {
+        for (int kt = 0; kt < nkl; ++kt) {
             const int s = kt % kStages;
             const uint32_t round = (uint32_t)(kt / kStages);
             if (!mbar_wait(smem_u32(&empty_bar[s]), (round & 1u) ^ 1u) || abort_s) {
@@ -202,7 +206,7 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
             }
             const uint32_t fb = smem_u32(&full_bar[s]);
             mbar_expect_tx(fb, kLoadBytes);
-            const int k0 = kt * kKE;   // a multiple of 64 bytes
+            const int k0 = (kt0 + kt) * kKE;   // a multiple of 64 bytes
             // Toeplitz: A columns start at the tile's output time n0 (a multiple of 128), B is the
             // same band matrix for every tile
             const int ax = (MODE == kToeplitz) ? n0 + k0 : k0;
@@ -218,7 +222,7 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
             if (!mbar_wait(smem_u32(&full_bar[kt % kStages]), (uint32_t)(kt / kStages) & 1u)) atomicOr(err, 4);
     } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer ----
-        for (int kt = 0; kt < nk; ++kt) {
+        for (int kt = 0; kt < nkl; ++kt) {
             const int s = kt % kStages;
             const uint32_t round = (uint32_t)(kt / kStages);
             if (!mbar_wait(smem_u32(&full_bar[s]), round & 1u) || abort_s) {
@@ -291,7 +295,7 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
             continue;
         }
         if (ok && row < M) {
-            float* crow = args.out + (int64_t)row * args.ldc + n0 + c0;
+            float* crow = args.out + ((int64_t)blockIdx.z * M + row) * args.ldc + n0 + c0;
             const int ncol = min(32, N - (n0 + c0));
             if (args.zt_hi) {
                 // lanes hold consecutive rows = consecutive times of one channel row of zt
@@ -791,6 +795,46 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
     a.zt_bf16 = zt_bf16 ? 1 : 0;
     dim3 grid((N + kPlainBN - 1) / kPlainBN, (M + kBM - 1) / kBM);
     kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
+    return cudaGetLastError();
+}
+
+// C[m][n] = sum over the slices of ws[s][m][n], in slice order
+__global__ void sum_slices_kernel(const float* __restrict__ ws, float* __restrict__ Cm, int M, int N, int64_t ldc,
+                                  int S) {
+    const int64_t total = (int64_t)M * N;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t m = i / N, n = i - m * N;
+        float acc = ws[m * ldc + n];
+        for (int s = 1; s < S; ++s) acc += ws[((int64_t)s * M + m) * ldc + n];
+        Cm[m * ldc + n] = acc;
+    }
+}
+
+cudaError_t launch_umma_gemm_splitk(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* ws, int S,
+                                    int* err, cudaStream_t s) {
+    if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN || S < 1 || !ws)
+        return cudaErrorInvalidValue;
+    const int nk = u->K / (u->bf16 ? 2 * kBK : kBK);
+    S = std::min(S, nk);
+    if (S <= 1) return launch_umma_gemm(u, Cm, M, N, ldc, err, s);
+    auto kern = u->bf16       ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
+                : u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true>
+                              : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
+    constexpr int smem = smem_bytes<kPlainBN>();
+    const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
+    if (attr_err != cudaSuccess) return attr_err;
+    UmmaArgs a{};
+    a.out = ws;
+    a.M = M;
+    a.N = N;
+    a.K = u->K;
+    a.ldc = ldc;
+    a.err = err;
+    a.wlen = 1;
+    dim3 grid((N + kPlainBN - 1) / kPlainBN, (M + kBM - 1) / kBM, S);
+    kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
+    const int blocks = (int)std::min<int64_t>(((int64_t)M * N + 255) / 256, 2048);
+    sum_slices_kernel<<<blocks, 256, 0, s>>>(ws, Cm, M, N, ldc, S);
     return cudaGetLastError();
 }
 

@@ -81,6 +81,10 @@ UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, co
                         int64_t rows_b, int K);
 void umma_free(UmmaOperands* u);
 cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, int* err, cudaStream_t s);
+// the same with K split S ways across CTAs (for launches too small to fill the GPU): partial tiles in
+// ws [S][M][ldc], then summed in slice order into C (deterministic)
+cudaError_t launch_umma_gemm_splitk(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* ws, int S,
+                                    int* err, cudaStream_t s);
 // circular high-pass on the tensor cores: x = channel-major windows [rows][cols] (tf32 split),
 // g = the 128 x K band matrix of the taps (tf32 split)
 UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t rows, int64_t cols, int tile, const float* g_hi,

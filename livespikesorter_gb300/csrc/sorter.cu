@@ -98,6 +98,9 @@ struct TapSet {
 constexpr int kHighpassTile[2] = {kHighpassTileSmall, kHighpassTileLarge};
 
 constexpr int kSlots = 4;   // groups in flight + the one collecting the stream's next rows
+// the projection of a launch of at most kSplitBatches windows (26 CTAs for one 1622-sample window)
+// splits K kSplitK ways to fill the GPU
+constexpr int kSplitBatches = 2, kSplitK = 4;
 
 struct Slot {
     int16_t* h_stage = nullptr;
@@ -170,6 +173,7 @@ struct Handle {
     float *d_Y_lo = nullptr, *d_Bpc_lo = nullptr;   // tf32 remainders (tensor-core path)
     float *d_Xt_hi = nullptr, *d_Xt_lo = nullptr;   // channel-major wrapped windows (tensor-core high-pass)
     float *d_Zt_hi = nullptr, *d_Zt_lo = nullptr;   // channel-major whitened windows (tensor-core convolution)
+    float* d_split = nullptr;   // partial projections of split-K launches [kSplitK][rows][T]
     MatchScratch sc{};
     MatchOut mo{};
     int64_t work_bytes = 0;
@@ -276,6 +280,7 @@ void Handle::free_work() {
     }
     for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
                     (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo, (void*)d_Zt_hi, (void*)d_Zt_lo,
+                    (void*)d_split,
                     (void*)sc.cfmax, (void*)sc.at_t, (void*)sc.at_amp, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
                     (void*)mo.sp_t, (void*)mo.sp_amp, (void*)mo.sp_iter})
         if (p) cudaFree(p);
@@ -285,6 +290,7 @@ void Handle::free_work() {
     d_Y_lo = d_Bpc_lo = nullptr;
     d_Xt_hi = d_Xt_lo = nullptr;
     d_Zt_hi = d_Zt_lo = nullptr;
+    d_split = nullptr;
     sc = MatchScratch{};
     mo = MatchOut{};
     dev_bytes -= work_bytes;
@@ -524,7 +530,8 @@ void Handle::ensure_work(int Wn, int nb) {
                          (int64_t)nba * Wa * K * C * 4 * (tc_project && !tf32_data ? 2 : 1) +
                          (int64_t)nba * Wa * C * 4 * (tc_whiten && !tf32_data ? 1 : 0) +
                          (int64_t)nba * ((Wa + 7) / 8 * 8) * C * 4 * (tc_conv ? (tf32_data ? 1 : 2) : 0) +
-                         (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16;
+                         (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16 +
+                         (tc_project ? (int64_t)kSplitK * std::min(nba, kSplitBatches) * Wa * T * 4 : 0);
     if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
         throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
                                            " device bytes, budget " + std::to_string(p.mem_budget)};
@@ -554,6 +561,7 @@ void Handle::ensure_work(int Wn, int nb) {
     d_Bt = dev_alloc<float>((size_t)nba * Wa * T, dev_bytes);
     if (tc_whiten && !tf32_data) d_Y_lo = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     if (tc_project && !tf32_data) d_Bpc_lo = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
+    if (tc_project) d_split = dev_alloc<float>((size_t)kSplitK * std::min(nba, kSplitBatches) * Wa * T, dev_bytes);
     sc.cfmax = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
     sc.at_t = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
     sc.at_amp = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
@@ -668,7 +676,10 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
     }
     ++nl;
     mark();
-    if (tc_project)
+    if (tc_project && nb <= kSplitBatches) {
+        LSS_CUDA(launch_umma_gemm_splitk(um_project, d_Bt, nb * Wn, T, T, d_split, kSplitK, d_gemm_err, st));
+        ++nl;   // and the slice sum
+    } else if (tc_project)
         LSS_CUDA(launch_umma_gemm(um_project, d_Bt, nb * Wn, T, T, d_gemm_err, st));
     else
         launch_sgemm_nt(d_Bpc, (int64_t)K * C, (int64_t)Wn * K * C, d_Wall3, (int64_t)K * C, d_Bt, T, (int64_t)Wn * T, Wn,
