@@ -269,6 +269,23 @@ def spike_agreement(ref, got, tol=1):
     return matched / len(ref), amp_ok / max(1, matched)
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The largest of every rank's x: a replicated job takes its slowest replica's time (all
+    ranks of the process group call this; with world 1 it is x)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, seconds: float, world: int) -> float:
+    """Units of every replica over the job's (slowest replica's) time."""
+    return world * units_per_rank / seconds
+
+
 def run_gpu(a):
     import torch
     rank = int(os.environ.get("RANK", "0"))
@@ -332,12 +349,9 @@ def run_gpu(a):
     ms = e0.elapsed_time(e1)
     spikes_seen[0] = drain(s)
     torch.cuda.synchronize(dev)
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, f"cuda:{dev}")
     units = a.steps * G * NT * C
-    value = world * units / (ms / 1e3)
+    value = whole_job_rate(units, ms / 1e3, world)
     t_all, n_all = s.stage_times()
     stage = {k: t_all[k] - t_base[k] for k in t_all}
     n_timed = n_all - n_base
@@ -464,11 +478,8 @@ def run_gpu(a):
         t_poll += time.perf_counter() - tb
     n_sp += drain(s2)
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * units / e2e_s, "unit": UNIT,
+    e2e_s = max_over_ranks(e2e_s, world, f"cuda:{dev}")
+    e2e = {"value": whole_job_rate(units, e2e_s, world), "unit": UNIT,
            "h2d_bytes_per_step": chunk * C * 2, "d2h_bytes_per_step": int(n_sp / a.steps * SPIKE_REC_BYTES),
            "path": "lss_push_batch + lss_poll from pinned host int16 rows, one group in flight",
            "host_ms_per_step": {"push": 1e3 * t_push / a.steps, "poll": 1e3 * t_poll / a.steps}}
