@@ -24,6 +24,11 @@ channels, 64-1000 templates, 750-3000-sample batches) paced at 30 kHz with +/-20
 (per-batch push-to-spikes latency p50/p99), the same streams unpaced (aggregate ch*samples/s),
 and eight 384-channel / 500-template streams unpaced (aggregate, as a multiple of real time).
 
+``--path proposal`` trains the learned proposal gate on the device (labels from the plain matcher on
+the first ``--prop-train-windows`` windows of the recording), then reports, on held-out seeds of
+the same units at 5-40 Hz, the fraction of the plain matcher's spikes the gated sorter keeps, the
+fraction of (neighbourhood, window) cells it leaves open, and device throughput gated and plain.
+
 ``--path tc`` measures the reference's other sorter, threshold crossing, instead: 384 channels of
 raw int16 at 30 kHz, one step = one push of ``--tc-rows`` rows (20 s, 461 MB, larger than L2)
 tested against 3 x the per-channel median; same JSON keys, roofline of the count kernel (2 bytes
@@ -68,8 +73,11 @@ def args_():
     ap.add_argument("--no-tier", action="store_true", help="skip the chosen-tier measurement")
     ap.add_argument("--tier-path", type=int, default=3,
                     help="gemm_path of the chosen tier reported beside FP32: 3 BF16 splits, 2 TF32 activations")
-    ap.add_argument("--path", default="sort", choices=["sort", "tc"],
-                    help="sort = template matching (default); tc = threshold crossing")
+    ap.add_argument("--path", default="sort", choices=["sort", "tc", "proposal"],
+                    help="sort = template matching (default); tc = threshold crossing; proposal = the learned "
+                         "proposal gate (train, then recall / cells closed / throughput against the plain matcher)")
+    ap.add_argument("--prop-train-windows", type=int, default=256, help="batch windows the gate trains on")
+    ap.add_argument("--prop-steps", type=int, default=400, help="Adam steps of 64 examples")
     ap.add_argument("--tc-rows", type=int, default=600_000, help="rows per threshold-crossing push")
     ap.add_argument("--serving", action="store_true", help="several concurrent probe streams")
     ap.add_argument("--serving-seconds", type=float, default=8.0, help="signal per stream")
@@ -763,10 +771,112 @@ def run_serving(a):
     return 0
 
 
+def run_proposal(a):
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    from livespikesorter_gb300 import proposal, sorter, synth
+    t_start = time.perf_counter()
+    cfg = synth.config_stream(seconds=a.seconds, seed=1)
+    oss_dir, data, rec = synth.cached_dataset(cfg)
+    C, nt = cfg.n_chan, cfg.nt
+    W = NT + 2 * nt
+    oss_Wall3 = np.load(Path(oss_dir) / "Wall3.npy")
+    starts = proposal.neighbourhoods(C)
+    owner = proposal.template_owner(oss_Wall3)
+    nw = min(a.prop_train_windows, (data.shape[0] - 2 * nt) // NT)
+    G = a.group
+    with sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G) as s:
+        wins = proposal.batch_windows(data, 0, nw, NT, nt)
+        labels, _ = proposal.plain_labels(s, wins, owner, len(starts))
+        z = proposal.whitened(s, wins)
+    with proposal.ProposalTrainer(W, nt, max_examples=64, seed=0) as tr:
+        tr.step(z, proposal.all_pairs(1, starts)[:64], labels[0].reshape(-1, labels.shape[-1])[:64])  # warm-up
+        tr.params = proposal.init_params(0)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        losses = proposal.train(tr, z, labels, starts, steps=a.prop_steps, batch=64, seed=0)
+        train_s = time.perf_counter() - t0
+        zw = proposal.window_logits(tr, z, starts)
+        params = tr.params
+    del z
+    thr = proposal.choose_threshold(zw, labels, 1, 0.995)
+    step_flop = 3 * 2 * 64 * W * 7 * sum(o * i for o, i in proposal.SHAPES)   # forward + two backward passes
+    held = {}
+    rate_gated = rate_plain = None
+    for rate, seed in ((5.0, 301), (10.0, 302), (20.0, 303), (40.0, 304)):
+        r = synth.rerecord(rec, seed, rate_hz=rate, n_samples=G * NT + 2 * nt)
+        hw = proposal.batch_windows(r.data, 0, G, NT, nt)
+        with sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
+                                 profile=1) as s:
+            plain = np.concatenate(s.sort_windows(hw))
+            s.set_proposal(params, logit_threshold=thr, dilate=1)
+            gated = np.concatenate(s.sort_windows(hw))
+            cells, opened = s.proposal_stats()
+            if rate == 10.0:
+                d_rows = torch.from_numpy(r.data).to(f"cuda:{dev}")
+                ext = torch.cuda.ExternalStream(s.cuda_stream(), device=f"cuda:{dev}")
+
+                ctr = [0]
+
+                def push():
+                    # the same G windows again, as a continuing stream
+                    s.push_device_span(d_rows.data_ptr(), G, ctr[0] * G * NT)
+                    ctr[0] += 1
+
+                def dev_ms(reps=5):
+                    for _ in range(2):
+                        push()
+                    s.poll_all()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    with torch.cuda.stream(ext):
+                        e0.record(ext)
+                    for i in range(reps):
+                        push()
+                    with torch.cuda.stream(ext):
+                        e1.record(ext)
+                    e1.synchronize()
+                    s.poll_all()
+                    return e0.elapsed_time(e1) / reps
+
+                ms_g = dev_ms()
+                s.set_proposal(None)
+                ms_p = dev_ms()
+                rate_gated = G * NT * C / (ms_g / 1e3)
+                rate_plain = G * NT * C / (ms_p / 1e3)
+                del d_rows
+        recall, amp_ok = spike_agreement(plain, gated)
+        held[f"{rate:g}Hz"] = {"spikes_plain": int(len(plain)), "spikes_gated": int(len(gated)),
+                               "recall": recall, "amp_within_1e-3": amp_ok, "cells_open_frac": opened / max(1, cells)}
+    line = {"metric": "proposal gate: recall of the plain matcher's spikes and cells closed, 384 ch / 500 templates",
+            "value": min(h["recall"] for h in held.values()), "unit": "recall (min over firing rates)",
+            "n_gpus": 1, "steps": a.prop_steps, "warmup": 1, "ms_per_step": 1e3 * train_s / a.prop_steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 train, bf16 weights gate",
+            "data": "synthetic (seeded generator; held-out seeds of the same units)",
+            "config": {"workload": "4-layer channel-local conv net (16 ch neighbourhoods, 64 hidden, 7 taps), "
+                                   "32-sample windows, dilation 1, threshold for 0.995 cell recall on the training "
+                                   "windows", "train_windows": nw, "batch_examples": 64, "adam_lr": 1e-3,
+                       "neighbourhoods": int(len(starts)), "logit_threshold": thr},
+            "training": {"steps": a.prop_steps, "s": train_s, "loss_first20": float(losses[:20].mean()),
+                         "loss_last20": float(losses[-20:].mean()),
+                         "tflops": step_flop * a.prop_steps / train_s / 1e12,
+                         "label_positive_frac": float(labels.mean())},
+            "held_out": held,
+            "throughput_10Hz": {"gated": rate_gated, "plain": rate_plain, "unit": UNIT,
+                                "group_batches": G},
+            "wall_s": time.perf_counter() - t_start}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     a = args_()
     if a.serving:
         return run_serving(a)
+    if a.path == "proposal":
+        return run_proposal(a)
     if a.path == "tc":
         return run_tc_reference(a) if a.impl == "reference" else run_tc_gpu(a)
     if a.impl == "reference":

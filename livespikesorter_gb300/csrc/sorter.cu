@@ -11,8 +11,10 @@
 // start + s - M/2 - M + nt0min - lookback (OnlineSpikesV2.cu:1186-1187) for its framing; here the
 // time is window_start + s - nt//2 + nt0min, Kilosort's formula.
 #include "../../include/lss_gb300.h"
+#include "../../include/lss_proposal.h"
 #include "lss_kernels.cuh"
 #include "oss_input.hpp"
+#include "proposal.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -209,6 +211,7 @@ struct Handle {
     cudaEvent_t ev_push = nullptr;   // a caller's page-locked rows have reached the device
     std::vector<int64_t> last_kept;     // per final cluster: last kept spike time (duplicate removal)
     std::vector<char> has_kept;
+    PropGate* gate = nullptr;           // learned proposal gate (lss_set_proposal), off when null
 
     ~Handle();
     void init(const char* dir, const lss_params* prm);
@@ -237,6 +240,7 @@ Handle::~Handle() {
     if (st_copy) cudaStreamSynchronize(st_copy);
     if (st) cudaStreamSynchronize(st);
     free_work();
+    if (gate) prop_gate_destroy(gate);
     for (auto& kv : taps) {
         cudaFree(kv.second.d);
         for (int v = 0; v < 2; ++v) {
@@ -718,6 +722,7 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     mark();
     int64_t nl = 0;
     run_stages_to_scores(raw, nb, Wn, NTs, ts, nl, mark);
+    if (gate) nl += prop_gate_run(gate, d_Z, d_Bt, nb, Wn, nt, st);
     LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
     LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st,
                           p.match_variant));
@@ -1269,6 +1274,30 @@ int lss_stage_times(lss_handle* hp, double* ms, int32_t n, int64_t* n_groups) {
     for (int i = 0; i < n && i < LSS_N_STAGES; ++i) ms[i] = hp->h.stage_ms[i];
     if (n_groups) *n_groups = hp->h.groups_timed;
     return LSS_OK;
+}
+
+int lss_set_proposal(lss_handle* hp, const float* params, float logit_threshold, int32_t dilate) {
+    if (!hp) return LSS_ERR_ARG;
+    Handle& h = hp->h;
+    LSS_TRY(hp, {
+        cudaSetDevice(h.dev);
+        h.drain_all();   // groups in flight finish with the gate they were launched with
+        LSS_CUDA(cudaStreamSynchronize(h.st));
+        if (h.gate) lss::prop_gate_destroy(h.gate);
+        h.gate = nullptr;
+        if (params)
+            h.gate = lss::prop_gate_create(h.dev, params, logit_threshold, dilate, h.m.Wall3.data(), h.T, h.K, h.C);
+    })
+}
+
+int lss_proposal_stats(lss_handle* hp, int64_t* cells, int64_t* open) {
+    if (!hp || !cells || !open) return LSS_ERR_ARG;
+    Handle& h = hp->h;
+    LSS_TRY(hp, {
+        cudaSetDevice(h.dev);
+        *cells = *open = 0;
+        if (h.gate) lss::prop_gate_stats(h.gate, h.st, cells, open);
+    })
 }
 
 int lss_kernel_launches(const lss_handle* hp, int64_t* n) {

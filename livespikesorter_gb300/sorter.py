@@ -92,6 +92,24 @@ _SIGS.update({
     "lss_tc_close": (ct.c_int, [ct.c_void_p]),
     "lss_tc_last_error": (ct.c_char_p, [ct.c_void_p]),
 })
+# include/lss_proposal.h (learned proposal gate; Python side in proposal.py)
+_SIGS.update({
+    "lss_prop_neighbourhoods": (ct.c_int, [ct.c_int32, _P(ct.c_int32), ct.c_void_p, ct.c_int32]),
+    "lss_prop_template_owner": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p]),
+    "lss_prop_trainer_open": (ct.c_int, [ct.c_void_p, ct.c_void_p, _P(ct.c_void_p)]),
+    "lss_prop_trainer_close": (ct.c_int, [ct.c_void_p]),
+    "lss_prop_trainer_last_error": (ct.c_char_p, [ct.c_void_p]),
+    "lss_prop_train_step": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_int32, ct.c_void_p, ct.c_void_p,
+                                       ct.c_int32, _P(ct.c_float)]),
+    "lss_prop_loss_grad": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_int32, ct.c_void_p, ct.c_void_p,
+                                      ct.c_int32, _P(ct.c_float), ct.c_void_p]),
+    "lss_prop_forward": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_int32, ct.c_void_p, ct.c_int32,
+                                    ct.c_void_p, ct.c_void_p]),
+    "lss_prop_get_params": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "lss_prop_set_params": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "lss_set_proposal": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_float, ct.c_int32]),
+    "lss_proposal_stats": (ct.c_int, [ct.c_void_p, _P(ct.c_int64), _P(ct.c_int64)]),
+})
 STAGES = ("h2d", "colsum", "car", "highpass", "whiten", "basis_conv", "project", "match", "features", "d2h")
 
 _lib = None
@@ -191,6 +209,23 @@ class OnlineSorter:
         n = ct.c_int64()
         self._check(self.lib.lss_kernel_launches(self.h, ct.byref(n)))
         return n.value
+
+    # -- learned proposal gate (include/lss_proposal.h) ----------------------------------
+    def set_proposal(self, params, logit_threshold: float = 0.0, dilate: int = 1):
+        """Gate the matching loop with a trained proposal network (None removes the gate)."""
+        if params is None:
+            self._check(self.lib.lss_set_proposal(self.h, None, ct.c_float(0.0), 0))
+            return
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != 65153:
+            raise ValueError("expected 65153 parameters")
+        self._check(self.lib.lss_set_proposal(self.h, p.ctypes.data, ct.c_float(logit_threshold), dilate))
+
+    def proposal_stats(self):
+        """(cells evaluated, cells left open) since the gate was set."""
+        c, o = ct.c_int64(), ct.c_int64()
+        self._check(self.lib.lss_proposal_stats(self.h, ct.byref(c), ct.byref(o)))
+        return c.value, o.value
 
     # -- streaming -----------------------------------------------------------------------
     def push(self, samples: np.ndarray, stream_sample_ct: int = -1):

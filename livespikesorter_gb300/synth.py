@@ -294,6 +294,17 @@ def make_recording(cfg: SynthConfig) -> Recording:
     return Recording(cfg=cfg, data=data, xc=xc, yc=yc, wPCA=wPCA, units=units, train=train)
 
 
+def rerecord(rec: Recording, seed: int, rate_hz: float = None, n_samples: int = None) -> Recording:
+    """A new recording of the same units and probe (so the same oss_input/ applies): fresh spike
+    times, amplitudes and noise from ``seed``, optionally another firing rate and length."""
+    cfg = dataclasses.replace(rec.cfg, seed=seed, rate_hz=rate_hz if rate_hz is not None else rec.cfg.rate_hz,
+                              n_samples=n_samples if n_samples is not None else rec.cfg.n_samples)
+    rng = np.random.default_rng(seed)
+    train = make_spike_train(cfg, rng)
+    data = render(cfg, rec.units, train, rec.xc, rec.yc, rng)
+    return Recording(cfg=cfg, data=data, xc=rec.xc, yc=rec.yc, wPCA=rec.wPCA, units=rec.units, train=train)
+
+
 # ----------------------------------------------------------------------------------------
 # export: the oss_input/ directory
 # ----------------------------------------------------------------------------------------
