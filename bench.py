@@ -679,11 +679,15 @@ def _serving_data(streams, seconds, seed0):
     return out
 
 
-def _run_streams(sets, paced: bool, jitter: float = 0.2, seed: int = 0):
+def _run_streams(sets, paced: bool, jitter: float = 0.2, seed: int = 0, gate=None):
     """One thread per stream: push each batch (paced at 30 kHz with +/-jitter, or back to back),
-    then poll its spikes; returns per-batch latencies (ms), wall seconds and new samples x channels."""
+    then poll its spikes; returns per-batch latencies (ms), wall seconds and new samples x channels.
+    gate = (params, logit threshold, dilation) sets the learned proposal gate on every handle."""
     from livespikesorter_gb300 import sorter
     handles = [sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=1) for d, _, NT in sets]
+    if gate is not None:
+        for h in handles:
+            h.set_proposal(*gate)
     for (d, data, NT), h in zip(sets, handles):   # warm-up: one window each
         h.push(data[:NT + 2 * 61], 0)
         h.poll_all()
@@ -850,6 +854,19 @@ def run_proposal(a):
         recall, amp_ok = spike_agreement(plain, gated)
         held[f"{rate:g}Hz"] = {"spikes_plain": int(len(plain)), "spikes_gated": int(len(gated)),
                                "recall": recall, "amp_within_1e-3": amp_ok, "cells_open_frac": opened / max(1, cells)}
+    # eight 384-channel streams at once, every handle gated (held-out seeds, 10 Hz)
+    secs = min(a.serving_seconds, 4.0)
+    sets = [(oss_dir, synth.rerecord(rec, 500 + i, rate_hz=10.0, n_samples=int(secs * 30000)).data, NT)
+            for i in range(8)]
+    gate = (params, thr, 1)
+    lat_p, wall_p, work_p = _run_streams(sets, paced=True, gate=gate)
+    lat_u, wall_u, work_u = _run_streams(sets, paced=False, gate=gate)
+    lp, lu = np.concatenate([np.asarray(x) for x in lat_p]), np.concatenate([np.asarray(x) for x in lat_u])
+    eight = {"paced_p50_ms": float(np.percentile(lp, 50)), "paced_p99_ms": float(np.percentile(lp, 99)),
+             "paced_batches": int(lp.size), "unpaced_ch_samples_per_s": sum(work_u) / wall_u,
+             "unpaced_realtime_factor": (sum(work_u) / wall_u) / (8 * C * 30000.0),
+             "unpaced_p99_ms": float(np.percentile(lu, 99)), "seconds_per_stream": secs,
+             "batch_ms_of_signal": 1e3 * NT / 30000.0}
     line = {"metric": "proposal gate: recall of the plain matcher's spikes and cells closed, 384 ch / 500 templates",
             "value": min(h["recall"] for h in held.values()), "unit": "recall (min over firing rates)",
             "n_gpus": 1, "steps": a.prop_steps, "warmup": 1, "ms_per_step": 1e3 * train_s / a.prop_steps,
@@ -866,6 +883,7 @@ def run_proposal(a):
             "held_out": held,
             "throughput_10Hz": {"gated": rate_gated, "plain": rate_plain, "unit": UNIT,
                                 "group_batches": G},
+            "eight_384ch_streams_gated": eight,
             "wall_s": time.perf_counter() - t_start}
     print(json.dumps(line))
     return 0

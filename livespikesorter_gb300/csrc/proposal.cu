@@ -183,8 +183,9 @@ __global__ void window_loss_kernel(const float* __restrict__ logit, int E, int L
     }
 }
 
-// out[0] = sum of v[0..n) in a fixed order (one block).
-__global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ v, int n, float* __restrict__ out) {
+// out[0] = scale * (sum of v[0..n) in a fixed order) (one block).
+__global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ v, int n, float scale,
+                                                  float* __restrict__ out) {
     __shared__ float red[256];
     float s = 0.f;
     for (int i = threadIdx.x; i < n; i += 256) s += v[i];
@@ -194,7 +195,7 @@ __global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ v, i
         if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[0] = red[0];
+    if (threadIdx.x == 0) out[0] = red[0] * scale;
 }
 
 // wt[i][o][k] = w[o][i][6 - k]: the data gradient of a layer as a forward convolution,
@@ -594,7 +595,7 @@ void loss_and_backward(lss_prop_trainer* tr, int E) {
     PROP_CUDA(cudaMemsetAsync(tr->dlogit, 0, (size_t)E * L * sizeof(float), st));
     window_loss_kernel<<<cdiv(n, 256), 256, 0, st>>>(tr->logit, E, L, tr->nt, tr->nwin, tr->labels, 1.f / n, tr->z,
                                                      tr->term, tr->dlogit);
-    sum_kernel<<<1, 256, 0, st>>>(tr->term, n, tr->loss);
+    sum_kernel<<<1, 256, 0, st>>>(tr->term, n, 1.f / n, tr->loss);   // the mean
     // flipped weights of layers 2..4 at wt + {0, 28672, 57344}
     float* wt2 = tr->wt;
     float* wt3 = tr->wt + kHid * kHid * kTaps;

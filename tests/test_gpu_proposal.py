@@ -207,7 +207,8 @@ def test_learned_gate_keeps_the_plain_matchers_spikes(dense_probe):
             s.set_proposal(params, logit_threshold=thr, dilate=1)
             ri, _ = match_spikes(plain["time"], plain["tmpl"], gated["time"], gated["tmpl"])
             results[rate] = (len(ri) / max(1, len(plain)), (o1 - o0) / (c1 - c0), len(plain), len(gated))
+    # the gain: most cells closed at 5 Hz; at 40 Hz most cells hold a spike and stay open
     for rate, (recall, open_frac, n_plain, n_gated) in results.items():
         assert n_plain > 200, results
         assert recall >= 0.97, results
-        assert open_frac <= 0.75, results
+        assert open_frac <= (0.4 if rate == 5.0 else 0.95), results
