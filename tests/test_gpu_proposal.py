@@ -64,6 +64,39 @@ def test_forward_matches_oracle(small):
     assert np.abs(zw - zr).max() <= 1e-4 * scale
 
 
+@pytest.mark.parametrize("C,W,nt", [(8, 97, 10), (16, 300, 61), (23, 1622, 61)])
+def test_forward_ragged_shapes(C, W, nt):
+    """Probes narrower than a neighbourhood (zero-padded channels), a last window shorter than 32
+    samples, a neighbourhood start that is not a multiple of 8."""
+    rng = np.random.default_rng(C)
+    Z = rng.normal(0.0, 1.0, (2, W, C)).astype(np.float32)
+    pairs = proposal.all_pairs(2, proposal.neighbourhoods(C))
+    p = _test_params(9)
+    with proposal.ProposalTrainer(W, nt, max_examples=len(pairs), params=p) as tr:
+        lg, zw = tr.forward(torch.from_numpy(Z).cuda(), pairs)
+    _, ref = po.forward(p, po.gather_examples(Z, pairs))
+    assert np.abs(lg - ref).max() <= 1e-4 * np.abs(ref).max()
+    zr, _ = po.window_max(ref, W, nt)
+    assert zw.shape == zr.shape and np.abs(zw - zr).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_trainer_rejects_bad_examples(small):
+    _, z, pairs, lab = small
+    with proposal.ProposalTrainer(W_S, NT_S, max_examples=4, params=_test_params(2)) as tr:
+        with pytest.raises(sorter.SorterError):
+            tr.forward(z, pairs[:5])                      # more than max_examples
+        bad = pairs[:2].copy()
+        bad[0, 0] = 3                                     # window past the 3 given
+        with pytest.raises(sorter.SorterError):
+            tr.forward(z, bad)
+        bad = pairs[:2].copy()
+        bad[1, 1] = C_S - 8                               # neighbourhood past the last channel
+        with pytest.raises(sorter.SorterError):
+            tr.step(z, bad, lab[:2])
+        lg, _ = tr.forward(z, pairs[:4])                  # the handle still works
+        assert np.isfinite(lg).all()
+
+
 def test_gradient_matches_oracle(small):
     Z, z, pairs, lab = small
     p = _test_params(3)
