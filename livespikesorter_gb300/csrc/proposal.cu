@@ -8,7 +8,6 @@
 // Reductions over examples are written as per-example partials and summed in example order, so a
 // training step is deterministic.
 #include "../../include/lss_proposal.h"
-#include "lss_kernels.cuh"
 #include "oss_input.hpp"
 #include "proposal.hpp"
 
@@ -73,78 +72,48 @@ __global__ void __launch_bounds__(256) gather_kernel(const float* __restrict__ Z
     }
 }
 
-// two fp32 fused multiply-adds per instruction: d.{x,y} = a.{x,y} * b.{x,y} + d.{x,y}, each
-// rounded like fmaf
-__device__ __forceinline__ void fma2(unsigned long long& d, unsigned long long a, unsigned long long b) {
-    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(d) : "l"(a), "l"(b));
-}
-__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ float2 unpack2(unsigned long long v) {
-    float2 r;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-    return r;
-}
-
-constexpr int kConvPitch = kTile + 8;   // 136: rows of staged input, 16-byte aligned
-constexpr size_t kConvSmem = sizeof(float2) * kCi * kTaps * kHid + sizeof(float) * kCi * kConvPitch;
-
 // out[e][o][l] = act(bias[o] + sum_i sum_k w[o][i][k] in[e][i][l + k - 3]) for 64 outputs, zeroed
 // where mask[e][o][l] <= 0 (the ReLU of the layer below, in the data gradient).  Block: 128
-// samples of one example; warp w owns outputs 8w..8w+7, lane j the samples 4j..4j+3.  Per pass of
-// 16 input channels the weights sit in shared memory as duplicated pairs [i][k][o] (one 16-byte
-// load gives two outputs' weights) and each thread keeps its 10 input samples of a channel in
-// registers; the products go two at a time (fma.rn.f32x2) into 8 x 2 packed accumulators.
+// samples of one example; warp w owns outputs 8w..8w+7, lane j the samples j, j+32, j+64, j+96.
 template <typename WT>
 __global__ void __launch_bounds__(256) conv64_kernel(const float* __restrict__ in, int cin, int L,
                                                      const WT* __restrict__ w, const float* __restrict__ bias,
                                                      const float* __restrict__ mask, int relu,
                                                      float* __restrict__ out) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* ws = reinterpret_cast<float2*>(smem_raw);                                   // [i][k][o]
-    float* xs = reinterpret_cast<float*>(smem_raw + sizeof(float2) * kCi * kTaps * kHid);   // [i][kConvPitch]
+    __shared__ float ws[kHid * kCi * kTaps];
+    __shared__ float xs[kCi * kXPitch];
     const int e = blockIdx.y, l0 = blockIdx.x * kTile;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, o0 = warp * 8;
-    unsigned long long acc[8][2];
+    float acc[8][4];
 #pragma unroll
-    for (int o = 0; o < 8; ++o) acc[o][0] = acc[o][1] = 0ull;
+    for (int o = 0; o < 8; ++o)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[o][j] = 0.f;
     const float* inb = in + (size_t)e * cin * L;
     for (int c0 = 0; c0 < cin; c0 += kCi) {
         const int nci = min(kCi, cin - c0);
         __syncthreads();
-        // global order (o, i, k): each output's 16 x 7 weights of this pass are contiguous
         for (int q = threadIdx.x; q < kHid * kCi * kTaps; q += blockDim.x) {
             const int o = q / (kCi * kTaps), r = q - o * (kCi * kTaps), i = r / kTaps, k = r - i * kTaps;
-            const float v = i < nci ? ld_w(w + ((size_t)o * cin + c0 + i) * kTaps + k) : 0.f;
-            ws[(i * kTaps + k) * kHid + o] = make_float2(v, v);
+            ws[q] = i < nci ? ld_w(w + ((size_t)o * cin + c0 + i) * kTaps + k) : 0.f;
         }
         for (int q = threadIdx.x; q < kCi * (kTile + 2 * kPad); q += blockDim.x) {
             const int i = q / (kTile + 2 * kPad), ll = q - i * (kTile + 2 * kPad), l = l0 - kPad + ll;
-            xs[i * kConvPitch + ll] = (i < nci && l >= 0 && l < L) ? inb[(size_t)(c0 + i) * L + l] : 0.f;
+            xs[i * kXPitch + ll] = (i < nci && l >= 0 && l < L) ? inb[(size_t)(c0 + i) * L + l] : 0.f;
         }
         __syncthreads();
-#pragma unroll 1
+#pragma unroll 2
         for (int i = 0; i < kCi; ++i) {
-            const float* xr = xs + i * kConvPitch + 4 * lane;
-            const float4 x0 = *reinterpret_cast<const float4*>(xr);
-            const float4 x1 = *reinterpret_cast<const float4*>(xr + 4);
-            const float2 x2 = *reinterpret_cast<const float2*>(xr + 8);
-            const float x[10] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x, x2.y};
-            const float2* wr = ws + i * kTaps * kHid + o0;
 #pragma unroll
             for (int k = 0; k < kTaps; ++k) {
-                const unsigned long long xa = pack2(x[k], x[k + 1]), xb = pack2(x[k + 2], x[k + 3]);
-                const ulonglong2* wk = reinterpret_cast<const ulonglong2*>(wr + k * kHid);
+                float xv[4];
 #pragma unroll
-                for (int o2 = 0; o2 < 4; ++o2) {
-                    const ulonglong2 wp = wk[o2];   // outputs o0 + 2*o2, o0 + 2*o2 + 1
-                    fma2(acc[2 * o2][0], xa, wp.x);
-                    fma2(acc[2 * o2][1], xb, wp.x);
-                    fma2(acc[2 * o2 + 1][0], xa, wp.y);
-                    fma2(acc[2 * o2 + 1][1], xb, wp.y);
+                for (int j = 0; j < 4; ++j) xv[j] = xs[i * kXPitch + lane + 32 * j + k];
+#pragma unroll
+                for (int o = 0; o < 8; ++o) {
+                    const float wv = ws[((o0 + o) * kCi + i) * kTaps + k];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[o][j] = fmaf(wv, xv[j], acc[o][j]);
                 }
             }
         }
@@ -153,14 +122,12 @@ __global__ void __launch_bounds__(256) conv64_kernel(const float* __restrict__ i
     for (int o = 0; o < 8; ++o) {
         const int oc = o0 + o;
         const float bv = bias ? bias[oc] : 0.f;
-        const float2 p0 = unpack2(acc[o][0]), p1 = unpack2(acc[o][1]);
-        const float v4[4] = {p0.x, p0.y, p1.x, p1.y};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int l = l0 + 4 * lane + j;
+            const int l = l0 + lane + 32 * j;
             if (l >= L) continue;
             const size_t idx = ((size_t)e * kHid + oc) * L + l;
-            float v = v4[j] + bv;
+            float v = acc[o][j] + bv;
             if (relu) v = fmaxf(v, 0.f);
             if (mask && !(mask[idx] > 0.f)) v = 0.f;
             out[idx] = v;
@@ -373,20 +340,12 @@ __global__ void __launch_bounds__(256) gate_scores_kernel(float* __restrict__ Bt
 inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 template <typename WT>
-void launch_conv64(const float* in, int cin, int L, const WT* w, const float* bias, const float* mask, int relu,
-                   float* out, int E, cudaStream_t st) {
-    const cudaError_t e = raise_smem_limit((const void*)conv64_kernel<WT>, kConvSmem);
-    if (e != cudaSuccess) throw CudaFail{std::string("conv64_kernel shared memory: ") + cudaGetErrorString(e)};
-    conv64_kernel<WT><<<dim3(cdiv(L, kTile), E), 256, kConvSmem, st>>>(in, cin, L, w, bias, mask, relu, out);
-}
-
-template <typename WT>
 void launch_forward(const float* x, const WT* w, const float* bias, float* a, float* b, float* logit, int E, int L,
                     cudaStream_t st) {
-    const dim3 g1(cdiv(L, 256), E);
-    launch_conv64<WT>(x, kNbc, L, w + kLayers[0].w, bias + kLayers[0].b, nullptr, 1, a, E, st);
-    launch_conv64<WT>(a, kHid, L, w + kLayers[1].w, bias + kLayers[1].b, nullptr, 1, b, E, st);
-    launch_conv64<WT>(b, kHid, L, w + kLayers[2].w, bias + kLayers[2].b, nullptr, 1, a, E, st);
+    const dim3 g64(cdiv(L, kTile), E), g1(cdiv(L, 256), E);
+    conv64_kernel<WT><<<g64, 256, 0, st>>>(x, kNbc, L, w + kLayers[0].w, bias + kLayers[0].b, nullptr, 1, a);
+    conv64_kernel<WT><<<g64, 256, 0, st>>>(a, kHid, L, w + kLayers[1].w, bias + kLayers[1].b, nullptr, 1, b);
+    conv64_kernel<WT><<<g64, 256, 0, st>>>(b, kHid, L, w + kLayers[2].w, bias + kLayers[2].b, nullptr, 1, a);
     conv1_kernel<WT><<<g1, 256, 0, st>>>(a, kHid, L, w + kLayers[3].w, bias + kLayers[3].b, logit);
 }
 
@@ -618,10 +577,13 @@ void forward(lss_prop_trainer* tr, int E) {
 void forward_keep(lss_prop_trainer* tr, int E) {
     using namespace lss;
     const int L = tr->W;
-    const dim3 g1(cdiv(L, 256), E);
-    launch_conv64<float>(tr->x, kNbc, L, tr->p + kLayers[0].w, tr->p + kLayers[0].b, nullptr, 1, tr->a1, E, tr->st);
-    launch_conv64<float>(tr->a1, kHid, L, tr->p + kLayers[1].w, tr->p + kLayers[1].b, nullptr, 1, tr->a2, E, tr->st);
-    launch_conv64<float>(tr->a2, kHid, L, tr->p + kLayers[2].w, tr->p + kLayers[2].b, nullptr, 1, tr->a3, E, tr->st);
+    const dim3 g64(cdiv(L, kTile), E), g1(cdiv(L, 256), E);
+    conv64_kernel<float><<<g64, 256, 0, tr->st>>>(tr->x, kNbc, L, tr->p + kLayers[0].w, tr->p + kLayers[0].b, nullptr,
+                                                  1, tr->a1);
+    conv64_kernel<float><<<g64, 256, 0, tr->st>>>(tr->a1, kHid, L, tr->p + kLayers[1].w, tr->p + kLayers[1].b,
+                                                  nullptr, 1, tr->a2);
+    conv64_kernel<float><<<g64, 256, 0, tr->st>>>(tr->a2, kHid, L, tr->p + kLayers[2].w, tr->p + kLayers[2].b,
+                                                  nullptr, 1, tr->a3);
     conv1_kernel<float><<<g1, 256, 0, tr->st>>>(tr->a3, kHid, L, tr->p + kLayers[3].w, tr->p + kLayers[3].b,
                                                 tr->logit);
 }
@@ -641,6 +603,7 @@ void loss_and_backward(lss_prop_trainer* tr, int E) {
     flip_kernel<<<cdiv(kHid * kHid * kTaps, 256), 256, 0, st>>>(tr->p + kLayers[1].w, kHid, kHid, wt2);
     flip_kernel<<<cdiv(kHid * kHid * kTaps, 256), 256, 0, st>>>(tr->p + kLayers[2].w, kHid, kHid, wt3);
     flip_kernel<<<cdiv(kHid * kTaps, 256), 256, 0, st>>>(tr->p + kLayers[3].w, 1, kHid, wt4);
+    const dim3 g64(cdiv(L, kTile), E);
     auto reduce = [&](int li, int cout, int cin) {
         const int nw = cout * cin * kTaps;
         sum_examples_kernel<<<cdiv(nw, 256), 256, 0, st>>>(tr->pw, E, nw, tr->g + kLayers[li].w);
@@ -649,15 +612,15 @@ void loss_and_backward(lss_prop_trainer* tr, int E) {
     // layer 4 (64 -> 1)
     wgrad_kernel<kHid><<<dim3(1, E), 256, 0, st>>>(tr->dlogit, 1, tr->a3, L, tr->pw, tr->pb);
     reduce(3, 1, kHid);
-    launch_conv64<float>(tr->dlogit, 1, L, wt4, nullptr, tr->a3, 0, tr->ga, E, st);
+    conv64_kernel<float><<<g64, 256, 0, st>>>(tr->dlogit, 1, L, wt4, nullptr, tr->a3, 0, tr->ga);
     // layer 3
     wgrad_kernel<kHid><<<dim3(kHid / 8, E), 256, 0, st>>>(tr->ga, kHid, tr->a2, L, tr->pw, tr->pb);
     reduce(2, kHid, kHid);
-    launch_conv64<float>(tr->ga, kHid, L, wt3, nullptr, tr->a2, 0, tr->gb, E, st);
+    conv64_kernel<float><<<g64, 256, 0, st>>>(tr->ga, kHid, L, wt3, nullptr, tr->a2, 0, tr->gb);
     // layer 2
     wgrad_kernel<kHid><<<dim3(kHid / 8, E), 256, 0, st>>>(tr->gb, kHid, tr->a1, L, tr->pw, tr->pb);
     reduce(1, kHid, kHid);
-    launch_conv64<float>(tr->gb, kHid, L, wt2, nullptr, tr->a1, 0, tr->ga, E, st);
+    conv64_kernel<float><<<g64, 256, 0, st>>>(tr->gb, kHid, L, wt2, nullptr, tr->a1, 0, tr->ga);
     // layer 1 (16 -> 64)
     wgrad_kernel<kNbc><<<dim3(kHid / 8, E), 256, 0, st>>>(tr->ga, kHid, tr->x, L, tr->pw, tr->pb);
     reduce(0, kHid, kNbc);
