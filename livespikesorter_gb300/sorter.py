@@ -1,6 +1,7 @@
 """Python mirror of the sorter's C ABI (``include/lss_gb300.h``) over ctypes.  The library's
-threshold-crossing functions (``include/lss_threshold.h``) are declared here too and wrapped in
-``threshold.py``.
+other functions are declared here too: threshold crossing (``include/lss_threshold.h``, wrapped
+in ``threshold.py``), the learned proposal gate (``include/lss_proposal.h``, ``proposal.py``) and
+the per-batch spike message (``include/lss_payload.h``, ``payload.py``).
 
 ``OnlineSorter`` follows the reference's sorter surface (src/SpikeSorter/OnlineSpikesV2.h:29-34):
 construct it on an ``oss_input/`` directory, push int16 samples, and poll the sorted spikes.
@@ -109,6 +110,15 @@ _SIGS.update({
     "lss_prop_set_params": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "lss_set_proposal": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_float, ct.c_int32]),
     "lss_proposal_stats": (ct.c_int, [ct.c_void_p, _P(ct.c_int64), _P(ct.c_int64)]),
+})
+# include/lss_payload.h (the per-batch spike message; Python side in payload.py)
+_SIGS.update({
+    "lss_payload_size": (ct.c_int, [ct.c_int64, ct.c_int32, _P(ct.c_int64)]),
+    "lss_payload_serialize": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int32, ct.c_void_p, ct.c_int64,
+                                         _P(ct.c_int64)]),
+    "lss_payload_parse": (ct.c_int, [ct.c_void_p, ct.c_int64, ct.c_int32, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                     ct.c_void_p, ct.c_int64, _P(ct.c_int64)]),
+    "lss_batch_p2p": (ct.c_int, [ct.c_void_p, ct.c_int64, ct.c_int32, _P(ct.c_float)]),
 })
 STAGES = ("h2d", "colsum", "car", "highpass", "whiten", "basis_conv", "project", "match", "features", "d2h")
 
