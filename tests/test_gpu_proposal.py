@@ -148,7 +148,7 @@ def gate_data(tmp_path_factory):
     oss = synth.build_oss_input(rec)
     d = synth.write_oss_input(oss, tmp_path_factory.mktemp("prop") / "oss_input")
     wins = proposal.batch_windows(rec.data, 0, 6, 1500, 61)
-    return d, wins, oss
+    return d, wins, oss, rec.data
 
 
 def _same_spikes(a, b):
@@ -158,7 +158,7 @@ def _same_spikes(a, b):
 
 
 def test_gate_with_every_cell_open_is_the_plain_sorter(gate_data):
-    d, wins, _ = gate_data
+    d, wins, _, _ = gate_data
     with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=4) as s:
         plain = s.sort_windows(wins)
         s.set_proposal(_test_params(1), logit_threshold=-np.inf, dilate=0)
@@ -173,8 +173,31 @@ def test_gate_with_every_cell_open_is_the_plain_sorter(gate_data):
     assert cells == opened == len(wins) * len(proposal.neighbourhoods(64)) * 47
 
 
+def test_gate_on_the_streaming_path(gate_data):
+    """The gate applies to pushed streams as well: all cells open gives the plain stream's spikes
+    bit for bit; a gate with cells closed changes them and counts every batch's cells."""
+    d, _, _, data = gate_data
+    with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=3) as s:
+        plain = s.sort_stream(data, chunk=2000)
+    with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=3) as s:
+        s.set_proposal(_test_params(1), logit_threshold=-np.inf, dilate=0)
+        gated = s.sort_stream(data, chunk=2000)
+        cells, opened = s.proposal_stats()
+    _same_spikes([plain], [gated])
+    n_full = len(data) // 1500 - 1                   # windows certainly launched at full length
+    assert cells == opened and cells % len(proposal.neighbourhoods(64)) == 0
+    assert cells >= n_full * len(proposal.neighbourhoods(64)) * 47
+    with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=3) as s:
+        s.set_proposal(_test_params(1), logit_threshold=1e30, dilate=0)   # every cell closed
+        none = s.sort_stream(data, chunk=2000)
+        cells, opened = s.proposal_stats()
+    assert opened == 0 and cells > 0
+    # the cells cover every window's interior, and the loop never accepts outside it
+    assert len(plain) > 50 and len(none) == 0
+
+
 def test_gated_spikes_lie_in_open_cells(gate_data):
-    d, wins, oss = gate_data
+    d, wins, oss, _ = gate_data
     p = _test_params(6)
     starts = proposal.neighbourhoods(64)
     owner = po.template_owner(oss.Wall3)
