@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(256) conv64_kernel(const float* __restrict__ i
         __syncthreads();
 #pragma unroll 2
         for (int i = 0; i < kCi; ++i) {
+            if (i >= nci) break;   // a pass with fewer channels (the output layer's data gradient has one)
 #pragma unroll
             for (int k = 0; k < kTaps; ++k) {
                 float xv[4];
@@ -207,16 +208,19 @@ __global__ void flip_kernel(const float* __restrict__ w, int O, int I, float* __
     wt[((size_t)i * O + o) * kTaps + (kTaps - 1 - k)] = w[q];
 }
 
-// Partial gradients of one example for 8 output channels:
-//   pw[e][o][i][k] = sum_l g[e][o][l] a[e][i][l + k - 3],   pb[e][o] = sum_l g[e][o][l].
+// Partial gradients of one slice of one example's samples for 8 output channels (slice z of
+// gridDim.z, samples [z * Ls, (z + 1) * Ls), written as partial p = e * gridDim.z + z):
+//   pw[p][o][i][k] = sum_l g[e][o][l] a[e][i][l + k - 3],   pb[p][o] = sum_l g[e][o][l].
 // Thread p owns the (o, i) pairs p, p + 256, ...; a register window slides along the samples.
 template <int CIN>
 __global__ void __launch_bounds__(256) wgrad_kernel(const float* __restrict__ g, int cout, const float* __restrict__ a,
-                                                    int L, float* __restrict__ pw, float* __restrict__ pb) {
+                                                    int L, int Ls, float* __restrict__ pw, float* __restrict__ pb) {
     constexpr int kPairs = 8 * CIN, R = (kPairs + 255) / 256;
     __shared__ float gs[8][kTile];
     __shared__ float as[CIN * kXPitch];
     const int e = blockIdx.y, og = blockIdx.x * 8, tid = threadIdx.x;
+    const int part = e * gridDim.z + blockIdx.z;
+    const int lbeg = blockIdx.z * Ls, lend = min(L, lbeg + Ls);
     float acc[R][kTaps];
 #pragma unroll
     for (int r = 0; r < R; ++r)
@@ -225,11 +229,11 @@ __global__ void __launch_bounds__(256) wgrad_kernel(const float* __restrict__ g,
     float bacc = 0.f;
     const float* gb = g + (size_t)e * cout * L;
     const float* ab = a + (size_t)e * CIN * L;
-    for (int l0 = 0; l0 < L; l0 += kTile) {
+    for (int l0 = lbeg; l0 < lend; l0 += kTile) {
         __syncthreads();
         for (int q = tid; q < 8 * kTile; q += 256) {
             const int o = q / kTile, ll = q - o * kTile, l = l0 + ll;
-            gs[o][ll] = (og + o < cout && l < L) ? gb[(size_t)(og + o) * L + l] : 0.f;
+            gs[o][ll] = (og + o < cout && l < lend) ? gb[(size_t)(og + o) * L + l] : 0.f;
         }
         for (int q = tid; q < CIN * (kTile + 2 * kPad); q += 256) {
             const int i = q / (kTile + 2 * kPad), ll = q - i * (kTile + 2 * kPad), l = l0 - kPad + ll;
@@ -267,10 +271,10 @@ __global__ void __launch_bounds__(256) wgrad_kernel(const float* __restrict__ g,
             const int o = p / CIN, i = p - o * CIN;
             if (og + o < cout)
 #pragma unroll
-                for (int k = 0; k < kTaps; ++k) pw[(((size_t)e * cout + og + o) * CIN + i) * kTaps + k] = acc[r][k];
+                for (int k = 0; k < kTaps; ++k) pw[(((size_t)part * cout + og + o) * CIN + i) * kTaps + k] = acc[r][k];
         }
     }
-    if (tid < 8 && og + tid < cout) pb[(size_t)e * cout + og + tid] = bacc;
+    if (tid < 8 && og + tid < cout) pb[(size_t)part * cout + og + tid] = bacc;
 }
 
 // out[j] = sum_e part[e][j], examples in order.
@@ -604,26 +608,29 @@ void loss_and_backward(lss_prop_trainer* tr, int E) {
     flip_kernel<<<cdiv(kHid * kHid * kTaps, 256), 256, 0, st>>>(tr->p + kLayers[2].w, kHid, kHid, wt3);
     flip_kernel<<<cdiv(kHid * kTaps, 256), 256, 0, st>>>(tr->p + kLayers[3].w, 1, kHid, wt4);
     const dim3 g64(cdiv(L, kTile), E);
-    auto reduce = [&](int li, int cout, int cin) {
+    auto reduce = [&](int li, int cout, int cin, int parts) {
         const int nw = cout * cin * kTaps;
-        sum_examples_kernel<<<cdiv(nw, 256), 256, 0, st>>>(tr->pw, E, nw, tr->g + kLayers[li].w);
-        sum_examples_kernel<<<cdiv(cout, 256), 256, 0, st>>>(tr->pb, E, cout, tr->g + kLayers[li].b);
+        sum_examples_kernel<<<cdiv(nw, 256), 256, 0, st>>>(tr->pw, parts, nw, tr->g + kLayers[li].w);
+        sum_examples_kernel<<<cdiv(cout, 256), 256, 0, st>>>(tr->pb, parts, cout, tr->g + kLayers[li].b);
     };
-    // layer 4 (64 -> 1)
-    wgrad_kernel<kHid><<<dim3(1, E), 256, 0, st>>>(tr->dlogit, 1, tr->a3, L, tr->pw, tr->pb);
-    reduce(3, 1, kHid);
+    // layer 4 (64 -> 1): one output channel, so the samples are split into slices of 256 (at most
+    // 64 per example, within the partial buffers' E * 64 rows) to fill the GPU
+    const int zs = std::min(64, cdiv(L, 2 * kTile));
+    const int ls = cdiv(cdiv(L, zs), kTile) * kTile;
+    wgrad_kernel<kHid><<<dim3(1, E, zs), 256, 0, st>>>(tr->dlogit, 1, tr->a3, L, ls, tr->pw, tr->pb);
+    reduce(3, 1, kHid, E * zs);
     conv64_kernel<float><<<g64, 256, 0, st>>>(tr->dlogit, 1, L, wt4, nullptr, tr->a3, 0, tr->ga);
     // layer 3
-    wgrad_kernel<kHid><<<dim3(kHid / 8, E), 256, 0, st>>>(tr->ga, kHid, tr->a2, L, tr->pw, tr->pb);
-    reduce(2, kHid, kHid);
+    wgrad_kernel<kHid><<<dim3(kHid / 8, E, 1), 256, 0, st>>>(tr->ga, kHid, tr->a2, L, L, tr->pw, tr->pb);
+    reduce(2, kHid, kHid, E);
     conv64_kernel<float><<<g64, 256, 0, st>>>(tr->ga, kHid, L, wt3, nullptr, tr->a2, 0, tr->gb);
     // layer 2
-    wgrad_kernel<kHid><<<dim3(kHid / 8, E), 256, 0, st>>>(tr->gb, kHid, tr->a1, L, tr->pw, tr->pb);
-    reduce(1, kHid, kHid);
+    wgrad_kernel<kHid><<<dim3(kHid / 8, E, 1), 256, 0, st>>>(tr->gb, kHid, tr->a1, L, L, tr->pw, tr->pb);
+    reduce(1, kHid, kHid, E);
     conv64_kernel<float><<<g64, 256, 0, st>>>(tr->gb, kHid, L, wt2, nullptr, tr->a1, 0, tr->ga);
     // layer 1 (16 -> 64)
-    wgrad_kernel<kNbc><<<dim3(kHid / 8, E), 256, 0, st>>>(tr->ga, kHid, tr->x, L, tr->pw, tr->pb);
-    reduce(0, kHid, kNbc);
+    wgrad_kernel<kNbc><<<dim3(kHid / 8, E, 1), 256, 0, st>>>(tr->ga, kHid, tr->x, L, L, tr->pw, tr->pb);
+    reduce(0, kHid, kNbc, E);
     PROP_CUDA(cudaGetLastError());
 }
 
