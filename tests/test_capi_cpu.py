@@ -49,6 +49,30 @@ def test_struct_layout_matches_header(tmp_path):
                    sorter.Spike.pcfeat.offset, sorter.Params.mem_budget.offset]
 
 
+def test_other_headers_struct_layouts(tmp_path):
+    """The proposal, payload and threshold-crossing structs as C sees them, against the ctypes
+    mirrors (every field's offset and the size)."""
+    from livespikesorter_gb300 import payload, proposal, threshold
+    mirrors = [("lss_prop_train_params", "lss_proposal.h", proposal.TrainParams),
+               ("lss_payload_header", "lss_payload.h", payload.PayloadHeader),
+               ("lss_tc_params", "lss_threshold.h", threshold.TcParams),
+               ("lss_tc_event", "lss_threshold.h", threshold.TcEvent)]
+    lines = []
+    for cname, _, py in mirrors:
+        fields = [f for f, _ in py._fields_]
+        lines.append('printf("%zu' + " %zu" * len(fields) + '\\n", sizeof(' + cname + ")"
+                     + "".join(f", offsetof({cname}, {f})" for f in fields) + ");")
+    incs = "".join(f'#include "{h}"\n' for h in sorted({h for _, h, _ in mirrors}))
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n" + incs + "int main(){" + "".join(lines) + "return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines()
+    for (cname, _, py), line in zip(mirrors, out):
+        want = [ct.sizeof(py)] + [getattr(py, f).offset for f, _ in py._fields_]
+        assert [int(v) for v in line.split()] == want, cname
+
+
 def test_default_params(lib):
     p = sorter.default_params()
     assert p.abi_version == sorter.ABI_VERSION
