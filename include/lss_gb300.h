@@ -115,6 +115,15 @@ int lss_open(const char* oss_dir, const lss_params* p, lss_handle** out);
 /* Shapes and counters. */
 int lss_get_info(const lss_handle* h, lss_info* info);
 
+/* Load and check an oss_input/ directory on the host alone, without a GPU: every file, shape,
+ * word size and cross-dimension that lss_open checks (the exporter's own checks,
+ * run_online_spikes.py:598-672 and subset_templates.py:48-66, and the loaders' in
+ * SorterHelpers.cpp:24-115).  Returns lss_open's status for the same directory under the
+ * default lss_params (cluster_centroids_pca.npy, read only for cluster_rule = 1, is not checked);
+ * info (may be NULL) receives C, T, T_final, K, nt, nC, nt0min, dup_bins and th, the other fields
+ * 0.  The message is lss_last_error(NULL). */
+int lss_validate_oss_input(const char* oss_dir, lss_info* info);
+
 /* Push n_samples rows of int16 [n_samples][n_chan_in] (channel fastest, SpikeGLX order).
  * stream_sample_ct = stream index of row 0, or -1 for "continues the previous push"; a
  * discontinuity flushes the current segment and starts a new one (the skip / behind policy

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <functional>
@@ -302,6 +303,13 @@ void Handle::free_work() {
     Wcap = nbcap = 0;
 }
 
+// The sorter's own limits on a loaded model (beyond the loader's file checks).
+static void check_model(const OssModel& m) {
+    if (m.nt % 2 == 0) throw LoadError{LSS_ERR_FORMAT, "template length must be odd"};
+    if (m.C > 1024) throw LoadError{LSS_ERR_FORMAT, "more than 1024 channels"};
+    if (m.K > 8) throw LoadError{LSS_ERR_FORMAT, "more than 8 PCs"};
+}
+
 void Handle::init(const char* dir, const lss_params* prm) {
     lss_default_params(&p);
     if (prm) {
@@ -311,15 +319,13 @@ void Handle::init(const char* dir, const lss_params* prm) {
     if (p.batch_samples <= 0 || p.max_iters <= 0 || p.group_batches <= 0 || p.hp_half_taps < 0)
         throw LoadError{LSS_ERR_ARG, "lss_params: non-positive batch_samples / max_iters / group_batches"};
     m = load_oss_input(dir ? dir : "");
-    if (m.nt % 2 == 0) throw LoadError{LSS_ERR_FORMAT, "template length must be odd"};
-    if (m.C > 1024) throw LoadError{LSS_ERR_FORMAT, "more than 1024 channels"};
+    check_model(m);
     C = (int)m.C;
     T = (int)m.T;
     K = (int)m.K;
     nt = (int)m.nt;
     nC = (int)m.nC;
     Tf = (int)(m.centroids.size() / 2);
-    if (K > 8) throw LoadError{LSS_ERR_FORMAT, "more than 8 PCs"};
     Cin = p.n_chan_in > 0 ? p.n_chan_in : C;
     if (Cin < C) throw LoadError{LSS_ERR_ARG, "n_chan_in smaller than the channel count"};
     NT = p.batch_samples;
@@ -1102,6 +1108,37 @@ int lss_get_info(const lss_handle* hp, lss_info* info) {
     info->batches_done = h.batches_done;
     info->spikes_done = h.spikes_done;
     return LSS_OK;
+}
+
+int lss_validate_oss_input(const char* oss_dir, lss_info* info) {
+    try {
+        const std::string dir = oss_dir ? oss_dir : "";
+        const lss::OssModel m = lss::load_oss_input(dir);
+        lss::check_model(m);
+        if (info) {
+            std::memset(info, 0, sizeof(*info));
+            info->C = (int32_t)m.C;
+            info->T = (int32_t)m.T;
+            info->T_final = (int32_t)(m.centroids.size() / 2);
+            info->K = (int32_t)m.K;
+            info->nt = (int32_t)m.nt;
+            info->nC = (int32_t)m.nC;
+            info->nt0min = (int32_t)m.nt0min;
+            info->dup_bins = (int32_t)m.dup_bins;
+            info->th = m.th;
+        }
+        g_open_error.clear();
+        return LSS_OK;
+    } catch (const lss::LoadError& e) {
+        g_open_error = e.msg;
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        g_open_error = "host allocation failed";
+        return LSS_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        g_open_error = e.what();
+        return LSS_ERR_INTERNAL;
+    }
 }
 
 int lss_push_batch(lss_handle* hp, const int16_t* samples, int64_t n_samples, int64_t stream_sample_ct) {

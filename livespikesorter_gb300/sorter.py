@@ -59,6 +59,7 @@ _SIGS = {
     "lss_default_params": (ct.c_int, [_P(Params)]),
     "lss_open": (ct.c_int, [ct.c_char_p, _P(Params), _P(ct.c_void_p)]),
     "lss_get_info": (ct.c_int, [ct.c_void_p, _P(Info)]),
+    "lss_validate_oss_input": (ct.c_int, [ct.c_char_p, _P(Info)]),
     "lss_push_batch": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int64]),
     "lss_flush": (ct.c_int, [ct.c_void_p]),
     "lss_poll": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, _P(ct.c_int64)]),
@@ -148,6 +149,17 @@ class SorterError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"{STATUS.get(status, status)}: {msg}")
         self.status = status
+
+
+def validate_oss_input(oss_dir) -> Info:
+    """Check an oss_input/ directory on the host (no GPU): lss_open's loader and shape checks.
+    Returns its dimensions; raises SorterError with lss_open's status for a bad directory."""
+    lib = load_library()
+    info = Info()
+    st = lib.lss_validate_oss_input(str(oss_dir).encode(), ct.byref(info))
+    if st:
+        raise SorterError(st, (lib.lss_last_error(None) or b"").decode())
+    return info
 
 
 def default_params(**kw) -> Params:

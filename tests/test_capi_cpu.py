@@ -120,6 +120,39 @@ def test_truncated_npy_is_format_error(lib, small_oss, tmp_path):
     assert st == 3 and "ctc" in msg
 
 
+def test_validator_without_a_gpu(lib, small_oss, tmp_path):
+    """lss_validate_oss_input: the dimensions of a good directory; for broken ones the status and
+    message lss_open gives; the command-line tool's exit status."""
+    from livespikesorter_gb300 import validate
+    info = sorter.validate_oss_input(small_oss)
+    w = np.load(small_oss / "Wall3.npy")
+    assert (info.C, info.T, info.K) == (w.shape[2], w.shape[0], w.shape[1])
+    assert info.nt == np.load(small_oss / "wPCA.npy").shape[1] and info.th == pytest.approx(8.0)
+    assert info.device_bytes == 0 and info.NT == 0
+    assert validate.main([str(small_oss)]) == 0
+    broken = []
+    d = tmp_path / "shape"
+    shutil.copytree(small_oss, d)
+    np.save(d / "Wall3.npy", w[:, :, :-1])
+    broken.append(d)
+    d = tmp_path / "misc"
+    shutil.copytree(small_oss, d)
+    (d / "misc.txt").write_text("nt0min:20\nnumNearestChans:10\n")
+    broken.append(d)
+    d = tmp_path / "truncated"
+    shutil.copytree(small_oss, d)
+    raw = (d / "ctc.npy").read_bytes()
+    (d / "ctc.npy").write_bytes(raw[: len(raw) // 2])
+    broken.append(d)
+    broken.append(tmp_path / "missing")
+    for d in broken:
+        with pytest.raises(sorter.SorterError) as e:
+            sorter.validate_oss_input(d)
+        st, msg = _open_status(lib, d)
+        assert e.value.status == st and msg in str(e.value)
+    assert validate.main([str(small_oss), str(broken[0])]) == 1
+
+
 def test_bad_params_rejected(lib, small_oss):
     st, _ = _open_status(lib, small_oss, batch_samples=0)
     assert st == 1
