@@ -1,0 +1,49 @@
+"""The precision-study oracle (oracle/precision_oracle.py): its exact variants are Kilosort's loop
+(ks_oracle.run_matching) on the golden window, its rounding matches the formats' grids, and
+re-scoring makes the amplitudes of the spikes it keeps exact."""
+import numpy as np
+import pytest
+
+from oracle import ks_oracle as ko
+from oracle import precision_oracle as po
+
+
+@pytest.fixture(scope="module")
+def window(golden_dir):
+    z = np.load(golden_dir / "ks_window.npz")
+    oss = ko.oss_from_arrays(z)
+    X = ko.preprocess(z["window"].T, oss)
+    return X, oss, int(z["max_iters"])
+
+
+def test_exact_variants_are_kilosorts_loop(window):
+    X, oss, it = window
+    ref = ko.run_matching(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned, max_iters=it)
+    for kw in ({}, {"keep": oss.Wall3.shape[0]}, {"rescore": True}):
+        st, amps = po.run_matching_variant(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned, max_iters=it, **kw)
+        np.testing.assert_array_equal(st, ref.st)
+        np.testing.assert_allclose(amps, ref.amps, rtol=1e-12)
+
+
+def test_rounding_grids():
+    assert po.round_fp8(448.0, "e4m3") == 448.0 and po.round_fp8(1e6, "e4m3") == 448.0
+    assert po.round_fp8(1.0625, "e4m3") == 1.0          # 1 + 1/16 ties to the even neighbour
+    assert po.round_fp8(1.1875, "e4m3") == 1.25
+    assert po.round_fp8(2.0 ** -9, "e4m3") == 2.0 ** -9  # smallest subnormal
+    assert po.round_fp8(-3.0, "e5m2") == -3.0 and po.round_fp8(3.25, "e5m2") == 3.0
+    assert po.round_bf16(np.float32(1.00390625)) == 1.0  # 1 + 2^-8 ties to even
+    x = np.random.default_rng(0).normal(0, 10, 1000)
+    assert np.max(np.abs(po.round_fp8(x, "e4m3") - x) / np.maximum(np.abs(x), 2.0 ** -6)) <= 2.0 ** -4 + 1e-12
+
+
+def test_rescored_amplitudes_are_exact_for_the_spikes_kept(window):
+    X, oss, it = window
+    ref = ko.run_matching(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned, max_iters=it)
+    st, amps = po.run_matching_variant(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned, fmt="e4m3", rescore=True,
+                                       max_iters=it)
+    # where the accepted sequence matches Kilosort's (spike for spike, in order), so does every amplitude
+    n = 0
+    while n < min(len(st), len(ref.st)) and tuple(st[n]) == tuple(ref.st[n]):
+        n += 1
+    assert n > 0
+    np.testing.assert_allclose(amps[:n], ref.amps[:n], rtol=1e-9)
