@@ -208,13 +208,18 @@ int lss_stage_times(lss_handle* h, double* ms, int32_t n, int64_t* n_groups);
  *   ctc_perm        [T][2*nt+1][T]  ctc_perm[s][l][t] = ctc[t][s][l]
  *   waveforms       [T][nt][C]      preclustered_template_waveforms
  *   template_norms  [T]             sum of squares of each Wall3 template
- *   n_spikes        [1]     spikes accepted (may exceed cap; the lists then hold the first cap)
+ *   n_spikes        [1]     spikes accepted (may exceed cap; the lists then hold the first cap);
+ *                           negative when the kernel reported a fault (-2: it did not run with the
+ *                           thread-block cluster shape it was launched for) -- the lists are then
+ *                           not valid
  *   spike_sample / spike_template / spike_amp / spike_iter  [cap]  in (iteration, sample) order
  * Its working memory is a fixed device array of LSS_NOALLOC_SCRATCH_BYTES inside the library
  * (held on every GPU that loads it until the process exits), enough for windows of at most
- * LSS_NOALLOC_MAX_SAMPLES samples; a larger W returns LSS_ERR_ARG.  The first call on a device
- * looks up that array's device address, so make it before any stream capture.  All calls share
- * the array: calls whose work overlaps on the GPU race, so serialise them (one stream, or events).
+ * LSS_NOALLOC_MAX_SAMPLES samples; a larger W returns LSS_ERR_ARG.  A call outside stream capture
+ * looks up that array's device address on the current device (again after a cudaDeviceReset); a
+ * call on a capturing stream reuses the address found before, so the first call on a device must
+ * come before any capture (else LSS_ERR_ARG).  All calls share the array: calls whose work
+ * overlaps on the GPU race, so serialise them (one stream, or events).
  * Errors: LSS_ERR_ARG / LSS_ERR_CUDA, message via lss_last_error(NULL). */
 #define LSS_NOALLOC_MAX_SAMPLES 16384
 #define LSS_NOALLOC_SCRATCH_BYTES 196864

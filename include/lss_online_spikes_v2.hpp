@@ -77,6 +77,67 @@ public:
 
 using SpikeSink = std::function<void(const lss_spike* spikes, int64_t n)>;
 
+// Where the next fetch starts: the behind/skip policy of OnlineSpikesV2::runSpikeSorting
+// (OnlineSpikesV2.cu:705-746), one branch per case.
+enum class FetchBranch {
+    Normal,      // at most one batch behind: the rows after the last processed one (:712-719)
+    JumpNewest,  // behind, and being behind is not allowed (iTimeBehind == 0): the newest batch (:720-724)
+    CatchUp,     // behind, but within iTimeBehind ms: keep going from the last processed row (:728-732)
+    SmallSkip,   // further behind than allowed, bSmallskip: from the newest row allowed (:734-738)
+    BigSkip      // further behind than allowed, no small skip: the newest batch (:740-746)
+};
+
+struct FetchPlan {
+    t_ull start;        // stream sample of the first row to fetch
+    bool skip;          // rows between the last processed one and start are dropped
+    FetchBranch branch;
+};
+
+// The reference computes allowedCt = latestCt - timeBehind * samplingRate / 1000 in float
+// (OnlineSpikesV2.cu:707), which rounds sample counts above 2^24; here the allowed lag is an exact
+// sample count and allowedCt never goes below 0.
+inline FetchPlan plan_fetch(t_ull latest, t_ull processed, long maxRows, long timeBehindMs, double rateHz,
+                            bool smallSkip) {
+    const t_ull lag = timeBehindMs > 0 ? (t_ull)((double)timeBehindMs * rateHz / 1000.0) : 0;
+    const t_ull allowedCt = latest > lag ? latest - lag : 0;
+    const t_ull newest = latest > (t_ull)maxRows ? latest - (t_ull)maxRows : 0;
+    if (latest - processed <= (t_ull)maxRows) return {processed, false, FetchBranch::Normal};
+    if (timeBehindMs == 0) return {newest, true, FetchBranch::JumpNewest};
+    if (processed >= allowedCt) return {processed, false, FetchBranch::CatchUp};
+    if (smallSkip) return {allowedCt, true, FetchBranch::SmallSkip};
+    return {newest, true, FetchBranch::BigSkip};
+}
+
+// The acquisition loop of runSpikeSorting (OnlineSpikesV2.cu:698-849) over any DataSocket: wait for
+// iMinScanWindow new rows, plan the fetch, fetch up to iMaxScanWindow rows from the planned start,
+// hand them to push(rows, n, first_stream_sample), then emit().  Returns when the socket stops
+// running or *running turns false.  Counts skips in *skips.  Header-only so that the policy can be
+// driven without a GPU.
+template <typename Push, typename Emit>
+void run_ingest_loop(DataSocket* sock, const OSSSpecificParams& os, const InputParameters& prm,
+                     std::vector<int16_t>& buf, Push&& push, Emit&& emit, const volatile bool* running,
+                     int64_t* skips) {
+    const long maxRows = prm.iMaxScanWindow;
+    t_ull latest = sock->getStreamSampleCt(IMEC, os);
+    t_ull processed = latest;
+    while (*running && sock->isRunning()) {
+        sock->waitUntil(processed + (t_ull)prm.iMinScanWindow, os);
+        latest = sock->getStreamSampleCt(IMEC, os);
+        if (latest <= processed) {
+            if (!sock->isRunning()) break;
+            continue;
+        }
+        const FetchPlan fp = plan_fetch(latest, processed, maxRows, prm.iTimeBehind, prm.fImecSamplingRate,
+                                        prm.bSmallskip);
+        if (fp.skip) ++*skips;
+        const t_ull end = sock->fetchFromPlace(buf.data(), maxRows, os, fp.start);
+        if (end <= fp.start) continue;
+        push(buf.data(), (int64_t)(end - fp.start), (int64_t)fp.start);
+        processed = end;
+        emit();
+    }
+}
+
 class OnlineSpikesV2 {
 public:
     OnlineSpikesV2(const InputParameters& params, DataSocket* socket, SpikeSink sink = nullptr);

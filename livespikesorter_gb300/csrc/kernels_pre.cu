@@ -11,30 +11,52 @@
 namespace lss {
 
 // ---------------------------------------------------------------------------------------
-// channel sums over each window, exact in integers (mean = sum / W, rounded once)
+// channel means over each window: exact integer sums, then mean = q + r / W in FP32 (q, r the
+// integer quotient and remainder of sum / W), once per (window, channel) by the last of the
+// window's row blocks to finish
 // ---------------------------------------------------------------------------------------
 constexpr int kSumRows = 128;
+constexpr int kSumThreads = 256;
 
-__global__ void colsum_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan,
-                              int C, int W, int NT, long long* __restrict__ colsum) {
+// colsum [nb][C] and ticket [nb][gridDim.x] are zero on entry and left zero on exit (the last row
+// block of a (window, channel block) clears them after taking the means), so no launch clears them
+__global__ void __launch_bounds__(kSumThreads)
+colsum_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C, int W,
+              int NT, long long* __restrict__ colsum, int* __restrict__ ticket, float* __restrict__ mean) {
+    __shared__ int s_last;
     const int b = blockIdx.z;
     const int r0 = blockIdx.y * kSumRows;
     const int r1 = min(W, r0 + kSumRows);
     const int64_t base = (int64_t)b * NT;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+    const int c = blockIdx.x * kSumThreads + threadIdx.x;   // gridDim.x * kSumThreads >= C
+    long long* cs = colsum + (int64_t)b * C + c;
+    if (c < C) {
         const int src = chan ? chan[c] : c;
         int acc = 0;
         for (int r = r0; r < r1; ++r) acc += raw[(base + r) * row_stride + src];
-        atomicAdd(reinterpret_cast<unsigned long long*>(colsum + (int64_t)b * C + c),
-                  (unsigned long long)(long long)acc);
+        atomicAdd(reinterpret_cast<unsigned long long*>(cs), (unsigned long long)(long long)acc);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int* tk = ticket + (int64_t)b * gridDim.x + blockIdx.x;
+        s_last = atomicAdd(tk, 1) == (int)gridDim.y - 1;
+        if (s_last) *tk = 0;
+    }
+    __syncthreads();
+    if (s_last && c < C) {
+        const long long sum = __ldcg(cs);   // every row block's sum is in L2 (fenced before its ticket)
+        const long long q = sum / W;        // |q| <= 32768: exact in FP32
+        const int r = (int)(sum - q * W);   // |r| < W
+        mean[(int64_t)b * C + c] = (float)q + __fdiv_rn((float)r, (float)W);
+        *cs = 0;
     }
 }
 
 void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
-                   long long* colsum, cudaStream_t s) {
-    cudaMemsetAsync(colsum, 0, sizeof(long long) * (size_t)nb * C, s);
-    dim3 grid((C + 255) / 256, (W + kSumRows - 1) / kSumRows, nb);
-    colsum_kernel<<<grid, 256, 0, s>>>(raw, row_stride, chan, C, W, NT, colsum);
+                   long long* colsum, int* ticket, float* mean, cudaStream_t s) {
+    dim3 grid((C + kSumThreads - 1) / kSumThreads, (W + kSumRows - 1) / kSumRows, nb);
+    colsum_kernel<<<grid, kSumThreads, 0, s>>>(raw, row_stride, chan, C, W, NT, colsum, ticket, mean);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -96,7 +118,7 @@ __device__ __forceinline__ uint32_t warp_kth_key(const uint32_t (&key)[NJ], int 
 template <int NJ>
 __global__ void __launch_bounds__(kCarWarps * 32)
 car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C, int W,
-           int NT, const long long* __restrict__ colsum, int L, int R, float* __restrict__ Xw) {
+           int NT, const float* __restrict__ mean, int L, int R, float* __restrict__ Xw) {
     constexpr int kMaxChanPerLane = NJ;
     const int b = blockIdx.y;
     const int lane = threadIdx.x & 31;
@@ -106,13 +128,11 @@ car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* _
     const int nj = (C + 31) >> 5;
     float v[kMaxChanPerLane];
     uint32_t key[kMaxChanPerLane];
-    const double invW = 1.0 / (double)W;
 #pragma unroll
     for (int j = 0; j < kMaxChanPerLane; ++j) {
         const int c = lane + 32 * j;
         if (j < nj && c < C) {
-            const float mean = (float)((double)colsum[(int64_t)b * C + c] * invW);
-            const float x = (float)raw[rowp + (chan ? chan[c] : c)] - mean;
+            const float x = (float)raw[rowp + (chan ? chan[c] : c)] - mean[(int64_t)b * C + c];
             v[j] = x;
             key[j] = f2key(x);
         } else {
@@ -148,7 +168,7 @@ constexpr int kCarTRows = 32;
 template <int NJ, int OUT>
 __global__ void __launch_bounds__(kCarWarps * 32)
 car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C, int W,
-             int NT, const long long* __restrict__ colsum, int L, int R, int pitch, float* __restrict__ Xt_hi,
+             int NT, const float* __restrict__ mean, int L, int R, int pitch, float* __restrict__ Xt_hi,
              float* __restrict__ Xt_lo) {
     constexpr bool LO = OUT != 0;
     extern __shared__ float s_y[];   // [kCarTRows][C + 1]
@@ -156,7 +176,6 @@ car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t*
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int w0 = blockIdx.x * kCarTRows;
     const int ld = C + 1;
-    const double invW = 1.0 / (double)W;
     for (int rr = warp; rr < kCarTRows; rr += kCarWarps) {
         const int w = w0 + rr;
         if (w >= W) break;
@@ -167,8 +186,7 @@ car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t*
         for (int j = 0; j < NJ; ++j) {
             const int c = lane + 32 * j;
             if (c < C) {
-                const float mean = (float)((double)colsum[(int64_t)b * C + c] * invW);
-                const float x = (float)raw[rowp + (chan ? chan[c] : c)] - mean;
+                const float x = (float)raw[rowp + (chan ? chan[c] : c)] - mean[(int64_t)b * C + c];
                 v[j] = x;
                 key[j] = f2key(x);
             } else {
@@ -238,7 +256,7 @@ car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t*
 }
 
 void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
-                  const long long* colsum, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s,
+                  const float* mean, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s,
                   bool bf16) {
     dim3 grid((W + kCarTRows - 1) / kCarTRows, nb);
     const int nj = (C + 31) / 32;
@@ -247,15 +265,15 @@ void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, i
     do {                                                                                                   \
         if (bf16 && Xt_lo) {                                                                               \
             raise_smem_limit((const void*)car_t_kernel<N, 2>, smem);                                       \
-            car_t_kernel<N, 2><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
+            car_t_kernel<N, 2><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, mean, \
                                                                   L, R, pitch, Xt_hi, Xt_lo);              \
         } else if (Xt_lo) {                                                                                \
             raise_smem_limit((const void*)car_t_kernel<N, 1>, smem);                                       \
-            car_t_kernel<N, 1><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
+            car_t_kernel<N, 1><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, mean, \
                                                                   L, R, pitch, Xt_hi, Xt_lo);              \
         } else {                                                                                           \
             raise_smem_limit((const void*)car_t_kernel<N, 0>, smem);                                       \
-            car_t_kernel<N, 0><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, colsum, \
+            car_t_kernel<N, 0><<<grid, kCarWarps * 32, smem, s>>>(raw, row_stride, chan, C, W, NT, mean, \
                                                                   L, R, pitch, Xt_hi, nullptr);            \
         }                                                                                                  \
     } while (0)
@@ -269,10 +287,10 @@ void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, i
 }
 
 void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
-                const long long* colsum, int L, int R, float* Xw, cudaStream_t s) {
+                const float* mean, int L, int R, float* Xw, cudaStream_t s) {
     dim3 grid((W + kCarWarps - 1) / kCarWarps, nb);
     const int nj = (C + 31) / 32;
-#define LSS_CAR(N) car_kernel<N><<<grid, kCarWarps * 32, 0, s>>>(raw, row_stride, chan, C, W, NT, colsum, L, R, Xw)
+#define LSS_CAR(N) car_kernel<N><<<grid, kCarWarps * 32, 0, s>>>(raw, row_stride, chan, C, W, NT, mean, L, R, Xw)
     if (nj <= 4) LSS_CAR(4);
     else if (nj <= 8) LSS_CAR(8);
     else if (nj <= 12) LSS_CAR(12);

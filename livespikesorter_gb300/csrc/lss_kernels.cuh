@@ -55,14 +55,16 @@ constexpr int kHighpassTileSmall = 128, kHighpassTileLarge = 256, kHighpassSmall
 // raise (never lower) a kernel's dynamic shared-memory limit on the current device
 cudaError_t raise_smem_limit(const void* kernel, size_t bytes);
 
+// per-(window, channel) means (FP32) from exact integer sums; colsum [nb][C] and ticket
+// [nb][ceil(C / 256)] must be zero before the first launch and are zero again after each launch
 void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT,
-                   int nb, long long* colsum, cudaStream_t s);
+                   int nb, long long* colsum, int* ticket, float* mean, cudaStream_t s);
 void launch_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
-                const long long* colsum, int L, int R, float* Xw, cudaStream_t s);
+                const float* mean, int L, int R, float* Xw, cudaStream_t s);
 // channel-major, tf32-split variant feeding the tensor-core high-pass: Xt[(b, c)][pitch]
 // bf16: Xt_hi / Xt_lo receive the BF16 split (viewed as bf16 arrays)
 void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
-                  const long long* colsum, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s,
+                  const float* mean, int L, int R, int pitch, float* Xt_hi, float* Xt_lo, cudaStream_t s,
                   bool bf16 = false);
 // Ylo != nullptr: Y receives tf32(y) and Ylo the remainder (operands of the tensor-core GEMM)
 void launch_highpass(const float* Xw, int C, int W, int L, int R, const float* taps, int nb, float* Y,

@@ -10,11 +10,15 @@
 //
 // The array is a file-scope __device__ variable: every GPU that loads this library holds it
 // (LSS_NOALLOC_SCRATCH_BYTES) until the process exits.  Host code cannot use its name as a
-// device address, so the first call on each device looks the address up with
-// cudaGetSymbolAddress (with that device current) and caches it; that first call should happen
-// before any stream capture.  Every call shares the one array and it keeps the previous call's
-// contents, so the parts that must start at zero are cleared on the caller's stream at each
-// call; calls whose kernels overlap on the GPU race on the array.
+// device address, so each call made outside stream capture looks the address up with
+// cudaGetSymbolAddress (with the caller's device current) and keeps it per device; a call made
+// while its stream is being captured uses the kept address, so the first call on a device must
+// come before any capture.  Looking the address up again on every uncaptured call keeps it valid
+// after cudaDeviceReset, which reloads the module at a new address.  Every call shares the one
+// array and it keeps the previous call's contents, so the parts that must start at zero are
+// cleared on the caller's stream at each call; calls whose kernels overlap on the GPU race on the
+// array.  The kernel's status word also lives there; a small kernel after the loop turns a fault
+// it reports into a negative *n_spikes, so no host read of the array is needed.
 #include "../../include/lss_gb300.h"
 #include "lss_kernels.cuh"
 
@@ -45,6 +49,13 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned char* g_addr[kMaxDevices] = {};
 
+// status bit 0 (more spikes than cap) is visible as *n_spikes > cap already; any other bit means
+// the loop did not run as launched and its lists are not valid: report -(those bits)
+__global__ void noalloc_status_kernel(const int* status, int* n_spikes) {
+    const int bad = *status & ~1;
+    if (bad) *n_spikes = -bad;
+}
+
 }  // namespace
 
 extern "C" int lss_match_noalloc(float* scores, float* residual, const float* ctc_perm, const float* waveforms,
@@ -73,10 +84,17 @@ extern "C" int lss_match_noalloc(float* scores, float* residual, const float* ct
         g_noalloc_error = std::string("lss_match_noalloc: cudaGetDevice: ") + cudaGetErrorString(e);
         return LSS_ERR_CUDA;
     }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap_st = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cap_st);
+    if (e != cudaSuccess) {
+        g_noalloc_error = std::string("lss_match_noalloc: cudaStreamIsCapturing: ") + cudaGetErrorString(e);
+        return LSS_ERR_CUDA;
+    }
     unsigned char* base = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[dev]) {
+        if (cap_st == cudaStreamCaptureStatusNone) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_scratch);   // the current device is dev
             if (e != cudaSuccess) {
@@ -84,10 +102,12 @@ extern "C" int lss_match_noalloc(float* scores, float* residual, const float* ct
                 return LSS_ERR_CUDA;
             }
             g_addr[dev] = static_cast<unsigned char*>(p);
+        } else if (!g_addr[dev]) {
+            g_noalloc_error = "lss_match_noalloc: the first call on a device must come before stream capture";
+            return LSS_ERR_ARG;
         }
         base = g_addr[dev];
     }
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     lss::MatchScratch sc;
     sc.cfmax = reinterpret_cast<float*>(base + kOffCfmax);
     sc.at_t = reinterpret_cast<int*>(base + kOffAtT);
@@ -107,6 +127,10 @@ extern "C" int lss_match_noalloc(float* scores, float* residual, const float* ct
         e = lss::launch_match(scores, residual, ctc_perm, waveforms, template_norms, th * th, W, T, C, nt, max_iters,
                               1, sc, out, s, 0);
     if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        noalloc_status_kernel<<<1, 1, 0, s>>>(out.status, n_spikes);
+        e = cudaGetLastError();
+    }
     if (e != cudaSuccess) {
         g_noalloc_error = std::string("lss_match_noalloc: ") + cudaGetErrorString(e);
         return LSS_ERR_CUDA;

@@ -75,35 +75,12 @@ void OnlineSpikesV2::emit() {
 }
 
 void OnlineSpikesV2::runSpikeSorting() {
-    const long maxRows = params_.iMaxScanWindow;
-    t_ull latest = sock_->getStreamSampleCt(IMEC, os_);
-    t_ull processed = latest;
-    const double per_ms = params_.fImecSamplingRate / 1000.0;
-    while (running_ && sock_->isRunning()) {
-        sock_->waitUntil(processed + (t_ull)params_.iMinScanWindow, os_);
-        latest = sock_->getStreamSampleCt(IMEC, os_);
-        if (latest <= processed) {
-            if (!sock_->isRunning()) break;
-            continue;
-        }
-        const t_ull behind = latest - processed;
-        const t_ull allowed = (t_ull)(params_.iTimeBehind * per_ms);
-        t_ull start = processed;
-        if (behind > (t_ull)maxRows + allowed && params_.iTimeBehind == 0) {
-            // behind and not allowed to be: jump to the newest batch (OnlineSpikesV2.cu:720-724)
-            start = latest - (t_ull)maxRows;
-            ++skips_;
-        } else if (behind > (t_ull)maxRows + allowed && params_.bSmallskip) {
-            start = latest - (t_ull)maxRows - allowed;   // small skip (:734-738)
-            ++skips_;
-        }
-        const t_ull end = sock_->fetchFromPlace(buf_.data(), maxRows, os_, start);
-        if (end <= start) continue;
-        const int64_t n = (int64_t)(end - start);
-        check(h_, lss_push_batch(h_, buf_.data(), n, (int64_t)start));
-        processed = end;
-        emit();
-    }
+    // a fetch that starts after the previous one's end (a skip) is a discontinuity: lss_push_batch
+    // flushes the segment and starts a new one there
+    run_ingest_loop(
+        sock_, os_, params_, buf_,
+        [this](const int16_t* rows, int64_t n, int64_t start) { check(h_, lss_push_batch(h_, rows, n, start)); },
+        [this]() { emit(); }, &running_, &skips_);
     check(h_, lss_flush(h_));
     int64_t pend = 0;
     check(h_, lss_pending(h_, &pend));

@@ -171,7 +171,9 @@ struct Handle {
     int Wcap = 0, nbcap = 0;
     size_t raw_rows_cap = 0;
     int16_t* d_raw = nullptr;   // [kSlots][raw_rows_cap][Cin]: each slot's rows on the device
-    long long* d_colsum = nullptr;
+    long long* d_colsum = nullptr;   // [nb][C] integer channel sums (zero between launches)
+    int* d_ticket = nullptr;         // [nb][ceil(C / 256)] row blocks done (zero between launches)
+    float* d_mean = nullptr;         // [nb][C] channel means
     float *d_Xw = nullptr, *d_Y = nullptr, *d_Z = nullptr, *d_Bpc = nullptr, *d_Bt = nullptr;
     float *d_Y_lo = nullptr, *d_Bpc_lo = nullptr;   // tf32 remainders (tensor-core path)
     float *d_Xt_hi = nullptr, *d_Xt_lo = nullptr;   // channel-major wrapped windows (tensor-core high-pass)
@@ -283,7 +285,7 @@ void Handle::free_work() {
         conv_tc_free(kv.second.conv);
         kv.second.conv = nullptr;
     }
-    for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
+    for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_ticket, (void*)d_mean, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
                     (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo, (void*)d_Zt_hi, (void*)d_Zt_lo,
                     (void*)d_split,
                     (void*)sc.cfmax, (void*)sc.at_t, (void*)sc.at_amp, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
@@ -291,6 +293,8 @@ void Handle::free_work() {
         if (p) cudaFree(p);
     d_raw = nullptr;
     d_colsum = nullptr;
+    d_ticket = nullptr;
+    d_mean = nullptr;
     d_Xw = d_Y = d_Z = d_Bpc = d_Bt = nullptr;
     d_Y_lo = d_Bpc_lo = nullptr;
     d_Xt_hi = d_Xt_lo = nullptr;
@@ -535,7 +539,7 @@ void Handle::ensure_work(int Wn, int nb) {
     // that with exact ties
     cap = p.spike_cap > 0 ? p.spike_cap : std::max(2048, 2 * max_iters * ((Wa + nt) / (nt + 1)));
     raw_rows_cap = (size_t)nba * (size_t)std::max(Wa, NT) + 2 * (size_t)nt;
-    const int64_t need = (int64_t)kSlots * raw_rows_cap * Cin * 2 + (int64_t)nba * C * 8 +
+    const int64_t need = (int64_t)kSlots * raw_rows_cap * Cin * 2 + (int64_t)nba * C * 12 + (int64_t)nba * 16 +
                          (int64_t)nba * (Wa + LRmax) * C * 4 + 2LL * nba * Wa * C * 4 +
                          (int64_t)nba * Wa * K * C * 4 * (tc_project && !tf32_data ? 2 : 1) +
                          (int64_t)nba * Wa * C * 4 * (tc_whiten && !tf32_data ? 1 : 0) +
@@ -547,6 +551,10 @@ void Handle::ensure_work(int Wn, int nb) {
                                            " device bytes, budget " + std::to_string(p.mem_budget)};
     d_raw = dev_alloc<int16_t>((size_t)kSlots * raw_rows_cap * Cin, dev_bytes);
     d_colsum = dev_alloc<long long>((size_t)nba * C, dev_bytes);
+    d_ticket = dev_alloc<int>((size_t)nba * ((C + 255) / 256), dev_bytes);
+    d_mean = dev_alloc<float>((size_t)nba * C, dev_bytes);
+    LSS_CUDA(cudaMemsetAsync(d_colsum, 0, sizeof(long long) * (size_t)nba * C, st));
+    LSS_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(int) * (size_t)nba * ((C + 255) / 256), st));
     if (tc_highpass) {
         // row pitch of any window length up to Wa: W + L + R <= 2W - 1, rounded up to 8
         const size_t n = (size_t)nba * C * (size_t)((2 * Wa + 7) / 8 * 8);
@@ -641,7 +649,7 @@ int Handle::acquire_slot() {
 // the device) into d_Z (whitened windows) and d_Bt (scores).  mark() is called after each stage.
 void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
                                   const std::function<void()>& mark) {
-    launch_colsum(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, st), ++nl;
+    launch_colsum(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, d_ticket, d_mean, st), ++nl;
     mark();
     if (tc_highpass) {
         TapSet& tw = const_cast<TapSet&>(ts);
@@ -653,14 +661,14 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
                                                      tw.g_hi[v], tw.g_lo[v], tw.Kt[v]);
             if (!tw.um[v]) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (high-pass band GEMM)"};
         }
-        launch_car_t(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, tw.pitch, d_Xt_hi, d_Xt_lo, st, bf16_pre),
+        launch_car_t(raw, Cin, d_chan, C, Wn, NTs, nb, d_mean, ts.L, ts.R, tw.pitch, d_Xt_hi, d_Xt_lo, st, bf16_pre),
             ++nl;
         mark();
         LSS_CUDA(launch_umma_highpass(tw.um[v], d_Y, d_Y_lo, nb, C, Wn, d_gemm_err, st));
         ++nl;
         mark();
     } else {
-        launch_car(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, ts.L, ts.R, d_Xw, st), ++nl;
+        launch_car(raw, Cin, d_chan, C, Wn, NTs, nb, d_mean, ts.L, ts.R, d_Xw, st), ++nl;
         mark();
         launch_highpass(d_Xw, C, Wn, ts.L, ts.R, ts.d, nb, d_Y, st, tc_whiten ? d_Y_lo : nullptr), ++nl;
         mark();

@@ -14,7 +14,8 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REFERENCE = Path(os.environ.get("LSS_REFERENCE_DIR", "/root/reference"))
+# the reference checkout: LSS_REFERENCE_DIR, else a "reference" directory beside this repository
+REFERENCE = Path(os.environ.get("LSS_REFERENCE_DIR") or (HERE.parent.parent / "reference"))
 
 
 def build(verbose: bool = False):

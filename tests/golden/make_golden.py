@@ -1,6 +1,7 @@
 """Generate the golden fixtures that pin the oracle to the reference's own code.
 
-Runs only where the reference tree is mounted (/root/reference); the fixtures it writes
+Runs only where the reference checkout is present (LSS_REFERENCE_DIR, else a "reference"
+directory beside this repository); the fixtures it writes
 (``*.npz`` beside this script) travel with the repository so the tests need no reference.
 
 * ``kat_conv1d.npz``   -- the reference's known-answer script src/Python/conv1d_test.py,
@@ -22,6 +23,7 @@ import builtins
 import contextlib
 import importlib
 import io
+import os
 import sys
 import tempfile
 import types
@@ -31,7 +33,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-REF = Path("/root/reference")
+REF = Path(os.environ.get("LSS_REFERENCE_DIR") or (REPO.parent / "reference"))
 KS_DIR = REF / "src/Python/run_online_spikes/Lib/site-packages/kilosort"
 sys.path.insert(0, str(REPO))
 

@@ -39,6 +39,7 @@ def _run_noalloc(lib, torch, B0, X0, ctcP, pre_wf, nm, th, W, T, C, nt, max_iter
     assert rc == 0, (lib.lss_last_error(None) or b"").decode()
     torch.cuda.synchronize(dev)
     k = int(n.item())
+    assert k >= 0, f"the matching kernel reported a fault (status bits {-k})"
     assert 0 < k <= CAP
     return (sw[:k].cpu().numpy(), stt[:k].cpu().numpy(), sa[:k].cpu().numpy(), si[:k].cpu().numpy(),
             X.cpu().numpy())
