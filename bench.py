@@ -71,6 +71,10 @@ def args_():
     ap.add_argument("--gemm-path", type=int, default=0,
                     help="0 tcgen05 FP32 (3xTF32), 1 FP32 SIMT, 2 tcgen05 with TF32 data (two products)")
     ap.add_argument("--no-tier", action="store_true", help="skip the chosen-tier measurement")
+    ap.add_argument("--tier-keep", type=int, default=32,
+                    help="match_keep of the chosen tier (templates per sample in the pruned loop; 0 = full loop)")
+    ap.add_argument("--chosen-seconds", type=float, default=4.0,
+                    help="signal per stream of the 8-stream chosen-path measurement (0 = skip it)")
     ap.add_argument("--tier-path", type=int, default=3,
                     help="gemm_path of the chosen tier reported beside FP32: 3 BF16 splits, 2 TF32 activations")
     ap.add_argument("--path", default="sort", choices=["sort", "tc", "proposal"],
@@ -370,10 +374,10 @@ def run_gpu(a):
 
     obuf = np.zeros(1 << 16, sorter.SPIKE_DTYPE)
 
-    def batch_latency(path, n):
+    def batch_latency(path, n, keep=0):
         """push-to-spikes wall time of single 1500-sample batches (one batch per launch)"""
         s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1, profile=1,
-                                 match_variant=a.match_variant, gemm_path=path)
+                                 match_variant=a.match_variant, gemm_path=path, match_keep=keep)
         lat = []
         s3.push(data[:NT + 2 * nt], 0)
         drain(s3)
@@ -399,7 +403,7 @@ def run_gpu(a):
     if a.gemm_path == 0 and not a.no_tier:
         tp = a.tier_path
         st = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1,
-                                 match_variant=a.match_variant, gemm_path=tp)
+                                 match_variant=a.match_variant, gemm_path=tp, match_keep=a.tier_keep)
         ext2 = torch.cuda.ExternalStream(st.cuda_stream(), device=f"cuda:{dev}")
 
         def step2(i):
@@ -429,15 +433,16 @@ def run_gpu(a):
         got = {}
         for path in (0, tp):
             with sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
-                                     match_variant=a.match_variant, gemm_path=path) as sa:
+                                     match_variant=a.match_variant, gemm_path=path,
+                                     match_keep=a.tier_keep if path == tp else 0) as sa:
                 got[path] = sa.sort_stream(data[:n_rows])
         frac, amp_ok = spike_agreement(got[0], got[tp])
         dt = {3: "bf16 splits (hi*hi + hi*lo + lo*hi on kind::f16), fp32 accumulate",
               2: "tf32 activations x fp32-split fixed matrices, fp32 accumulate"}.get(tp, f"gemm_path {tp}")
-        tier = {"gemm_path": tp, "value": a.steps * G * NT * C / (ms2 / 1e3), "unit": UNIT,
+        tier = {"gemm_path": tp, "match_keep": a.tier_keep, "value": a.steps * G * NT * C / (ms2 / 1e3), "unit": UNIT,
                 "ms_per_step": ms2 / a.steps, "dtype": dt,
                 "stage_ms_per_launch": {k: (ta[k] - tb[k]) / max(1, na - nb0) for k in ta},
-                "latency": {k: v for k, v in batch_latency(tp, min(a.latency_batches, 100)).items()
+                "latency": {k: v for k, v in batch_latency(tp, min(a.latency_batches, 100), a.tier_keep).items()
                             if k in ("p50_ms", "p99_ms", "batches")},
                 "agreement_vs_fp32": {"batches": (n_rows - 2 * nt) // NT, "spikes_fp32": int(len(got[0])),
                                       "spikes_tier": int(len(got[tp])), "matched": frac, "amp_within_1e-3": amp_ok,
@@ -496,6 +501,11 @@ def run_gpu(a):
     # ---- per-batch latency (one batch per launch) --------------------------------------------
     latency = batch_latency(a.gemm_path, a.latency_batches)
 
+    # ---- the chosen path on eight concurrent probe streams (rank 0) ----------------------------
+    chosen_block = None
+    if rank == 0 and a.chosen_seconds > 0 and a.gemm_path == 0:
+        chosen_block = run_chosen(a, dev)
+
     # ---- CPU baseline (rank 0) ----------------------------------------------------------------
     cpu = None
     if rank == 0 and not a.no_cpu:
@@ -511,7 +521,7 @@ def run_gpu(a):
                 "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded generator, shapes of the named config)",
                 "config": workload_config(a, cfg, G), "e2e": e2e, "latency": latency, "roofline": roof,
-                "cpu_baseline": cpu, "clocks": clk.summary(), "chosen_tier": tier,
+                "cpu_baseline": cpu, "clocks": clk.summary(), "chosen_tier": tier, "chosen": chosen_block,
                 "gpu_launches": launches_per_step * a.steps,
                 "spikes_per_batch": spikes_per_batch,
                 "realtime_factor": value / (C * 30000.0)}
@@ -679,12 +689,15 @@ def _serving_data(streams, seconds, seed0):
     return out
 
 
-def _run_streams(sets, paced: bool, jitter: float = 0.2, seed: int = 0, gate=None):
+def _run_streams(sets, paced: bool, jitter: float = 0.2, seed: int = 0, gate=None, opts=None, spikes=None):
     """One thread per stream: push each batch (paced at 30 kHz with +/-jitter, or back to back),
     then poll its spikes; returns per-batch latencies (ms), wall seconds and new samples x channels.
-    gate = (params, logit threshold, dilation) sets the learned proposal gate on every handle."""
+    gate = (params, logit threshold, dilation) sets the learned proposal gate on every handle; opts =
+    extra sorter parameters (gemm_path, match_keep); spikes = a list that receives each stream's
+    spikes."""
     from livespikesorter_gb300 import sorter
-    handles = [sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=1) for d, _, NT in sets]
+    handles = [sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=1, **(opts or {}))
+               for d, _, NT in sets]
     if gate is not None:
         for h in handles:
             h.set_proposal(*gate)
@@ -693,6 +706,7 @@ def _run_streams(sets, paced: bool, jitter: float = 0.2, seed: int = 0, gate=Non
         h.poll_all()
     lat = [[] for _ in sets]
     work = [0] * len(sets)
+    got = [[] for _ in sets]
     errors = []
     barrier = threading.Barrier(len(sets) + 1)
 
@@ -713,8 +727,10 @@ def _run_streams(sets, paced: bool, jitter: float = 0.2, seed: int = 0, gate=Non
                         time.sleep(dt)
                 t1 = time.perf_counter()
                 h.push(data[p:p + NT])
-                h.poll(out=out)
+                r = h.poll(out=out)
                 lat[i].append(1e3 * (time.perf_counter() - t1))
+                if spikes is not None and len(r):
+                    got[i].append(r.copy())
                 work[i] += NT * data.shape[1]
                 p += NT
         except Exception as e:
@@ -732,7 +748,59 @@ def _run_streams(sets, paced: bool, jitter: float = 0.2, seed: int = 0, gate=Non
         h.close()
     if errors:
         raise RuntimeError(errors[0])
+    if spikes is not None:
+        from livespikesorter_gb300 import sorter as _s
+        spikes.extend(np.concatenate(g) if g else np.zeros(0, _s.SPIKE_DTYPE) for g in got)
     return lat, wall, work
+
+
+def run_chosen(a, dev):
+    """The headline of the metric: the chosen precision path against plain FP32 on eight concurrent
+    384-channel / 500-template probe streams of 1500-sample (50 ms) batches, one handle (CUDA stream)
+    and host thread each -- the reference's one-sorter-per-probe model (src/main.cpp:77-85) on one
+    GPU.  Paced at 30 kHz (+/-20 % jitter): per-batch push-to-spikes p50/p99.  Unpaced (every stream
+    pushes its next batch as soon as the last one's spikes are back): aggregate throughput of each
+    path, hence the times-real-time factor and the speed-up.  Spike agreement of the chosen path with
+    plain FP32 over every batch of the eight streams."""
+    streams = [(384, 500, NT)] * 8
+    sets = _serving_data(streams, a.chosen_seconds, seed0=200)
+    chosen = {"gemm_path": a.tier_path, "match_keep": a.tier_keep}
+    plain = {"gemm_path": 0, "match_keep": 0}
+    rt = 8 * 384 * 30000.0
+    with ClockSampler(dev) as clk:
+        lat_p, wall_p, work_p = _run_streams(sets, paced=True, opts=chosen)
+        sp_c, sp_f = [], []
+        lat_c, wall_c, work_c = _run_streams(sets, paced=False, opts=chosen, spikes=sp_c)
+        lat_f, wall_f, work_f = _run_streams(sets, paced=False, opts=plain, spikes=sp_f)
+    lp = np.concatenate([np.asarray(x) for x in lat_p])
+    n_ref = n_m = n_amp = 0
+    for f, c in zip(sp_f, sp_c):
+        frac, amp_ok = spike_agreement(f, c)
+        n_ref += len(f)
+        n_m += frac * len(f)
+        n_amp += amp_ok * frac * len(f)
+    rate_c, rate_f = sum(work_c) / wall_c, sum(work_f) / wall_f
+    batches = sum(len(x) for x in lat_c)
+    return {"path": {"gemm_path": a.tier_path, "match_keep": a.tier_keep, "proposal_gate": False},
+            "streams": "8 x (384 ch, 500 templates, 1500-sample batches = 50 ms), one handle + host thread each",
+            "paced": {"p50_ms": float(np.percentile(lp, 50)), "p99_ms": float(np.percentile(lp, 99)),
+                      "max_ms": float(lp.max()), "batches": int(lp.size), "batch_ms_of_signal": 1e3 * NT / 30000.0,
+                      "pacing": "30 kHz, +/-20 % jitter per batch"},
+            "unpaced": {"ch_samples_per_s": rate_c, "realtime_factor": rate_c / rt,
+                        "spikes_per_s": sum(len(x) for x in sp_c) / wall_c,
+                        "p50_ms": float(np.percentile(np.concatenate(lat_c), 50)),
+                        "p99_ms": float(np.percentile(np.concatenate(lat_c), 99))},
+            "plain_fp32_unpaced": {"ch_samples_per_s": rate_f, "realtime_factor": rate_f / rt,
+                                   "spikes_per_s": sum(len(x) for x in sp_f) / wall_f,
+                                   "p50_ms": float(np.percentile(np.concatenate(lat_f), 50)),
+                                   "p99_ms": float(np.percentile(np.concatenate(lat_f), 99))},
+            "speedup_vs_plain_fp32": rate_c / rate_f,
+            "agreement_vs_plain_fp32": {"batches": batches, "spikes_fp32": int(n_ref),
+                                        "spikes_chosen": int(sum(len(x) for x in sp_c)),
+                                        "matched": n_m / max(n_ref, 1), "amp_within_1e-3": n_amp / max(n_m, 1e-9),
+                                        "rule": "same template, |dt| <= 1 sample, amplitude within 1e-3 relative"},
+            "targets": {"realtime_factor": 10.0, "p99_ms": 5.0, "agreement": 0.995},
+            "clocks": clk.summary()}
 
 
 def run_serving(a):

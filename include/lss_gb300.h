@@ -67,7 +67,10 @@ typedef struct lss_params {
                                1 = best PC score 2 tF.mu - |mu|^2 among the clusters within cluster_radius_um of the
                                spike (OnlineKilosort.py:233-284; cluster_centroids_pca.npy [T_final, nC*K]), -1 if none */
     float cluster_radius_um;  /* radius of rule 1; 0 = 80 um (OnlineKilosort.py:449) */
-    int32_t reserved[1];
+    int32_t match_keep;     /* 0 = Kilosort's matching loop over every template (default); 1..32 = the pruned tier:
+                               per sample only the match_keep templates of largest initial Cf = relu(B)^2 / nm
+                               are scored through the loop (same updates on them, so the spikes equal the full
+                               loop's unless an unlisted template would have won; agreement measured) */
 } lss_params;
 
 /* One sorted spike.  time is the stream sample (Kilosort template_matching.py:68). */

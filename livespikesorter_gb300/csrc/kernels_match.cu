@@ -856,6 +856,11 @@ cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float*
         e = launch_match_cfg<8, false, kMatchThreads>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc,
                                                       out, s);
     if (e != cudaSuccess) return e;
+    return launch_residual(Xres, pre_wf, out, W, C, nt, nb, s);
+}
+
+cudaError_t launch_residual(float* Xres, const float* pre_wf, const MatchOut& out, int W, int C, int nt, int nb,
+                            cudaStream_t s) {
     dim3 grid((W + kResRows - 1) / kResRows, nb);
     const bool vec = (C & 3) == 0 && ((reinterpret_cast<uintptr_t>(Xres) | reinterpret_cast<uintptr_t>(pre_wf)) & 15) == 0;
     if (vec)

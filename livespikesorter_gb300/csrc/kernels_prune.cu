@@ -1,0 +1,426 @@
+// kernels_prune.cu -- the pruned matching tier: Kilosort's matching loop (template_matching.py:
+// 157-198) restricted, at every sample, to the keep templates with the largest initial
+// Cf = relu(B)^2 / nm.
+//
+// Kilosort scores every template at every sample in every iteration; almost all of those scores
+// stay far below the threshold for the whole loop.  Here a selection kernel keeps, per sample,
+// the templates that can plausibly win (the largest initial Cf; ties to the lower template id)
+// with their scores, and the loop runs on those lists only: the per-sample maximum reads keep
+// scores instead of T, and an accepted spike (w_s, t_s, amp) updates only the listed entries of
+// the 2nt+1 samples around it, gathering ctc[t][t_s][w - w_s + nt] for each listed t.  A listed
+// entry receives exactly the full loop's fmaf sequence (spikes applied in sample order), so the
+// result equals the full loop's unless a template that is not listed at a sample would have won
+// there after subtractions.
+//
+// Gathers: the templates listed at one sample are the ones that overlap the spikes near it, i.e.
+// spatial neighbours.  Templates are renumbered by their position along the probe (rank), the
+// lists hold ranks in ascending order, and the ctc copy of this tier is indexed
+// ctcQ[t_s][l][rank] -- so one warp, its lanes on the listed entries of one sample, reads a few
+// neighbouring cache lines of one row instead of one line per entry.
+//
+// Layouts (device):
+//   lrk   u16 [nb][W][KP]     listed ranks of sample w, ascending (KP = kPruneKeepMax slots, keep used)
+//   lsc   f32 [nb][W][KP]     their running scores (initial B on entry), updated in place
+//   ctcQ  f32 [T][2nt+1][T]   ctcQ[s][l][r] = ctc[order[r]][s][l]
+//   order u16 [T]             template of each rank; rank_of u16 [T] its inverse
+//
+// The loop kernel runs one CTA per window; the per-sample maxima and the ranks live in shared
+// memory when they fit (windows up to ~1700 samples at 32 entries), else in global memory; the
+// scores stay in global memory (L2) -- 64 windows of 1622 samples hold 13 MB.
+#include "lss_kernels.cuh"
+
+#include <cfloat>
+#include <climits>
+
+namespace lss {
+
+constexpr int kSelWarps = 8;
+constexpr int KP = kPruneKeepMax;   // list slots per sample (32: one per lane)
+
+// order-preserving key of a non-negative-or-padding float, inverted so the largest value has the
+// smallest key
+__device__ __forceinline__ uint32_t desc_key(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return ~((u & 0x80000000u) ? ~u : (u | 0x80000000u));
+}
+
+// One warp per sample: the keep templates of largest Cf (ties: lower id), written in ascending rank
+// order with their scores.  NJ = templates per lane (T <= 32 NJ); template t = lane + 32 j.
+// The keep-th largest Cf is found by an MSB-first bitwise selection over the warp's keys (one
+// ballot-count per bit, stopping once a single key matches the prefix); every key above it is
+// taken, then the ties at it in ascending template order until keep are taken.
+template <int NJ>
+__global__ void __launch_bounds__(kSelWarps * 32)
+prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, const uint16_t* __restrict__ rank_of,
+                    int nb, int W, int T, int keep, uint16_t* __restrict__ lrk, float* __restrict__ lsc) {
+    const int lane = threadIdx.x & 31;
+    const int64_t g = (int64_t)blockIdx.x * kSelWarps + (threadIdx.x >> 5);
+    if (g >= (int64_t)nb * W) return;
+    const float* row = Bt + g * T;
+    uint32_t key[NJ];
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+        const int t = lane + 32 * j;
+        if (t < T) {
+            const float r = fmaxf(row[t], 0.f);
+            key[j] = desc_key(r * r * (1.f / nm[t]));   // the loop's Cf, bit for bit
+        } else {
+            key[j] = 0xffffffffu;                         // after every real key (keep <= T)
+        }
+    }
+    // the (keep - 1)-th smallest key
+    uint32_t prefix = 0;
+    int k = keep - 1, alive = 32 * NJ;
+    for (int bit = 31; bit >= 0; --bit) {
+        const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
+        int cnt = 0;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) cnt += ((key[j] & hi_mask) == prefix) && !((key[j] >> bit) & 1u);
+        cnt = __reduce_add_sync(0xffffffffu, cnt);
+        if (k >= cnt) {
+            k -= cnt;
+            prefix |= (1u << bit);
+            alive -= cnt;
+        } else {
+            alive = cnt;
+        }
+        if (alive == 1) {
+            const uint32_t m = 0xffffffffu << bit;
+            uint32_t got = 0;
+#pragma unroll
+            for (int j = 0; j < NJ; ++j)
+                if ((key[j] & m) == prefix) got = key[j];
+            prefix = __reduce_or_sync(0xffffffffu, got);
+            break;
+        }
+    }
+    const uint32_t thr = prefix;
+    int below = 0;   // keys strictly before the threshold (larger Cf): all taken
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) below += key[j] < thr;
+    below = __reduce_add_sync(0xffffffffu, below);
+    int ties_left = keep - below;
+    // compaction of the taken templates into lanes 0..keep-1 (in template order)
+    int pos = 0, my_t = -1;
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+        const bool tie = key[j] == thr;
+        const unsigned tm = __ballot_sync(0xffffffffu, tie);
+        const bool take_tie = tie && __popc(tm & lt) < ties_left;
+        ties_left -= min(__popc(tm), max(ties_left, 0));
+        const bool take = key[j] < thr || take_tie;
+        const unsigned m = __ballot_sync(0xffffffffu, take);
+        // the taken entry with index lane - pos among this j's taken lanes goes to this lane
+        const int want = lane - pos;
+        if (want >= 0 && want < __popc(m)) {
+            unsigned mm = m;   // clear the lowest want set bits
+            for (int q = 0; q < want; ++q) mm &= mm - 1u;
+            my_t = __ffs(mm) - 1 + 32 * j;
+        }
+        pos += __popc(m);
+    }
+    // order the kept entries by rank: slot = number of kept ranks below this one
+    const int my_r = my_t >= 0 ? (int)rank_of[my_t] : INT_MAX;
+    int slot = 0;
+    for (int q = 0; q < keep; ++q) slot += __shfl_sync(0xffffffffu, my_r, q) < my_r;
+    if (lane < keep) {
+        const int64_t o = g * KP + slot;
+        lrk[o] = (uint16_t)my_r;
+        lsc[o] = row[my_t];
+    }
+}
+
+void launch_prune_select(const float* Bt, const float* nm, const uint16_t* rank_of, int nb, int W, int T, int keep,
+                         uint16_t* lrk, float* lsc, cudaStream_t s) {
+    const int64_t warps = (int64_t)nb * W;
+    const dim3 grid((unsigned)((warps + kSelWarps - 1) / kSelWarps));
+    const int nj = (T + 31) / 32;
+#define LSS_SEL(N) \
+    prune_select_kernel<N><<<grid, kSelWarps * 32, 0, s>>>(Bt, nm, rank_of, nb, W, T, keep, lrk, lsc)
+    if (nj <= 4) LSS_SEL(4);
+    else if (nj <= 8) LSS_SEL(8);
+    else if (nj <= 16) LSS_SEL(16);
+    else LSS_SEL(32);
+#undef LSS_SEL
+}
+
+// accepted spikes one iteration can hold: the (2nt+1) max pool admits one per nt + 1 samples,
+// twice that with exact ties
+__host__ __device__ inline int prune_iter_cap(int W, int nt) { return 2 * ((W + nt) / (nt + 1)) + 32; }
+
+// dynamic shared memory: [1/nm by rank: T f32][nm by rank: T f32][template by rank: T u16, to 16 B]
+// [unordered + sorted accepted lists: 2 x cap x 12 B, to 16 B], then the per-sample maxima
+// [W + 2nt] f32 and list slots [W] u8 when they fit, then the ranks [W][KP] u16 when they fit as well
+__host__ __device__ inline size_t prune_smem_head(int T) {
+    return (size_t)T * 8 + (((size_t)T * 2 + 15) & ~(size_t)15);
+}
+__host__ __device__ inline size_t prune_smem_fixed(int W, int T, int nt) {
+    return prune_smem_head(T) + ((2 * (size_t)prune_iter_cap(W, nt) * 12 + 15) & ~(size_t)15);
+}
+__host__ __device__ inline size_t prune_smem_cf(int W, int nt) {
+    return (((size_t)(W + 2 * nt) * 4 + (size_t)W) + 15) & ~(size_t)15;
+}
+__host__ __device__ inline size_t prune_smem_ranks(int W) { return (size_t)W * KP * 2; }
+
+constexpr int kItemsPerWarp = 4;   // samples a warp updates at once (independent gathers in flight)
+
+// One CTA per window.  Per iteration:
+//   B1  every sample whose own maximum exceeds Th^2 and equals the maximum over +-nt is accepted
+//       (Kilosort's rule, template_matching.py:172-173): the lanes screen 32 samples at once, then
+//       the warp takes each candidate's window; template and amplitude come from the list slot of
+//       the sample's maximum;
+//   B2  the iteration's spikes are ranked by sample and appended to the output lists;
+//   C   every sample within +-nt of a spike -- taken by the first spike (in sample order) whose
+//       range covers it -- applies each covering spike in sample order to its listed scores (a
+//       warp per sample, a lane per entry) and recomputes its maximum with a warp reduction.
+// mode bit 0: maxima and slots in shared memory (else cf_g / slot_g); bit 1: ranks in shared memory
+template <int NTHR>
+__global__ void __launch_bounds__(NTHR, 1)
+match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_g, int keep,
+                    const float* __restrict__ ctcQ, const uint16_t* __restrict__ order, const float* __restrict__ nm,
+                    float th2, int W, int T, int nt, int max_iters, int mode, float* __restrict__ cf_g,
+                    unsigned char* __restrict__ slot_g, MatchOut out) {
+    constexpr int kWarps = NTHR / 32;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int b = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int L2 = 2 * nt + 1;
+    const int cap_it = prune_iter_cap(W, nt);
+    float* s_inm = reinterpret_cast<float*>(smraw);                     // [T] by rank
+    float* s_nm = s_inm + T;                                            // [T] by rank
+    uint16_t* s_tid = reinterpret_cast<uint16_t*>(s_nm + T);            // [T] template of each rank
+    int* s_aw = reinterpret_cast<int*>(smraw + prune_smem_head(T));     // [cap] accepted, unordered
+    int* s_at = s_aw + cap_it;
+    float* s_aa = reinterpret_cast<float*>(s_at + cap_it);
+    int* s_sw = reinterpret_cast<int*>(s_aa + cap_it);                  // [cap] the same, by sample
+    int* s_st = s_sw + cap_it;
+    float* s_sa = reinterpret_cast<float*>(s_st + cap_it);
+    __shared__ int s_cnt, s_over;
+
+    // per-sample state: cfmax of w at cf[w + nt] (pads of nt at both ends) and the list slot of its
+    // maximum; the ranks RK[w][i]; the scores SC[w][i] (global)
+    unsigned char* next = smraw + prune_smem_fixed(W, T, nt);
+    float* cf;
+    unsigned char* slot;
+    if (mode & 1) {
+        cf = reinterpret_cast<float*>(next);
+        slot = reinterpret_cast<unsigned char*>(cf + (W + 2 * nt));
+        next += prune_smem_cf(W, nt);
+    } else {
+        cf = cf_g + (int64_t)b * (W + 2 * nt);
+        slot = slot_g + (int64_t)b * W;
+    }
+    const uint16_t* RK;
+    const uint16_t* rk_g = lrk_g + (int64_t)b * W * KP;
+    if (mode & 2) {
+        uint16_t* r = reinterpret_cast<uint16_t*>(next);
+        const uint4* src = reinterpret_cast<const uint4*>(rk_g);   // rows of KP u16 = 64 bytes
+        uint4* dst = reinterpret_cast<uint4*>(r);
+        for (int q = tid; q < W * KP / 8; q += NTHR) dst[q] = src[q];
+        RK = r;
+    } else {
+        RK = rk_g;
+    }
+    float* SC = lsc_g + (int64_t)b * W * KP;
+    for (int r = tid; r < T; r += NTHR) {
+        const int t = order[r];
+        s_tid[r] = (uint16_t)t;
+        s_nm[r] = nm[t];
+        s_inm[r] = 1.f / nm[t];
+    }
+    for (int i = tid; i < nt; i += NTHR) {
+        cf[i] = -FLT_MAX;
+        cf[W + nt + i] = -FLT_MAX;
+    }
+    if (tid == 0) {
+        s_cnt = 0;
+        s_over = 0;
+    }
+    __syncthreads();
+
+    // the warp's sample w, lane i holding entry i (score x, rank r): Cf maximum over the list
+    // (ties: lower template) into cf / slot
+    auto finish = [&](int w, float x, int r) {
+        float best = -1.f;
+        int bt = INT_MAX, bs = 0;
+        if (lane < keep) {
+            const float q = fmaxf(x, 0.f);
+            best = q * q * s_inm[r];
+            bt = s_tid[r];
+            bs = lane;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int ot = __shfl_xor_sync(0xffffffffu, bt, o);
+            const int os = __shfl_xor_sync(0xffffffffu, bs, o);
+            if (ob > best || (ob == best && ot < bt)) { best = ob; bt = ot; bs = os; }
+        }
+        if (lane == 0) {
+            const bool inner = w >= nt && w < W - nt;
+            cf[w + nt] = inner ? best : 0.f;
+            slot[w] = (unsigned char)bs;
+        }
+    };
+    for (int w = warp; w < W; w += kWarps) {
+        const int r = lane < keep ? RK[(size_t)w * KP + lane] : 0;
+        const float x = lane < keep ? SC[(size_t)w * KP + lane] : 0.f;
+        finish(w, x, r);
+    }
+    __syncthreads();
+
+    int n_total = 0, iters = 0;
+    int* sp_w = out.sp_w + (int64_t)b * out.cap;
+    int* sp_t = out.sp_t + (int64_t)b * out.cap;
+    float* sp_amp = out.sp_amp + (int64_t)b * out.cap;
+    int* sp_iter = out.sp_iter + (int64_t)b * out.cap;
+    for (int it = 0; it < max_iters; ++it) {
+        // ---- B1: acceptance ----
+        for (int w0 = warp * 32; w0 < W; w0 += kWarps * 32) {
+            const int wl = w0 + lane;
+            unsigned m = __ballot_sync(0xffffffffu, wl < W && cf[wl + nt] > th2);
+            while (m) {
+                const int w = w0 + __ffs(m) - 1;
+                m &= m - 1u;
+                float cm = -FLT_MAX;
+                for (int d = lane; d < L2; d += 32) cm = fmaxf(cm, cf[w + d]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) cm = fmaxf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
+                if (lane == 0 && cm > th2 && cf[w + nt] == cm) {
+                    const int i = slot[w];
+                    const int tt = s_tid[RK[(size_t)w * KP + i]];
+                    const float amp = SC[(size_t)w * KP + i] / nm[tt];
+                    const int q = atomicAdd(&s_cnt, 1);
+                    if (q < cap_it) {
+                        s_aw[q] = w;
+                        s_at[q] = tt;
+                        s_aa[q] = amp;
+                    } else {
+                        s_over = 1;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const int total = min(s_cnt, cap_it);
+        if (total == 0) break;
+        ++iters;
+        // ---- B2: rank by sample (samples are distinct), append to the output ----
+        for (int k = tid; k < total; k += NTHR) {
+            const int w = s_aw[k];
+            int r = 0;
+            for (int q = 0; q < total; ++q) r += s_aw[q] < w;
+            s_sw[r] = w;
+            s_st[r] = s_at[k];
+            s_sa[r] = s_aa[k];
+            const int o = n_total + r;
+            if (o < out.cap) {
+                sp_w[o] = w;
+                sp_t[o] = s_at[k];
+                sp_amp[o] = s_aa[k];
+                sp_iter[o] = it;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) s_cnt = 0;   // read again only after the barrier ending C
+        // ---- C: subtract the spikes from the listed scores of the samples near them ----
+        const int n_items = total * L2;
+        for (int q0 = warp * kItemsPerWarp; q0 < n_items; q0 += kWarps * kItemsPerWarp) {
+            int wv[kItemsPerWarp], kv[kItemsPerWarp], rv[kItemsPerWarp];
+            float xv[kItemsPerWarp], cv[kItemsPerWarp];
+#pragma unroll
+            for (int u = 0; u < kItemsPerWarp; ++u) {
+                const int q = q0 + u;
+                int w = -1, k = 0;
+                if (q < n_items) {
+                    k = q / L2;
+                    w = s_sw[k] - nt + (q - k * L2);
+                    // outside the window, or taken by an earlier spike's item
+                    if (w < 0 || w >= W || (k > 0 && w <= s_sw[k - 1] + nt)) w = -1;
+                }
+                wv[u] = w;
+                kv[u] = k;
+                rv[u] = 0;
+                xv[u] = 0.f;
+                if (w >= 0 && lane < keep) {
+                    rv[u] = RK[(size_t)w * KP + lane];
+                    xv[u] = SC[(size_t)w * KP + lane];
+                }
+            }
+            // the owning spike's ctc entries, all items' loads in flight together
+#pragma unroll
+            for (int u = 0; u < kItemsPerWarp; ++u) {
+                cv[u] = 0.f;
+                if (wv[u] >= 0 && lane < keep)
+                    cv[u] = __ldg(ctcQ + ((int64_t)s_st[kv[u]] * L2 + (wv[u] - s_sw[kv[u]] + nt)) * T + rv[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < kItemsPerWarp; ++u) {
+                const int w = wv[u];
+                if (w < 0) continue;   // warp-uniform
+                float x = fmaf(-s_sa[kv[u]], cv[u], xv[u]);
+                // any further spike covering the same sample, in sample order
+                for (int kk = kv[u] + 1; kk < total && s_sw[kk] - nt <= w; ++kk) {
+                    const float c = lane < keep
+                                        ? __ldg(ctcQ + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u])
+                                        : 0.f;
+                    x = fmaf(-s_sa[kk], c, x);
+                }
+                if (lane < keep) SC[(size_t)w * KP + lane] = x;
+                finish(w, x, rv[u]);
+            }
+        }
+        n_total += total;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        out.n_spikes[b] = n_total;
+        out.n_iters[b] = iters;
+        if (n_total > out.cap || s_over) atomicOr(out.status + b, 1);
+    }
+}
+
+static int g_prune_smem_max = -1;
+
+static int prune_smem_max() {
+    if (g_prune_smem_max < 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+            cudaGetLastError();
+            v = 0;
+        }
+        g_prune_smem_max = v;
+    }
+    return g_prune_smem_max;
+}
+
+// where the per-sample state of a window goes: bit 0 = maxima and slots in shared memory, bit 1 =
+// the ranks too; -1 = the fixed part alone does not fit
+int prune_mode(int W, int T, int nt) {
+    const size_t lim = (size_t)prune_smem_max();
+    const size_t f = prune_smem_fixed(W, T, nt) + 1024;
+    if (f > lim) return -1;
+    const size_t c = prune_smem_cf(W, nt);
+    if (f + c > lim) return 0;
+    return f + c + prune_smem_ranks(W) <= lim ? 3 : 1;
+}
+
+cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcQ, const uint16_t* order,
+                                const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
+                                float* cf_scratch, unsigned char* slot_scratch, const MatchOut& out, cudaStream_t s) {
+    if (keep < 1 || keep > KP || keep > T || T > 1024) return cudaErrorInvalidValue;
+    const int mode = prune_mode(W, T, nt);
+    if (mode < 0 || (!(mode & 1) && (!cf_scratch || !slot_scratch))) return cudaErrorInvalidValue;
+    const size_t smem =
+        prune_smem_fixed(W, T, nt) + ((mode & 1) ? prune_smem_cf(W, nt) : 0) + ((mode & 2) ? prune_smem_ranks(W) : 0);
+    auto kern = match_pruned_kernel<kPruneThreads>;
+    cudaError_t e = raise_smem_limit((const void*)kern, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nb, kPruneThreads, smem, s>>>(lrk, lsc, keep, ctcQ, order, nm, th2, W, T, nt, max_iters, mode, cf_scratch,
+                                         slot_scratch, out);
+    return cudaGetLastError();
+}
+
+}  // namespace lss

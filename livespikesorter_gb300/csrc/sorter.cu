@@ -215,6 +215,16 @@ struct Handle {
     std::vector<int64_t> last_kept;     // per final cluster: last kept spike time (duplicate removal)
     std::vector<char> has_kept;
     PropGate* gate = nullptr;           // learned proposal gate (lss_set_proposal), off when null
+    // pruned matching tier (match_keep > 0): templates renumbered by probe position (rank), ctc with
+    // its target axis in rank order, per-sample lists of ranks and scores
+    int keep = 0;
+    float* d_ctc = nullptr;             // ctcQ [T][2nt+1][T]: ctcQ[s][l][r] = ctc[order[r]][s][l]
+    uint16_t* d_order = nullptr;        // [T] template of each rank
+    uint16_t* d_rank = nullptr;         // [T] rank of each template
+    uint16_t* d_lid = nullptr;          // [nb][W][kPruneKeepMax] ranks
+    float* d_lsc = nullptr;             // [nb][W][kPruneKeepMax] scores
+    float* d_pcf = nullptr;             // [nb][W + 2nt] per-sample maxima of windows too long for shared memory
+    unsigned char* d_pslot = nullptr;   // [nb][W]
 
     ~Handle();
     void init(const char* dir, const lss_params* prm);
@@ -236,6 +246,7 @@ struct Handle {
     void stage_to_device(Slot& s, int64_t upto);
     void run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
                               const std::function<void()>& mark);
+    void run_match(int nb, int Wn, int64_t& nl);
 };
 
 Handle::~Handle() {
@@ -254,7 +265,7 @@ Handle::~Handle() {
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
                     (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo,
-                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm})
+                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm, (void*)d_ctc, (void*)d_order, (void*)d_rank})
         if (p) cudaFree(p);
     if (h_gemm_err) cudaFreeHost(h_gemm_err);
     for (auto& s : slots) {
@@ -287,7 +298,7 @@ void Handle::free_work() {
     }
     for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_ticket, (void*)d_mean, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
                     (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo, (void*)d_Zt_hi, (void*)d_Zt_lo,
-                    (void*)d_split,
+                    (void*)d_split, (void*)d_lid, (void*)d_lsc, (void*)d_pcf, (void*)d_pslot,
                     (void*)sc.cfmax, (void*)sc.at_t, (void*)sc.at_amp, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
                     (void*)mo.sp_t, (void*)mo.sp_amp, (void*)mo.sp_iter})
         if (p) cudaFree(p);
@@ -300,6 +311,10 @@ void Handle::free_work() {
     d_Xt_hi = d_Xt_lo = nullptr;
     d_Zt_hi = d_Zt_lo = nullptr;
     d_split = nullptr;
+    d_lid = nullptr;
+    d_lsc = nullptr;
+    d_pcf = nullptr;
+    d_pslot = nullptr;
     sc = MatchScratch{};
     mo = MatchOut{};
     dev_bytes -= work_bytes;
@@ -458,6 +473,45 @@ void Handle::init(const char* dir, const lss_params* prm) {
         LSS_CUDA(cudaGetLastError());
         LSS_CUDA(cudaStreamSynchronize(st));
     }
+    if (p.match_keep < 0 || p.match_keep > kPruneKeepMax)
+        throw LoadError{LSS_ERR_ARG, "lss_params.match_keep must be 0 (full loop) or 1.." + std::to_string(kPruneKeepMax)};
+    keep = std::min(p.match_keep, T);
+    if (keep > 0) {
+        if (T > 1024) throw LoadError{LSS_ERR_ARG, "the pruned matching tier takes at most 1024 templates"};
+        // rank = position along the probe: the energy-weighted (y, x) centre of each template
+        std::vector<double> cy(T), cx(T);
+        for (int t = 0; t < T; ++t) {
+            double e = 0.0, sy = 0.0, sx = 0.0;
+            for (int c = 0; c < C; ++c) {
+                double ec = 0.0;
+                for (int k = 0; k < K; ++k) {
+                    const double v = m.Wall3[((size_t)t * K + k) * C + c];
+                    ec += v * v;
+                }
+                e += ec;
+                sy += ec * m.yc[c];
+                sx += ec * m.xc[c];
+            }
+            cy[t] = e > 0.0 ? sy / e : 0.0;
+            cx[t] = e > 0.0 ? sx / e : 0.0;
+        }
+        std::vector<uint16_t> order(T), rank(T);
+        for (int t = 0; t < T; ++t) order[t] = (uint16_t)t;
+        std::stable_sort(order.begin(), order.end(), [&](uint16_t a, uint16_t b) {
+            return cy[a] < cy[b] || (cy[a] == cy[b] && cx[a] < cx[b]);
+        });
+        for (int r = 0; r < T; ++r) rank[order[r]] = (uint16_t)r;
+        std::vector<float> q((size_t)T * L2 * T);
+        for (int t = 0; t < T; ++t)
+            for (int s = 0; s < T; ++s) {
+                const float* src = &m.ctc[((size_t)t * T + s) * L2];
+                for (int l = 0; l < L2; ++l) q[((size_t)s * L2 + l) * T + rank[t]] = src[l];
+            }
+        d_ctc = dev_upload(q, dev_bytes, st);
+        d_order = dev_upload(order, dev_bytes, st);
+        d_rank = dev_upload(rank, dev_bytes, st);
+        LSS_CUDA(cudaStreamSynchronize(st));
+    }
     LSS_CUDA(cudaHostAlloc((void**)&h_gemm_err, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable));
     *h_gemm_err = 0;
     LSS_CUDA(cudaHostGetDevicePointer((void**)&d_gemm_err, h_gemm_err, 0));
@@ -545,7 +599,8 @@ void Handle::ensure_work(int Wn, int nb) {
                          (int64_t)nba * Wa * C * 4 * (tc_whiten && !tf32_data ? 1 : 0) +
                          (int64_t)nba * ((Wa + 7) / 8 * 8) * C * 4 * (tc_conv ? (tf32_data ? 1 : 2) : 0) +
                          (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16 +
-                         (tc_project ? (int64_t)kSplitK * std::min(nba, kSplitBatches) * Wa * T * 4 : 0);
+                         (tc_project ? (int64_t)kSplitK * std::min(nba, kSplitBatches) * Wa * T * 4 : 0) +
+                         (keep > 0 ? (int64_t)nba * Wa * kPruneKeepMax * 6 + (int64_t)nba * (Wa + 2 * nt) * 5 : 0);
     if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
         throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
                                            " device bytes, budget " + std::to_string(p.mem_budget)};
@@ -583,6 +638,16 @@ void Handle::ensure_work(int Wn, int nb) {
     sc.cfmax = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
     sc.at_t = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
     sc.at_amp = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
+    if (keep > 0) {
+        d_lid = dev_alloc<uint16_t>((size_t)nba * Wa * kPruneKeepMax, dev_bytes);
+        d_lsc = dev_alloc<float>((size_t)nba * Wa * kPruneKeepMax, dev_bytes);
+        const int pm = prune_mode(Wa, T, nt);
+        if (pm < 0) throw LoadError{LSS_ERR_ARG, "window too long for the pruned matching tier"};
+        if (!(pm & 1)) {
+            d_pcf = dev_alloc<float>((size_t)nba * (Wa + 2 * nt), dev_bytes);
+            d_pslot = dev_alloc<unsigned char>((size_t)nba * Wa, dev_bytes);
+        }
+    }
     mo.n_spikes = dev_alloc<int>(nba, dev_bytes);
     mo.n_iters = dev_alloc<int>(nba, dev_bytes);
     mo.status = dev_alloc<int>(nba, dev_bytes);
@@ -737,10 +802,7 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     int64_t nl = 0;
     run_stages_to_scores(raw, nb, Wn, NTs, ts, nl, mark);
     if (gate) nl += prop_gate_run(gate, d_Z, d_Bt, nb, Wn, nt, st);
-    LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
-    LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st,
-                          p.match_variant));
-    nl += 2;   // the loop and the residual
+    run_match(nb, Wn, nl);
     mark();
     launch_rec_offsets(mo, nb, s.d_off, st), ++nl;
     launch_features(d_Z, mo, nb, Wn, C, T, K, nt, nC, d_wPCA, d_iCC, d_iU, d_Ucc, d_xc, d_yc, d_cent, Tf, d_cpca,
@@ -755,6 +817,25 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     s.nb = nb;
     s.W = Wn;
     launches_last += nl;
+}
+
+// The matching loop of nb windows on d_Bt (scores) and d_Z (becomes the residual): Kilosort's loop
+// over every template, or the pruned tier (per-sample lists of the keep best templates, then the
+// loop on them); the residual follows either way.
+void Handle::run_match(int nb, int Wn, int64_t& nl) {
+    LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
+    if (keep > 0) {
+        launch_prune_select(d_Bt, d_nm, d_rank, nb, Wn, T, keep, d_lid, d_lsc, st);
+        LSS_CUDA(cudaGetLastError());
+        LSS_CUDA(launch_match_pruned(d_lid, d_lsc, keep, d_ctc, d_order, d_nm, th * th, Wn, T, nt, max_iters, nb,
+                                     d_pcf, d_pslot, mo, st));
+        LSS_CUDA(launch_residual(d_Z, d_pre_wf, mo, Wn, C, nt, nb, st));
+        nl += 3;   // selection, loop, residual
+    } else {
+        LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st,
+                              p.match_variant));
+        nl += 2;   // the loop and the residual
+    }
 }
 
 void Handle::push_device(const int16_t* rows, int64_t n_batches, int64_t first_row_sample) {
@@ -1070,6 +1151,7 @@ int lss_default_params(lss_params* p) {
     p->gemm_path = 0;
     p->cluster_rule = 0;
     p->cluster_radius_um = 0.f;
+    p->match_keep = 0;
     return LSS_OK;
 }
 
@@ -1284,9 +1366,7 @@ int lss_debug_stage(lss_handle* hp, const int16_t* window, int32_t W, int32_t st
             if (stage == LSS_STAGE_SCORES) {
                 LSS_CUDA(cudaMemcpyAsync(out, h.d_Bt, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
             } else {
-                LSS_CUDA(cudaMemsetAsync(h.mo.status, 0, sizeof(int), st));
-                LSS_CUDA(lss::launch_match(h.d_Bt, h.d_Z, h.d_ctcP, h.d_pre_wf, h.d_nm, h.th * h.th, W, h.T, h.C, h.nt,
-                                           h.max_iters, 1, h.sc, h.mo, st, h.p.match_variant));
+                h.run_match(1, W, nl);
                 LSS_CUDA(cudaMemcpyAsync(out, h.d_Z, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
             }
         }

@@ -32,7 +32,7 @@ class Params(ct.Structure):
                 ("hp_half_taps", ct.c_int32), ("dedup", ct.c_int32), ("th_override", ct.c_float),
                 ("spike_cap", ct.c_int32), ("mem_budget", ct.c_int64), ("profile", ct.c_int32),
                 ("match_variant", ct.c_int32), ("gemm_path", ct.c_int32), ("cluster_rule", ct.c_int32),
-                ("cluster_radius_um", ct.c_float), ("reserved", ct.c_int32 * 1)]
+                ("cluster_radius_um", ct.c_float), ("match_keep", ct.c_int32)]
 
 
 class Spike(ct.Structure):

@@ -63,8 +63,10 @@ def project_rounded(U2, Bpc2, fmt: str):
     return (r * (round_fp8(U2 / r, fmt) * s.T)) @ round_fp8(Bpc2 / s, fmt)
 
 
-def run_matching_variant(X, U, W, ctc, Th, fmt="exact", rescore=False, keep=None, max_iters=50):
-    """-> (st [S, 2] (sample, template), amps [S]).  See the module docstring."""
+def run_matching_variant(X, U, W, ctc, Th, fmt="exact", rescore=False, keep=None, max_iters=50, block=1):
+    """-> (st [S, 2] (sample, template), amps [S]).  See the module docstring.  block > 1: one list
+    per block of that many consecutive samples (from sample 0), the keep templates of largest Cq
+    maximum over the block's samples, scored at every sample of the block."""
     U = np.asarray(U, np.float64)
     ctc = np.asarray(ctc, np.float64)
     nt = W.shape[1]
@@ -75,8 +77,16 @@ def run_matching_variant(X, U, W, ctc, Th, fmt="exact", rescore=False, keep=None
     if keep is not None:
         Cq = np.maximum(B0q, 0) ** 2 / nm[:, None]
         mask = np.zeros(B0e.shape, bool)
-        top = np.argpartition(-Cq, min(keep, len(nm)) - 1, axis=0)[:keep]
-        mask[top, np.arange(B0e.shape[1])[None, :]] = True
+        if block > 1:
+            nw = Cq.shape[1]
+            for w0 in range(0, nw, block):
+                bm = Cq[:, w0:w0 + block].max(1)
+                top = np.argsort(-bm, kind="stable")[:keep]
+                mask[np.ix_(top, np.arange(w0, min(nw, w0 + block)))] = True
+        else:
+            # the keep largest per sample, ties to the lower template (a stable sort of -Cq)
+            top = np.argsort(-Cq, axis=0, kind="stable")[:keep]
+            mask[top, np.arange(B0e.shape[1])[None, :]] = True
         B, D = np.where(mask, B0e, -1e30), None
     else:
         B, D = B0q.copy(), B0e - B0q

@@ -114,12 +114,6 @@ def test_stream_chunking_is_invisible(golden_dir, tmp_path):
 
 
 # ---------------------------------------------------------------- seeded configs vs the oracle
-@pytest.fixture(scope="module")
-def cfg_small(tmp_path_factory):
-    """96 channels, 64 units, one 60000-sample batch (+2*61)."""
-    return make_dataset(synth.config_small(seed=11), tmp_path_factory.mktemp("cfg1"))
-
-
 def test_config_small_one_batch(cfg_small):
     d, data, _ = cfg_small
     oss = ko.load_oss_input(d)
@@ -205,14 +199,6 @@ def test_ragged_shapes_scalar_paths(tmp_path):
     _rel_close(xres.T.astype(np.float64), r.match.Xres, 5e-5)
 
 
-@pytest.fixture(scope="module")
-def cfg_stream(tmp_path_factory):
-    """384 channels, 500 templates, 6 batches of 1500 new samples with a rigid drift."""
-    cfg = synth.SynthConfig(n_chan=384, n_units=500, n_samples=6 * 1500 + 300, drift_um=20.0,
-                            whiten_batch=3000, whiten_batches=3, seed=5)
-    return make_dataset(cfg, tmp_path_factory.mktemp("cfg2"))
-
-
 def test_config_stream_384ch(cfg_stream):
     d, data, _ = cfg_stream
     oss = ko.load_oss_input(d)
@@ -223,15 +209,6 @@ def test_config_stream_384ch(cfg_stream):
     a, amp_ok, amax = agreement(ref["time"][k], ref["template"][k], ref["amp"][k], sp["time"], sp["tmpl"], sp["amp"])
     assert k.sum() > 300
     assert a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax, len(sp), int(k.sum()))
-
-
-@pytest.fixture(scope="module")
-def cfg_dense(tmp_path_factory):
-    """The dense shape at oracle-friendly size: 128 channels, 200 units firing at 30 Hz with 30 %
-    of the spikes forced to overlap a neighbour unit's within 1 ms, one 12000-sample batch."""
-    cfg = synth.SynthConfig(n_chan=128, n_units=200, n_samples=12000 + 122, rate_hz=30.0, overlap_frac=0.3,
-                            whiten_batch=4000, whiten_batches=3, seed=21)
-    return make_dataset(cfg, tmp_path_factory.mktemp("cfg3s"))
 
 
 def test_config_dense_overlapping(cfg_dense):
