@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define LSS_ABI_VERSION 1
+#define LSS_ABI_VERSION 2
 #define LSS_MAX_PCFEAT 64 /* nearest channels x PCs carried per spike */
 
 enum lss_status {
@@ -71,6 +71,11 @@ typedef struct lss_params {
                                per sample only the match_keep templates of largest initial Cf = relu(B)^2 / nm
                                are scored through the loop (same updates on them, so the spikes equal the full
                                loop's unless an unlisted template would have won; agreement measured) */
+    float ctc_rel_eps;      /* a spike of template s is subtracted from the scores of the templates whose ctc with s
+                               reaches ctc_rel_eps of the largest |ctc[.][s][.]| (their range, in the sorter's
+                               internal numbering by probe position); the others' updates are below that fraction.
+                               Default 1e-6; 0 = every template (Kilosort's dense subtraction) */
+    int32_t reserved[1];
 } lss_params;
 
 /* One sorted spike.  time is the stream sample (Kilosort template_matching.py:68). */

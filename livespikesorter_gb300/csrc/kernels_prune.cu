@@ -12,17 +12,15 @@
 // result equals the full loop's unless a template that is not listed at a sample would have won
 // there after subtractions.
 //
-// Gathers: the templates listed at one sample are the ones that overlap the spikes near it, i.e.
-// spatial neighbours.  Templates are renumbered by their position along the probe (rank), the
-// lists hold ranks in ascending order, and the ctc copy of this tier is indexed
-// ctcQ[t_s][l][rank] -- so one warp, its lanes on the listed entries of one sample, reads a few
-// neighbouring cache lines of one row instead of one line per entry.
+// Template numbers are the sorter's internal ones (by position along the probe), so the templates
+// listed at one sample -- the ones overlapping the spikes near it -- have nearby numbers, and one
+// warp (its lanes on the listed entries of one sample) reads a few neighbouring cache lines of one
+// row of ctcP instead of one line per entry.
 //
 // Layouts (device):
-//   lrk   u16 [nb][W][KP]     listed ranks of sample w, ascending (KP = kPruneKeepMax slots, keep used)
+//   lrk   u16 [nb][W][KP]     listed templates of sample w, ascending (KP = kPruneKeepMax slots, keep used)
 //   lsc   f32 [nb][W][KP]     their running scores (initial B on entry), updated in place
-//   ctcQ  f32 [T][2nt+1][T]   ctcQ[s][l][r] = ctc[order[r]][s][l]
-//   order u16 [T]             template of each rank; rank_of u16 [T] its inverse
+//   ctcP  f32 [T][2nt+1][T]   ctcP[s][l][t] = ctc[t][s][l]
 //
 // The loop kernel runs one CTA per window; the per-sample maxima and the ranks live in shared
 // memory when they fit (windows up to ~1700 samples at 32 entries), else in global memory; the
@@ -44,15 +42,15 @@ __device__ __forceinline__ uint32_t desc_key(float f) {
     return ~((u & 0x80000000u) ? ~u : (u | 0x80000000u));
 }
 
-// One warp per sample: the keep templates of largest Cf (ties: lower id), written in ascending rank
+// One warp per sample: the keep templates of largest Cf (ties: lower id), written in ascending
 // order with their scores.  NJ = templates per lane (T <= 32 NJ); template t = lane + 32 j.
 // The keep-th largest Cf is found by an MSB-first bitwise selection over the warp's keys (one
 // ballot-count per bit, stopping once a single key matches the prefix); every key above it is
 // taken, then the ties at it in ascending template order until keep are taken.
 template <int NJ>
 __global__ void __launch_bounds__(kSelWarps * 32)
-prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, const uint16_t* __restrict__ rank_of,
-                    int nb, int W, int T, int keep, uint16_t* __restrict__ lrk, float* __restrict__ lsc) {
+prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, int nb, int W, int T, int keep,
+                    uint16_t* __restrict__ lrk, float* __restrict__ lsc) {
     const int lane = threadIdx.x & 31;
     const int64_t g = (int64_t)blockIdx.x * kSelWarps + (threadIdx.x >> 5);
     if (g >= (int64_t)nb * W) return;
@@ -100,7 +98,7 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
     for (int j = 0; j < NJ; ++j) below += key[j] < thr;
     below = __reduce_add_sync(0xffffffffu, below);
     int ties_left = keep - below;
-    // compaction of the taken templates into lanes 0..keep-1 (in template order)
+    // compaction of the taken templates into lanes 0..keep-1, in template order
     int pos = 0, my_t = -1;
     const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
@@ -120,24 +118,20 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
         }
         pos += __popc(m);
     }
-    // order the kept entries by rank: slot = number of kept ranks below this one
-    const int my_r = my_t >= 0 ? (int)rank_of[my_t] : INT_MAX;
-    int slot = 0;
-    for (int q = 0; q < keep; ++q) slot += __shfl_sync(0xffffffffu, my_r, q) < my_r;
     if (lane < keep) {
-        const int64_t o = g * KP + slot;
-        lrk[o] = (uint16_t)my_r;
+        const int64_t o = g * KP + lane;
+        lrk[o] = (uint16_t)my_t;
         lsc[o] = row[my_t];
     }
 }
 
-void launch_prune_select(const float* Bt, const float* nm, const uint16_t* rank_of, int nb, int W, int T, int keep,
-                         uint16_t* lrk, float* lsc, cudaStream_t s) {
+void launch_prune_select(const float* Bt, const float* nm, int nb, int W, int T, int keep, uint16_t* lrk, float* lsc,
+                         cudaStream_t s) {
     const int64_t warps = (int64_t)nb * W;
     const dim3 grid((unsigned)((warps + kSelWarps - 1) / kSelWarps));
     const int nj = (T + 31) / 32;
 #define LSS_SEL(N) \
-    prune_select_kernel<N><<<grid, kSelWarps * 32, 0, s>>>(Bt, nm, rank_of, nb, W, T, keep, lrk, lsc)
+    prune_select_kernel<N><<<grid, kSelWarps * 32, 0, s>>>(Bt, nm, nb, W, T, keep, lrk, lsc)
     if (nj <= 4) LSS_SEL(4);
     else if (nj <= 8) LSS_SEL(8);
     else if (nj <= 16) LSS_SEL(16);
@@ -149,12 +143,10 @@ void launch_prune_select(const float* Bt, const float* nm, const uint16_t* rank_
 // twice that with exact ties
 __host__ __device__ inline int prune_iter_cap(int W, int nt) { return 2 * ((W + nt) / (nt + 1)) + 32; }
 
-// dynamic shared memory: [1/nm by rank: T f32][nm by rank: T f32][template by rank: T u16, to 16 B]
-// [unordered + sorted accepted lists: 2 x cap x 12 B, to 16 B], then the per-sample maxima
-// [W + 2nt] f32 and list slots [W] u8 when they fit, then the ranks [W][KP] u16 when they fit as well
-__host__ __device__ inline size_t prune_smem_head(int T) {
-    return (size_t)T * 8 + (((size_t)T * 2 + 15) & ~(size_t)15);
-}
+// dynamic shared memory: [1/nm: T f32][nm: T f32][unordered + sorted accepted lists: 2 x cap x 12 B,
+// to 16 B], then the per-sample maxima [W + 2nt] f32 and list slots [W] u8 when they fit, then the
+// listed templates [W][KP] u16 when they fit as well
+__host__ __device__ inline size_t prune_smem_head(int T) { return ((size_t)T * 8 + 15) & ~(size_t)15; }
 __host__ __device__ inline size_t prune_smem_fixed(int W, int T, int nt) {
     return prune_smem_head(T) + ((2 * (size_t)prune_iter_cap(W, nt) * 12 + 15) & ~(size_t)15);
 }
@@ -174,22 +166,22 @@ constexpr int kItemsPerWarp = 4;   // samples a warp updates at once (independen
 //   C   every sample within +-nt of a spike -- taken by the first spike (in sample order) whose
 //       range covers it -- applies each covering spike in sample order to its listed scores (a
 //       warp per sample, a lane per entry) and recomputes its maximum with a warp reduction.
-// mode bit 0: maxima and slots in shared memory (else cf_g / slot_g); bit 1: ranks in shared memory
+// mode bit 0: maxima and slots in shared memory (else cf_g / slot_g); bit 1: listed templates in
+// shared memory
 template <int NTHR>
 __global__ void __launch_bounds__(NTHR, 1)
 match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_g, int keep,
-                    const float* __restrict__ ctcQ, const uint16_t* __restrict__ order, const float* __restrict__ nm,
-                    float th2, int W, int T, int nt, int max_iters, int mode, float* __restrict__ cf_g,
-                    unsigned char* __restrict__ slot_g, MatchOut out) {
+                    const float* __restrict__ ctcP, const float* __restrict__ nm, float th2, int W, int T, int nt,
+                    int max_iters, int mode, float* __restrict__ cf_g, unsigned char* __restrict__ slot_g,
+                    MatchOut out) {
     constexpr int kWarps = NTHR / 32;
     extern __shared__ __align__(16) unsigned char smraw[];
     const int b = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int L2 = 2 * nt + 1;
     const int cap_it = prune_iter_cap(W, nt);
-    float* s_inm = reinterpret_cast<float*>(smraw);                     // [T] by rank
-    float* s_nm = s_inm + T;                                            // [T] by rank
-    uint16_t* s_tid = reinterpret_cast<uint16_t*>(s_nm + T);            // [T] template of each rank
+    float* s_inm = reinterpret_cast<float*>(smraw);                     // [T]
+    float* s_nm = s_inm + T;                                            // [T]
     int* s_aw = reinterpret_cast<int*>(smraw + prune_smem_head(T));     // [cap] accepted, unordered
     int* s_at = s_aw + cap_it;
     float* s_aa = reinterpret_cast<float*>(s_at + cap_it);
@@ -223,11 +215,9 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
         RK = rk_g;
     }
     float* SC = lsc_g + (int64_t)b * W * KP;
-    for (int r = tid; r < T; r += NTHR) {
-        const int t = order[r];
-        s_tid[r] = (uint16_t)t;
-        s_nm[r] = nm[t];
-        s_inm[r] = 1.f / nm[t];
+    for (int t = tid; t < T; t += NTHR) {
+        s_nm[t] = nm[t];
+        s_inm[t] = 1.f / nm[t];
     }
     for (int i = tid; i < nt; i += NTHR) {
         cf[i] = -FLT_MAX;
@@ -239,7 +229,7 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
     }
     __syncthreads();
 
-    // the warp's sample w, lane i holding entry i (score x, rank r): Cf maximum over the list
+    // the warp's sample w, lane i holding entry i (score x, template r): Cf maximum over the list
     // (ties: lower template) into cf / slot
     auto finish = [&](int w, float x, int r) {
         float best = -1.f;
@@ -247,7 +237,7 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
         if (lane < keep) {
             const float q = fmaxf(x, 0.f);
             best = q * q * s_inm[r];
-            bt = s_tid[r];
+            bt = r;
             bs = lane;
         }
 #pragma unroll
@@ -289,8 +279,8 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
                 for (int o = 16; o > 0; o >>= 1) cm = fmaxf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
                 if (lane == 0 && cm > th2 && cf[w + nt] == cm) {
                     const int i = slot[w];
-                    const int tt = s_tid[RK[(size_t)w * KP + i]];
-                    const float amp = SC[(size_t)w * KP + i] / nm[tt];
+                    const int tt = RK[(size_t)w * KP + i];
+                    const float amp = SC[(size_t)w * KP + i] / s_nm[tt];
                     const int q = atomicAdd(&s_cnt, 1);
                     if (q < cap_it) {
                         s_aw[q] = w;
@@ -353,7 +343,7 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
             for (int u = 0; u < kItemsPerWarp; ++u) {
                 cv[u] = 0.f;
                 if (wv[u] >= 0 && lane < keep)
-                    cv[u] = __ldg(ctcQ + ((int64_t)s_st[kv[u]] * L2 + (wv[u] - s_sw[kv[u]] + nt)) * T + rv[u]);
+                    cv[u] = __ldg(ctcP + ((int64_t)s_st[kv[u]] * L2 + (wv[u] - s_sw[kv[u]] + nt)) * T + rv[u]);
             }
 #pragma unroll
             for (int u = 0; u < kItemsPerWarp; ++u) {
@@ -363,7 +353,7 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
                 // any further spike covering the same sample, in sample order
                 for (int kk = kv[u] + 1; kk < total && s_sw[kk] - nt <= w; ++kk) {
                     const float c = lane < keep
-                                        ? __ldg(ctcQ + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u])
+                                        ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u])
                                         : 0.f;
                     x = fmaf(-s_sa[kk], c, x);
                 }
@@ -407,9 +397,9 @@ int prune_mode(int W, int T, int nt) {
     return f + c + prune_smem_ranks(W) <= lim ? 3 : 1;
 }
 
-cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcQ, const uint16_t* order,
-                                const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
-                                float* cf_scratch, unsigned char* slot_scratch, const MatchOut& out, cudaStream_t s) {
+cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcP, const float* nm,
+                                float th2, int W, int T, int nt, int max_iters, int nb, float* cf_scratch,
+                                unsigned char* slot_scratch, const MatchOut& out, cudaStream_t s) {
     if (keep < 1 || keep > KP || keep > T || T > 1024) return cudaErrorInvalidValue;
     const int mode = prune_mode(W, T, nt);
     if (mode < 0 || (!(mode & 1) && (!cf_scratch || !slot_scratch))) return cudaErrorInvalidValue;
@@ -418,7 +408,7 @@ cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const
     auto kern = match_pruned_kernel<kPruneThreads>;
     cudaError_t e = raise_smem_limit((const void*)kern, smem);
     if (e != cudaSuccess) return e;
-    kern<<<nb, kPruneThreads, smem, s>>>(lrk, lsc, keep, ctcQ, order, nm, th2, W, T, nt, max_iters, mode, cf_scratch,
+    kern<<<nb, kPruneThreads, smem, s>>>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, mode, cf_scratch,
                                          slot_scratch, out);
     return cudaGetLastError();
 }

@@ -24,6 +24,7 @@ cudaError_t raise_smem_limit(const void* kernel, size_t bytes) {
     if (bytes <= cur) return cudaSuccess;
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) cur = bytes;
+    else cudaGetLastError();   // a refused size is reported here, not to the caller's next check
     return e;
 }
 

@@ -131,29 +131,30 @@ void conv_tc_free(ConvOperands* u);
 // out_hi / out_lo viewed as bf16 arrays
 cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* out_lo, bool hi_only, int nb, int C,
                                    int W, int* err, cudaStream_t s, bool out_bf16 = false);
+// crange [T] (may be null = every template): per spike template, the float4 range [x, y) of the
+// score rows a spike of it updates, in whole 32-template segments
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                          float th2, int W, int T, int C, int nt, int max_iters, int nb,
-                         const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0);
+                         const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0,
+                         const int2* crange = nullptr);
 // the residual after a matching loop: Xres[w][:] -= amp * waveform[t][w - w_s + nt/2][:] for the
 // spikes of out, in list order
 cudaError_t launch_residual(float* Xres, const float* pre_wf, const MatchOut& out, int W, int C, int nt, int nb,
                             cudaStream_t s);
 
 // pruned matching tier (kernels_prune.cu): per sample the keep (<= kPruneKeepMax) templates of
-// largest initial Cf as ranks (templates renumbered by probe position: order[rank] = template,
-// rank_of its inverse), lists lrk / lsc [nb][W][kPruneKeepMax]; the loop on those lists with
-// ctcQ[s][l][rank] = ctc[order[rank]][s][l]
+// largest initial Cf, lists lrk / lsc [nb][W][kPruneKeepMax]; the loop on those lists
 constexpr int kPruneKeepMax = 32;
 constexpr int kPruneThreads = 512;
-void launch_prune_select(const float* Bt, const float* nm, const uint16_t* rank_of, int nb, int W, int T, int keep,
-                         uint16_t* lrk, float* lsc, cudaStream_t s);
+void launch_prune_select(const float* Bt, const float* nm, int nb, int W, int T, int keep, uint16_t* lrk, float* lsc,
+                         cudaStream_t s);
 // cf_scratch [nb][W + 2nt] and slot_scratch [nb][W] hold the per-sample maxima of windows whose
 // maxima do not fit in shared memory (prune_mode without bit 0); may be null otherwise
-cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcQ, const uint16_t* order,
-                                const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
-                                float* cf_scratch, unsigned char* slot_scratch, const MatchOut& out, cudaStream_t s);
-// where a window's per-sample state lives: bit 0 = maxima in shared memory, bit 1 = ranks too; 0 =
-// maxima in the caller's scratch; -1 = too large for the tier
+cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcP, const float* nm,
+                                float th2, int W, int T, int nt, int max_iters, int nb, float* cf_scratch,
+                                unsigned char* slot_scratch, const MatchOut& out, cudaStream_t s);
+// where a window's per-sample state lives: bit 0 = maxima in shared memory, bit 1 = listed
+// templates too; 0 = maxima in the caller's scratch; -1 = too large for the tier
 int prune_mode(int W, int T, int nt);
 
 void launch_features(const float* Xres, const MatchOut& out, int nb, int W, int C, int T, int K, int nt, int nC,

@@ -215,13 +215,13 @@ struct Handle {
     std::vector<int64_t> last_kept;     // per final cluster: last kept spike time (duplicate removal)
     std::vector<char> has_kept;
     PropGate* gate = nullptr;           // learned proposal gate (lss_set_proposal), off when null
-    // pruned matching tier (match_keep > 0): templates renumbered by probe position (rank), ctc with
-    // its target axis in rank order, per-sample lists of ranks and scores
+    // templates are numbered internally by their position along the probe (tmpl_orig[internal] =
+    // the oss_input row), so the templates a spike's ctc reaches form one contiguous range
+    std::vector<int32_t> tmpl_orig;
+    int2* d_crange = nullptr;           // [T] per spike template: float4 range of targets it updates
+    // pruned matching tier (match_keep > 0): per-sample lists of internal ids and scores
     int keep = 0;
-    float* d_ctc = nullptr;             // ctcQ [T][2nt+1][T]: ctcQ[s][l][r] = ctc[order[r]][s][l]
-    uint16_t* d_order = nullptr;        // [T] template of each rank
-    uint16_t* d_rank = nullptr;         // [T] rank of each template
-    uint16_t* d_lid = nullptr;          // [nb][W][kPruneKeepMax] ranks
+    uint16_t* d_lid = nullptr;          // [nb][W][kPruneKeepMax] internal template ids
     float* d_lsc = nullptr;             // [nb][W][kPruneKeepMax] scores
     float* d_pcf = nullptr;             // [nb][W + 2nt] per-sample maxima of windows too long for shared memory
     unsigned char* d_pslot = nullptr;   // [nb][W]
@@ -265,7 +265,7 @@ Handle::~Handle() {
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
                     (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo,
-                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm, (void*)d_ctc, (void*)d_order, (void*)d_rank})
+                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm, (void*)d_crange})
         if (p) cudaFree(p);
     if (h_gemm_err) cudaFreeHost(h_gemm_err);
     for (auto& s : slots) {
@@ -322,6 +322,90 @@ void Handle::free_work() {
     Wcap = nbcap = 0;
 }
 
+// Internal template numbering: by the energy-weighted (y, x) centre of each template on the probe
+// (ties by row), so that templates which overlap in space -- the only pairs with a non-negligible
+// ctc -- have nearby numbers.  Every template-indexed array of the model is permuted in place;
+// orig[internal] = the oss_input row.  Nothing about a template changes, only its number: the
+// matching loop's tie rule (the lower number wins an exactly equal Cf) then applies to this
+// numbering.
+static void renumber_templates(OssModel& m, std::vector<int32_t>& orig) {
+    const int64_t T = m.T, K = m.K, C = m.C, nt = m.nt, nC = m.nC, L2 = 2 * m.nt + 1;
+    std::vector<double> cy(T), cx(T);
+    for (int64_t t = 0; t < T; ++t) {
+        double e = 0.0, sy = 0.0, sx = 0.0;
+        for (int64_t c = 0; c < C; ++c) {
+            double ec = 0.0;
+            for (int64_t k = 0; k < K; ++k) {
+                const double v = m.Wall3[(t * K + k) * C + c];
+                ec += v * v;
+            }
+            e += ec;
+            sy += ec * m.yc[c];
+            sx += ec * m.xc[c];
+        }
+        cy[t] = e > 0.0 ? sy / e : 0.0;
+        cx[t] = e > 0.0 ? sx / e : 0.0;
+    }
+    orig.resize(T);
+    for (int64_t t = 0; t < T; ++t) orig[t] = (int32_t)t;
+    std::stable_sort(orig.begin(), orig.end(),
+                     [&](int32_t a, int32_t b) { return cy[a] < cy[b] || (cy[a] == cy[b] && cx[a] < cx[b]); });
+    auto rows = [&](std::vector<float>& a, int64_t len) {
+        std::vector<float> o(a.size());
+        for (int64_t r = 0; r < T; ++r) std::copy_n(&a[orig[r] * len], len, &o[r * len]);
+        a.swap(o);
+    };
+    rows(m.Wall3, K * C);
+    rows(m.pre_wf, nt * C);
+    std::vector<float> ctc(m.ctc.size());
+    for (int64_t t = 0; t < T; ++t)
+        for (int64_t u = 0; u < T; ++u)
+            std::copy_n(&m.ctc[((int64_t)orig[t] * T + orig[u]) * L2], L2, &ctc[(t * T + u) * L2]);
+    m.ctc.swap(ctc);
+    std::vector<int64_t> iU(T);
+    for (int64_t t = 0; t < T; ++t) iU[t] = m.iU[orig[t]];
+    m.iU.swap(iU);
+    std::vector<float> Ucc(m.Ucc.size());
+    for (int64_t n = 0; n < nC; ++n)
+        for (int64_t t = 0; t < T; ++t)
+            std::copy_n(&m.Ucc[(n * T + orig[t]) * K], K, &Ucc[(n * T + t) * K]);
+    m.Ucc.swap(Ucc);
+}
+
+// Per spike template s, the float4 range [x, y) of target templates whose ctc with s reaches
+// rel_eps of the largest |ctc[.][s][.]| (all of them when rel_eps <= 0), widened to whole
+// 32-template segments; the matching loop subtracts a spike of s from that range only.
+static std::vector<int2> ctc_ranges(const OssModel& m, float rel_eps) {
+    const int64_t T = m.T, L2 = 2 * m.nt + 1;
+    const int T4 = (int)((T + 3) / 4);
+    std::vector<int2> r(T, make_int2(0, T4));
+    if (!(rel_eps > 0.f)) return r;
+    std::vector<float> amax((size_t)T * T);   // [s][t]: max over lags of |ctc[t][s][l]|
+    for (int64_t t = 0; t < T; ++t)
+        for (int64_t s = 0; s < T; ++s) {
+            float a = 0.f;
+            const float* c = &m.ctc[(t * T + s) * L2];
+            for (int64_t l = 0; l < L2; ++l) a = std::max(a, std::fabs(c[l]));
+            amax[s * T + t] = a;
+        }
+    for (int64_t s = 0; s < T; ++s) {
+        const float* a = &amax[s * T];
+        const float top = *std::max_element(a, a + T);
+        int64_t lo = T, hi = -1;
+        for (int64_t t = 0; t < T; ++t)
+            if (a[t] > rel_eps * top) {
+                lo = std::min(lo, t);
+                hi = t;
+            }
+        if (hi < 0) {
+            r[s] = make_int2(0, 0);   // a spike of s changes no score
+            continue;
+        }
+        r[s] = make_int2((int)(lo / 32) * 8, std::min(T4, (int)((hi / 32) + 1) * 8));
+    }
+    return r;
+}
+
 // The sorter's own limits on a loaded model (beyond the loader's file checks).
 static void check_model(const OssModel& m) {
     if (m.nt % 2 == 0) throw LoadError{LSS_ERR_FORMAT, "template length must be odd"};
@@ -339,6 +423,7 @@ void Handle::init(const char* dir, const lss_params* prm) {
         throw LoadError{LSS_ERR_ARG, "lss_params: non-positive batch_samples / max_iters / group_batches"};
     m = load_oss_input(dir ? dir : "");
     check_model(m);
+    renumber_templates(m, tmpl_orig);
     C = (int)m.C;
     T = (int)m.T;
     K = (int)m.K;
@@ -476,42 +561,9 @@ void Handle::init(const char* dir, const lss_params* prm) {
     if (p.match_keep < 0 || p.match_keep > kPruneKeepMax)
         throw LoadError{LSS_ERR_ARG, "lss_params.match_keep must be 0 (full loop) or 1.." + std::to_string(kPruneKeepMax)};
     keep = std::min(p.match_keep, T);
-    if (keep > 0) {
-        if (T > 1024) throw LoadError{LSS_ERR_ARG, "the pruned matching tier takes at most 1024 templates"};
-        // rank = position along the probe: the energy-weighted (y, x) centre of each template
-        std::vector<double> cy(T), cx(T);
-        for (int t = 0; t < T; ++t) {
-            double e = 0.0, sy = 0.0, sx = 0.0;
-            for (int c = 0; c < C; ++c) {
-                double ec = 0.0;
-                for (int k = 0; k < K; ++k) {
-                    const double v = m.Wall3[((size_t)t * K + k) * C + c];
-                    ec += v * v;
-                }
-                e += ec;
-                sy += ec * m.yc[c];
-                sx += ec * m.xc[c];
-            }
-            cy[t] = e > 0.0 ? sy / e : 0.0;
-            cx[t] = e > 0.0 ? sx / e : 0.0;
-        }
-        std::vector<uint16_t> order(T), rank(T);
-        for (int t = 0; t < T; ++t) order[t] = (uint16_t)t;
-        std::stable_sort(order.begin(), order.end(), [&](uint16_t a, uint16_t b) {
-            return cy[a] < cy[b] || (cy[a] == cy[b] && cx[a] < cx[b]);
-        });
-        for (int r = 0; r < T; ++r) rank[order[r]] = (uint16_t)r;
-        std::vector<float> q((size_t)T * L2 * T);
-        for (int t = 0; t < T; ++t)
-            for (int s = 0; s < T; ++s) {
-                const float* src = &m.ctc[((size_t)t * T + s) * L2];
-                for (int l = 0; l < L2; ++l) q[((size_t)s * L2 + l) * T + rank[t]] = src[l];
-            }
-        d_ctc = dev_upload(q, dev_bytes, st);
-        d_order = dev_upload(order, dev_bytes, st);
-        d_rank = dev_upload(rank, dev_bytes, st);
-        LSS_CUDA(cudaStreamSynchronize(st));
-    }
+    if (keep > 0 && T > 1024) throw LoadError{LSS_ERR_ARG, "the pruned matching tier takes at most 1024 templates"};
+    if (!(p.ctc_rel_eps >= 0.f)) throw LoadError{LSS_ERR_ARG, "lss_params.ctc_rel_eps must be >= 0"};
+    d_crange = dev_upload(ctc_ranges(m, p.ctc_rel_eps), dev_bytes, st);
     LSS_CUDA(cudaHostAlloc((void**)&h_gemm_err, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable));
     *h_gemm_err = 0;
     LSS_CUDA(cudaHostGetDevicePointer((void**)&d_gemm_err, h_gemm_err, 0));
@@ -825,15 +877,15 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
 void Handle::run_match(int nb, int Wn, int64_t& nl) {
     LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
     if (keep > 0) {
-        launch_prune_select(d_Bt, d_nm, d_rank, nb, Wn, T, keep, d_lid, d_lsc, st);
+        launch_prune_select(d_Bt, d_nm, nb, Wn, T, keep, d_lid, d_lsc, st);
         LSS_CUDA(cudaGetLastError());
-        LSS_CUDA(launch_match_pruned(d_lid, d_lsc, keep, d_ctc, d_order, d_nm, th * th, Wn, T, nt, max_iters, nb,
-                                     d_pcf, d_pslot, mo, st));
+        LSS_CUDA(launch_match_pruned(d_lid, d_lsc, keep, d_ctcP, d_nm, th * th, Wn, T, nt, max_iters, nb, d_pcf,
+                                     d_pslot, mo, st));
         LSS_CUDA(launch_residual(d_Z, d_pre_wf, mo, Wn, C, nt, nb, st));
         nl += 3;   // selection, loop, residual
     } else {
         LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st,
-                              p.match_variant));
+                              p.match_variant, d_crange));
         nl += 2;   // the loop and the residual
     }
 }
@@ -909,13 +961,13 @@ void Handle::collect(int si, std::vector<lss_spike>* direct, std::vector<int64_t
         for (int i = 0; i < n; ++i) {
             const int64_t t = s.win_start[b] + recs[i].w - hw + m.nt0min;
             if (t < s.drop_before[b]) continue;
-            keys.push_back({t, recs[i].t, i});
+            keys.push_back({t, tmpl_orig[recs[i].t], i});
         }
         std::sort(keys.begin(), keys.end());
         auto make = [&](const Key& k, lss_spike& o) {
             const SpikeRec& r = recs[k.i];
             o.time = k.time;
-            o.tmpl = r.t;
+            o.tmpl = k.tmpl;
             o.cluster = r.cluster;
             o.amp = r.amp;
             o.x = r.x;
@@ -1152,6 +1204,7 @@ int lss_default_params(lss_params* p) {
     p->cluster_rule = 0;
     p->cluster_radius_um = 0.f;
     p->match_keep = 0;
+    p->ctc_rel_eps = 1e-6f;
     return LSS_OK;
 }
 
@@ -1364,7 +1417,12 @@ int lss_debug_stage(lss_handle* hp, const int16_t* window, int32_t W, int32_t st
             LSS_CUDA(cudaMemcpyAsync(out, h.d_Z, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
         } else {
             if (stage == LSS_STAGE_SCORES) {
-                LSS_CUDA(cudaMemcpyAsync(out, h.d_Bt, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
+                // columns back in oss_input order
+                std::vector<float> bt((size_t)need);
+                LSS_CUDA(cudaMemcpyAsync(bt.data(), h.d_Bt, sizeof(float) * need, cudaMemcpyDeviceToHost, st));
+                LSS_CUDA(cudaStreamSynchronize(st));
+                for (int64_t w = 0; w < W; ++w)
+                    for (int t = 0; t < h.T; ++t) out[w * h.T + h.tmpl_orig[t]] = bt[(size_t)w * h.T + t];
             } else {
                 h.run_match(1, W, nl);
                 LSS_CUDA(cudaMemcpyAsync(out, h.d_Z, sizeof(float) * need, cudaMemcpyDeviceToHost, st));

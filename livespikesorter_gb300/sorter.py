@@ -19,7 +19,7 @@ import numpy as np
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = Path(os.environ.get("LSS_GB300_LIB", _PKG / "lib" / "liblss_gb300.so"))
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_PCFEAT = 64
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_FORMAT", 4: "ERR_CUDA", 5: "ERR_NOMEM",
           6: "ERR_OVERFLOW", 7: "ERR_STATE", 8: "ERR_INTERNAL"}
@@ -32,7 +32,8 @@ class Params(ct.Structure):
                 ("hp_half_taps", ct.c_int32), ("dedup", ct.c_int32), ("th_override", ct.c_float),
                 ("spike_cap", ct.c_int32), ("mem_budget", ct.c_int64), ("profile", ct.c_int32),
                 ("match_variant", ct.c_int32), ("gemm_path", ct.c_int32), ("cluster_rule", ct.c_int32),
-                ("cluster_radius_um", ct.c_float), ("match_keep", ct.c_int32)]
+                ("cluster_radius_um", ct.c_float), ("match_keep", ct.c_int32),
+                ("ctc_rel_eps", ct.c_float), ("reserved", ct.c_int32 * 1)]
 
 
 class Spike(ct.Structure):
