@@ -204,6 +204,13 @@ int lss_cuda_stream(const lss_handle* h, void** stream);
 #define LSS_N_STAGES 10
 int lss_stage_times(lss_handle* h, double* ms, int32_t n, int64_t* n_groups);
 
+/* Per template (oss_input order), how many templates' scores a spike of it updates in the matching
+ * loop: those whose ctc with it reaches lss_params.ctc_rel_eps of its largest, as one contiguous
+ * range of the sorter's internal numbering widened to 32-template segments (T when ctc_rel_eps =
+ * 0).  The reference subtracts every template (subtractSpikeContributions, myGPUhelpers.cu:121-188);
+ * n_targets has room for T entries. */
+int lss_ctc_reach(const lss_handle* h, int32_t* n_targets, int32_t n);
+
 /* The matching loop of one window on buffers the caller owns, allocating no memory.
  *
  * No counterpart in the reference.  For callers that cannot allocate device memory when they

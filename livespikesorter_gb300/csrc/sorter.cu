@@ -219,6 +219,7 @@ struct Handle {
     // the oss_input row), so the templates a spike's ctc reaches form one contiguous range
     std::vector<int32_t> tmpl_orig;
     int2* d_crange = nullptr;           // [T] per spike template: float4 range of targets it updates
+    std::vector<int32_t> reach;         // per oss_input template: templates a spike of it updates
     // pruned matching tier (match_keep > 0): per-sample lists of internal ids and scores
     int keep = 0;
     uint16_t* d_lid = nullptr;          // [nb][W][kPruneKeepMax] internal template ids
@@ -563,7 +564,12 @@ void Handle::init(const char* dir, const lss_params* prm) {
     keep = std::min(p.match_keep, T);
     if (keep > 0 && T > 1024) throw LoadError{LSS_ERR_ARG, "the pruned matching tier takes at most 1024 templates"};
     if (!(p.ctc_rel_eps >= 0.f)) throw LoadError{LSS_ERR_ARG, "lss_params.ctc_rel_eps must be >= 0"};
-    d_crange = dev_upload(ctc_ranges(m, p.ctc_rel_eps), dev_bytes, st);
+    {
+        const std::vector<int2> cr = ctc_ranges(m, p.ctc_rel_eps);
+        reach.assign(T, 0);
+        for (int t = 0; t < T; ++t) reach[tmpl_orig[t]] = std::min(4 * cr[t].y, T) - std::min(4 * cr[t].x, T);
+        d_crange = dev_upload(cr, dev_bytes, st);
+    }
     LSS_CUDA(cudaHostAlloc((void**)&h_gemm_err, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable));
     *h_gemm_err = 0;
     LSS_CUDA(cudaHostGetDevicePointer((void**)&d_gemm_err, h_gemm_err, 0));
@@ -1456,6 +1462,12 @@ int lss_stage_times(lss_handle* hp, double* ms, int32_t n, int64_t* n_groups) {
     if (!hp || !ms || n < 0) return LSS_ERR_ARG;
     for (int i = 0; i < n && i < LSS_N_STAGES; ++i) ms[i] = hp->h.stage_ms[i];
     if (n_groups) *n_groups = hp->h.groups_timed;
+    return LSS_OK;
+}
+
+int lss_ctc_reach(const lss_handle* hp, int32_t* n_targets, int32_t n) {
+    if (!hp || !n_targets || n < hp->h.T) return LSS_ERR_ARG;
+    std::copy(hp->h.reach.begin(), hp->h.reach.end(), n_targets);
     return LSS_OK;
 }
 

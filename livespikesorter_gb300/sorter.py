@@ -74,6 +74,7 @@ _SIGS = {
     "lss_push_device_span": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int64]),
     "lss_cuda_stream": (ct.c_int, [ct.c_void_p, _P(ct.c_void_p)]),
     "lss_stage_times": (ct.c_int, [ct.c_void_p, _P(ct.c_double), ct.c_int32, _P(ct.c_int64)]),
+    "lss_ctc_reach": (ct.c_int, [ct.c_void_p, _P(ct.c_int32), ct.c_int32]),
     "lss_match_noalloc": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_float,
                                      ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p,
                                      ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_void_p]),
@@ -224,6 +225,12 @@ class OnlineSorter:
         n = ct.c_int64()
         self._check(self.lib.lss_stage_times(self.h, ms, len(STAGES), ct.byref(n)))
         return dict(zip(STAGES, list(ms))), n.value
+
+    def ctc_reach(self) -> np.ndarray:
+        """Per template (oss_input order): how many templates' scores a spike of it updates."""
+        n = np.zeros(self.info.T, np.int32)
+        self._check(self.lib.lss_ctc_reach(self.h, n.ctypes.data_as(_P(ct.c_int32)), len(n)))
+        return n
 
     def push_device_span(self, dev_ptr: int, n_batches: int, first_row_sample: int = 0):
         self._check(self.lib.lss_push_device_span(self.h, ct.c_void_p(dev_ptr), int(n_batches), int(first_row_sample)))
