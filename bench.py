@@ -371,8 +371,6 @@ def run_gpu(a):
     ms = e0.elapsed_time(e1)
     timed_spikes = s.poll(max(s.pending(), 1))
     spikes_seen[0] = len(timed_spikes)
-    reach = s.ctc_reach()
-    mean_reach = float(reach[timed_spikes["tmpl"]].mean()) if len(timed_spikes) else float(T)
     torch.cuda.synchronize(dev)
     ms = max_over_ranks(ms, world, f"cuda:{dev}")
     units = a.steps * G * NT * C
@@ -382,7 +380,7 @@ def run_gpu(a):
     n_timed = n_all - n_base
     spikes_per_batch = spikes_seen[0] / max(1, a.steps * G)
     ntaps = 885   # the FIR the library cuts from this filter: taps beyond are < 1e-8 of the centre tap
-    roof = roofline(stage, n_timed, G, C, T, K, nt, W, ntaps, spikes_per_batch, mean_reach)
+    roof = roofline(stage, n_timed, G, C, T, K, nt, W, ntaps, spikes_per_batch)
     s.close()
 
     obuf = np.zeros(1 << 16, sorter.SPIKE_DTYPE)

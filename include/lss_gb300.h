@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define LSS_ABI_VERSION 2
+#define LSS_ABI_VERSION 1
 #define LSS_MAX_PCFEAT 64 /* nearest channels x PCs carried per spike */
 
 enum lss_status {
@@ -71,11 +71,6 @@ typedef struct lss_params {
                                per sample only the match_keep templates of largest initial Cf = relu(B)^2 / nm
                                are scored through the loop (same updates on them, so the spikes equal the full
                                loop's unless an unlisted template would have won; agreement measured) */
-    float ctc_rel_eps;      /* a spike of template s is subtracted from the scores of the templates whose ctc with s
-                               reaches ctc_rel_eps of the largest |ctc[.][s][.]| (their range, in the sorter's
-                               internal numbering by probe position); the others' updates are below that fraction.
-                               Default 1e-6; 0 = every template (Kilosort's dense subtraction) */
-    int32_t reserved[1];
 } lss_params;
 
 /* One sorted spike.  time is the stream sample (Kilosort template_matching.py:68). */
@@ -203,13 +198,6 @@ int lss_cuda_stream(const lss_handle* h, void** stream);
  * (Timer.h:7-21) prints nothing; this is its working counterpart. */
 #define LSS_N_STAGES 10
 int lss_stage_times(lss_handle* h, double* ms, int32_t n, int64_t* n_groups);
-
-/* Per template (oss_input order), how many templates' scores a spike of it updates in the matching
- * loop: those whose ctc with it reaches lss_params.ctc_rel_eps of its largest, as one contiguous
- * range of the sorter's internal numbering widened to 32-template segments (T when ctc_rel_eps =
- * 0).  The reference subtracts every template (subtractSpikeContributions, myGPUhelpers.cu:121-188);
- * n_targets has room for T entries. */
-int lss_ctc_reach(const lss_handle* h, int32_t* n_targets, int32_t n);
 
 /* The matching loop of one window on buffers the caller owns, allocating no memory.
  *

@@ -55,20 +55,16 @@ __host__ __device__ inline int match_near_cap(int W, int nt) { return 2 * ((W + 
 
 constexpr int kStageChunk = 4096;   // samples of per-sample maxima staged at once in B1
 
-constexpr int kSeg = 32;   // templates per segment of a score row (8 float4)
-
 // dynamic shared memory of one CTA: [owned score rows if SMEM_B][cfmax of a window chunk + 2nt]
 // [1/nm][nm][own samples' argmax][per-32-sample accepted masks and prefix]
 // [two accepted-spike lists (sample, template, amp), by iteration parity]
-// [own samples' segment maxima and their templates, when seg][each template's update range]
-__host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, bool smem_b, bool seg = false) {
+__host__ __device__ inline size_t match_smem_bytes(int W, int T, int nt, int G, bool smem_b) {
     const size_t span = (size_t)(W + G - 1) / G;
     const size_t chunk = (size_t)(W < kStageChunk ? W : kStageChunk);
     const size_t pad = (chunk + 2 * nt + 3) & ~(size_t)3;   // 1/nm starts 16-byte aligned
     const size_t words = (size_t)(W + 31) / 32 + 1;
-    const size_t nseg = (size_t)(T + kSeg - 1) / kSeg;
     return (smem_b ? span * T * 4 : 0) + pad * 4 + (size_t)T * 8 + span * 4 + words * 8 +
-           2 * (size_t)match_near_cap(W, nt) * 12 + (seg ? span * nseg * 8 : 0) + (size_t)T * 8;
+           2 * (size_t)match_near_cap(W, nt) * 12;
 }
 
 // shared::cluster address of the same shared variable in CTA `rank` of the cluster
@@ -108,17 +104,11 @@ __device__ __forceinline__ float4 ld_keep(const float4* p, uint64_t pol) {
 //   C   each CTA subtracts amp * ctc from the score rows of its own samples within +-nt of a spike,
 //       in ascending spike order, and recomputes those samples' maxima;
 //   --  cluster barrier.
-// A spike of template s changes only the scores of the templates in crange[s] (float4 units, whole
-// 32-template segments; null = all): its ctc with the others is below the sorter's relative
-// threshold.  So a pass reads and writes that part of a row only.  The row maximum stays exact:
-// with the scores in L2 each own sample keeps the maximum of every segment (the pass recomputes
-// the segments it holds, the row maximum is the maximum of the segment maxima) when SEG and they
-// fit in shared memory; else the row is rescanned (in shared memory with SMEM_B).
-template <int G, bool SMEM_B, int NTHR, bool SEG>
+template <int G, bool SMEM_B, int NTHR>
 __global__ void __launch_bounds__(NTHR, (SMEM_B || NTHR > 512) ? 1 : 2)
 match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __restrict__ ctcP,
              const float* __restrict__ pre_wf, const float* __restrict__ nm, float th2, int W, int T, int C,
-             int nt, int max_iters, const int2* __restrict__ crange, MatchScratch sc, MatchOut out) {
+             int nt, int max_iters, MatchScratch sc, MatchOut out) {
     constexpr int kWarps = NTHR / 32;
     constexpr int kVec = SMEM_B ? kVecSmem : kVecGlobal;
     extern __shared__ float smem[];
@@ -142,11 +132,6 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     int* s_lw = s_woff + nwords + 1;                                    // [2][near_cap] sample
     int* s_lt = s_lw + 2 * near_cap;                                    // [2][near_cap] template
     float* s_la = reinterpret_cast<float*>(s_lt + 2 * near_cap);        // [2][near_cap] amplitude
-    const int nseg = (T + kSeg - 1) / kSeg;
-    float* s_smax = s_la + 2 * near_cap;                                // [span][nseg] segment maxima (SEG)
-    int* s_sarg = reinterpret_cast<int*>(s_smax + (SEG ? (size_t)span * nseg : 0));   // their templates
-    int* s_rlo = s_sarg + (SEG ? (size_t)span * nseg : 0);             // [T] crange[t].x
-    int* s_rhi = s_rlo + T;                                             // [T] crange[t].y
     __shared__ int s_wcnt[kWarps];
     __shared__ int s_lcnt[2];                                           // spikes received, by parity
 
@@ -184,9 +169,6 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
     for (int t = tid; t < T; t += NTHR) {
         s_nm[t] = nm[t];
         s_inm[t] = 1.f / nm[t];
-        const int2 r = crange ? crange[t] : make_int2(0, (T + 3) >> 2);
-        s_rlo[t] = r.x;
-        s_rhi[t] = r.y;
     }
     // a window of at most kStageChunk samples keeps every sample's maximum in every CTA: owners
     // push each new value into all CTAs, so phase B1 reads shared memory only
@@ -217,38 +199,16 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                          : "memory");
     };
 
-    // (max, template) of a lane group of width n (n a power of two <= 32), lower template on ties
-    auto group_max = [&](float& v, int& t, int n) {
-        for (int o = 1; o < n; o <<= 1) {
-            const float ov = __shfl_xor_sync(0xffffffffu, v, o);
-            const int ot = __shfl_xor_sync(0xffffffffu, t, o);
-            if (ov > v || (ov == v && ot < t)) { v = ov; t = ot; }
-        }
-    };
-    // ---- A (once): per-sample max / argmax over templates of the own samples (and, with the
-    // scores in L2, of every segment) ----
+    // ---- A (once): per-sample max / argmax over templates of the own samples ----
     for (int j = warp; j < own; j += kWarps) {
         const int w = rank + G * j;
         const float* row = brow(w);
         float best = -1.f;
         int bi = 0x7fffffff;
-        for (int t0 = 0; t0 < T; t0 += kSeg) {
-            const int t = t0 + lane;
-            float v = -1.f;
-            if (t < T) {
-                const float r = fmaxf(row[t], 0.f);
-                v = r * r * s_inm[t];
-            }
+        for (int t = lane; t < T; t += 32) {
+            const float r = fmaxf(row[t], 0.f);
+            const float v = r * r * s_inm[t];
             if (v > best) { best = v; bi = t; }
-            if constexpr (SEG) {
-                float sv = v;
-                int si = t < T ? t : 0x7fffffff;
-                group_max(sv, si, 32);
-                if (lane == 0) {
-                    s_smax[(size_t)j * nseg + t0 / kSeg] = sv;
-                    s_sarg[(size_t)j * nseg + t0 / kSeg] = si;
-                }
-            }
         }
         finish_sample(w, best, bi);
     }
@@ -480,48 +440,6 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
             auto ctc_row = [&](int kk, int w) {
                 return reinterpret_cast<const float4*>(ctcP + ((int64_t)s_nt[kk] * L2 + (w - s_nw[kk] + nt)) * T);
             };
-            auto range_of = [&](int kk) {
-                const int t = s_nt[kk];
-                return make_int2(s_rlo[t], s_rhi[t]);
-            };
-            // Cf maximum of the float4 x (templates 4f..4f+3) of a lane, lower template on ties
-            auto f4_max = [&](const float4& x, int f, float& v, int& t) {
-                const float4 im = reinterpret_cast<const float4*>(s_inm)[f];
-                float r, q;
-                r = fmaxf(x.x, 0.f); q = r * r * im.x; if (q > v) { v = q; t = 4 * f; }
-                r = fmaxf(x.y, 0.f); q = r * r * im.y; if (q > v) { v = q; t = 4 * f + 1; }
-                r = fmaxf(x.z, 0.f); q = r * r * im.z; if (q > v) { v = q; t = 4 * f + 2; }
-                r = fmaxf(x.w, 0.f); q = r * r * im.w; if (q > v) { v = q; t = 4 * f + 3; }
-            };
-            // the segment maxima of own sample j for the float4s f of this step (8 lanes a segment;
-            // the step's segments at or beyond hi are not the pass's and keep their maxima)
-            auto seg_store = [&](int jj_own, const float4& x, int f, bool ok, int hi) {
-                float v = -1.f;
-                int t = 0x7fffffff;
-                if (ok) f4_max(x, f, v, t);
-                group_max(v, t, 8);
-                const int f0 = f - (lane & 7);
-                if ((lane & 7) == 0 && f0 < hi) {
-                    s_smax[(size_t)jj_own * nseg + f0 / 8] = v;
-                    s_sarg[(size_t)jj_own * nseg + f0 / 8] = t;
-                }
-            };
-            // the row maximum of own sample j into cfmax / imax
-            auto row_finish = [&](int w, const float4* brw) {
-                float best = -1.f;
-                int bi = 0x7fffffff;
-                if constexpr (!SEG) {
-                    for (int f = lane; f < T4; f += 32) f4_max(brw[f], f, best, bi);
-                } else {
-                    __syncwarp();
-                    const int jo = w / G;
-                    for (int q = lane; q < nseg; q += 32) {
-                        const float v = s_smax[(size_t)jo * nseg + q];
-                        if (v > best) { best = v; bi = s_sarg[(size_t)jo * nseg + q]; }
-                    }
-                }
-                finish_sample(w, best, bi);
-            };
             while (j < own) {
                 const int wA = rank + G * j;
                 const int kA = k;
@@ -549,72 +467,70 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                 const float4* c0 = ctc_row(kA, wA);
                 const float4* c1 = twoA ? ctc_row(kA + 1, wA) : (hasB ? ctc_row(kB, wB) : c0);
                 const bool has1 = twoA || hasB;
-                // the float4 ranges of the two rows, and the pass's span of both
-                const int2 r0 = range_of(kA);
-                const int2 r1 = has1 ? range_of(twoA ? kA + 1 : kB) : make_int2(0, 0);
-                const int lo = has1 ? min(r0.x, r1.x) : r0.x;
-                const int hi = has1 ? max(r0.y, r1.y) : r0.y;
                 float4* bA = reinterpret_cast<float4*>(brow(wA));
                 float4* bB = reinterpret_cast<float4*>(hasB ? brow(wB) : brow(wA));
-                const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-                for (int fb = lo; fb < hi; fb += 32 * kVec) {
+                float bestA = -1.f, bestB = -1.f;
+                int biA = 0x7fffffff, biB = 0x7fffffff;
+                for (int fb = 0; fb < T4; fb += 32 * kVec) {
                     float4 v0[kVec], v1[kVec], xa[kVec], xb[kVec];
                     // the ctc rows and, when the scores live in L2, the score rows in one batch of
                     // loads: one round trip per step instead of two
 #pragma unroll
                     for (int jj = 0; jj < kVec; ++jj) {
                         const int f = fb + lane + 32 * jj;
-                        const bool ok = f < hi;
-                        const bool in0 = ok && f >= r0.x && f < r0.y;
-                        const bool in1 = ok && has1 && f >= r1.x && f < r1.y;
-                        if (fb + 32 * jj >= hi) {   // the step's later columns are past the span (warp-uniform)
-                            v0[jj] = v1[jj] = xa[jj] = xb[jj] = z4;
-                            continue;
-                        }
-                        v0[jj] = in0 ? ld_keep(c0 + f, pol_keep) : z4;
-                        v1[jj] = in1 ? ld_keep(c1 + f, pol_keep) : z4;
+                        const bool ok = f < T4;
+                        v0[jj] = ok ? ld_keep(c0 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        v1[jj] = (ok && has1) ? ld_keep(c1 + f, pol_keep) : make_float4(0.f, 0.f, 0.f, 0.f);
                         if constexpr (!SMEM_B) {
-                            xa[jj] = ok ? bA[f] : z4;
-                            xb[jj] = (ok && hasB) ? bB[f] : z4;
+                            xa[jj] = ok ? bA[f] : make_float4(0.f, 0.f, 0.f, 0.f);
+                            xb[jj] = (ok && hasB) ? bB[f] : make_float4(0.f, 0.f, 0.f, 0.f);
                         }
                     }
 #pragma unroll
                     for (int jj = 0; jj < kVec; ++jj) {
                         const int f = fb + lane + 32 * jj;
-                        const bool ok = f < hi;
-                        const bool in0 = ok && f >= r0.x && f < r0.y;
-                        const bool in1 = ok && has1 && f >= r1.x && f < r1.y;
-                        if (fb + 32 * jj >= hi) continue;   // warp-uniform
-                        float4 x = ok ? (SMEM_B ? bA[f] : xa[jj]) : z4;
-                        if (in0) {
+                        if (f < T4) {
+                            const int t = 4 * f;
+                            float4 x = SMEM_B ? bA[f] : xa[jj];
                             x.x = fmaf(-aA0, v0[jj].x, x.x);
                             x.y = fmaf(-aA0, v0[jj].y, x.y);
                             x.z = fmaf(-aA0, v0[jj].z, x.z);
                             x.w = fmaf(-aA0, v0[jj].w, x.w);
-                        }
-                        if (twoA && in1) {
-                            x.x = fmaf(-a1, v1[jj].x, x.x);
-                            x.y = fmaf(-a1, v1[jj].y, x.y);
-                            x.z = fmaf(-a1, v1[jj].z, x.z);
-                            x.w = fmaf(-a1, v1[jj].w, x.w);
-                        }
-                        if (in0 || (twoA && in1)) bA[f] = x;
-                        if constexpr (SEG) seg_store(wA / G, x, f, ok, hi);
-                        if (hasB) {
-                            float4 y = ok ? (SMEM_B ? bB[f] : xb[jj]) : z4;
-                            if (in1) {
+                            if (twoA) {
+                                x.x = fmaf(-a1, v1[jj].x, x.x);
+                                x.y = fmaf(-a1, v1[jj].y, x.y);
+                                x.z = fmaf(-a1, v1[jj].z, x.z);
+                                x.w = fmaf(-a1, v1[jj].w, x.w);
+                            }
+                            bA[f] = x;
+                            const float4 im = reinterpret_cast<const float4*>(s_inm)[f];
+                            if (lastA) {
+                                float r, v;
+                                r = fmaxf(x.x, 0.f); v = r * r * im.x; if (v > bestA) { bestA = v; biA = t; }
+                                r = fmaxf(x.y, 0.f); v = r * r * im.y; if (v > bestA) { bestA = v; biA = t + 1; }
+                                r = fmaxf(x.z, 0.f); v = r * r * im.z; if (v > bestA) { bestA = v; biA = t + 2; }
+                                r = fmaxf(x.w, 0.f); v = r * r * im.w; if (v > bestA) { bestA = v; biA = t + 3; }
+                            }
+                            if (hasB) {
+                                float4 y = SMEM_B ? bB[f] : xb[jj];
                                 y.x = fmaf(-a1, v1[jj].x, y.x);
                                 y.y = fmaf(-a1, v1[jj].y, y.y);
                                 y.z = fmaf(-a1, v1[jj].z, y.z);
                                 y.w = fmaf(-a1, v1[jj].w, y.w);
                                 bB[f] = y;
+                                if (lastB) {
+                                    float r, v;
+                                    r = fmaxf(y.x, 0.f); v = r * r * im.x; if (v > bestB) { bestB = v; biB = t; }
+                                    r = fmaxf(y.y, 0.f); v = r * r * im.y; if (v > bestB) { bestB = v; biB = t + 1; }
+                                    r = fmaxf(y.z, 0.f); v = r * r * im.z; if (v > bestB) { bestB = v; biB = t + 2; }
+                                    r = fmaxf(y.w, 0.f); v = r * r * im.w; if (v > bestB) { bestB = v; biB = t + 3; }
+                                }
                             }
-                            if constexpr (SEG) seg_store(wB / G, y, f, ok, hi);
                         }
                     }
                 }
-                if (lastA) row_finish(wA, bA);
-                if (hasB && lastB) row_finish(wB, bB);
+                if (lastA) finish_sample(wA, bestA, biA);
+                if (hasB && lastB) finish_sample(wB, bestB, biB);
             }
         } else {
             for (int j = warp; j < own; j += kWarps) {
@@ -644,26 +560,13 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                         const int w2 = wp - nt + ee;
                         const float a = __ldcg(at_amp + w2);
                         const float* c = ctcP + ((int64_t)__ldcg(at_t + w2) * L2 + (2 * nt - ee)) * T;
-                        for (int t0 = 0; t0 < T; t0 += kSeg) {
-                            const int t = t0 + lane;
-                            float v = -1.f;
-                            if (t < T) {
-                                const float x = fmaf(-a, __ldg(c + t), br[t]);
-                                br[t] = x;
-                                const float r = fmaxf(x, 0.f);
-                                v = r * r * s_inm[t];
-                            }
+                        for (int t = lane; t < T; t += 32) {
+                            const float x = fmaf(-a, __ldg(c + t), br[t]);
+                            br[t] = x;
                             if (last) {
+                                const float r = fmaxf(x, 0.f);
+                                const float v = r * r * s_inm[t];
                                 if (v > best) { best = v; bi = t; }
-                                if constexpr (SEG) {
-                                    float sv = v;
-                                    int si = t < T ? t : 0x7fffffff;
-                                    group_max(sv, si, 32);
-                                    if (lane == 0) {
-                                        s_smax[(size_t)j * nseg + t0 / kSeg] = sv;
-                                        s_sarg[(size_t)j * nseg + t0 / kSeg] = si;
-                                    }
-                                }
                             }
                         }
                         touched = true;
@@ -828,13 +731,12 @@ residual_kernel(float* __restrict__ Xres, const float* __restrict__ pre_wf, Matc
     }
 }
 
-template <int G, bool SMEM_B, int NTHR, bool SEG>
+template <int G, bool SMEM_B, int NTHR>
 static cudaError_t launch_match_cfg(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                                     float th2, int W, int T, int C, int nt, int max_iters, int nb,
-                                    const MatchScratch& sc, const MatchOut& out, cudaStream_t s,
-                                    const int2* crange) {
-    const size_t smem = match_smem_bytes(W, T, nt, G, SMEM_B, SEG);
-    auto kern = match_kernel<G, SMEM_B, NTHR, SEG>;
+                                    const MatchScratch& sc, const MatchOut& out, cudaStream_t s) {
+    const size_t smem = match_smem_bytes(W, T, nt, G, SMEM_B);
+    auto kern = match_kernel<G, SMEM_B, NTHR>;
     cudaError_t e = raise_smem_limit((const void*)kern, smem);
     if (e != cudaSuccess) return e;
     if (G > 8) {
@@ -853,17 +755,17 @@ static cudaError_t launch_match_cfg(float* Bt, float* Xres, const float* ctcP, c
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, crange, sc, out);
+    return cudaLaunchKernelEx(&cfg, kern, Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, sc, out);
 }
 
 // Can a cluster of 16 CTAs with the whole score slice in shared memory run on this device?
 static int smem16_ok(int W, int T, int nt) {
-    const size_t smem = match_smem_bytes(W, T, nt, 16, true, false);
+    const size_t smem = match_smem_bytes(W, T, nt, 16, true);
     int dev = 0, maxopt = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
     if (smem + 12288 > (size_t)maxopt) return 0;   // static shared memory and the driver reserve
-    auto kern = match_kernel<16, true, kMatchThreadsSmem, false>;
+    auto kern = match_kernel<16, true, kMatchThreadsSmem>;
     if (raise_smem_limit((const void*)kern, smem) != cudaSuccess ||
         cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
         cudaGetLastError();
@@ -890,8 +792,8 @@ static int smem16_ok(int W, int T, int nt) {
 
 // Can a cluster of 16 CTAs of 1024 threads (scores in L2, one CTA per SM) run on this device?
 static int wide16_ok(int W, int T, int nt) {
-    const size_t smem = match_smem_bytes(W, T, nt, 16, false, false);
-    auto kern = match_kernel<16, false, kMatchThreadsWide, false>;
+    const size_t smem = match_smem_bytes(W, T, nt, 16, false);
+    auto kern = match_kernel<16, false, kMatchThreadsWide>;
     if (raise_smem_limit((const void*)kern, smem) != cudaSuccess ||
         cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
         cudaGetLastError();
@@ -931,7 +833,7 @@ int match_variant(int W, int T, int nt, bool* wide) {
 
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm, float th2,
                          int W, int T, int C, int nt, int max_iters, int nb, const MatchScratch& sc,
-                         const MatchOut& out, cudaStream_t s, int variant, const int2* crange) {
+                         const MatchOut& out, cudaStream_t s, int variant) {
     // variant: 0 = automatic -- for groups of at most 8 batches (latency), scores in shared memory
     // when they fit, else in L2 with 16-CTA clusters of 1024 threads (one CTA per SM); larger
     // groups (throughput) scores in L2 with 8-CTA clusters, two CTAs per SM.  1 = the 8-CTA L2
@@ -943,29 +845,16 @@ cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float*
     if (variant == 2) kind = fit == 16 ? 2 : 1;
     else if (variant == 3) kind = wide ? 3 : 1;
     else if (variant == 0 && nb <= 8) kind = fit == 16 ? 2 : (wide ? 3 : 1);
-    // segment maxima in shared memory when they fit beside the rest (scores in L2 only)
-    int dev = 0, maxopt = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&maxopt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    auto seg_fits = [&](int G, int per_sm) {
-        return (match_smem_bytes(W, T, nt, G, false, true) + 2048) * per_sm <= (size_t)maxopt;
-    };
     cudaError_t e;
     if (kind == 2)
-        e = launch_match_cfg<16, true, kMatchThreadsSmem, false>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt,
-                                                                 max_iters, nb, sc, out, s, crange);
-    else if (kind == 3 && seg_fits(16, 1))
-        e = launch_match_cfg<16, false, kMatchThreadsWide, true>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt,
-                                                                 max_iters, nb, sc, out, s, crange);
+        e = launch_match_cfg<16, true, kMatchThreadsSmem>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb,
+                                                          sc, out, s);
     else if (kind == 3)
-        e = launch_match_cfg<16, false, kMatchThreadsWide, false>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt,
-                                                                  max_iters, nb, sc, out, s, crange);
-    else if (seg_fits(8, 2))
-        e = launch_match_cfg<8, false, kMatchThreads, true>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters,
-                                                            nb, sc, out, s, crange);
+        e = launch_match_cfg<16, false, kMatchThreadsWide>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters,
+                                                           nb, sc, out, s);
     else
-        e = launch_match_cfg<8, false, kMatchThreads, false>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters,
-                                                             nb, sc, out, s, crange);
+        e = launch_match_cfg<8, false, kMatchThreads>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc,
+                                                      out, s);
     if (e != cudaSuccess) return e;
     return launch_residual(Xres, pre_wf, out, W, C, nt, nb, s);
 }

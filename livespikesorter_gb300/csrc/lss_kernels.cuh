@@ -131,12 +131,9 @@ void conv_tc_free(ConvOperands* u);
 // out_hi / out_lo viewed as bf16 arrays
 cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* out_lo, bool hi_only, int nb, int C,
                                    int W, int* err, cudaStream_t s, bool out_bf16 = false);
-// crange [T] (may be null = every template): per spike template, the float4 range [x, y) of the
-// score rows a spike of it updates, in whole 32-template segments
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                          float th2, int W, int T, int C, int nt, int max_iters, int nb,
-                         const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0,
-                         const int2* crange = nullptr);
+                         const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0);
 // the residual after a matching loop: Xres[w][:] -= amp * waveform[t][w - w_s + nt/2][:] for the
 // spikes of out, in list order
 cudaError_t launch_residual(float* Xres, const float* pre_wf, const MatchOut& out, int W, int C, int nt, int nb,

@@ -216,10 +216,8 @@ struct Handle {
     std::vector<char> has_kept;
     PropGate* gate = nullptr;           // learned proposal gate (lss_set_proposal), off when null
     // templates are numbered internally by their position along the probe (tmpl_orig[internal] =
-    // the oss_input row), so the templates a spike's ctc reaches form one contiguous range
+    // the oss_input row), so templates that overlap in space have nearby numbers
     std::vector<int32_t> tmpl_orig;
-    int2* d_crange = nullptr;           // [T] per spike template: float4 range of targets it updates
-    std::vector<int32_t> reach;         // per oss_input template: templates a spike of it updates
     // pruned matching tier (match_keep > 0): per-sample lists of internal ids and scores
     int keep = 0;
     uint16_t* d_lid = nullptr;          // [nb][W][kPruneKeepMax] internal template ids
@@ -266,7 +264,7 @@ Handle::~Handle() {
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
                     (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo,
-                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm, (void*)d_crange})
+                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm})
         if (p) cudaFree(p);
     if (h_gemm_err) cudaFreeHost(h_gemm_err);
     for (auto& s : slots) {
@@ -371,40 +369,6 @@ static void renumber_templates(OssModel& m, std::vector<int32_t>& orig) {
         for (int64_t t = 0; t < T; ++t)
             std::copy_n(&m.Ucc[(n * T + orig[t]) * K], K, &Ucc[(n * T + t) * K]);
     m.Ucc.swap(Ucc);
-}
-
-// Per spike template s, the float4 range [x, y) of target templates whose ctc with s reaches
-// rel_eps of the largest |ctc[.][s][.]| (all of them when rel_eps <= 0), widened to whole
-// 32-template segments; the matching loop subtracts a spike of s from that range only.
-static std::vector<int2> ctc_ranges(const OssModel& m, float rel_eps) {
-    const int64_t T = m.T, L2 = 2 * m.nt + 1;
-    const int T4 = (int)((T + 3) / 4);
-    std::vector<int2> r(T, make_int2(0, T4));
-    if (!(rel_eps > 0.f)) return r;
-    std::vector<float> amax((size_t)T * T);   // [s][t]: max over lags of |ctc[t][s][l]|
-    for (int64_t t = 0; t < T; ++t)
-        for (int64_t s = 0; s < T; ++s) {
-            float a = 0.f;
-            const float* c = &m.ctc[(t * T + s) * L2];
-            for (int64_t l = 0; l < L2; ++l) a = std::max(a, std::fabs(c[l]));
-            amax[s * T + t] = a;
-        }
-    for (int64_t s = 0; s < T; ++s) {
-        const float* a = &amax[s * T];
-        const float top = *std::max_element(a, a + T);
-        int64_t lo = T, hi = -1;
-        for (int64_t t = 0; t < T; ++t)
-            if (a[t] > rel_eps * top) {
-                lo = std::min(lo, t);
-                hi = t;
-            }
-        if (hi < 0) {
-            r[s] = make_int2(0, 0);   // a spike of s changes no score
-            continue;
-        }
-        r[s] = make_int2((int)(lo / 32) * 8, std::min(T4, (int)((hi / 32) + 1) * 8));
-    }
-    return r;
 }
 
 // The sorter's own limits on a loaded model (beyond the loader's file checks).
@@ -563,13 +527,6 @@ void Handle::init(const char* dir, const lss_params* prm) {
         throw LoadError{LSS_ERR_ARG, "lss_params.match_keep must be 0 (full loop) or 1.." + std::to_string(kPruneKeepMax)};
     keep = std::min(p.match_keep, T);
     if (keep > 0 && T > 1024) throw LoadError{LSS_ERR_ARG, "the pruned matching tier takes at most 1024 templates"};
-    if (!(p.ctc_rel_eps >= 0.f)) throw LoadError{LSS_ERR_ARG, "lss_params.ctc_rel_eps must be >= 0"};
-    {
-        const std::vector<int2> cr = ctc_ranges(m, p.ctc_rel_eps);
-        reach.assign(T, 0);
-        for (int t = 0; t < T; ++t) reach[tmpl_orig[t]] = std::min(4 * cr[t].y, T) - std::min(4 * cr[t].x, T);
-        d_crange = dev_upload(cr, dev_bytes, st);
-    }
     LSS_CUDA(cudaHostAlloc((void**)&h_gemm_err, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable));
     *h_gemm_err = 0;
     LSS_CUDA(cudaHostGetDevicePointer((void**)&d_gemm_err, h_gemm_err, 0));
@@ -891,7 +848,7 @@ void Handle::run_match(int nb, int Wn, int64_t& nl) {
         nl += 3;   // selection, loop, residual
     } else {
         LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st,
-                              p.match_variant, d_crange));
+                              p.match_variant));
         nl += 2;   // the loop and the residual
     }
 }
@@ -1210,7 +1167,6 @@ int lss_default_params(lss_params* p) {
     p->cluster_rule = 0;
     p->cluster_radius_um = 0.f;
     p->match_keep = 0;
-    p->ctc_rel_eps = 1e-6f;
     return LSS_OK;
 }
 
@@ -1462,12 +1418,6 @@ int lss_stage_times(lss_handle* hp, double* ms, int32_t n, int64_t* n_groups) {
     if (!hp || !ms || n < 0) return LSS_ERR_ARG;
     for (int i = 0; i < n && i < LSS_N_STAGES; ++i) ms[i] = hp->h.stage_ms[i];
     if (n_groups) *n_groups = hp->h.groups_timed;
-    return LSS_OK;
-}
-
-int lss_ctc_reach(const lss_handle* hp, int32_t* n_targets, int32_t n) {
-    if (!hp || !n_targets || n < hp->h.T) return LSS_ERR_ARG;
-    std::copy(hp->h.reach.begin(), hp->h.reach.end(), n_targets);
     return LSS_OK;
 }
 

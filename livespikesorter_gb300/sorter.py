@@ -19,7 +19,7 @@ import numpy as np
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = Path(os.environ.get("LSS_GB300_LIB", _PKG / "lib" / "liblss_gb300.so"))
 
-ABI_VERSION = 2
+ABI_VERSION = 1
 MAX_PCFEAT = 64
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_FORMAT", 4: "ERR_CUDA", 5: "ERR_NOMEM",
           6: "ERR_OVERFLOW", 7: "ERR_STATE", 8: "ERR_INTERNAL"}
@@ -32,8 +32,7 @@ class Params(ct.Structure):
                 ("hp_half_taps", ct.c_int32), ("dedup", ct.c_int32), ("th_override", ct.c_float),
                 ("spike_cap", ct.c_int32), ("mem_budget", ct.c_int64), ("profile", ct.c_int32),
                 ("match_variant", ct.c_int32), ("gemm_path", ct.c_int32), ("cluster_rule", ct.c_int32),
-                ("cluster_radius_um", ct.c_float), ("match_keep", ct.c_int32),
-                ("ctc_rel_eps", ct.c_float), ("reserved", ct.c_int32 * 1)]
+                ("cluster_radius_um", ct.c_float), ("match_keep", ct.c_int32)]
 
 
 class Spike(ct.Structure):
@@ -74,7 +73,6 @@ _SIGS = {
     "lss_push_device_span": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int64]),
     "lss_cuda_stream": (ct.c_int, [ct.c_void_p, _P(ct.c_void_p)]),
     "lss_stage_times": (ct.c_int, [ct.c_void_p, _P(ct.c_double), ct.c_int32, _P(ct.c_int64)]),
-    "lss_ctc_reach": (ct.c_int, [ct.c_void_p, _P(ct.c_int32), ct.c_int32]),
     "lss_match_noalloc": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_float,
                                      ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p,
                                      ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_void_p]),
@@ -225,12 +223,6 @@ class OnlineSorter:
         n = ct.c_int64()
         self._check(self.lib.lss_stage_times(self.h, ms, len(STAGES), ct.byref(n)))
         return dict(zip(STAGES, list(ms))), n.value
-
-    def ctc_reach(self) -> np.ndarray:
-        """Per template (oss_input order): how many templates' scores a spike of it updates."""
-        n = np.zeros(self.info.T, np.int32)
-        self._check(self.lib.lss_ctc_reach(self.h, n.ctypes.data_as(_P(ct.c_int32)), len(n)))
-        return n
 
     def push_device_span(self, dev_ptr: int, n_batches: int, first_row_sample: int = 0):
         self._check(self.lib.lss_push_device_span(self.h, ct.c_void_p(dev_ptr), int(n_batches), int(first_row_sample)))
