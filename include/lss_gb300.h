@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define LSS_ABI_VERSION 1
+#define LSS_ABI_VERSION 2
 #define LSS_MAX_PCFEAT 64 /* nearest channels x PCs carried per spike */
 
 enum lss_status {
@@ -71,6 +71,15 @@ typedef struct lss_params {
                                per sample only the match_keep templates of largest initial Cf = relu(B)^2 / nm
                                are scored through the loop (same updates on them, so the spikes equal the full
                                loop's unless an unlisted template would have won; agreement measured) */
+    int32_t highpass_mode;  /* 0 = Kilosort's zero-phase high-pass, circular over each batch window (preprocessing.py:
+                               120-154, OnlineSpikesV2.cu:1006-1056; hp_filter.npy), after the mean removal and median
+                               CAR (default); 1 = the same 3rd-order Butterworth (butter(3, highpass_hz, 'high')) run
+                               forward as second-order sections over the stream with FP32 state per channel carried
+                               from batch to batch on the device (starting at a segment's first sample in its steady
+                               state), then the median CAR; no mean removal (the filter removes DC).  The windows API
+                               filters each window alone. */
+    float highpass_hz;      /* edge of mode 1 (default 300, Kilosort's) */
+    float sample_rate_hz;   /* sample rate of mode 1 (default 30000) */
 } lss_params;
 
 /* One sorted spike.  time is the stream sample (Kilosort template_matching.py:68). */
@@ -198,6 +207,14 @@ int lss_cuda_stream(const lss_handle* h, void** stream);
  * (Timer.h:7-21) prints nothing; this is its working counterpart. */
 #define LSS_N_STAGES 10
 int lss_stage_times(lss_handle* h, double* ms, int32_t n, int64_t* n_groups);
+
+/* The second-order sections (b0, b1, b2, 1, a1, a2 each, sos[6 * n_sections]) of the Butterworth
+ * high-pass that highpass_mode 1 runs: order 1..4, edge cutoff_hz < fs_hz / 2.  Kilosort designs the
+ * same filter with scipy.signal.butter (preprocessing.py:121-136); this is the library's own design
+ * (bilinear transform of the analog prototype), exported so a caller can check it.  Sections are
+ * ordered by pole radius, the gain on the first. */
+int lss_butter_highpass_sos(int32_t order, double cutoff_hz, double fs_hz, double* sos, int32_t cap_sections,
+                            int32_t* n_sections);
 
 /* The matching loop of one window on buffers the caller owns, allocating no memory.
  *

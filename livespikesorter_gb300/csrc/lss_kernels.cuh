@@ -13,6 +13,7 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <vector>
 
 namespace lss {
 
@@ -69,6 +70,39 @@ void launch_car_t(const int16_t* raw, int64_t row_stride, const int32_t* chan, i
 // Ylo != nullptr: Y receives tf32(y) and Ylo the remainder (operands of the tensor-core GEMM)
 void launch_highpass(const float* Xw, int C, int W, int L, int R, const float* taps, int nb, float* Y,
                      cudaStream_t s, float* Ylo = nullptr);
+
+// stateful high-pass mode (kernels_iir.cu): a causal Butterworth high-pass as second-order sections
+// with FP32 state per channel, then the median CAR, written to Y in the whitening GEMM's format
+constexpr int kIirMaxSections = 2;   // orders up to 4
+constexpr int kHighpassOrder = 3;    // Kilosort's high-pass: butter(3, fc, 'high') (preprocessing.py:121-136)
+constexpr int kIirChunk = 32;        // rows per chunk of the chunked recurrence
+struct IirCoeffs {
+    int ns;                          // sections (unused ones are identity)
+    float b[kIirMaxSections][3];     // b0, b1, b2 of each section
+    float a[kIirMaxSections][2];     // a1, a2 (a0 = 1)
+    float zi[2 * kIirMaxSections];   // state of the steady response to a unit constant input
+    float P[4 * kIirMaxSections * kIirMaxSections];   // zero-input state transition over kIirChunk rows
+};
+// the rows of one group: window b = rows [b NT, b NT + W); independent: every window is its own
+// chain (windows API), else the group is one chain of span rows whose entering state is carried
+// (reset: a segment starts, the steady state of the first row instead); carry_row: the row whose
+// entering state the next group continues from (nb NT)
+struct IirGroup {
+    int nb, W, NT, span;
+    bool independent, reset;
+    int carry_row;
+    int chunks;   // set by the launcher
+};
+// sections (b0, b1, b2, 1, a1, a2) of a Butterworth high-pass; returns their count, -1 on bad args
+int butter_highpass_sos(int order, double fc, double fs, std::vector<double>& sos);
+IirCoeffs make_iir_coeffs(const std::vector<double>& sos);
+int iir_chunks(const IirGroup& g);
+// zs, sin: [iir_chunks(g)][C] float4 scratch; carried [C] float4 (read on continuation, written at
+// carry_row); out_mode 0 = FP32 Y, 1 = TF32 split (Ylo may be null: tf32 alone), 2 = BF16 split
+cudaError_t launch_iir_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, IirGroup g,
+                           const IirCoeffs& k, float4* zs, float4* sin, float4* carried, float* Y, float* Ylo,
+                           int out_mode, cudaStream_t s, int64_t& nl);
+
 void launch_sgemm_nt(const float* A, int64_t lda, int64_t strideA, const float* B, int64_t ldb,
                      float* Cm, int64_t ldc, int64_t strideC, int M, int N, int K, int nb, cudaStream_t s);
 // wPCA_host (K*nt floats) enables the specialisation with the basis in the parameter bank;

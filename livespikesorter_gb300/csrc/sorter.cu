@@ -165,6 +165,13 @@ struct Handle {
     int* d_gemm_err = nullptr;
     int64_t *d_iCC = nullptr, *d_iU = nullptr;
     int32_t* d_chan = nullptr;
+    // stateful high-pass mode (highpass_mode 1): coefficients, the state entering the next group's
+    // first row, the stream time that group must start at to continue the chain
+    bool iir = false;
+    IirCoeffs iirk{};
+    float4* d_iir_state = nullptr;   // [C]
+    int64_t iir_expect = INT64_MIN;
+    bool iir_reset = true;           // the next streaming group starts a chain
     std::map<int, TapSet> taps;
 
     // work buffers
@@ -179,6 +186,7 @@ struct Handle {
     float *d_Xt_hi = nullptr, *d_Xt_lo = nullptr;   // channel-major wrapped windows (tensor-core high-pass)
     float *d_Zt_hi = nullptr, *d_Zt_lo = nullptr;   // channel-major whitened windows (tensor-core convolution)
     float* d_split = nullptr;   // partial projections of split-K launches [kSplitK][rows][T]
+    float4 *d_iir_zs = nullptr, *d_iir_sin = nullptr;   // stateful high-pass: per-chunk states [chunks][C]
     MatchScratch sc{};
     MatchOut mo{};
     int64_t work_bytes = 0;
@@ -229,6 +237,10 @@ struct Handle {
     void init(const char* dir, const lss_params* prm);
     TapSet& taps_for(int Wn);
     void ensure_work(int Wn, int nb);
+    // chunks of the stateful high-pass for any group up to nba windows of up to Wa samples
+    size_t iir_chunk_cap(int Wa, int nba) const {
+        return (size_t)nba * (size_t)((std::max(Wa, NT) + kIirChunk - 1) / kIirChunk) + 1;
+    }
     void free_work();
     int acquire_slot();
     void launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, int stage_rows,
@@ -243,6 +255,8 @@ struct Handle {
     void launch_pending(int g, int pad_mode);
     int16_t* slot_raw(const Slot& s) { return d_raw + (size_t)(&s - slots.data()) * raw_rows_cap * Cin; }
     void stage_to_device(Slot& s, int64_t upto);
+    void run_zero_phase(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
+                        const std::function<void()>& mark);
     void run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
                               const std::function<void()>& mark);
     void run_match(int nb, int Wn, int64_t& nl);
@@ -264,7 +278,7 @@ Handle::~Handle() {
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
                     (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo,
-                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm})
+                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm, (void*)d_iir_state})
         if (p) cudaFree(p);
     if (h_gemm_err) cudaFreeHost(h_gemm_err);
     for (auto& s : slots) {
@@ -297,7 +311,8 @@ void Handle::free_work() {
     }
     for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_ticket, (void*)d_mean, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
                     (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo, (void*)d_Zt_hi, (void*)d_Zt_lo,
-                    (void*)d_split, (void*)d_lid, (void*)d_lsc, (void*)d_pcf, (void*)d_pslot,
+                    (void*)d_split, (void*)d_lid, (void*)d_lsc, (void*)d_pcf, (void*)d_pslot, (void*)d_iir_zs,
+                    (void*)d_iir_sin,
                     (void*)sc.cfmax, (void*)sc.at_t, (void*)sc.at_amp, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
                     (void*)mo.sp_t, (void*)mo.sp_amp, (void*)mo.sp_iter})
         if (p) cudaFree(p);
@@ -310,6 +325,7 @@ void Handle::free_work() {
     d_Xt_hi = d_Xt_lo = nullptr;
     d_Zt_hi = d_Zt_lo = nullptr;
     d_split = nullptr;
+    d_iir_zs = d_iir_sin = nullptr;
     d_lid = nullptr;
     d_lsc = nullptr;
     d_pcf = nullptr;
@@ -402,6 +418,16 @@ void Handle::init(const char* dir, const lss_params* prm) {
     G = p.group_batches;
     max_iters = p.max_iters;
     th = p.th_override > 0.f ? p.th_override : m.th;
+    if (p.highpass_mode != 0 && p.highpass_mode != 1)
+        throw LoadError{LSS_ERR_ARG, "lss_params.highpass_mode must be 0 (zero-phase) or 1 (stateful sections)"};
+    iir = p.highpass_mode == 1;
+    if (iir) {
+        std::vector<double> sos;
+        if (butter_highpass_sos(kHighpassOrder, p.highpass_hz, p.sample_rate_hz, sos) < 0)
+            throw LoadError{LSS_ERR_ARG, "lss_params: high-pass edge must lie in (0, sample_rate_hz / 2)"};
+        iirk = make_iir_coeffs(sos);
+        if (C > 1024) throw LoadError{LSS_ERR_ARG, "the stateful high-pass takes at most 1024 channels"};
+    }
     if (Cin > C) {
         for (int64_t v : m.channel_map)
             if (v < 0 || v >= Cin) throw LoadError{LSS_ERR_FORMAT, "channelMap entry outside n_chan_in"};
@@ -527,6 +553,7 @@ void Handle::init(const char* dir, const lss_params* prm) {
         throw LoadError{LSS_ERR_ARG, "lss_params.match_keep must be 0 (full loop) or 1.." + std::to_string(kPruneKeepMax)};
     keep = std::min(p.match_keep, T);
     if (keep > 0 && T > 1024) throw LoadError{LSS_ERR_ARG, "the pruned matching tier takes at most 1024 templates"};
+    if (iir) d_iir_state = dev_alloc<float4>((size_t)C, dev_bytes);
     LSS_CUDA(cudaHostAlloc((void**)&h_gemm_err, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable));
     *h_gemm_err = 0;
     LSS_CUDA(cudaHostGetDevicePointer((void**)&d_gemm_err, h_gemm_err, 0));
@@ -615,7 +642,8 @@ void Handle::ensure_work(int Wn, int nb) {
                          (int64_t)nba * ((Wa + 7) / 8 * 8) * C * 4 * (tc_conv ? (tf32_data ? 1 : 2) : 0) +
                          (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16 +
                          (tc_project ? (int64_t)kSplitK * std::min(nba, kSplitBatches) * Wa * T * 4 : 0) +
-                         (keep > 0 ? (int64_t)nba * Wa * kPruneKeepMax * 6 + (int64_t)nba * (Wa + 2 * nt) * 5 : 0);
+                         (keep > 0 ? (int64_t)nba * Wa * kPruneKeepMax * 6 + (int64_t)nba * (Wa + 2 * nt) * 5 : 0) +
+                         (iir ? (int64_t)iir_chunk_cap(Wa, nba) * C * 32 : 0);
     if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
         throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
                                            " device bytes, budget " + std::to_string(p.mem_budget)};
@@ -650,6 +678,11 @@ void Handle::ensure_work(int Wn, int nb) {
     if (tc_whiten && !tf32_data) d_Y_lo = dev_alloc<float>((size_t)nba * Wa * C, dev_bytes);
     if (tc_project && !tf32_data) d_Bpc_lo = dev_alloc<float>((size_t)nba * Wa * K * C, dev_bytes);
     if (tc_project) d_split = dev_alloc<float>((size_t)kSplitK * std::min(nba, kSplitBatches) * Wa * T, dev_bytes);
+    if (iir) {
+        const size_t ch = iir_chunk_cap(Wa, nba);
+        d_iir_zs = dev_alloc<float4>(ch * C, dev_bytes);
+        d_iir_sin = dev_alloc<float4>(ch * C, dev_bytes);
+    }
     sc.cfmax = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
     sc.at_t = dev_alloc<int>((size_t)nba * Wa, dev_bytes);
     sc.at_amp = dev_alloc<float>((size_t)nba * Wa, dev_bytes);
@@ -727,8 +760,10 @@ int Handle::acquire_slot() {
 
 // Preprocessing, whitening, basis convolution and projection of nb windows (raw rows already on
 // the device) into d_Z (whitened windows) and d_Bt (scores).  mark() is called after each stage.
-void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
-                                  const std::function<void()>& mark) {
+// Kilosort's preprocessing up to Y (io.py:757-790): channel means, median CAR, circular zero-phase
+// high-pass
+void Handle::run_zero_phase(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
+                            const std::function<void()>& mark) {
     launch_colsum(raw, Cin, d_chan, C, Wn, NTs, nb, d_colsum, d_ticket, d_mean, st), ++nl;
     mark();
     if (tc_highpass) {
@@ -752,6 +787,29 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
         mark();
         launch_highpass(d_Xw, C, Wn, ts.L, ts.R, ts.d, nb, d_Y, st, tc_whiten ? d_Y_lo : nullptr), ++nl;
         mark();
+    }
+}
+
+void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, const TapSet& ts, int64_t& nl,
+                                  const std::function<void()>& mark) {
+    if (iir) {
+        // stateful high-pass + median CAR straight into Y (timed as the high-pass stage); windows
+        // of the windows API (NTs == Wn) are chains of their own, a streaming group continues the
+        // previous one unless a segment starts
+        IirGroup g{};
+        g.nb = nb, g.W = Wn, g.NT = NTs, g.span = (nb - 1) * NTs + Wn;
+        g.independent = NTs == Wn;
+        g.reset = iir_reset;
+        g.carry_row = nb * NTs;
+        mark();
+        mark();
+        const int mode = bf16_pre ? 2 : (tc_whiten ? 1 : 0);
+        LSS_CUDA(launch_iir_car(raw, Cin, d_chan, C, g, iirk, d_iir_zs, d_iir_sin, d_iir_state, d_Y,
+                                tc_whiten ? d_Y_lo : nullptr, mode, st, nl));
+        if (!g.independent) iir_reset = false;
+        mark();
+    } else {
+        run_zero_phase(raw, nb, Wn, NTs, ts, nl, mark);
     }
     if (tc_whiten)
         LSS_CUDA(launch_umma_gemm_zt(um_whiten, d_Z, nb * Wn, C, C, tc_conv ? d_Zt_hi : nullptr,
@@ -872,6 +930,9 @@ void Handle::push_device(const int16_t* rows, int64_t n_batches, int64_t first_r
             s.win_start[b] = first_row_sample + (b0 + b) * (int64_t)NT;
             s.batch_id[b] = batch_counter + b;
         }
+        // the stateful high-pass continues when these rows follow the previous span's
+        iir_reset = s.win_start[0] != iir_expect;
+        iir_expect = s.win_start[0] + (int64_t)g * NT;
         launch_group(s, g, W, NT, taps_for(W), 0, rows + (size_t)b0 * NT * Cin);
         inflight.push_back(si);
         batch_counter += g;
@@ -1027,6 +1088,8 @@ void Handle::launch_pending(int g, int pad_mode) {
     pend = -1;
     pend_rows = 0;
     pend_dev = 0;
+    iir_reset = next_batch == 0;   // a segment's first group starts the stateful high-pass afresh
+    iir_expect = s.win_start[0] + (int64_t)g * NT;
     launch_group(s, g, W, NT, taps_for(W), (int)rows_need, slot_raw(s), true);
     inflight.push_back(si);
     next_batch += g;
@@ -1167,6 +1230,9 @@ int lss_default_params(lss_params* p) {
     p->cluster_rule = 0;
     p->cluster_radius_um = 0.f;
     p->match_keep = 0;
+    p->highpass_mode = 0;
+    p->highpass_hz = 300.f;
+    p->sample_rate_hz = 30000.f;
     return LSS_OK;
 }
 
@@ -1418,6 +1484,17 @@ int lss_stage_times(lss_handle* hp, double* ms, int32_t n, int64_t* n_groups) {
     if (!hp || !ms || n < 0) return LSS_ERR_ARG;
     for (int i = 0; i < n && i < LSS_N_STAGES; ++i) ms[i] = hp->h.stage_ms[i];
     if (n_groups) *n_groups = hp->h.groups_timed;
+    return LSS_OK;
+}
+
+int lss_butter_highpass_sos(int32_t order, double cutoff_hz, double fs_hz, double* sos, int32_t cap_sections,
+                            int32_t* n_sections) {
+    if (!sos || !n_sections) return LSS_ERR_ARG;
+    std::vector<double> v;
+    const int n = lss::butter_highpass_sos(order, cutoff_hz, fs_hz, v);
+    if (n < 0 || n > cap_sections) return LSS_ERR_ARG;
+    std::copy(v.begin(), v.end(), sos);
+    *n_sections = n;
     return LSS_OK;
 }
 

@@ -19,7 +19,7 @@ import numpy as np
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = Path(os.environ.get("LSS_GB300_LIB", _PKG / "lib" / "liblss_gb300.so"))
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_PCFEAT = 64
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_FORMAT", 4: "ERR_CUDA", 5: "ERR_NOMEM",
           6: "ERR_OVERFLOW", 7: "ERR_STATE", 8: "ERR_INTERNAL"}
@@ -32,7 +32,8 @@ class Params(ct.Structure):
                 ("hp_half_taps", ct.c_int32), ("dedup", ct.c_int32), ("th_override", ct.c_float),
                 ("spike_cap", ct.c_int32), ("mem_budget", ct.c_int64), ("profile", ct.c_int32),
                 ("match_variant", ct.c_int32), ("gemm_path", ct.c_int32), ("cluster_rule", ct.c_int32),
-                ("cluster_radius_um", ct.c_float), ("match_keep", ct.c_int32)]
+                ("cluster_radius_um", ct.c_float), ("match_keep", ct.c_int32),
+                ("highpass_mode", ct.c_int32), ("highpass_hz", ct.c_float), ("sample_rate_hz", ct.c_float)]
 
 
 class Spike(ct.Structure):
@@ -73,6 +74,8 @@ _SIGS = {
     "lss_push_device_span": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int64]),
     "lss_cuda_stream": (ct.c_int, [ct.c_void_p, _P(ct.c_void_p)]),
     "lss_stage_times": (ct.c_int, [ct.c_void_p, _P(ct.c_double), ct.c_int32, _P(ct.c_int64)]),
+    "lss_butter_highpass_sos": (ct.c_int, [ct.c_int32, ct.c_double, ct.c_double, _P(ct.c_double), ct.c_int32,
+                                           _P(ct.c_int32)]),
     "lss_match_noalloc": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_float,
                                      ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p,
                                      ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32, ct.c_void_p]),
@@ -171,6 +174,17 @@ def default_params(**kw) -> Params:
             raise AttributeError(k)
         setattr(p, k, v)
     return p
+
+
+def butter_highpass_sos(order: int = 3, cutoff_hz: float = 300.0, fs_hz: float = 30000.0) -> np.ndarray:
+    """The library's second-order sections [n, 6] of the Butterworth high-pass of highpass_mode 1."""
+    lib = load_library()
+    sos = np.zeros((4, 6), np.float64)
+    n = ct.c_int32()
+    st = lib.lss_butter_highpass_sos(order, cutoff_hz, fs_hz, sos.ctypes.data_as(_P(ct.c_double)), 4, ct.byref(n))
+    if st != 0:
+        raise SorterError(st, "lss_butter_highpass_sos: bad arguments")
+    return sos[: n.value].copy()
 
 
 class OnlineSorter:

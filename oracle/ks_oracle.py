@@ -24,6 +24,11 @@ Functions and the reference lines they restate:
 * ``stream_times``       -- the spike-time formula of ``extract`` (KS/template_matching.py:56-68)
 * ``remove_duplicates``  -- KS/postprocessing.py:9-30
 * ``nearest_centroid``   -- ``OnlineSpikesV2::closestCluster`` (OnlineSpikesV2.cu:1058-1074)
+* ``sos_highpass`` / ``sort_stream_biquad`` -- the sorter's stateful high-pass mode, which has no
+                            counterpart in the reference: Kilosort's filter design
+                            (KS/preprocessing.py:121-136, ``butter(3, 300, 'high')``) run forward
+                            with ``scipy.signal.sosfilt`` in float64 over the stream, then the median
+                            CAR and ``(M @ Wrot)``; the matching after it is Kilosort's
 """
 from __future__ import annotations
 
@@ -385,7 +390,12 @@ class WindowResult:
 
 def sort_window(window_CW: np.ndarray, oss: OssArrays, max_iters: int = 50,
                 dtype=np.float64, amp_dtype=None) -> WindowResult:
-    X = preprocess(window_CW, oss, dtype=dtype)
+    return sort_preprocessed(preprocess(window_CW, oss, dtype=dtype), oss, max_iters, dtype, amp_dtype)
+
+
+def sort_preprocessed(X: np.ndarray, oss: OssArrays, max_iters: int = 50, dtype=np.float64,
+                      amp_dtype=None) -> WindowResult:
+    """Kilosort's matching, features and positions on an already preprocessed [C, W] window."""
     m = run_matching(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned, max_iters=max_iters,
                      dtype=dtype, amp_dtype=amp_dtype)
     tF = pc_features(m.Xres, m.st, m.amps, oss, dtype=dtype)
@@ -419,5 +429,75 @@ def sort_stream(data_NC: np.ndarray, oss: OssArrays, NT: int, max_iters: int = 5
         res["cluster"] = nearest_centroid(res["x"], res["y"], oss.centroids)
     else:
         res["cluster"] = pc_score_cluster(res["tF"], res["x"], res["y"], oss.centroids, centroids_pca, radius)
+    res["keep"] = remove_duplicates(res["time"], res["cluster"], oss.dup_bins)
+    return res
+
+
+# ----------------------------------------------------------------------------------------
+# stateful high-pass mode (no counterpart in the reference)
+# ----------------------------------------------------------------------------------------
+
+
+def highpass_sos(order: int = 3, cutoff_hz: float = 300.0, fs: float = 30000.0) -> np.ndarray:
+    """Kilosort's high-pass design (KS/preprocessing.py:121-136) as second-order sections."""
+    from scipy.signal import butter
+    return butter(order, cutoff_hz, btype="high", fs=fs, output="sos")
+
+
+def sos_highpass(x_NC: np.ndarray, sos: np.ndarray, zi=None):
+    """The causal high-pass along time (axis 0) in float64; from the steady state of the first row
+    (``sosfilt_zi * x[0]``) unless ``zi`` [n_sections, 2, C] continues an earlier call.  Returns
+    the filtered rows and the final state."""
+    from scipy.signal import sosfilt, sosfilt_zi
+    x = np.asarray(x_NC, np.float64)
+    if zi is None:
+        zi = sosfilt_zi(sos)[:, :, None] * x[0][None, None, :]
+    return sosfilt(sos, x, axis=0, zi=zi)
+
+
+def biquad_padded_stream(data_NC: np.ndarray, NT: int, nt: int) -> np.ndarray:
+    """The rows the streaming sorter filters, with Kilosort's batch framing (KS/io.py:584-637):
+    nt copies of the first sample, the recording, then the last window's right pad (copies of the
+    last sample, or zeros when the first batch is also the last); window j = rows [j NT, j NT + W)."""
+    N, C = data_NC.shape
+    nb = n_batches(N, NT)
+    W = NT + 2 * nt
+    tail = (nb - 1) * NT + W - nt - N
+    x = np.asarray(data_NC, np.float64)
+    pad = np.zeros((max(tail, 0), C)) if nb == 1 else np.repeat(x[-1:], max(tail, 0), axis=0)
+    return np.concatenate([np.repeat(x[:1], nt, axis=0), x, pad])[: (nb - 1) * NT + W]
+
+
+def preprocess_biquad(F_WC: np.ndarray, oss: OssArrays) -> np.ndarray:
+    """Filtered rows [W, C] of one window -> [C, W]: lower-median CAR per sample, then (M @ Wrot)."""
+    X = np.asarray(F_WC, np.float64).T
+    X = X - lower_median(X, 0)[None, :]
+    WD = oss.drift.astype(np.float64) @ oss.whitening.astype(np.float64)
+    return WD @ X
+
+
+def sort_stream_biquad(data_NC: np.ndarray, oss: OssArrays, NT: int, sos: np.ndarray, max_iters: int = 50):
+    """``sort_stream`` with the stateful high-pass: the padded stream filtered once, forward, each
+    batch window cut from it, CAR'd, whitened and matched.  Nearest-centroid clusters and duplicate
+    removal as in ``sort_stream``."""
+    nt = oss.wPCA.shape[1]
+    W = NT + 2 * nt
+    F, _ = sos_highpass(biquad_padded_stream(data_NC, NT, nt), sos)
+    nb = n_batches(data_NC.shape[0], NT)
+    out = {k: [] for k in ("time", "template", "amp", "x", "y", "tF")}
+    for ib in range(nb):
+        r = sort_preprocessed(preprocess_biquad(F[ib * NT: ib * NT + W], oss), oss, max_iters=max_iters)
+        t = stream_times(r.match.st[:, 0], ib * NT - nt, nt, oss.nt0min)
+        keep = t >= 0 if ib == 0 else np.ones(len(t), bool)
+        out["time"].append(t[keep])
+        out["template"].append(r.match.st[keep, 1])
+        out["amp"].append(r.match.amps[keep])
+        out["x"].append(r.xs[keep])
+        out["y"].append(r.ys[keep])
+        out["tF"].append(r.tF[keep])
+    res = {k: (np.concatenate(v) if len(v) else np.zeros(0)) for k, v in out.items()}
+    order = np.lexsort((res["template"], res["time"]))
+    res = {k: v[order] for k, v in res.items()}
+    res["cluster"] = nearest_centroid(res["x"], res["y"], oss.centroids)
     res["keep"] = remove_duplicates(res["time"], res["cluster"], oss.dup_bins)
     return res

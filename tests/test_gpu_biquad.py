@@ -1,0 +1,86 @@
+"""The stateful high-pass mode (highpass_mode 1) on the GPU against the float64 oracle: the causal
+Butterworth sections over the stream (scipy.signal.sosfilt from the first sample's steady state),
+median CAR, (M @ Wrot), then Kilosort's matching.  Tolerances: the preprocessed window within 2e-5
+of the largest magnitude on every GEMM path; spikes >= 99.5 % agreement (same template, |dt| <= 1)
+with >= 99.5 % of the matched amplitudes within 1e-3 relative; the state carried across groups and
+device spans gives the same spikes as one long group, bit for bit."""
+import numpy as np
+import pytest
+
+from livespikesorter_gb300 import sorter
+from oracle import ks_oracle as ko
+
+from lss_testutil import agreement
+
+pytestmark = pytest.mark.gpu
+
+AGREE = 0.995
+
+
+def _rel_close(got, ref, frac):
+    scale = np.abs(ref).max()
+    err = np.abs(got - ref).max()
+    assert err <= frac * scale, f"max err {err:.3e} vs scale {scale:.3e} ({err / scale:.2e})"
+
+
+@pytest.mark.parametrize("gemm_path", [0, 1, 3])
+def test_biquad_window_preprocessed(cfg_stream, gemm_path):
+    """Windows API: each window filtered alone from its first sample's steady state."""
+    d, data, _ = cfg_stream
+    oss = ko.load_oss_input(d)
+    sos = ko.highpass_sos()
+    win = data[1500 - 61: 3000 + 61]
+    F, _ = ko.sos_highpass(win, sos)
+    ref = ko.preprocess_biquad(F, oss)
+    with sorter.OnlineSorter(d, batch_samples=1500, highpass_mode=1, gemm_path=gemm_path) as s:
+        got = s.debug_stage(win, sorter.STAGE_PREPROCESSED)
+    _rel_close(got.T.astype(np.float64), ref, 2e-5)
+
+
+def test_biquad_stream_matches_oracle(cfg_stream):
+    """Streaming: six 1500-sample batches in groups of four (the state crosses a group boundary),
+    the last window padded at the flush."""
+    d, data, _ = cfg_stream
+    oss = ko.load_oss_input(d)
+    ref = ko.sort_stream_biquad(data, oss, 1500, ko.highpass_sos(), max_iters=50)
+    with sorter.OnlineSorter(d, batch_samples=1500, max_iters=50, group_batches=4, highpass_mode=1) as s:
+        sp = s.sort_stream(data, chunk=1111)
+    k = ref["keep"]
+    a, amp_ok, amax = agreement(ref["time"][k], ref["template"][k], ref["amp"][k], sp["time"], sp["tmpl"], sp["amp"])
+    assert k.sum() > 300
+    assert a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax, len(sp), int(k.sum()))
+
+
+def test_biquad_state_carries_across_groups_and_spans(cfg_stream):
+    """The same rows as one group, as groups of one, and as device spans of two and one batches
+    give the same spikes bit for bit; a span that does not follow the previous one restarts."""
+    import torch
+    d, data, _ = cfg_stream
+    NT, nb = 1500, 6
+    rows = np.ascontiguousarray(data[: nb * NT + 122])
+    dev = torch.from_numpy(rows).cuda()
+    ptr, row_bytes = dev.data_ptr(), rows.shape[1] * 2
+    outs = []
+    for group, spans in ((6, (6,)), (1, (6,)), (2, (2, 2, 2)), (1, (1, 3, 2))):
+        with sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=group, highpass_mode=1) as s:
+            b0 = 0
+            for n in spans:
+                s.push_device_span(ptr + b0 * NT * row_bytes, n, b0 * NT)
+                b0 += n
+            outs.append(s.poll_all())
+    assert len(outs[0]) > 100
+    for o in outs[1:]:
+        assert len(o) == len(outs[0])
+        for f in ("time", "tmpl", "amp", "x", "y"):
+            np.testing.assert_array_equal(o[f], outs[0][f])
+    # a gap in the stream times: the second span starts its own chain
+    with sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=3, highpass_mode=1) as s:
+        s.push_device_span(ptr, 3, 0)
+        s.push_device_span(ptr + 3 * NT * row_bytes, 3, 10 ** 7)
+        gap = s.poll_all()
+    with sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=3, highpass_mode=1) as s:
+        s.push_device_span(ptr + 3 * NT * row_bytes, 3, 10 ** 7)
+        alone = s.poll_all()
+    late = gap[gap["time"] >= 10 ** 6]
+    assert len(late) == len(alone)
+    np.testing.assert_array_equal(late["amp"], alone["amp"])
