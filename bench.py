@@ -458,6 +458,51 @@ def run_gpu(a):
                 "agreement_vs_fp32": {"batches": (n_rows - 2 * nt) // NT, "spikes_fp32": int(len(got[0])),
                                       "spikes_tier": int(len(got[tp])), "matched": frac, "amp_within_1e-3": amp_ok,
                                       "rule": "same template, |dt| <= 1 sample, amplitude within 1e-3 relative"}}
+    # ---- the stateful high-pass mode beside the zero-phase one ----------------------------------
+    stateful = None
+    if a.gemm_path == 0 and not a.no_tier:
+        ss = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1,
+                                 match_variant=a.match_variant, highpass_mode=1)
+        ext3 = torch.cuda.ExternalStream(ss.cuda_stream(), device=f"cuda:{dev}")
+        for i in range(a.warmup):
+            ss.push_device_span(base_ptr + (i % n_groups) * G * NT * row_bytes, G, i * G * NT)
+        drain(ss)
+        tb, nb0 = ss.stage_times()
+        torch.cuda.synchronize(dev)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext3):
+            f0.record(ext3)
+        for i in range(a.warmup, a.warmup + a.steps):
+            # consecutive spans of the recording: the filter state carries from group to group
+            ss.push_device_span(base_ptr + (i % n_groups) * G * NT * row_bytes, G, i * G * NT)
+        with torch.cuda.stream(ext3):
+            f1.record(ext3)
+        f1.synchronize()
+        ms3 = f0.elapsed_time(f1)
+        drain(ss)
+        ta, na = ss.stage_times()
+        ss.close()
+        n_rows = min(data.shape[0], 256 * NT + 2 * nt)
+        got = {}
+        for mode in (0, 1):
+            with sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
+                                     match_variant=a.match_variant, highpass_mode=mode) as sa:
+                got[mode] = sa.sort_stream(data[:n_rows])
+        frac, amp_ok = spike_agreement(got[0], got[1])
+        per = {k: (ta[k] - tb[k]) / max(1, na - nb0) for k in ta}
+        stateful = {"highpass_mode": 1, "value": a.steps * G * NT * C / (ms3 / 1e3), "unit": UNIT,
+                    "ms_per_step": ms3 / a.steps,
+                    "filter": "Butterworth 3rd order 300 Hz high-pass, second-order sections run forward, FP32 state "
+                              "carried across groups; median CAR after it",
+                    "stage_ms_per_launch": per,
+                    "filter_and_car_ms_per_launch": per.get("colsum", 0) + per.get("car", 0) + per.get("highpass", 0),
+                    "spikes_vs_zero_phase": {"batches": (n_rows - 2 * nt) // NT, "spikes_zero_phase": int(len(got[0])),
+                                             "spikes_stateful": int(len(got[1])), "matched": frac,
+                                             "amp_within_1e-3": amp_ok,
+                                             "note": "different filters (causal vs zero-phase): agreement is not "
+                                                     "expected to be 1; each mode is checked against its own float64 "
+                                                     "oracle in the tests"}}
     del d_data
 
     # ---- end to end through the host API ---------------------------------------------------
@@ -533,6 +578,7 @@ def run_gpu(a):
                 "data": "synthetic (seeded generator, shapes of the named config)",
                 "config": workload_config(a, cfg, G), "e2e": e2e, "latency": latency, "roofline": roof,
                 "cpu_baseline": cpu, "clocks": clk.summary(), "chosen_tier": tier, "chosen": chosen_block,
+                "highpass_stateful": stateful,
                 "gpu_launches": launches_per_step * a.steps,
                 "spikes_per_batch": spikes_per_batch,
                 "realtime_factor": value / (C * 30000.0)}

@@ -52,27 +52,33 @@ def test_biquad_stream_matches_oracle(cfg_stream):
 
 
 def test_biquad_state_carries_across_groups_and_spans(cfg_stream):
-    """The same rows as one group, as groups of one, and as device spans of two and one batches
-    give the same spikes bit for bit; a span that does not follow the previous one restarts."""
+    """The same rows as one group, as groups of one, and as device spans of two and one batches give
+    the same spikes (>= 99.9 %, amplitudes within 1e-3): the chunk boundaries of the recurrence follow
+    each group, so regrouping moves FP32 rounding only.  One configuration run twice is bitwise
+    identical.  A span that does not follow the previous one restarts the chain."""
     import torch
     d, data, _ = cfg_stream
     NT, nb = 1500, 6
     rows = np.ascontiguousarray(data[: nb * NT + 122])
     dev = torch.from_numpy(rows).cuda()
     ptr, row_bytes = dev.data_ptr(), rows.shape[1] * 2
-    outs = []
-    for group, spans in ((6, (6,)), (1, (6,)), (2, (2, 2, 2)), (1, (1, 3, 2))):
+
+    def run(group, spans, first=0):
         with sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=group, highpass_mode=1) as s:
             b0 = 0
             for n in spans:
-                s.push_device_span(ptr + b0 * NT * row_bytes, n, b0 * NT)
+                s.push_device_span(ptr + b0 * NT * row_bytes, n, first + b0 * NT)
                 b0 += n
-            outs.append(s.poll_all())
+            return s.poll_all()
+
+    outs = [run(g, sp) for g, sp in ((6, (6,)), (1, (6,)), (2, (2, 2, 2)), (1, (1, 3, 2)))]
     assert len(outs[0]) > 100
     for o in outs[1:]:
-        assert len(o) == len(outs[0])
-        for f in ("time", "tmpl", "amp", "x", "y"):
-            np.testing.assert_array_equal(o[f], outs[0][f])
+        a, amp_ok, amax = agreement(outs[0]["time"], outs[0]["tmpl"], outs[0]["amp"], o["time"], o["tmpl"], o["amp"])
+        assert a >= 0.999 and amp_ok >= 0.999, (a, amp_ok, amax)
+    again = run(2, (2, 2, 2))
+    for f in ("time", "tmpl", "amp", "x", "y"):
+        np.testing.assert_array_equal(again[f], outs[2][f])
     # a gap in the stream times: the second span starts its own chain
     with sorter.OnlineSorter(d, batch_samples=NT, max_iters=50, group_batches=3, highpass_mode=1) as s:
         s.push_device_span(ptr, 3, 0)
