@@ -101,7 +101,7 @@ static double cascade_step(const std::vector<double>& sos, int ns, double* z, do
     return u;
 }
 
-IirCoeffs make_iir_coeffs(const std::vector<double>& sos) {
+IirCoeffs make_iir_coeffs(const std::vector<double>& sos, std::vector<float>& powers) {
     const int ns = (int)(sos.size() / 6);
     IirCoeffs k{};
     k.ns = kIirMaxSections;
@@ -151,6 +151,23 @@ IirCoeffs make_iir_coeffs(const std::vector<double>& sos) {
     }
     for (int i = 0; i < S; ++i)
         for (int j = 0; j < S; ++j) k.P[i * S + j] = (float)P[i][j];
+    // P^0 .. P^kIirChunk for the warp scan
+    powers.assign((size_t)(kIirChunk + 1) * S * S, 0.f);
+    double Q[S][S];
+    for (int i = 0; i < S; ++i)
+        for (int j = 0; j < S; ++j) Q[i][j] = i == j;
+    for (int n = 0; n <= kIirChunk; ++n) {
+        for (int i = 0; i < S; ++i)
+            for (int j = 0; j < S; ++j) powers[(size_t)n * S * S + i * S + j] = (float)Q[i][j];
+        double R[S][S];
+        for (int i = 0; i < S; ++i)
+            for (int j = 0; j < S; ++j) {
+                double acc = 0.0;
+                for (int q = 0; q < S; ++q) acc += P[i][q] * Q[q][j];
+                R[i][j] = acc;
+            }
+        std::copy(&R[0][0], &R[0][0] + S * S, &Q[0][0]);
+    }
     return k;
 }
 
@@ -210,34 +227,77 @@ iir_zero_state_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const
     zs[(int64_t)q * C + c] = z;
 }
 
-// per channel, sequentially over the chunks: the state entering each chunk
-__global__ void __launch_bounds__(kIirThreads)
-iir_scan_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C,
-                IirGroup g, IirCoeffs k, const float4* __restrict__ zs, const float4* __restrict__ carried,
-                float4* __restrict__ sin) {
-    const int c = blockIdx.x * kIirThreads + threadIdx.x;
+__device__ __forceinline__ float4 matvec4(const float* P, const float4 s, const float4 add) {
+    float4 n;
+    n.x = fmaf(P[0], s.x, fmaf(P[1], s.y, fmaf(P[2], s.z, fmaf(P[3], s.w, add.x))));
+    n.y = fmaf(P[4], s.x, fmaf(P[5], s.y, fmaf(P[6], s.z, fmaf(P[7], s.w, add.y))));
+    n.z = fmaf(P[8], s.x, fmaf(P[9], s.y, fmaf(P[10], s.z, fmaf(P[11], s.w, add.z))));
+    n.w = fmaf(P[12], s.x, fmaf(P[13], s.y, fmaf(P[14], s.z, fmaf(P[15], s.w, add.w))));
+    return n;
+}
+
+__device__ __forceinline__ float4 shfl_up4(float4 v, int d) {
+    return make_float4(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d),
+                       __shfl_up_sync(0xffffffffu, v.z, d), __shfl_up_sync(0xffffffffu, v.w, d));
+}
+
+constexpr int kScanWarps = 4;
+
+// Streaming chain: one warp per channel, 32 chunks per step.  With the same transition P for every
+// chunk, the end state of chunk i when chunk q0 is entered with zero state is the prefix
+// v_i = sum_{j <= i} P^(i-j) z_j, a warp scan (v_i += P^d v_(i-d) for d = 1, 2, 4, 8, 16); the state
+// entering chunk q0 + i is P^i s0 + v_(i-1), and s0 advances to P^32 s0 + v_31.  pw = P^0 .. P^32.
+__global__ void __launch_bounds__(kScanWarps * 32)
+iir_scan_stream_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C,
+                       IirGroup g, IirCoeffs k, const float* __restrict__ pw, const float4* __restrict__ zs,
+                       const float4* __restrict__ carried, float4* __restrict__ sin) {
+    __shared__ float s_pw[(kIirChunk + 1) * 16];
+    for (int i = threadIdx.x; i < (kIirChunk + 1) * 16; i += blockDim.x) s_pw[i] = pw[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kScanWarps + (threadIdx.x >> 5);
     if (c >= C) return;
-    const int src = chan ? chan[c] : c;
-    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int q = 0; q < g.chunks; ++q) {
-        const ChunkRows cr = chunk_rows(q, g);
-        if (cr.first) {
-            if (g.independent || g.reset) {
-                const float x0 = (float)raw[(int64_t)cr.r0 * row_stride + src];
-                s = make_float4(k.zi[0] * x0, k.zi[1] * x0, k.zi[2] * x0, k.zi[3] * x0);
-            } else {
-                s = carried[c];
-            }
+    float4 s0;
+    if (g.reset) {
+        const float x0 = (float)raw[chan ? chan[c] : c];
+        s0 = make_float4(k.zi[0] * x0, k.zi[1] * x0, k.zi[2] * x0, k.zi[3] * x0);
+    } else {
+        s0 = carried[c];
+    }
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int q0 = 0; q0 < g.chunks; q0 += 32) {
+        const int q = q0 + lane;
+        float4 v = q < g.chunks ? zs[(int64_t)q * C + c] : z4;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const float4 t = shfl_up4(v, d);
+            if (lane >= d) v = matvec4(s_pw + d * 16, t, v);
         }
-        sin[(int64_t)q * C + c] = s;
-        const float4 z = zs[(int64_t)q * C + c];
-        const float* P = k.P;
-        float4 n;
-        n.x = fmaf(P[0], s.x, fmaf(P[1], s.y, fmaf(P[2], s.z, fmaf(P[3], s.w, z.x))));
-        n.y = fmaf(P[4], s.x, fmaf(P[5], s.y, fmaf(P[6], s.z, fmaf(P[7], s.w, z.y))));
-        n.z = fmaf(P[8], s.x, fmaf(P[9], s.y, fmaf(P[10], s.z, fmaf(P[11], s.w, z.z))));
-        n.w = fmaf(P[12], s.x, fmaf(P[13], s.y, fmaf(P[14], s.z, fmaf(P[15], s.w, z.w))));
-        s = n;
+        float4 ev = shfl_up4(v, 1);
+        if (lane == 0) ev = z4;
+        if (q < g.chunks) sin[(int64_t)q * C + c] = matvec4(s_pw + lane * 16, s0, ev);
+        const float4 v31 = make_float4(__shfl_sync(0xffffffffu, v.x, 31), __shfl_sync(0xffffffffu, v.y, 31),
+                                       __shfl_sync(0xffffffffu, v.z, 31), __shfl_sync(0xffffffffu, v.w, 31));
+        s0 = matvec4(s_pw + 32 * 16, s0, v31);
+    }
+}
+
+// Windows API: every window its own chain, one thread per (window, channel), sequentially over the
+// window's chunks from the steady state of its first row
+__global__ void __launch_bounds__(kIirThreads)
+iir_scan_windows_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* __restrict__ chan, int C,
+                        IirGroup g, IirCoeffs k, const float* __restrict__ pw, const float4* __restrict__ zs,
+                        float4* __restrict__ sin) {
+    const int c = blockIdx.x * kIirThreads + threadIdx.x;
+    const int b = blockIdx.y;
+    if (c >= C) return;
+    const int cpw = (g.W + kIirChunk - 1) / kIirChunk;
+    const float x0 = (float)raw[(int64_t)b * g.NT * row_stride + (chan ? chan[c] : c)];
+    float4 s = make_float4(k.zi[0] * x0, k.zi[1] * x0, k.zi[2] * x0, k.zi[3] * x0);
+    for (int i = 0; i < cpw; ++i) {
+        const int64_t q = (int64_t)b * cpw + i;
+        sin[q * C + c] = s;
+        s = matvec4(pw + 16, s, zs[q * C + c]);
     }
 }
 
@@ -249,10 +309,12 @@ __device__ __forceinline__ float iir_unkey(uint32_t k) {
     return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
-// the k-th smallest of the warp's 32 * NJ keys (padding keys 0xffffffff), MSB first
+// the k-th smallest of the warp's 32 * NJ keys (padding keys 0xffffffff), MSB first, one bit per
+// pass; once a single key is left matching the prefix, that key is the answer
 template <int NJ>
 __device__ __forceinline__ uint32_t iir_kth_key(const uint32_t (&key)[NJ], int kth) {
     uint32_t prefix = 0;
+    int alive = 32 * NJ;
     for (int bit = 31; bit >= 0; --bit) {
         const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
         int cnt = 0;
@@ -262,6 +324,17 @@ __device__ __forceinline__ uint32_t iir_kth_key(const uint32_t (&key)[NJ], int k
         if (kth >= cnt) {
             kth -= cnt;
             prefix |= (1u << bit);
+            alive -= cnt;
+        } else {
+            alive = cnt;
+        }
+        if (alive == 1) {
+            const uint32_t m = 0xffffffffu << bit;
+            uint32_t got = 0;
+#pragma unroll
+            for (int j = 0; j < NJ; ++j)
+                if ((key[j] & m) == prefix) got = key[j];
+            return __reduce_or_sync(0xffffffffu, got);
         }
     }
     return prefix;
@@ -283,6 +356,7 @@ iir_apply_car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const 
     for (int c = threadIdx.x; c < C; c += kIirApplyThreads) {
         const int src = chan ? chan[c] : c;
         float4 z = sin[(int64_t)q * C + c];
+#pragma unroll 8
         for (int r = cr.r0; r < cr.r1; ++r) {
             // the state entering the next group's first row (streaming chains only)
             if (!g.independent && r == g.carry_row) carried[c] = z;
@@ -339,14 +413,18 @@ int iir_chunks(const IirGroup& g) {
 }
 
 cudaError_t launch_iir_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, IirGroup g,
-                           const IirCoeffs& k, float4* zs, float4* sin, float4* carried, float* Y, float* Ylo,
-                           int out_mode, cudaStream_t s, int64_t& nl) {
+                           const IirCoeffs& k, const float* pw, float4* zs, float4* sin, float4* carried, float* Y,
+                           float* Ylo, int out_mode, cudaStream_t s, int64_t& nl) {
     g.chunks = iir_chunks(g);
     if (g.chunks <= 0 || C <= 0 || C > 1024 || (out_mode == 2 && !Ylo)) return cudaErrorInvalidValue;
     const dim3 g1(g.chunks, (C + kIirThreads - 1) / kIirThreads);
     iir_zero_state_kernel<<<g1, kIirThreads, 0, s>>>(raw, row_stride, chan, C, g, k, zs);
-    iir_scan_kernel<<<(C + kIirThreads - 1) / kIirThreads, kIirThreads, 0, s>>>(raw, row_stride, chan, C, g, k, zs,
-                                                                             carried, sin);
+    if (g.independent)
+        iir_scan_windows_kernel<<<dim3((C + kIirThreads - 1) / kIirThreads, g.nb), kIirThreads, 0, s>>>(
+            raw, row_stride, chan, C, g, k, pw, zs, sin);
+    else
+        iir_scan_stream_kernel<<<(C + kScanWarps - 1) / kScanWarps, kScanWarps * 32, 0, s>>>(raw, row_stride, chan, C,
+                                                                                          g, k, pw, zs, carried, sin);
     const size_t smem = (size_t)kIirChunk * (C + 1) * sizeof(float);
     const int nj = (C + 31) / 32;
     cudaError_t e = cudaSuccess;

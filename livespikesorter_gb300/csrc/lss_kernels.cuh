@@ -95,13 +95,15 @@ struct IirGroup {
 };
 // sections (b0, b1, b2, 1, a1, a2) of a Butterworth high-pass; returns their count, -1 on bad args
 int butter_highpass_sos(int order, double fc, double fs, std::vector<double>& sos);
-IirCoeffs make_iir_coeffs(const std::vector<double>& sos);
+// the coefficients, and the powers P^0 .. P^kIirChunk of the chunk transition ([kIirChunk + 1][4][4])
+IirCoeffs make_iir_coeffs(const std::vector<double>& sos, std::vector<float>& powers);
 int iir_chunks(const IirGroup& g);
-// zs, sin: [iir_chunks(g)][C] float4 scratch; carried [C] float4 (read on continuation, written at
-// carry_row); out_mode 0 = FP32 Y, 1 = TF32 split (Ylo may be null: tf32 alone), 2 = BF16 split
+// pw: the powers of make_iir_coeffs on the device; zs, sin: [iir_chunks(g)][C] float4 scratch;
+// carried [C] float4 (read on continuation, written at carry_row); out_mode 0 = FP32 Y, 1 = TF32
+// split (Ylo may be null: tf32 alone), 2 = BF16 split
 cudaError_t launch_iir_car(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, IirGroup g,
-                           const IirCoeffs& k, float4* zs, float4* sin, float4* carried, float* Y, float* Ylo,
-                           int out_mode, cudaStream_t s, int64_t& nl);
+                           const IirCoeffs& k, const float* pw, float4* zs, float4* sin, float4* carried, float* Y,
+                           float* Ylo, int out_mode, cudaStream_t s, int64_t& nl);
 
 void launch_sgemm_nt(const float* A, int64_t lda, int64_t strideA, const float* B, int64_t ldb,
                      float* Cm, int64_t ldc, int64_t strideC, int M, int N, int K, int nb, cudaStream_t s);

@@ -170,6 +170,8 @@ struct Handle {
     bool iir = false;
     IirCoeffs iirk{};
     float4* d_iir_state = nullptr;   // [C]
+    std::vector<float> iir_pow;      // P^0 .. P^kIirChunk of the chunk transition
+    float* d_iir_pow = nullptr;
     int64_t iir_expect = INT64_MIN;
     bool iir_reset = true;           // the next streaming group starts a chain
     std::map<int, TapSet> taps;
@@ -278,7 +280,8 @@ Handle::~Handle() {
     for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
                     (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo,
-                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm, (void*)d_iir_state})
+                    (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm, (void*)d_iir_state,
+                    (void*)d_iir_pow})
         if (p) cudaFree(p);
     if (h_gemm_err) cudaFreeHost(h_gemm_err);
     for (auto& s : slots) {
@@ -425,7 +428,7 @@ void Handle::init(const char* dir, const lss_params* prm) {
         std::vector<double> sos;
         if (butter_highpass_sos(kHighpassOrder, p.highpass_hz, p.sample_rate_hz, sos) < 0)
             throw LoadError{LSS_ERR_ARG, "lss_params: high-pass edge must lie in (0, sample_rate_hz / 2)"};
-        iirk = make_iir_coeffs(sos);
+        iirk = make_iir_coeffs(sos, iir_pow);
         if (C > 1024) throw LoadError{LSS_ERR_ARG, "the stateful high-pass takes at most 1024 channels"};
     }
     if (Cin > C) {
@@ -553,7 +556,10 @@ void Handle::init(const char* dir, const lss_params* prm) {
         throw LoadError{LSS_ERR_ARG, "lss_params.match_keep must be 0 (full loop) or 1.." + std::to_string(kPruneKeepMax)};
     keep = std::min(p.match_keep, T);
     if (keep > 0 && T > 1024) throw LoadError{LSS_ERR_ARG, "the pruned matching tier takes at most 1024 templates"};
-    if (iir) d_iir_state = dev_alloc<float4>((size_t)C, dev_bytes);
+    if (iir) {
+        d_iir_state = dev_alloc<float4>((size_t)C, dev_bytes);
+        d_iir_pow = dev_upload(iir_pow, dev_bytes, st);
+    }
     LSS_CUDA(cudaHostAlloc((void**)&h_gemm_err, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable));
     *h_gemm_err = 0;
     LSS_CUDA(cudaHostGetDevicePointer((void**)&d_gemm_err, h_gemm_err, 0));
@@ -804,7 +810,7 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
         mark();
         mark();
         const int mode = bf16_pre ? 2 : (tc_whiten ? 1 : 0);
-        LSS_CUDA(launch_iir_car(raw, Cin, d_chan, C, g, iirk, d_iir_zs, d_iir_sin, d_iir_state, d_Y,
+        LSS_CUDA(launch_iir_car(raw, Cin, d_chan, C, g, iirk, d_iir_pow, d_iir_zs, d_iir_sin, d_iir_state, d_Y,
                                 tc_whiten ? d_Y_lo : nullptr, mode, st, nl));
         if (!g.independent) iir_reset = false;
         mark();

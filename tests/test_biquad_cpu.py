@@ -66,11 +66,26 @@ def test_chunked_recurrence_equals_sosfilt():
         _cascade(sos, c, z)
         zs.append(z.ravel())
     s = zi.ravel().copy()
-    out = []
+    out, entering = [], []
     for c, z in zip(chunks, zs):
+        entering.append(s.copy())
         out.append(_cascade(sos, c, s.reshape(ns, 2).copy()))
         s = P @ s + z
     np.testing.assert_allclose(np.concatenate(out), ref, rtol=0, atol=1e-9 * np.abs(ref).max())
+    # the streaming kernel's warp scan over 32 chunks at a time: inclusive prefixes by
+    # v_i += P^d v_(i-d) (d = 1, 2, 4, 8, 16), entering state of chunk q0 + i = P^i s0 + v_(i-1)
+    Pw = [np.linalg.matrix_power(P, i) for i in range(33)]
+    s0 = zi.ravel().copy()
+    got = []
+    for q0 in range(0, len(zs), 32):
+        v = [zs[q] if q < len(zs) else np.zeros(2 * ns) for q in range(q0, q0 + 32)]
+        d = 1
+        while d < 32:
+            v = [v[i] + (Pw[d] @ v[i - d] if i >= d else 0) for i in range(32)]
+            d *= 2
+        got += [Pw[i] @ s0 + (v[i - 1] if i else 0) for i in range(32) if q0 + i < len(zs)]
+        s0 = Pw[32] @ s0 + v[31]
+    np.testing.assert_allclose(np.array(got), np.array(entering), rtol=0, atol=1e-9 * np.abs(entering).max())
 
 
 def test_oracle_filter_chunked_equals_whole():
