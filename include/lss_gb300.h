@@ -136,6 +136,33 @@ int lss_get_info(const lss_handle* h, lss_info* info);
  * 0.  The message is lss_last_error(NULL). */
 int lss_validate_oss_input(const char* oss_dir, lss_info* info);
 
+/* Template subsetting of an oss_input/ directory: keep only some preclustered templates so a
+ * stream's device state and per-batch work shrink (admission of more streams under mem_budget).
+ * Replaces the reference's subset_templates.py (src/Python/subset_templates.py:1-343) with this
+ * library's own selection on the loader's shape model.  A template's footprint is its energy per
+ * channel, sum_k Wall3[t][k][c]^2.  Candidates: every template, or (chan_lo <= chan_hi) those whose
+ * strongest channel's probe channel (channelMap.npy) lies in [chan_lo, chan_hi] (chan_rule 0), or
+ * that have any in-range channel with RMS >= overlap_frac of the strongest's (chan_rule 1).  Then at
+ * most max_templates (0 = all candidates): by spikes per template in
+ * spike_detection_templates.npy, ties by energy then index (rank 0; energy when the file is
+ * absent), or by energy (rank 1).  The kept indices come back ascending. */
+typedef struct lss_subset_spec {
+    int32_t max_templates;
+    int32_t rank;          /* 0 = activity, 1 = energy */
+    int32_t chan_lo, chan_hi;
+    int32_t chan_rule;     /* 0 = strongest channel in range, 1 = any channel above overlap_frac */
+    float overlap_frac;    /* default 0.1 */
+} lss_subset_spec;
+void lss_subset_default_spec(lss_subset_spec* spec);   /* no cap, no channel range, rank 0, 0.1 */
+/* The kept indices (keep may be NULL to ask for the count; LSS_ERR_OVERFLOW if cap is too small). */
+int lss_subset_plan(const char* oss_dir, const lss_subset_spec* spec, int32_t* keep, int32_t cap,
+                    int32_t* n_keep);
+/* Write the subset directory out_dir (must not exist): Wall3, ctc (both template axes), iU, Ucc,
+ * the preclustered waveforms cut, every other file copied, subset_manifest.json with the kept
+ * indices.  A spike's tmpl from the subset directory indexes that list.  LSS_ERR_ARG when nothing
+ * would be cut.  Messages via lss_last_error(NULL). */
+int lss_subset_write(const char* in_dir, const char* out_dir, const lss_subset_spec* spec);
+
 /* Push n_samples rows of int16 [n_samples][n_chan_in] (channel fastest, SpikeGLX order).
  * stream_sample_ct = stream index of row 0, or -1 for "continues the previous push"; a
  * discontinuity flushes the current segment and starts a new one (the skip / behind policy

@@ -124,6 +124,12 @@ _SIGS.update({
                                      ct.c_void_p, ct.c_int64, _P(ct.c_int64)]),
     "lss_batch_p2p": (ct.c_int, [ct.c_void_p, ct.c_int64, ct.c_int32, _P(ct.c_float)]),
 })
+# template subsetting (Python side in subset.py; spec pointers are lss_subset_spec)
+_SIGS.update({
+    "lss_subset_default_spec": (None, [ct.c_void_p]),
+    "lss_subset_plan": (ct.c_int, [ct.c_char_p, ct.c_void_p, _P(ct.c_int32), ct.c_int32, _P(ct.c_int32)]),
+    "lss_subset_write": (ct.c_int, [ct.c_char_p, ct.c_char_p, ct.c_void_p]),
+})
 STAGES = ("h2d", "colsum", "car", "highpass", "whiten", "basis_conv", "project", "match", "features", "d2h")
 
 _lib = None
@@ -335,5 +341,5 @@ def header_functions(header=None):
     hs = [Path(header)] if header else sorted((_PKG.parent / "include").glob("*.h"))
     names = set()
     for h in hs:
-        names |= set(re.findall(r"^\s*(?:int|const char\*)\s+(lss_\w+)\s*\(", h.read_text(), re.M))
+        names |= set(re.findall(r"^\s*(?:int|void|const char\*)\s+(lss_\w+)\s*\(", h.read_text(), re.M))
     return sorted(names)

@@ -128,8 +128,9 @@ def test_config_small_one_batch(cfg_small):
 
 
 def test_template_subset_directory(cfg_small, tmp_path):
-    """A directory cut to the 40 most active of 64 preclustered templates (livespikesorter_gb300.subset,
-    the reference's subset_templates.py) sorts like the float64 oracle on that same directory."""
+    """A directory cut to the 40 most active of 64 preclustered templates (lss_subset_write through
+    livespikesorter_gb300.subset, in place of the reference's subset_templates.py) sorts like the
+    float64 oracle on that same directory."""
     from livespikesorter_gb300 import subset
     d0, data, _ = cfg_small
     d = tmp_path / "sub"
