@@ -22,9 +22,9 @@
 //   lsc   f32 [nb][W][KP]     their running scores (initial B on entry), updated in place
 //   ctcP  f32 [T][2nt+1][T]   ctcP[s][l][t] = ctc[t][s][l]
 //
-// The loop kernel runs one CTA per window; the per-sample maxima and the ranks live in shared
-// memory when they fit (windows up to ~1700 samples at 32 entries), else in global memory; the
-// scores stay in global memory (L2) -- 64 windows of 1622 samples hold 13 MB.
+// The loop kernel runs one CTA of 1024 threads per window; the per-sample maxima, the listed
+// templates and their scores live in shared memory as far as they fit (all three for windows up
+// to ~1700 samples at 16 entries), the rest in global memory (L2).
 #include "lss_kernels.cuh"
 
 #include <cfloat>
@@ -145,7 +145,8 @@ __host__ __device__ inline int prune_iter_cap(int W, int nt) { return 2 * ((W + 
 
 // dynamic shared memory: [1/nm: T f32][nm: T f32][unordered + sorted accepted lists: 2 x cap x 12 B,
 // to 16 B], then the per-sample maxima [W + 2nt] f32 and list slots [W] u8 when they fit, then the
-// listed templates [W][KP] u16 when they fit as well
+// listed templates [W][ks] u16 when they fit as well, then their scores [W][ks] f32 (ks = keep
+// rounded up to 8) when those fit too
 __host__ __device__ inline size_t prune_smem_head(int T) { return ((size_t)T * 8 + 15) & ~(size_t)15; }
 __host__ __device__ inline size_t prune_smem_fixed(int W, int T, int nt) {
     return prune_smem_head(T) + ((2 * (size_t)prune_iter_cap(W, nt) * 12 + 15) & ~(size_t)15);
@@ -153,9 +154,11 @@ __host__ __device__ inline size_t prune_smem_fixed(int W, int T, int nt) {
 __host__ __device__ inline size_t prune_smem_cf(int W, int nt) {
     return (((size_t)(W + 2 * nt) * 4 + (size_t)W) + 15) & ~(size_t)15;
 }
-__host__ __device__ inline size_t prune_smem_ranks(int W) { return (size_t)W * KP * 2; }
+__host__ __device__ inline int prune_stride(int keep) { return (keep + 7) & ~7; }
+__host__ __device__ inline size_t prune_smem_ranks(int W, int ks) { return ((size_t)W * ks * 2 + 15) & ~(size_t)15; }
+__host__ __device__ inline size_t prune_smem_scores(int W, int ks) { return (size_t)W * ks * 4; }
 
-constexpr int kItemsPerWarp = 4;   // samples a warp updates at once (independent gathers in flight)
+constexpr int kItemsPerGroup = 4;   // samples a lane group updates at once (independent gathers in flight)
 
 // One CTA per window.  Per iteration:
 //   B1  every sample whose own maximum exceeds Th^2 and equals the maximum over +-nt is accepted
@@ -165,19 +168,24 @@ constexpr int kItemsPerWarp = 4;   // samples a warp updates at once (independen
 //   B2  the iteration's spikes are ranked by sample and appended to the output lists;
 //   C   every sample within +-nt of a spike -- taken by the first spike (in sample order) whose
 //       range covers it -- applies each covering spike in sample order to its listed scores (a
-//       warp per sample, a lane per entry) and recomputes its maximum with a warp reduction.
+//       group of LPS lanes per sample, a lane per entry; 32 / LPS samples per warp at once) and
+//       recomputes its maximum with a reduction over the group.
 // mode bit 0: maxima and slots in shared memory (else cf_g / slot_g); bit 1: listed templates in
-// shared memory
-template <int NTHR>
+// shared memory (stride ks); bit 2: their scores as well (else in lsc_g, stride KP)
+template <int NTHR, int LPS>
 __global__ void __launch_bounds__(NTHR, 1)
 match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_g, int keep,
                     const float* __restrict__ ctcP, const float* __restrict__ nm, float th2, int W, int T, int nt,
                     int max_iters, int mode, float* __restrict__ cf_g, unsigned char* __restrict__ slot_g,
                     MatchOut out) {
     constexpr int kWarps = NTHR / 32;
+    constexpr int kGroups = 32 / LPS;            // samples a warp holds at once
+    constexpr unsigned kGroupMask = LPS == 32 ? 0xffffffffu : ((1u << LPS) - 1u);
     extern __shared__ __align__(16) unsigned char smraw[];
     const int b = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gl = lane % LPS;                   // lane within its group = list entry
+    const int grp = lane / LPS;                  // the warp's group
     const int L2 = 2 * nt + 1;
     const int cap_it = prune_iter_cap(W, nt);
     float* s_inm = reinterpret_cast<float*>(smraw);                     // [T]
@@ -191,7 +199,7 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
     __shared__ int s_cnt, s_over;
 
     // per-sample state: cfmax of w at cf[w + nt] (pads of nt at both ends) and the list slot of its
-    // maximum; the ranks RK[w][i]; the scores SC[w][i] (global)
+    // maximum; the listed templates RK[w][i] and their scores SC[w][i]
     unsigned char* next = smraw + prune_smem_fixed(W, T, nt);
     float* cf;
     unsigned char* slot;
@@ -203,18 +211,27 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
         cf = cf_g + (int64_t)b * (W + 2 * nt);
         slot = slot_g + (int64_t)b * W;
     }
-    const uint16_t* RK;
     const uint16_t* rk_g = lrk_g + (int64_t)b * W * KP;
+    float* sc_g = lsc_g + (int64_t)b * W * KP;
+    const int ks = (mode & 2) ? prune_stride(keep) : KP;   // row stride of RK and SC
+    const uint16_t* RK;
+    float* SC;
     if (mode & 2) {
         uint16_t* r = reinterpret_cast<uint16_t*>(next);
-        const uint4* src = reinterpret_cast<const uint4*>(rk_g);   // rows of KP u16 = 64 bytes
-        uint4* dst = reinterpret_cast<uint4*>(r);
-        for (int q = tid; q < W * KP / 8; q += NTHR) dst[q] = src[q];
+        next += prune_smem_ranks(W, ks);
+        float* sc = (mode & 4) ? reinterpret_cast<float*>(next) : nullptr;
+        for (int q = tid; q < W * ks; q += NTHR) {
+            const int w = q / ks, i = q - w * ks;
+            r[q] = rk_g[(size_t)w * KP + i];
+            if (sc) sc[q] = sc_g[(size_t)w * KP + i];
+        }
         RK = r;
+        SC = sc ? sc : sc_g;
     } else {
         RK = rk_g;
+        SC = sc_g;
     }
-    float* SC = lsc_g + (int64_t)b * W * KP;
+    const int ss = (mode & 4) ? ks : KP;   // row stride of SC
     for (int t = tid; t < T; t += NTHR) {
         s_nm[t] = nm[t];
         s_inm[t] = 1.f / nm[t];
@@ -229,34 +246,36 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
     }
     __syncthreads();
 
-    // the warp's sample w, lane i holding entry i (score x, template r): Cf maximum over the list
+    // the group's sample w, lane gl holding entry gl (score x, template r): Cf maximum over the list
     // (ties: lower template) into cf / slot
-    auto finish = [&](int w, float x, int r) {
+    auto finish = [&](int w, float x, int r, bool valid) {
         float best = -1.f;
         int bt = INT_MAX, bs = 0;
-        if (lane < keep) {
+        if (valid && gl < keep) {
             const float q = fmaxf(x, 0.f);
             best = q * q * s_inm[r];
             bt = r;
-            bs = lane;
+            bs = gl;
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
+        for (int o = LPS / 2; o > 0; o >>= 1) {
             const float ob = __shfl_xor_sync(0xffffffffu, best, o);
             const int ot = __shfl_xor_sync(0xffffffffu, bt, o);
             const int os = __shfl_xor_sync(0xffffffffu, bs, o);
             if (ob > best || (ob == best && ot < bt)) { best = ob; bt = ot; bs = os; }
         }
-        if (lane == 0) {
+        if (valid && gl == 0) {
             const bool inner = w >= nt && w < W - nt;
             cf[w + nt] = inner ? best : 0.f;
             slot[w] = (unsigned char)bs;
         }
     };
-    for (int w = warp; w < W; w += kWarps) {
-        const int r = lane < keep ? RK[(size_t)w * KP + lane] : 0;
-        const float x = lane < keep ? SC[(size_t)w * KP + lane] : 0.f;
-        finish(w, x, r);
+    for (int w0 = warp * kGroups; w0 < W; w0 += kWarps * kGroups) {
+        const int w = w0 + grp;
+        const bool valid = w < W;
+        const int r = valid && gl < keep ? RK[(size_t)w * ks + gl] : 0;
+        const float x = valid && gl < keep ? SC[(size_t)w * ss + gl] : 0.f;
+        finish(w, x, r, valid);
     }
     __syncthreads();
 
@@ -279,8 +298,8 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
                 for (int o = 16; o > 0; o >>= 1) cm = fmaxf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
                 if (lane == 0 && cm > th2 && cf[w + nt] == cm) {
                     const int i = slot[w];
-                    const int tt = RK[(size_t)w * KP + i];
-                    const float amp = SC[(size_t)w * KP + i] / s_nm[tt];
+                    const int tt = RK[(size_t)w * ks + i];
+                    const float amp = SC[(size_t)w * ss + i] / s_nm[tt];
                     const int q = atomicAdd(&s_cnt, 1);
                     if (q < cap_it) {
                         s_aw[q] = w;
@@ -316,12 +335,13 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
         if (tid == 0) s_cnt = 0;   // read again only after the barrier ending C
         // ---- C: subtract the spikes from the listed scores of the samples near them ----
         const int n_items = total * L2;
-        for (int q0 = warp * kItemsPerWarp; q0 < n_items; q0 += kWarps * kItemsPerWarp) {
-            int wv[kItemsPerWarp], kv[kItemsPerWarp], rv[kItemsPerWarp];
-            float xv[kItemsPerWarp], cv[kItemsPerWarp];
+        constexpr int kPerWarp = kItemsPerGroup * kGroups;
+        for (int q0 = warp * kPerWarp; q0 < n_items; q0 += kWarps * kPerWarp) {
+            int wv[kItemsPerGroup], kv[kItemsPerGroup], rv[kItemsPerGroup];
+            float xv[kItemsPerGroup], cv[kItemsPerGroup];
 #pragma unroll
-            for (int u = 0; u < kItemsPerWarp; ++u) {
-                const int q = q0 + u;
+            for (int u = 0; u < kItemsPerGroup; ++u) {
+                const int q = q0 + u * kGroups + grp;
                 int w = -1, k = 0;
                 if (q < n_items) {
                     k = q / L2;
@@ -333,33 +353,40 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
                 kv[u] = k;
                 rv[u] = 0;
                 xv[u] = 0.f;
-                if (w >= 0 && lane < keep) {
-                    rv[u] = RK[(size_t)w * KP + lane];
-                    xv[u] = SC[(size_t)w * KP + lane];
+                if (w >= 0 && gl < keep) {
+                    rv[u] = RK[(size_t)w * ks + gl];
+                    xv[u] = SC[(size_t)w * ss + gl];
                 }
             }
             // the owning spike's ctc entries, all items' loads in flight together
 #pragma unroll
-            for (int u = 0; u < kItemsPerWarp; ++u) {
+            for (int u = 0; u < kItemsPerGroup; ++u) {
                 cv[u] = 0.f;
-                if (wv[u] >= 0 && lane < keep)
+                if (wv[u] >= 0 && gl < keep)
                     cv[u] = __ldg(ctcP + ((int64_t)s_st[kv[u]] * L2 + (wv[u] - s_sw[kv[u]] + nt)) * T + rv[u]);
             }
 #pragma unroll
-            for (int u = 0; u < kItemsPerWarp; ++u) {
+            for (int u = 0; u < kItemsPerGroup; ++u) {
                 const int w = wv[u];
-                if (w < 0) continue;   // warp-uniform
-                float x = fmaf(-s_sa[kv[u]], cv[u], xv[u]);
-                // any further spike covering the same sample, in sample order
-                for (int kk = kv[u] + 1; kk < total && s_sw[kk] - nt <= w; ++kk) {
-                    const float c = lane < keep
-                                        ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u])
-                                        : 0.f;
-                    x = fmaf(-s_sa[kk], c, x);
+                // a group's item may be empty while its warp's other groups have one (the finish
+                // reduction is warp-wide, so every lane takes part)
+                const bool live = __any_sync(0xffffffffu, w >= 0);
+                if (!live) continue;
+                float x = 0.f;
+                if (w >= 0) {
+                    x = fmaf(-s_sa[kv[u]], cv[u], xv[u]);
+                    // any further spike covering the same sample, in sample order
+                    for (int kk = kv[u] + 1; kk < total && s_sw[kk] - nt <= w; ++kk) {
+                        const float c = gl < keep
+                                            ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u])
+                                            : 0.f;
+                        x = fmaf(-s_sa[kk], c, x);
+                    }
+                    if (gl < keep) SC[(size_t)w * ss + gl] = x;
                 }
-                if (lane < keep) SC[(size_t)w * KP + lane] = x;
-                finish(w, x, rv[u]);
+                finish(w, x, rv[u], w >= 0);
             }
+            (void)kGroupMask;
         }
         n_total += total;
         __syncthreads();
@@ -387,30 +414,52 @@ static int prune_smem_max() {
 }
 
 // where the per-sample state of a window goes: bit 0 = maxima and slots in shared memory, bit 1 =
-// the ranks too; -1 = the fixed part alone does not fit
-int prune_mode(int W, int T, int nt) {
+// the listed templates too, bit 2 = their scores too; -1 = the fixed part alone does not fit
+int prune_mode(int W, int T, int nt, int keep) {
     const size_t lim = (size_t)prune_smem_max();
     const size_t f = prune_smem_fixed(W, T, nt) + 1024;
     if (f > lim) return -1;
     const size_t c = prune_smem_cf(W, nt);
     if (f + c > lim) return 0;
-    return f + c + prune_smem_ranks(W) <= lim ? 3 : 1;
+    const int ks = prune_stride(keep);
+    const size_t r = prune_smem_ranks(W, ks);
+    if (f + c + r > lim) return 1;
+    return f + c + r + prune_smem_scores(W, ks) <= lim ? 7 : 3;
+}
+
+static size_t prune_smem(int W, int T, int nt, int keep, int mode) {
+    const int ks = prune_stride(keep);
+    return prune_smem_fixed(W, T, nt) + ((mode & 1) ? prune_smem_cf(W, nt) : 0) +
+           ((mode & 2) ? prune_smem_ranks(W, ks) : 0) + ((mode & 4) ? prune_smem_scores(W, ks) : 0);
+}
+
+template <int LPS>
+static cudaError_t launch_pruned_lps(const uint16_t* lrk, float* lsc, int keep, const float* ctcP, const float* nm,
+                                     float th2, int W, int T, int nt, int max_iters, int nb, int mode, float* cf_scratch,
+                                     unsigned char* slot_scratch, const MatchOut& out, cudaStream_t s) {
+    const size_t smem = prune_smem(W, T, nt, keep, mode);
+    auto kern = match_pruned_kernel<kPruneThreads, LPS>;
+    cudaError_t e = raise_smem_limit((const void*)kern, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nb, kPruneThreads, smem, s>>>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, mode, cf_scratch,
+                                         slot_scratch, out);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcP, const float* nm,
                                 float th2, int W, int T, int nt, int max_iters, int nb, float* cf_scratch,
                                 unsigned char* slot_scratch, const MatchOut& out, cudaStream_t s) {
     if (keep < 1 || keep > KP || keep > T || T > 1024) return cudaErrorInvalidValue;
-    const int mode = prune_mode(W, T, nt);
+    const int mode = prune_mode(W, T, nt, keep);
     if (mode < 0 || (!(mode & 1) && (!cf_scratch || !slot_scratch))) return cudaErrorInvalidValue;
-    const size_t smem =
-        prune_smem_fixed(W, T, nt) + ((mode & 1) ? prune_smem_cf(W, nt) : 0) + ((mode & 2) ? prune_smem_ranks(W) : 0);
-    auto kern = match_pruned_kernel<kPruneThreads>;
-    cudaError_t e = raise_smem_limit((const void*)kern, smem);
-    if (e != cudaSuccess) return e;
-    kern<<<nb, kPruneThreads, smem, s>>>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, mode, cf_scratch,
-                                         slot_scratch, out);
-    return cudaGetLastError();
+    if (keep <= 8)
+        return launch_pruned_lps<8>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, mode, cf_scratch,
+                                    slot_scratch, out, s);
+    if (keep <= 16)
+        return launch_pruned_lps<16>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, mode, cf_scratch,
+                                     slot_scratch, out, s);
+    return launch_pruned_lps<32>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, mode, cf_scratch,
+                                 slot_scratch, out, s);
 }
 
 }  // namespace lss

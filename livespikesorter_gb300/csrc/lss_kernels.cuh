@@ -178,7 +178,7 @@ cudaError_t launch_residual(float* Xres, const float* pre_wf, const MatchOut& ou
 // pruned matching tier (kernels_prune.cu): per sample the keep (<= kPruneKeepMax) templates of
 // largest initial Cf, lists lrk / lsc [nb][W][kPruneKeepMax]; the loop on those lists
 constexpr int kPruneKeepMax = 32;
-constexpr int kPruneThreads = 512;
+constexpr int kPruneThreads = 1024;
 void launch_prune_select(const float* Bt, const float* nm, int nb, int W, int T, int keep, uint16_t* lrk, float* lsc,
                          cudaStream_t s);
 // cf_scratch [nb][W + 2nt] and slot_scratch [nb][W] hold the per-sample maxima of windows whose
@@ -187,8 +187,9 @@ cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const
                                 float th2, int W, int T, int nt, int max_iters, int nb, float* cf_scratch,
                                 unsigned char* slot_scratch, const MatchOut& out, cudaStream_t s);
 // where a window's per-sample state lives: bit 0 = maxima in shared memory, bit 1 = listed
-// templates too; 0 = maxima in the caller's scratch; -1 = too large for the tier
-int prune_mode(int W, int T, int nt);
+// templates too, bit 2 = their scores too; 0 = maxima in the caller's scratch; -1 = too large for
+// the tier
+int prune_mode(int W, int T, int nt, int keep);
 
 void launch_features(const float* Xres, const MatchOut& out, int nb, int W, int C, int T, int K, int nt, int nC,
                      const float* wPCA, const int64_t* iCC, const int64_t* iU, const float* Ucc, const float* xc,

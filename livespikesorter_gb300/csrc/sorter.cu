@@ -695,7 +695,7 @@ void Handle::ensure_work(int Wn, int nb) {
     if (keep > 0) {
         d_lid = dev_alloc<uint16_t>((size_t)nba * Wa * kPruneKeepMax, dev_bytes);
         d_lsc = dev_alloc<float>((size_t)nba * Wa * kPruneKeepMax, dev_bytes);
-        const int pm = prune_mode(Wa, T, nt);
+        const int pm = prune_mode(Wa, T, nt, keep);
         if (pm < 0) throw LoadError{LSS_ERR_ARG, "window too long for the pruned matching tier"};
         if (!(pm & 1)) {
             d_pcf = dev_alloc<float>((size_t)nba * (Wa + 2 * nt), dev_bytes);
