@@ -144,15 +144,17 @@ void launch_prune_select(const float* Bt, const float* nm, int nb, int W, int T,
 __host__ __device__ inline int prune_iter_cap(int W, int nt) { return 2 * ((W + nt) / (nt + 1)) + 32; }
 
 // dynamic shared memory: [1/nm: T f32][nm: T f32][unordered + sorted accepted lists: 2 x cap x 12 B,
-// to 16 B], then the per-sample maxima [W + 2nt] f32 and list slots [W] u8 when they fit, then the
+// to 16 B], then the per-sample maxima [W + 2nt] f32, the max pool's block prefix and suffix
+// maxima [2][W + 2nt] f32 and list slots [W] u8 when they fit, then the
 // listed templates [W][ks] u16 when they fit as well, then their scores [W][ks] f32 (ks = keep
 // rounded up to 8) when those fit too
 __host__ __device__ inline size_t prune_smem_head(int T) { return ((size_t)T * 8 + 15) & ~(size_t)15; }
 __host__ __device__ inline size_t prune_smem_fixed(int W, int T, int nt) {
     return prune_smem_head(T) + ((2 * (size_t)prune_iter_cap(W, nt) * 12 + 15) & ~(size_t)15);
 }
+// (per-sample maxima, the prefix and suffix block maxima of the max pool, list slots)
 __host__ __device__ inline size_t prune_smem_cf(int W, int nt) {
-    return (((size_t)(W + 2 * nt) * 4 + (size_t)W) + 15) & ~(size_t)15;
+    return (((size_t)(W + 2 * nt) * 12 + (size_t)W) + 15) & ~(size_t)15;
 }
 __host__ __device__ inline int prune_stride(int keep) { return (keep + 7) & ~7; }
 __host__ __device__ inline size_t prune_smem_ranks(int W, int ks) { return ((size_t)W * ks * 2 + 15) & ~(size_t)15; }
@@ -202,10 +204,13 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
     // maximum; the listed templates RK[w][i] and their scores SC[w][i]
     unsigned char* next = smraw + prune_smem_fixed(W, T, nt);
     float* cf;
+    float *pg = nullptr, *ph = nullptr;   // block prefix / suffix maxima of cf (shared-memory state only)
     unsigned char* slot;
     if (mode & 1) {
         cf = reinterpret_cast<float*>(next);
-        slot = reinterpret_cast<unsigned char*>(cf + (W + 2 * nt));
+        pg = cf + (W + 2 * nt);
+        ph = pg + (W + 2 * nt);
+        slot = reinterpret_cast<unsigned char*>(ph + (W + 2 * nt));
         next += prune_smem_cf(W, nt);
     } else {
         cf = cf_g + (int64_t)b * (W + 2 * nt);
@@ -286,6 +291,58 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
     int* sp_iter = out.sp_iter + (int64_t)b * out.cap;
     for (int it = 0; it < max_iters; ++it) {
         // ---- B1: acceptance ----
+        if (mode & 1) {
+            // the (2nt+1) max pool of the padded maxima P = cf [W + 2nt] by blocks of L2 (van Herk /
+            // Gil-Werman): pg[i] = max P[block start .. i], ph[i] = max P[i .. block end], and the
+            // window of sample w, P[w .. w + 2nt], spans at most two blocks: max(ph[w], pg[w + 2nt])
+            const int n = W + 2 * nt;
+            for (int blk = warp; blk * L2 < n; blk += kWarps) {
+                const int b0 = blk * L2, b1 = min(n, b0 + L2);
+                float carry = -FLT_MAX;
+                for (int c0 = b0; c0 < b1; c0 += 32) {
+                    const int i = c0 + lane;
+                    float v = i < b1 ? cf[i] : -FLT_MAX;
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const float o = __shfl_up_sync(0xffffffffu, v, d);
+                        if (lane >= d) v = fmaxf(v, o);
+                    }
+                    v = fmaxf(v, carry);
+                    if (i < b1) pg[i] = v;
+                    carry = __shfl_sync(0xffffffffu, v, 31);
+                }
+                carry = -FLT_MAX;
+                for (int c1 = b1; c1 > b0; c1 -= 32) {
+                    const int i = c1 - 32 + lane;
+                    float v = i >= b0 ? cf[i] : -FLT_MAX;
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const float o = __shfl_down_sync(0xffffffffu, v, d);
+                        if (lane + d < 32) v = fmaxf(v, o);
+                    }
+                    v = fmaxf(v, carry);
+                    if (i >= b0) ph[i] = v;
+                    carry = __shfl_sync(0xffffffffu, v, 0);
+                }
+            }
+            __syncthreads();
+            for (int w = tid; w < W; w += NTHR) {
+                const float c = cf[w + nt];
+                if (c > th2 && c == fmaxf(ph[w], pg[w + 2 * nt])) {
+                    const int i = slot[w];
+                    const int tt = RK[(size_t)w * ks + i];
+                    const float amp = SC[(size_t)w * ss + i] / s_nm[tt];
+                    const int q = atomicAdd(&s_cnt, 1);
+                    if (q < cap_it) {
+                        s_aw[q] = w;
+                        s_at[q] = tt;
+                        s_aa[q] = amp;
+                    } else {
+                        s_over = 1;
+                    }
+                }
+            }
+        } else
         for (int w0 = warp * 32; w0 < W; w0 += kWarps * 32) {
             const int wl = w0 + lane;
             unsigned m = __ballot_sync(0xffffffffu, wl < W && cf[wl + nt] > th2);
