@@ -160,7 +160,7 @@ __host__ __device__ inline int prune_stride(int keep) { return (keep + 7) & ~7; 
 __host__ __device__ inline size_t prune_smem_ranks(int W, int ks) { return ((size_t)W * ks * 2 + 15) & ~(size_t)15; }
 __host__ __device__ inline size_t prune_smem_scores(int W, int ks) { return (size_t)W * ks * 4; }
 
-constexpr int kItemsPerGroup = 4;   // samples a lane group updates at once (independent gathers in flight)
+constexpr int kItemsPerGroup = 8;   // samples a lane group updates at once (independent gathers in flight)
 
 // One CTA per window.  Per iteration:
 //   B1  every sample whose own maximum exceeds Th^2 and equals the maximum over +-nt is accepted
@@ -182,7 +182,6 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
                     MatchOut out) {
     constexpr int kWarps = NTHR / 32;
     constexpr int kGroups = 32 / LPS;            // samples a warp holds at once
-    constexpr unsigned kGroupMask = LPS == 32 ? 0xffffffffu : ((1u << LPS) - 1u);
     extern __shared__ __align__(16) unsigned char smraw[];
     const int b = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -395,7 +394,8 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
         constexpr int kPerWarp = kItemsPerGroup * kGroups;
         for (int q0 = warp * kPerWarp; q0 < n_items; q0 += kWarps * kPerWarp) {
             int wv[kItemsPerGroup], kv[kItemsPerGroup], rv[kItemsPerGroup];
-            float xv[kItemsPerGroup], cv[kItemsPerGroup];
+            float xv[kItemsPerGroup], cv[kItemsPerGroup], cv2[kItemsPerGroup];
+            bool two[kItemsPerGroup];
 #pragma unroll
             for (int u = 0; u < kItemsPerGroup; ++u) {
                 const int q = q0 + u * kGroups + grp;
@@ -408,6 +408,7 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
                 }
                 wv[u] = w;
                 kv[u] = k;
+                two[u] = w >= 0 && k + 1 < total && s_sw[k + 1] - nt <= w;   // a second spike covers w
                 rv[u] = 0;
                 xv[u] = 0.f;
                 if (w >= 0 && gl < keep) {
@@ -415,35 +416,59 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
                     xv[u] = SC[(size_t)w * ss + gl];
                 }
             }
-            // the owning spike's ctc entries, all items' loads in flight together
+            // the ctc entries of the owning spike and of a second covering spike, every item's loads
+            // in flight together
 #pragma unroll
             for (int u = 0; u < kItemsPerGroup; ++u) {
-                cv[u] = 0.f;
-                if (wv[u] >= 0 && gl < keep)
-                    cv[u] = __ldg(ctcP + ((int64_t)s_st[kv[u]] * L2 + (wv[u] - s_sw[kv[u]] + nt)) * T + rv[u]);
+                cv[u] = cv2[u] = 0.f;
+                if (wv[u] >= 0 && gl < keep) {
+                    const int k = kv[u];
+                    cv[u] = __ldg(ctcP + ((int64_t)s_st[k] * L2 + (wv[u] - s_sw[k] + nt)) * T + rv[u]);
+                    if (two[u]) cv2[u] = __ldg(ctcP + ((int64_t)s_st[k + 1] * L2 + (wv[u] - s_sw[k + 1] + nt)) * T + rv[u]);
+                }
             }
+            // new scores, applied in sample order, and each lane's (Cf, template, slot) key: the
+            // largest Cf wins, then the lower template (Cf >= 0, so its bits order like the values)
+            unsigned long long key[kItemsPerGroup];
 #pragma unroll
             for (int u = 0; u < kItemsPerGroup; ++u) {
                 const int w = wv[u];
-                // a group's item may be empty while its warp's other groups have one (the finish
-                // reduction is warp-wide, so every lane takes part)
-                const bool live = __any_sync(0xffffffffu, w >= 0);
-                if (!live) continue;
-                float x = 0.f;
-                if (w >= 0) {
-                    x = fmaf(-s_sa[kv[u]], cv[u], xv[u]);
-                    // any further spike covering the same sample, in sample order
-                    for (int kk = kv[u] + 1; kk < total && s_sw[kk] - nt <= w; ++kk) {
-                        const float c = gl < keep
-                                            ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u])
-                                            : 0.f;
+                key[u] = 0ull;
+                if (w < 0) continue;
+                const int k = kv[u];
+                float x = fmaf(-s_sa[k], cv[u], xv[u]);
+                if (two[u]) {
+                    x = fmaf(-s_sa[k + 1], cv2[u], x);
+                    for (int kk = k + 2; kk < total && s_sw[kk] - nt <= w; ++kk) {   // rare: a third
+                        const float c =
+                            gl < keep ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u]) : 0.f;
                         x = fmaf(-s_sa[kk], c, x);
                     }
-                    if (gl < keep) SC[(size_t)w * ss + gl] = x;
                 }
-                finish(w, x, rv[u], w >= 0);
+                if (gl < keep) {
+                    SC[(size_t)w * ss + gl] = x;
+                    const float qv = fmaxf(x, 0.f);
+                    const float cfv = qv * qv * s_inm[rv[u]];
+                    key[u] = ((unsigned long long)__float_as_uint(cfv) << 32) |
+                             ((unsigned long long)(0xffffu - (unsigned)rv[u]) << 8) | (unsigned)gl;
+                }
             }
-            (void)kGroupMask;
+#pragma unroll
+            for (int o = LPS / 2; o > 0; o >>= 1)
+#pragma unroll
+                for (int u = 0; u < kItemsPerGroup; ++u) {
+                    const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key[u], o);
+                    key[u] = ok > key[u] ? ok : key[u];
+                }
+#pragma unroll
+            for (int u = 0; u < kItemsPerGroup; ++u) {
+                const int w = wv[u];
+                if (w >= 0 && gl == 0) {
+                    const bool inner = w >= nt && w < W - nt;
+                    cf[w + nt] = inner ? __uint_as_float((unsigned)(key[u] >> 32)) : 0.f;
+                    slot[w] = (unsigned char)(key[u] & 0xffu);
+                }
+            }
         }
         n_total += total;
         __syncthreads();
