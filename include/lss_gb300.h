@@ -62,7 +62,15 @@ typedef struct lss_params {
                                (hi = bf16(x), lo = bf16(x - hi), hi*hi + hi*lo + lo*hi in FP32: ~1e-5 relative
                                per product) at the BF16 rate, where C and K*C are multiples of 32 (the
                                high-pass and whitening need C, the convolution and projection K*C); a stage
-                               whose shape does not allow it runs as on 0 */
+                               whose shape does not allow it runs as on 0;
+                               4 = as 3, but the projection is one BF16 product (hi*hi) and 5 = one FP8 e4m3
+                               product (per-(component, channel) activation scales set from the first group
+                               and folded into the templates, per-template scales in the epilogue), FP32
+                               accumulation; every accepted candidate's amplitude is then recomputed from the
+                               exact FP32 projection of the split operands (its running score corrected by
+                               exact - low-precision initial score); spikes can differ where the
+                               low-precision score ranks candidates differently (agreement measured); both
+                               need the tensor-core convolution, K*C a multiple of 64 (5) and match_keep 0 */
     int32_t cluster_rule;   /* final cluster of a spike: 0 = nearest centroid in (x, y) (OnlineSpikesV2.cu:1058-1074);
                                1 = best PC score 2 tF.mu - |mu|^2 among the clusters within cluster_radius_um of the
                                spike (OnlineKilosort.py:233-284; cluster_centroids_pca.npy [T_final, nC*K]), -1 if none */

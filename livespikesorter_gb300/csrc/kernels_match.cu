@@ -276,6 +276,34 @@ match_kernel(float* __restrict__ Bt, float* __restrict__ Xres, const float* __re
                     }
                     tt = __shfl_sync(0xffffffffu, tt, 0);
                     amp = __shfl_sync(0xffffffffu, amp, 0);
+                    if (tt >= 0 && sc.rs.bt0) {
+                        // low-precision scores: the amplitude from the exact FP32 projection of the
+                        // split data operand, 16-byte loads, every lane's loads in flight at once
+                        const MatchRescore& rs = sc.rs;
+                        const int64_t xr = ((int64_t)b * W + w) * rs.kc;
+                        const uint4* xh = reinterpret_cast<const uint4*>(rs.x_hi + xr);
+                        const uint4* xl = reinterpret_cast<const uint4*>(rs.x_lo + xr);
+                        const float4* wr = reinterpret_cast<const float4*>(rs.wall3 + (int64_t)tt * rs.kc);
+                        float acc = 0.f;
+                        for (int v = lane; v < rs.kc / 8; v += 32) {
+                            const uint4 h = __ldg(xh + v), l = __ldg(xl + v);
+                            const float4 w0 = __ldg(wr + 2 * v), w1 = __ldg(wr + 2 * v + 1);
+                            const uint32_t hh[4] = {h.x, h.y, h.z, h.w}, ll[4] = {l.x, l.y, l.z, l.w};
+                            const float ww[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const float a0 = __uint_as_float(hh[e] << 16) + __uint_as_float(ll[e] << 16);
+                                const float a1 = __uint_as_float(hh[e] & 0xffff0000u) + __uint_as_float(ll[e] & 0xffff0000u);
+                                acc = fmaf(ww[2 * e], a0, acc);
+                                acc = fmaf(ww[2 * e + 1], a1, acc);
+                            }
+                        }
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                        const float b0 = __ldg(rs.bt0 + ((int64_t)b * W + w) * T + tt);
+                        amp = (brow(w)[tt] + (acc - b0)) / s_nm[tt];
+                        if (lane == 0) at_amp[w] = amp;
+                    }
                     if (tt >= 0 && lane < G) {
                         // into list p of CTA `lane`: claim a slot there, then write the entry
                         const int p = it & 1;

@@ -52,6 +52,7 @@ struct UmmaArgs {
     float* zt_lo;
     int zpitch;
     int zt_bf16;      // zt as its BF16 split (bf16 arrays)
+    const float* col_scale;   // kPlain, optional: C[m][n] *= col_scale[n] (the FP8 operands' scales)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -125,6 +126,22 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64
         : "memory");
 }
 
+// the same for A = B = FP8 e4m3 (kind::f8f6f4, K = 32 per instruction = the same 32 bytes)
+template <int BN>
+struct IdescE4m3 {
+    static constexpr uint32_t value =
+        (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+};
+
+template <int BN>
+__device__ __forceinline__ void mma_e4m3(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(IdescE4m3<BN>::value), "r"(accumulate)
+        : "memory");
+}
+
 template <int BN>
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
     asm volatile(
@@ -142,15 +159,18 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 // fixed B operand keeps its split), for the tensor-core tier whose activations are stored once.
 // BF16: the operands are BF16 splits (hi = bf16(x), lo = bf16(x - hi)) multiplied by kind::f16
 // MMAs: a K-step is 32 elements, still 64-byte rows, so tiles, swizzle and pipeline are unchanged.
-template <int BN, int MODE, bool ALO, bool BF16 = false>
+// LOWP: one product of the operands' hi parts only -- 1 = BF16 (kind::f16), 2 = FP8 e4m3
+// (kind::f8f6f4, a K-step of 64 elements); only hi tiles are loaded, so a stage is half the bytes
+// and twice the stages fit.  The epilogue then scales column n by args.col_scale[n] when given.
+template <int BN, int MODE, bool ALO, bool BF16 = false, int LOWP = 0>
 __global__ void __launch_bounds__(128, 1)
 umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
                  const __grid_constant__ CUtensorMap tB_hi, const __grid_constant__ CUtensorMap tB_lo, UmmaArgs args) {
     constexpr int kBN = BN;
-    constexpr int kKE = BF16 ? 2 * kBK : kBK;   // elements per K-step (64 bytes of each row)
+    constexpr int kKE = LOWP == 2 ? 4 * kBK : (BF16 ? 2 * kBK : kBK);   // elements per K-step (64 bytes of each row)
     constexpr int kTileB = kBN * kBK * 4;
-    constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;
-    constexpr int kLoadBytes = ALO ? kStageBytes : kTileA + 2 * kTileB;   // bytes the TMA lands per stage
+    constexpr int kStageBytes = LOWP ? kTileA + kTileB : 2 * kTileA + 2 * kTileB;
+    constexpr int kLoadBytes = LOWP ? kStageBytes : (ALO ? kStageBytes : kTileA + 2 * kTileB);   // bytes the TMA lands per stage
     constexpr int kStages = kSmemBudget / kStageBytes;
     const int M = args.M, N = args.N, K = args.K;
     int* err = args.err;
@@ -168,9 +188,10 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
     const int nkl = (int)((int64_t)nk * (blockIdx.z + 1) / gridDim.z) - kt0;
     // 1024-byte aligned stage buffers: [A_hi][A_lo][B_hi][B_lo] per stage
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    // (LOWP: [A_hi][B_hi] per stage)
     auto sA_hi = [&](int s) { return base + (uint32_t)(s * kStageBytes); };
     auto sA_lo = [&](int s) { return base + (uint32_t)(s * kStageBytes + kTileA); };
-    auto sB_hi = [&](int s) { return base + (uint32_t)(s * kStageBytes + 2 * kTileA); };
+    auto sB_hi = [&](int s) { return base + (uint32_t)(s * kStageBytes + (LOWP ? 1 : 2) * kTileA); };
     auto sB_lo = [&](int s) { return base + (uint32_t)(s * kStageBytes + 2 * kTileA + kTileB); };
 
     if (threadIdx.x == 0) {
@@ -212,9 +233,9 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
             const int ax = (MODE == kToeplitz) ? n0 + k0 : k0;
             const int by = (MODE == kToeplitz) ? 0 : n0;
             tma_load_2d(sA_hi(s), &tA_hi, fb, ax, m0);
-            if constexpr (ALO) tma_load_2d(sA_lo(s), &tA_lo, fb, ax, m0);
+            if constexpr (ALO && !LOWP) tma_load_2d(sA_lo(s), &tA_lo, fb, ax, m0);
             tma_load_2d(sB_hi(s), &tB_hi, fb, k0, by);
-            tma_load_2d(sB_lo(s), &tB_lo, fb, k0, by);
+            if constexpr (!LOWP) tma_load_2d(sB_lo(s), &tB_lo, fb, k0, by);
             ++issued;
         }
         // the copies of the last rounds must have landed before the CTA may exit
@@ -236,7 +257,11 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
                 const uint32_t off = (uint32_t)kk * 32u;
                 const uint64_t ah = smem_desc(sA_hi(s) + off), al = smem_desc(sA_lo(s) + off);
                 const uint64_t bh = smem_desc(sB_hi(s) + off), bl = smem_desc(sB_lo(s) + off);
-                if constexpr (BF16) {
+                if constexpr (LOWP == 1) {
+                    mma_bf16<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
+                } else if constexpr (LOWP == 2) {
+                    mma_e4m3<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
+                } else if constexpr (BF16) {
                     mma_bf16<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
                     mma_bf16<BN>(tmem, ah, bl, 1u);
                     if constexpr (ALO) mma_bf16<BN>(tmem, al, bh, 1u);
@@ -297,6 +322,11 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
         if (ok && row < M) {
             float* crow = args.out + ((int64_t)blockIdx.z * M + row) * args.ldc + n0 + c0;
             const int ncol = min(32, N - (n0 + c0));
+            if (args.col_scale) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (j < ncol) r[j] = __float_as_uint(__uint_as_float(r[j]) * __ldg(args.col_scale + n0 + c0 + j));
+            }
             if (args.zt_hi) {
                 // lanes hold consecutive rows = consecutive times of one channel row of zt
                 const int b = row / args.wlen, w = row - b * args.wlen;
@@ -681,10 +711,25 @@ static bool make_map_bf16(CUtensorMap* m, const void* ptr, uint64_t rows, uint64
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// rows x cols bytes (FP8) row-major, boxes of 64 columns (64 B) x box_rows rows, 64-byte swizzle
+static bool make_map_u8(CUtensorMap* m, const void* ptr, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+    auto fn = encode_fn();
+    if (!fn || ((uintptr_t)ptr & 15) || cols % 16) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols};
+    const cuuint32_t box[2] = {(cuuint32_t)(4 * kBK), box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
 struct UmmaOperands {
     CUtensorMap a_hi, a_lo, b_hi, b_lo;
     bool bf16 = false;        // BF16 splits (kind::f16) instead of TF32 splits
     bool has_a_lo = true;     // false: A is TF32 data alone (two products)
+    int lowp = 0;             // 1 = one BF16 product of the hi parts, 2 = one FP8 e4m3 product
+    const float* col_scale = nullptr;   // per output column (B row) scale applied in the epilogue
     int rows_a = 0, rows_b = 0, K = 0;
     int cols_a = 0;           // Toeplitz: columns of A (wrapped window length, padded)
 };
@@ -693,6 +738,10 @@ constexpr int kPlainBN = 256;
 template <int BN>
 constexpr int smem_bytes() {
     return (kSmemBudget / (2 * kTileA + 2 * BN * kBK * 4)) * (2 * kTileA + 2 * BN * kBK * 4) + 1024;
+}
+template <int BN>
+constexpr int smem_bytes_lowp() {
+    return (kSmemBudget / (kTileA + BN * kBK * 4)) * (kTileA + BN * kBK * 4) + 1024;
 }
 
 UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, const float* b_hi, const float* b_lo,
@@ -725,6 +774,28 @@ UmmaOperands* umma_make_bf16(const void* a_hi, const void* a_lo, int64_t rows_a,
         delete u;
         return nullptr;
     }
+    return u;
+}
+
+UmmaOperands* umma_make_lowp(const void* a, int64_t rows_a, const void* b, int64_t rows_b, int K, int lowp,
+                             const float* col_scale) {
+    const int ke = lowp == 2 ? 4 * kBK : 2 * kBK;   // elements per 64-byte K-step
+    if ((lowp != 1 && lowp != 2) || K % ke != 0 || rows_b > 2 * kPlainBN) return nullptr;
+    auto* u = new UmmaOperands();
+    u->bf16 = lowp == 1;
+    u->lowp = lowp;
+    u->rows_a = (int)rows_a;
+    u->rows_b = (int)rows_b;
+    u->K = K;
+    const bool ok = lowp == 2 ? make_map_u8(&u->a_hi, a, rows_a, K, kBM) && make_map_u8(&u->b_hi, b, rows_b, K, kPlainBN)
+                              : make_map_bf16(&u->a_hi, a, rows_a, K, kBM) && make_map_bf16(&u->b_hi, b, rows_b, K, kPlainBN);
+    if (!ok) {
+        delete u;
+        return nullptr;
+    }
+    u->a_lo = u->a_hi;   // never loaded
+    u->b_lo = u->b_hi;
+    u->col_scale = col_scale;
     return u;
 }
 
@@ -775,10 +846,12 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
                                 float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s, bool zt_bf16) {
     if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
     if (zt_hi && (wlen <= 0 || zpitch < wlen || (zt_bf16 && !zt_lo))) return cudaErrorInvalidValue;
-    auto kern = u->bf16       ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
+    auto kern = u->lowp == 2  ? umma_gemm_3xtf32<kPlainBN, kPlain, true, false, 2>
+                : u->lowp == 1 ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true, 1>
+                : u->bf16     ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
                 : u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true>
                               : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
-    constexpr int smem = smem_bytes<kPlainBN>();
+    const int smem = u->lowp ? smem_bytes_lowp<kPlainBN>() : smem_bytes<kPlainBN>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
     UmmaArgs a{};
@@ -793,6 +866,7 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
     a.wlen = wlen;
     a.zpitch = zpitch;
     a.zt_bf16 = zt_bf16 ? 1 : 0;
+    a.col_scale = u->col_scale;
     dim3 grid((N + kPlainBN - 1) / kPlainBN, (M + kBM - 1) / kBM);
     kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     return cudaGetLastError();
@@ -814,13 +888,15 @@ cudaError_t launch_umma_gemm_splitk(const UmmaOperands* u, float* Cm, int M, int
                                     int* err, cudaStream_t s) {
     if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN || S < 1 || !ws)
         return cudaErrorInvalidValue;
-    const int nk = u->K / (u->bf16 ? 2 * kBK : kBK);
+    const int nk = u->K / (u->lowp == 2 ? 4 * kBK : (u->bf16 ? 2 * kBK : kBK));
     S = std::min(S, nk);
     if (S <= 1) return launch_umma_gemm(u, Cm, M, N, ldc, err, s);
-    auto kern = u->bf16       ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
+    auto kern = u->lowp == 2  ? umma_gemm_3xtf32<kPlainBN, kPlain, true, false, 2>
+                : u->lowp == 1 ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true, 1>
+                : u->bf16     ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
                 : u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true>
                               : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
-    constexpr int smem = smem_bytes<kPlainBN>();
+    const int smem = u->lowp ? smem_bytes_lowp<kPlainBN>() : smem_bytes<kPlainBN>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
     UmmaArgs a{};
@@ -831,6 +907,7 @@ cudaError_t launch_umma_gemm_splitk(const UmmaOperands* u, float* Cm, int M, int
     a.ldc = ldc;
     a.err = err;
     a.wlen = 1;
+    a.col_scale = u->col_scale;   // the slices are scaled before they are summed: sum(s x) = s sum(x) up to rounding
     dim3 grid((N + kPlainBN - 1) / kPlainBN, (M + kBM - 1) / kBM, S);
     kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     const int blocks = (int)std::min<int64_t>(((int64_t)M * N + 255) / 256, 2048);

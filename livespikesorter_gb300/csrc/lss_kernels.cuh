@@ -29,11 +29,24 @@ struct MatchOut {
     int cap;
 };
 
+// Exact re-score of accepted candidates when the scores come from a low-precision projection
+// (bt0 null: off).  An accepted (t, w) takes the amplitude (B[w][t] + exact - bt0[w][t]) / nm[t]:
+// its running score corrected by the difference between the FP32 projection of the exact operands,
+// sum_i wall3[t][i] (x_hi[w][i] + x_lo[w][i]), and the low-precision initial score bt0.
+struct MatchRescore {
+    const float* bt0;       // [nb][W][T] the initial low-precision scores
+    const uint16_t* x_hi;   // [nb][W][kc] bf16 bits: the projection's data operand (split)
+    const uint16_t* x_lo;
+    const float* wall3;     // [T][kc]
+    int kc;                 // K * C, a multiple of 8
+};
+
 // Scratch of the matching loop (device), per batch.
 struct MatchScratch {
     float* cfmax;      // [nb][W]   per-sample maximum (windows longer than the staged chunk)
     int* at_t;         // [nb][W]   template of the spike accepted at w this iteration, -1 if none
     float* at_amp;     // [nb][W]
+    MatchRescore rs;   // exact re-score of accepted candidates (rs.bt0 null: off)
 };
 
 // One spike record as written by the feature kernel (host-mapped memory).
@@ -136,6 +149,18 @@ UmmaOperands* umma_make_toeplitz_bf16(const void* x_hi, const void* x_lo, int64_
 void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
 // BF16 split: hi = bf16(x), lo = bf16(x - hi) (bf16 arrays of n elements)
 void launch_split_bf16(const float* x, void* hi, void* lo, int64_t n, cudaStream_t s);
+// FP8 projection operands (kernels_lowp.cu).  Calibration, once: from the rows of a BF16-split data
+// operand x [rows][kc], the per-column scales sig / isig [kc] and the folded e4m3 templates w8
+// [T][kc] with their scales tscale [T] (colmax [kc] scratch).  Quantize: x8 = e4m3(x * isig).
+void launch_lowp_calibrate(const void* x_hi, const void* x_lo, int64_t rows, int kc, const float* wall3, int T,
+                           unsigned* colmax, float* sig, float* isig, uint8_t* w8, float* tscale, cudaStream_t s);
+void launch_lowp_quantize(const void* x_hi, const void* x_lo, int64_t rows, int kc, const float* isig, uint8_t* x8,
+                          cudaStream_t s);
+// one low-precision product: lowp 1 = A, B bf16 [rows][K] (kind::f16, K % 32 == 0), 2 = A, B FP8 e4m3
+// bytes [rows][K] (kind::f8f6f4, K % 64 == 0); col_scale (may be null) scales column n of C by
+// col_scale[n] in the epilogue
+UmmaOperands* umma_make_lowp(const void* a, int64_t rows_a, const void* b, int64_t rows_b, int K, int lowp,
+                             const float* col_scale);
 // the GEMM on BF16-split operands (kind::f16, hi*hi + hi*lo + lo*hi; K % 32 == 0)
 UmmaOperands* umma_make_bf16(const void* a_hi, const void* a_lo, int64_t rows_a, const void* b_hi, const void* b_lo,
                              int64_t rows_b, int K);

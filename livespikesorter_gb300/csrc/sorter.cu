@@ -153,6 +153,13 @@ struct Handle {
     bool tf32_data = false;   // gemm_path 2: activations stored once as TF32, two products per GEMM
     bool bf16_proj = false;   // gemm_path 3: projection on BF16 splits (kind::f16, three products)
     bool bf16_pre = false;    // gemm_path 3: high-pass and whitening on BF16 splits as well
+    // gemm_path 4 / 5: the projection as one BF16 (lowp 1) or FP8 e4m3 (lowp 2) product of the
+    // split operands' hi parts, accepted candidates re-scored exactly in the matching loop
+    int lowp = 0;
+    bool lowp_ready = false;            // FP8: scales calibrated, folded templates built
+    uint8_t* d_W8 = nullptr;            // [T][K*C] e4m3 templates (scales folded)
+    float *d_tau = nullptr, *d_sig = nullptr, *d_isig = nullptr;   // [T] template, [K*C] activation scales
+    unsigned* d_colmax = nullptr;       // [K*C] calibration scratch
     bool tc_conv = false;     // basis convolution as per-component band GEMMs on the tensor cores
     ConvGeometry conv_g;
     float *d_S_hi = nullptr, *d_S_lo = nullptr;   // its band strips (tf32 split)
@@ -189,6 +196,8 @@ struct Handle {
     float *d_Zt_hi = nullptr, *d_Zt_lo = nullptr;   // channel-major whitened windows (tensor-core convolution)
     float* d_split = nullptr;   // partial projections of split-K launches [kSplitK][rows][T]
     float4 *d_iir_zs = nullptr, *d_iir_sin = nullptr;   // stateful high-pass: per-chunk states [chunks][C]
+    float* d_Bt0 = nullptr;     // low-precision tiers: the initial scores [nb][W][T]
+    uint8_t* d_A8 = nullptr;    // FP8 tier: the quantized data operand [nb][W][K*C]
     MatchScratch sc{};
     MatchOut mo{};
     int64_t work_bytes = 0;
@@ -281,7 +290,7 @@ Handle::~Handle() {
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
                     (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo,
                     (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm, (void*)d_iir_state,
-                    (void*)d_iir_pow})
+                    (void*)d_iir_pow, (void*)d_W8, (void*)d_tau, (void*)d_sig, (void*)d_isig, (void*)d_colmax})
         if (p) cudaFree(p);
     if (h_gemm_err) cudaFreeHost(h_gemm_err);
     for (auto& s : slots) {
@@ -315,7 +324,7 @@ void Handle::free_work() {
     for (void* p : {(void*)d_raw, (void*)d_colsum, (void*)d_ticket, (void*)d_mean, (void*)d_Xw, (void*)d_Y, (void*)d_Z, (void*)d_Bpc, (void*)d_Bt,
                     (void*)d_Y_lo, (void*)d_Bpc_lo, (void*)d_Xt_hi, (void*)d_Xt_lo, (void*)d_Zt_hi, (void*)d_Zt_lo,
                     (void*)d_split, (void*)d_lid, (void*)d_lsc, (void*)d_pcf, (void*)d_pslot, (void*)d_iir_zs,
-                    (void*)d_iir_sin,
+                    (void*)d_iir_sin, (void*)d_Bt0, (void*)d_A8,
                     (void*)sc.cfmax, (void*)sc.at_t, (void*)sc.at_amp, (void*)mo.n_spikes, (void*)mo.n_iters, (void*)mo.status, (void*)mo.sp_w,
                     (void*)mo.sp_t, (void*)mo.sp_amp, (void*)mo.sp_iter})
         if (p) cudaFree(p);
@@ -329,6 +338,8 @@ void Handle::free_work() {
     d_Zt_hi = d_Zt_lo = nullptr;
     d_split = nullptr;
     d_iir_zs = d_iir_sin = nullptr;
+    d_Bt0 = nullptr;
+    d_A8 = nullptr;
     d_lid = nullptr;
     d_lsc = nullptr;
     d_pcf = nullptr;
@@ -486,8 +497,8 @@ void Handle::init(const char* dir, const lss_params* prm) {
     d_iU = dev_upload(m.iU, dev_bytes, st);
     d_chan = (Cin > C) ? dev_upload(chan, dev_bytes, st) : nullptr;
     // tensor-core GEMMs need K % 16 == 0 and N <= 512 (C for the whitening, T for the projection)
-    if (p.gemm_path < 0 || p.gemm_path > 3)
-        throw LoadError{LSS_ERR_ARG, "lss_params.gemm_path must be 0, 1, 2 or 3"};
+    if (p.gemm_path < 0 || p.gemm_path > 5)
+        throw LoadError{LSS_ERR_ARG, "lss_params.gemm_path must be 0 .. 5"};
     if (p.cluster_rule < 0 || p.cluster_rule > 1 || !(p.cluster_radius_um >= 0.f))
         throw LoadError{LSS_ERR_ARG, "lss_params.cluster_rule must be 0 or 1, cluster_radius_um >= 0"};
     if (p.cluster_rule == 1) {
@@ -511,7 +522,8 @@ void Handle::init(const char* dir, const lss_params* prm) {
     tc_highpass = tc_whiten;
     // the convolution reads the whitened windows the whitening GEMM also writes channel-major;
     // gemm_path 3 runs it and the projection on BF16 splits
-    const bool bf16_tier = p.gemm_path == 3 && (K * C) % 32 == 0;
+    const bool bf16_tier = p.gemm_path >= 3 && (K * C) % 32 == 0;
+    lowp = p.gemm_path == 4 ? 1 : (p.gemm_path == 5 ? 2 : 0);
     bf16_pre = bf16_tier && tc_whiten && C % 32 == 0;
     tc_conv = tc_whiten && tc_project && conv_tc_geometry(nt, K, conv_g, bf16_tier);
     if (tc_conv) {
@@ -551,6 +563,19 @@ void Handle::init(const char* dir, const lss_params* prm) {
         }
         LSS_CUDA(cudaGetLastError());
         LSS_CUDA(cudaStreamSynchronize(st));
+    }
+    if (lowp) {
+        if (!bf16_proj || (lowp == 2 && (K * C) % 64 != 0))
+            throw LoadError{LSS_ERR_ARG, "gemm_path 4 / 5 need the tensor-core convolution and K*C a multiple of 64"};
+        if (p.match_keep > 0)
+            throw LoadError{LSS_ERR_ARG, "gemm_path 4 / 5 re-score in the full matching loop (match_keep 0)"};
+        if (lowp == 2) {
+            d_W8 = dev_alloc<uint8_t>((size_t)T * K * C, dev_bytes);
+            d_tau = dev_alloc<float>((size_t)T, dev_bytes);
+            d_sig = dev_alloc<float>((size_t)K * C, dev_bytes);
+            d_isig = dev_alloc<float>((size_t)K * C, dev_bytes);
+            d_colmax = dev_alloc<unsigned>((size_t)K * C, dev_bytes);
+        }
     }
     if (p.match_keep < 0 || p.match_keep > kPruneKeepMax)
         throw LoadError{LSS_ERR_ARG, "lss_params.match_keep must be 0 (full loop) or 1.." + std::to_string(kPruneKeepMax)};
@@ -649,7 +674,8 @@ void Handle::ensure_work(int Wn, int nb) {
                          (int64_t)nba * Wa * T * 4 + (int64_t)nba * Wa * 17 + (int64_t)nba * cap * 16 +
                          (tc_project ? (int64_t)kSplitK * std::min(nba, kSplitBatches) * Wa * T * 4 : 0) +
                          (keep > 0 ? (int64_t)nba * Wa * kPruneKeepMax * 6 + (int64_t)nba * (Wa + 2 * nt) * 5 : 0) +
-                         (iir ? (int64_t)iir_chunk_cap(Wa, nba) * C * 32 : 0);
+                         (iir ? (int64_t)iir_chunk_cap(Wa, nba) * C * 32 : 0) +
+                         (lowp ? (int64_t)nba * Wa * T * 4 + (lowp == 2 ? (int64_t)nba * Wa * K * C : 0) : 0);
     if (p.mem_budget > 0 && dev_bytes + need > p.mem_budget)
         throw LoadError{LSS_ERR_NOMEM, "admission denied: the handle needs " + std::to_string(dev_bytes + need) +
                                            " device bytes, budget " + std::to_string(p.mem_budget)};
@@ -715,8 +741,14 @@ void Handle::ensure_work(int Wn, int nb) {
                              : umma_make(d_Y, d_Y_lo, (int64_t)nba * Wa, d_WD_hi, d_WD_lo, C, C);
         if (!um_whiten) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (whitening GEMM)"};
     }
+    if (lowp) {
+        d_Bt0 = dev_alloc<float>((size_t)nba * Wa * T, dev_bytes);
+        if (lowp == 2) d_A8 = dev_alloc<uint8_t>((size_t)nba * Wa * K * C, dev_bytes);
+    }
     if (tc_project) {
-        um_project = bf16_proj
+        um_project = lowp == 2   ? umma_make_lowp(d_A8, (int64_t)nba * Wa, d_W8, T, K * C, 2, d_tau)
+                     : lowp == 1 ? umma_make_lowp(d_Bpc, (int64_t)nba * Wa, d_Wall3_hi, T, K * C, 1, nullptr)
+                     : bf16_proj
                          ? umma_make_bf16(d_Bpc, d_Bpc_lo, (int64_t)nba * Wa, d_Wall3_hi, d_Wall3_lo, T, K * C)
                          : umma_make(d_Bpc, d_Bpc_lo, (int64_t)nba * Wa, d_Wall3_hi, d_Wall3_lo, T, K * C);
         if (!um_project) throw LoadError{LSS_ERR_INTERNAL, "tensor map setup failed (projection GEMM)"};
@@ -838,6 +870,16 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
     }
     ++nl;
     mark();
+    if (lowp == 2) {
+        // FP8 operands: scales from this first group, then the data operand quantized
+        const int64_t rows = (int64_t)nb * Wn;
+        if (!lowp_ready) {
+            launch_lowp_calibrate(d_Bpc, d_Bpc_lo, rows, K * C, d_Wall3, T, d_colmax, d_sig, d_isig, d_W8, d_tau, st);
+            nl += 3;
+            lowp_ready = true;
+        }
+        launch_lowp_quantize(d_Bpc, d_Bpc_lo, rows, K * C, d_isig, d_A8, st), ++nl;
+    }
     if (tc_project && nb <= kSplitBatches) {
         LSS_CUDA(launch_umma_gemm_splitk(um_project, d_Bt, nb * Wn, T, T, d_split, kSplitK, d_gemm_err, st));
         ++nl;   // and the slice sum
@@ -847,6 +889,8 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
         launch_sgemm_nt(d_Bpc, (int64_t)K * C, (int64_t)Wn * K * C, d_Wall3, (int64_t)K * C, d_Bt, T, (int64_t)Wn * T, Wn,
                         T, K * C, nb, st);
     ++nl;
+    // the initial low-precision scores, for the exact re-score of accepted candidates
+    if (lowp) LSS_CUDA(cudaMemcpyAsync(d_Bt0, d_Bt, sizeof(float) * (size_t)nb * Wn * T, cudaMemcpyDeviceToDevice, st));
     LSS_CUDA(cudaGetLastError());
     mark();
 }
@@ -911,7 +955,11 @@ void Handle::run_match(int nb, int Wn, int64_t& nl) {
         LSS_CUDA(launch_residual(d_Z, d_pre_wf, mo, Wn, C, nt, nb, st));
         nl += 3;   // selection, loop, residual
     } else {
-        LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, sc, mo, st,
+        MatchScratch scr = sc;
+        if (lowp)
+            scr.rs = MatchRescore{d_Bt0, reinterpret_cast<const uint16_t*>(d_Bpc),
+                                  reinterpret_cast<const uint16_t*>(d_Bpc_lo), d_Wall3, K * C};
+        LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, scr, mo, st,
                               p.match_variant));
         nl += 2;   // the loop and the residual
     }
