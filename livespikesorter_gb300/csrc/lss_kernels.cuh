@@ -34,11 +34,11 @@ struct MatchOut {
 // its running score corrected by the difference between the FP32 projection of the exact operands,
 // sum_i wall3[t][i] (x_hi[w][i] + x_lo[w][i]), and the low-precision initial score bt0.
 struct MatchRescore {
-    const float* bt0;       // [nb][W][T] the initial low-precision scores
-    const uint16_t* x_hi;   // [nb][W][kc] bf16 bits: the projection's data operand (split)
-    const uint16_t* x_lo;
-    const float* wall3;     // [T][kc]
-    int kc;                 // K * C, a multiple of 8
+    const float* bt0 = nullptr;       // [nb][W][T] the initial low-precision scores
+    const uint16_t* x_hi = nullptr;   // [nb][W][kc] bf16 bits: the projection's data operand (split)
+    const uint16_t* x_lo = nullptr;
+    const float* wall3 = nullptr;     // [T][kc]
+    int kc = 0;                       // K * C, a multiple of 8
 };
 
 // Scratch of the matching loop (device), per batch.

@@ -108,11 +108,11 @@ extern "C" int lss_match_noalloc(float* scores, float* residual, const float* ct
         }
         base = g_addr[dev];
     }
-    lss::MatchScratch sc;
+    lss::MatchScratch sc{};
     sc.cfmax = reinterpret_cast<float*>(base + kOffCfmax);
     sc.at_t = reinterpret_cast<int*>(base + kOffAtT);
     sc.at_amp = reinterpret_cast<float*>(base + kOffAtAmp);
-    lss::MatchOut out;
+    lss::MatchOut out{};
     out.n_spikes = n_spikes;
     out.n_iters = reinterpret_cast<int*>(base + kOffIters);
     out.status = reinterpret_cast<int*>(base + kOffStatus);
