@@ -4,10 +4,11 @@ bench.py's CPU-baseline / reference legs may import this module, and only as the
 CPU restatement of the reference's threshold-crossing sorter
 (src/SpikeSorter/ThresholdCrossing.cpp, class ThresholdCrossing), in numpy.
 
-Parity status: the reference's C++ for this path cannot be compiled here (it needs Winsock, the
-SpikeGLX SDK and the reference's networking layer, ThresholdCrossing.cpp:1-12, and ships no
-tests or fixtures for it), so this restatement is pinned only by reading the source: parity
-unpinned beyond that.  Each function cites the lines it follows.
+Parity: pinned against the reference's own code.  oracle/build_ref.py compiles the reference's
+src/SpikeSorter/ThresholdCrossing.cpp unmodified under stubs for its socket / SDK / networking
+types, tests/golden/make_tc_golden.py runs it on a scripted replay of seeded int16 rows, and
+tests/test_tc_reference_cpu.py checks that this restatement reproduces every payload's events in
+order (tests/golden/tc_reference.npz).  Each function cites the lines it follows.
 
 Semantics restated:
   * DC removal in float32: ``m_fY[j] = m_fY[j] - means[i]`` (ThresholdCrossing.cpp:210-214), the

@@ -229,3 +229,28 @@ def test_cpp_threshold_crossing_replay(tmp_path):
     np.testing.assert_array_equal(got[:, 0], t)
     np.testing.assert_array_equal(got[:, 1], c)
     assert r.stdout.strip() == f"events {len(t)}"
+
+
+def test_gpu_reproduces_the_reference_run():
+    """The events the reference's own ThresholdCrossing.cpp emitted on a scripted replay
+    (tests/golden/tc_reference.npz, see tests/test_tc_reference_cpu.py): each fetched block pushed
+    with the reference's stamp (its newest stream count) gives the same (time, channel) sequence."""
+    import sys
+    golden = ROOT / "tests" / "golden"
+    sys.path.insert(0, str(golden))
+    sys.path.insert(0, str(ROOT / "tests"))
+    import make_tc_golden as mk
+    from test_tc_reference_cpu import fetches
+    z = np.load(golden / "tc_reference.npz")
+    C = int(z["C"])
+    x = mk.rows(z["means"], z["medians"], int(z["seed"]), int(z["N"]), C)
+    times, chans = [], []
+    with threshold.ThresholdCrossing(z["means"][:C], z["medians"][:C], float(z["threshold_std"]),
+                                     max_rows=int(z["max_window"])) as tc:
+        for latest, a, b in fetches(z):
+            tc.push(np.ascontiguousarray(x[a:b]), first_row_sample=latest)
+            ev = tc.poll_all()
+            times.append(ev["time"])
+            chans.append(ev["channel"])
+    np.testing.assert_array_equal(np.concatenate(times), z["times"])
+    np.testing.assert_array_equal(np.concatenate(chans), z["channels"])
