@@ -249,7 +249,9 @@ def test_learned_gate_keeps_the_plain_matchers_spikes(dense_probe):
             zw = proposal.window_logits(tr, z, starts)
             params = tr.params
         assert losses[-20:].mean() < 0.5 * losses[:20].mean(), (losses[:5], losses[-5:])
-        thr = proposal.choose_threshold(zw, labels, 1, 0.995)
+        # the logit threshold keeps 99.9 % of the training windows' labelled cells open: held-out
+        # recall then clears the metric's 99.5 % (measured 99.9-100 % at 5-40 Hz)
+        thr = proposal.choose_threshold(zw, labels, 1, 0.999)
         s.set_proposal(params, logit_threshold=thr, dilate=1)
         results = {}
         for rate, seed in ((5.0, 101), (40.0, 102)):
@@ -263,8 +265,9 @@ def test_learned_gate_keeps_the_plain_matchers_spikes(dense_probe):
             s.set_proposal(params, logit_threshold=thr, dilate=1)
             ri, _ = match_spikes(plain["time"], plain["tmpl"], gated["time"], gated["tmpl"])
             results[rate] = (len(ri) / max(1, len(plain)), (o1 - o0) / (c1 - c0), len(plain), len(gated))
-    # the gain: most cells closed at 5 Hz; at 40 Hz most cells hold a spike and stay open
+    # the gain: most cells closed at 5 Hz (measured 23 % open); at 40 Hz most cells hold a spike
+    # and stay open
     for rate, (recall, open_frac, n_plain, n_gated) in results.items():
         assert n_plain > 200, results
-        assert recall >= 0.97, results
+        assert recall >= 0.995, results
         assert open_frac <= (0.4 if rate == 5.0 else 0.95), results
