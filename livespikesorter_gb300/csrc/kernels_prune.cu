@@ -480,6 +480,325 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// The same loop on a thread-block cluster of G CTAs per window, for windows whose per-sample state
+// fits in shared memory.  CTA r owns the samples w = r, r + G, r + 2G, ... (interleaved, so the
+// 2nt + 1 samples around a spike spread over the whole cluster): their listed templates and
+// scores.  Every CTA keeps a replica of every sample's maximum Cf and of the template and score
+// behind it; an owner pushes the new values of the samples it updates into all G CTAs through
+// distributed shared memory.  So every CTA finds the same accepted spikes (max pool, threshold)
+// and ranks them the same way on its own, and phase C updates the own samples near them: one
+// cluster barrier per iteration.
+// ---------------------------------------------------------------------------------------------
+template <int G>
+__device__ __forceinline__ void cluster_sync_all() {
+    __syncthreads();
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ unsigned prune_cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned prune_dsmem(const void* local, unsigned rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"((unsigned)__cvta_generic_to_shared(local)), "r"(rank));
+    return r;
+}
+
+constexpr int kClItems = 4;   // samples a lane group of the cluster form updates at once
+
+// shared memory of one CTA: [1/nm, nm: 2T f32][accepted lists: 6 x cap][own-item starts and
+// prefix: 2 x (cap + 1) int], to 16 B; [cf, block prefix, block suffix: 3 (W + 2nt) f32][winner
+// score W f32][winner template W i32][own lists: span x ks u16, to 16 B][own scores: span x ks f32]
+__host__ __device__ inline size_t prune_cl_smem(int W, int T, int nt, int keep, int G) {
+    const size_t cap = (size_t)prune_iter_cap(W, nt);
+    const size_t span = (size_t)(W + G - 1) / G;
+    const size_t ks = (size_t)prune_stride(keep);
+    size_t b = ((size_t)T * 8 + cap * 24 + (cap + 1) * 8 + 15) & ~(size_t)15;
+    b += (size_t)(W + 2 * nt) * 12 + (size_t)W * 8;
+    b += (span * ks * 2 + 15) & ~(size_t)15;
+    return b + span * ks * 4;
+}
+
+template <int G, int NTHR, int LPS>
+__global__ void __launch_bounds__(NTHR, 2)
+match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __restrict__ lsc_g, int keep,
+                            const float* __restrict__ ctcP, const float* __restrict__ nm, float th2, int W, int T,
+                            int nt, int max_iters, MatchOut out) {
+    constexpr int kWarps = NTHR / 32;
+    constexpr int kGroups = 32 / LPS;
+    static_assert(G <= LPS, "the lanes of a group push one CTA each");
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int b = blockIdx.x / G;
+    const int rank = (int)prune_cluster_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gl = lane % LPS, grp = lane / LPS;
+    const int L2 = 2 * nt + 1, n = W + 2 * nt;
+    const int cap_it = prune_iter_cap(W, nt);
+    const int span = (W + G - 1) / G;
+    const int own = rank < W ? (W - rank + G - 1) / G : 0;
+    const int ks = prune_stride(keep);
+    float* s_inm = reinterpret_cast<float*>(smraw);
+    float* s_nm = s_inm + T;
+    int* s_aw = reinterpret_cast<int*>(s_nm + T);
+    int* s_at = s_aw + cap_it;
+    float* s_aa = reinterpret_cast<float*>(s_at + cap_it);
+    int* s_sw = reinterpret_cast<int*>(s_aa + cap_it);
+    int* s_st = s_sw + cap_it;
+    float* s_sa = reinterpret_cast<float*>(s_st + cap_it);
+    int* s_lo = reinterpret_cast<int*>(s_sa + cap_it);     // [cap + 1] first own sample of spike k's items
+    int* s_pre = s_lo + cap_it + 1;                        // [cap + 1] own items before spike k
+    unsigned char* next = smraw + ((((size_t)T * 8 + (size_t)cap_it * 24 + (size_t)(cap_it + 1) * 8) + 15) & ~(size_t)15);
+    float* cf = reinterpret_cast<float*>(next);            // [n] maximum of w at cf[w + nt]
+    float* pg = cf + n;
+    float* ph = pg + n;
+    float* wsc = ph + n;                                   // [W] score behind cf
+    int* wt = reinterpret_cast<int*>(wsc + W);             // [W] template behind cf
+    uint16_t* RK = reinterpret_cast<uint16_t*>(wt + W);    // [span][ks] own lists
+    float* SC = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(RK) +
+                                         ((((size_t)span * ks * 2) + 15) & ~(size_t)15));   // [span][ks]
+    __shared__ int s_cnt, s_over;
+
+    const uint16_t* rk_g = lrk_g + (int64_t)b * W * KP;
+    const float* sc_g = lsc_g + (int64_t)b * W * KP;
+    for (int q = tid; q < own * ks; q += NTHR) {
+        const int j = q / ks, i = q - j * ks;
+        const int w = rank + G * j;
+        RK[q] = i < keep ? rk_g[(size_t)w * KP + i] : (uint16_t)0;
+        SC[q] = i < keep ? sc_g[(size_t)w * KP + i] : 0.f;
+    }
+    for (int t = tid; t < T; t += NTHR) {
+        s_nm[t] = nm[t];
+        s_inm[t] = 1.f / nm[t];
+    }
+    for (int i = tid; i < nt; i += NTHR) {
+        cf[i] = -FLT_MAX;
+        cf[W + nt + i] = -FLT_MAX;
+    }
+    if (tid == 0) {
+        s_cnt = 0;
+        s_over = 0;
+    }
+    // every CTA of the cluster has started before any pushes into another's shared memory
+    cluster_sync_all<G>();
+
+    // the group's own sample w (own index j), lane gl holding entry gl (score x, template r): the
+    // (Cf, template, slot) maximum of the list -- largest Cf, then the lower template -- pushed into
+    // every CTA (lane g < G of the group writes CTA g)
+    auto finish_push = [&](int w, float x, int r, bool valid) {
+        unsigned long long key = 0ull;
+        if (valid && gl < keep) {
+            const float q = fmaxf(x, 0.f);
+            key = ((unsigned long long)__float_as_uint(q * q * s_inm[r]) << 32) |
+                  ((unsigned long long)(0xffffu - (unsigned)r) << 8) | (unsigned)gl;
+        }
+#pragma unroll
+        for (int o = LPS / 2; o > 0; o >>= 1) {
+            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+            key = ok > key ? ok : key;
+        }
+        const float xw = __shfl_sync(0xffffffffu, x, grp * LPS + (int)(key & 0xffu));
+        if (valid && gl < G) {
+            const bool inner = w >= nt && w < W - nt;
+            const float v = inner ? __uint_as_float((unsigned)(key >> 32)) : 0.f;
+            const int tw = (int)(0xffffu - (unsigned)((key >> 8) & 0xffffu));
+            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(prune_dsmem(cf + w + nt, (unsigned)gl)), "f"(v)
+                         : "memory");
+            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(prune_dsmem(wsc + w, (unsigned)gl)), "f"(xw)
+                         : "memory");
+            asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(prune_dsmem(wt + w, (unsigned)gl)), "r"(tw)
+                         : "memory");
+        }
+    };
+    for (int j0 = warp * kGroups; j0 < span; j0 += kWarps * kGroups) {
+        const int j = j0 + grp;
+        const bool valid = j < own;
+        const int w = rank + G * j;
+        const int r = valid && gl < keep ? RK[(size_t)j * ks + gl] : 0;
+        const float x = valid && gl < keep ? SC[(size_t)j * ks + gl] : 0.f;
+        finish_push(w, x, r, valid);
+    }
+    cluster_sync_all<G>();
+
+    int n_total = 0, iters = 0;
+    int* sp_w = out.sp_w + (int64_t)b * out.cap;
+    int* sp_t = out.sp_t + (int64_t)b * out.cap;
+    float* sp_amp = out.sp_amp + (int64_t)b * out.cap;
+    int* sp_iter = out.sp_iter + (int64_t)b * out.cap;
+    for (int it = 0; it < max_iters; ++it) {
+        // ---- B1: the max pool of the replicated maxima (block prefix / suffix maxima), acceptance
+        for (int blk = warp; blk * L2 < n; blk += kWarps) {
+            const int b0 = blk * L2, b1 = min(n, b0 + L2);
+            float carry = -FLT_MAX;
+            for (int c0 = b0; c0 < b1; c0 += 32) {
+                const int i = c0 + lane;
+                float v = i < b1 ? cf[i] : -FLT_MAX;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const float o = __shfl_up_sync(0xffffffffu, v, d);
+                    if (lane >= d) v = fmaxf(v, o);
+                }
+                v = fmaxf(v, carry);
+                if (i < b1) pg[i] = v;
+                carry = __shfl_sync(0xffffffffu, v, 31);
+            }
+            carry = -FLT_MAX;
+            for (int c1 = b1; c1 > b0; c1 -= 32) {
+                const int i = c1 - 32 + lane;
+                float v = i >= b0 ? cf[i] : -FLT_MAX;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const float o = __shfl_down_sync(0xffffffffu, v, d);
+                    if (lane + d < 32) v = fmaxf(v, o);
+                }
+                v = fmaxf(v, carry);
+                if (i >= b0) ph[i] = v;
+                carry = __shfl_sync(0xffffffffu, v, 0);
+            }
+        }
+        __syncthreads();
+        for (int w = tid; w < W; w += NTHR) {
+            const float c = cf[w + nt];
+            if (c > th2 && c == fmaxf(ph[w], pg[w + 2 * nt])) {
+                const int tt = wt[w];
+                const int q = atomicAdd(&s_cnt, 1);
+                if (q < cap_it) {
+                    s_aw[q] = w;
+                    s_at[q] = tt;
+                    s_aa[q] = wsc[w] / s_nm[tt];
+                } else {
+                    s_over = 1;
+                }
+            }
+        }
+        __syncthreads();
+        const int total = min(s_cnt, cap_it);
+        if (total == 0) break;
+        ++iters;
+        // ---- B2: rank by sample; the own samples each spike's items cover ----
+        for (int k = tid; k < total; k += NTHR) {
+            const int w = s_aw[k];
+            int r = 0;
+            for (int q = 0; q < total; ++q) r += s_aw[q] < w;
+            s_sw[r] = w;
+            s_st[r] = s_at[k];
+            s_sa[r] = s_aa[k];
+            const int o = n_total + r;
+            if (rank == 0 && o < out.cap) {
+                sp_w[o] = w;
+                sp_t[o] = s_at[k];
+                sp_amp[o] = s_aa[k];
+                sp_iter[o] = it;
+            }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            // spike k takes the samples [lo, hi) near it that no earlier spike took; its own ones
+            // are lo' = the first w >= lo with w = rank (mod G), then every G-th
+            int carry = 0;
+            for (int k0 = 0; k0 < total; k0 += 32) {
+                const int k = k0 + lane;
+                int cnt = 0, first = 0;
+                if (k < total) {
+                    const int sw = s_sw[k];
+                    const int lo = max(max(sw - nt, 0), k > 0 ? s_sw[k - 1] + nt + 1 : 0);
+                    const int hi = min(W, sw + nt + 1);
+                    first = lo + (((rank - lo) % G) + G) % G;
+                    cnt = first < hi ? (hi - 1 - first) / G + 1 : 0;
+                }
+                int inc = cnt;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int o = __shfl_up_sync(0xffffffffu, inc, d);
+                    if (lane >= d) inc += o;
+                }
+                if (k < total) {
+                    s_lo[k] = first;
+                    s_pre[k] = carry + inc - cnt;
+                }
+                carry += __shfl_sync(0xffffffffu, inc, 31);
+            }
+            if (lane == 0) {
+                s_pre[total] = carry;
+                s_cnt = 0;   // read again only after the barrier ending C
+            }
+        }
+        __syncthreads();
+        // ---- C: subtract the spikes from the listed scores of the own samples near them ----
+        const int n_items = s_pre[total];
+        constexpr int kPerWarp = kClItems * kGroups;
+        for (int q0 = warp * kPerWarp; q0 < n_items; q0 += kWarps * kPerWarp) {
+            int wv[kClItems], kv[kClItems], rv[kClItems], jv[kClItems];
+            float xv[kClItems], cv[kClItems], cv2[kClItems];
+            bool two[kClItems];
+#pragma unroll
+            for (int u = 0; u < kClItems; ++u) {
+                const int q = q0 + u * kGroups + grp;
+                int w = -1, k = 0;
+                if (q < n_items) {
+                    int lo_k = 0, hi_k = total - 1;   // the last spike with s_pre[k] <= q
+                    while (lo_k < hi_k) {
+                        const int mid = (lo_k + hi_k + 1) >> 1;
+                        if (s_pre[mid] <= q) lo_k = mid;
+                        else hi_k = mid - 1;
+                    }
+                    k = lo_k;
+                    w = s_lo[k] + G * (q - s_pre[k]);
+                }
+                wv[u] = w;
+                kv[u] = k;
+                jv[u] = w >= 0 ? (w - rank) / G : 0;
+                two[u] = w >= 0 && k + 1 < total && s_sw[k + 1] - nt <= w;
+                rv[u] = 0;
+                xv[u] = 0.f;
+                if (w >= 0 && gl < keep) {
+                    rv[u] = RK[(size_t)jv[u] * ks + gl];
+                    xv[u] = SC[(size_t)jv[u] * ks + gl];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kClItems; ++u) {
+                cv[u] = cv2[u] = 0.f;
+                if (wv[u] >= 0 && gl < keep) {
+                    const int k = kv[u];
+                    cv[u] = __ldg(ctcP + ((int64_t)s_st[k] * L2 + (wv[u] - s_sw[k] + nt)) * T + rv[u]);
+                    if (two[u]) cv2[u] = __ldg(ctcP + ((int64_t)s_st[k + 1] * L2 + (wv[u] - s_sw[k + 1] + nt)) * T + rv[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kClItems; ++u) {
+                const int w = wv[u];
+                if (!__any_sync(0xffffffffu, w >= 0)) continue;
+                float x = 0.f;
+                if (w >= 0) {
+                    const int k = kv[u];
+                    x = fmaf(-s_sa[k], cv[u], xv[u]);
+                    if (two[u]) {
+                        x = fmaf(-s_sa[k + 1], cv2[u], x);
+                        for (int kk = k + 2; kk < total && s_sw[kk] - nt <= w; ++kk) {   // rare: a third
+                            const float c = gl < keep
+                                                ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u])
+                                                : 0.f;
+                            x = fmaf(-s_sa[kk], c, x);
+                        }
+                    }
+                    if (gl < keep) SC[(size_t)jv[u] * ks + gl] = x;
+                }
+                finish_push(w, x, rv[u], w >= 0);
+            }
+        }
+        n_total += total;
+        cluster_sync_all<G>();   // every CTA holds every updated maximum before the next B1
+    }
+    if (rank == 0 && tid == 0) {
+        out.n_spikes[b] = n_total;
+        out.n_iters[b] = iters;
+        if (n_total > out.cap || s_over) atomicOr(out.status + b, 1);
+    }
+}
+
 static int g_prune_smem_max = -1;
 
 static int prune_smem_max() {
@@ -528,10 +847,52 @@ static cudaError_t launch_pruned_lps(const uint16_t* lrk, float* lsc, int keep, 
     return cudaGetLastError();
 }
 
+template <int G, int NTHR, int LPS>
+static cudaError_t launch_pruned_cluster(const uint16_t* lrk, const float* lsc, int keep, const float* ctcP,
+                                         const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
+                                         const MatchOut& out, cudaStream_t s) {
+    const size_t smem = prune_cl_smem(W, T, nt, keep, G);
+    auto kern = match_pruned_cluster_kernel<G, NTHR, LPS>;
+    cudaError_t e = raise_smem_limit((const void*)kern, smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nb * G));
+    cfg.blockDim = dim3(NTHR);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = G;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, out);
+}
+
+// the cluster form when a CTA's share fits in shared memory: 4 CTAs of 512 threads per window for
+// groups (one wave for 64 windows), 8 CTAs for a few windows (latency)
+static cudaError_t try_pruned_cluster(const uint16_t* lrk, const float* lsc, int keep, const float* ctcP,
+                                      const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
+                                      const MatchOut& out, cudaStream_t s, bool* done) {
+    *done = false;
+    const int G = nb <= 8 ? 8 : 4;
+    if (keep > 16 || W < 2 * G * nt || prune_cl_smem(W, T, nt, keep, G) + 1024 > (size_t)prune_smem_max())
+        return cudaSuccess;
+    *done = true;
+    if (G == 8) return launch_pruned_cluster<8, 512, 16>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+    return launch_pruned_cluster<4, 512, 16>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+}
+
 cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcP, const float* nm,
                                 float th2, int W, int T, int nt, int max_iters, int nb, float* cf_scratch,
                                 unsigned char* slot_scratch, const MatchOut& out, cudaStream_t s) {
     if (keep < 1 || keep > KP || keep > T || T > 1024) return cudaErrorInvalidValue;
+    {
+        bool done = false;
+        const cudaError_t e = try_pruned_cluster(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s, &done);
+        if (done || e != cudaSuccess) return e == cudaSuccess ? cudaGetLastError() : e;
+    }
     const int mode = prune_mode(W, T, nt, keep);
     if (mode < 0 || (!(mode & 1) && (!cf_scratch || !slot_scratch))) return cudaErrorInvalidValue;
     if (keep <= 8)
