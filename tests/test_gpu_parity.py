@@ -13,6 +13,7 @@ from lss_testutil import agreement, make_dataset, match_spikes, write_oss_from_a
 pytestmark = pytest.mark.gpu
 
 AGREE = 0.995
+ROOT_GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden"
 
 
 @pytest.fixture(scope="module")
@@ -227,11 +228,12 @@ def test_config_dense_overlapping(cfg_dense):
 
 def test_config_dense_full_size(tmp_path):
     """The full dense shape -- 384 channels, 1000 templates, one 60000-sample batch, 30 Hz with 30 %
-    overlaps (about 60,000 spikes) -- is beyond the float64 oracle's reach in a test; checked by
-    size-independent properties: the FP32 tensor-core path agrees with the FP32-SIMT path and with
-    the TF32-data and BF16-split tiers (>= 99.5 %, amplitudes within 1e-3), a second run is bitwise identical, and the spike count is in a plausible range
-    (the generator places about 60,000 spikes; with 30 % overlaps and 1000 templates about a third
-    are resolved)."""
+    overlaps (about 60,000 spikes placed).  Against the float64 oracle: its spikes on this seeded
+    window are a committed fixture (tests/golden/cfg3_full_oracle.npz, a 4.5-minute CPU run by
+    tests/golden/make_cfg3_golden.py), and the FP32 path and the BF16-split tier agree with them at
+    >= 99.5 % with amplitudes within 1e-3.  Beside it, size-independent properties: the FP32
+    tensor-core path agrees with the FP32-SIMT path and the TF32-data tier, and a second run is
+    bitwise identical."""
     cfg = synth.SynthConfig(n_chan=384, n_units=1000, n_samples=60000 + 122, rate_hz=30.0, overlap_frac=0.3,
                             whiten_batch=6000, whiten_batches=3, seed=23)
     d, data, _ = make_dataset(cfg, tmp_path)
@@ -249,6 +251,13 @@ def test_config_dense_full_size(tmp_path):
         assert a >= AGREE and amp_ok >= AGREE, (path, a, amp_ok, amax)
     for f in ("time", "tmpl", "amp", "pcfeat"):
         np.testing.assert_array_equal(again[f], outs[0][f])
+    import hashlib
+    z = np.load(ROOT_GOLDEN / "cfg3_full_oracle.npz")
+    same_input = hashlib.sha256(np.ascontiguousarray(win).tobytes()).hexdigest() == str(z["data_sha256"])
+    for path in (0, 3):
+        a, amp_ok, amax = agreement(z["time"], z["template"], z["amp"], outs[path]["time"], outs[path]["tmpl"],
+                                    outs[path]["amp"])
+        assert a >= AGREE and amp_ok >= AGREE, (path, a, amp_ok, amax, len(z["time"]), same_input)
 
 
 # ---------------------------------------------------------------- edge cases
