@@ -42,13 +42,13 @@ def main(n_batches: int = 6):
     oss = synth.build_oss_input(rec)
     NT, nt, C = 1500, cfg.nt, cfg.n_chan
     d_last = float(synth.drift_um_at(cfg, cfg.n_samples - 1))
-    xc, yc = rec.xc.astype(np.float64), rec.yc.astype(np.float64)
+    xc, yc = rec.xc.astype(np.float32), rec.yc.astype(np.float32)   # float32 probe: the drift matrix in float32
     ops = {"settings": {"nearest_chans": cfg.n_nearest, "n_pcs": cfg.n_pcs, "sig_interp": 20.0},
            "nt": nt, "nt0min": cfg.nt0min, "Th_learned": cfg.th_learned, "batch_size": NT,
            "wPCA": torch.from_numpy(oss.wPCA.astype(np.float32)), "xc": xc, "yc": yc,
            "probe": {"xc": xc, "yc": yc}, "nblocks": 1, "yblk": np.zeros(1)}
     xp = np.stack([xc, yc], 1)
-    Kxx = torch.from_numpy(synth.kernel2d(xp, xp, 20.0)).float()
+    Kxx = torch.from_numpy(synth.kernel2d(xp, xp, 20.0).astype(np.float32))
     ops["iKxx"] = torch.linalg.inv(Kxx + 0.01 * torch.eye(C))
     bfile = ks["io"].BinaryFiltered(None, C, fs=int(cfg.fs), NT=NT, nt=nt, nt0min=cfg.nt0min, chan_map=np.arange(C),
                                     hp_filter=torch.from_numpy(oss.hp_filter.astype(np.float32)),
@@ -77,6 +77,18 @@ def main(n_batches: int = 6):
         tp.append(time.perf_counter() - t0)
     print(f"numpy port (float32): median {1e3 * np.median(tp):.1f} ms per batch = "
           f"{NT * C / float(np.median(tp)) / 1e6:.2f} M ch*samples/s")
+    # the torch form of the port (bench.py's CPU baseline and reference arm)
+    from oracle import ks_torch
+    mt = ks_torch.Matcher(o)
+    tt = []
+    for j in range(0, n_batches + 1):
+        t0 = time.perf_counter()
+        X = ks_torch.preprocess(ko.padded_batch(rec.data, 1 + j % n_batches, NT, nt), o)
+        mt.run(X, max_iters=50)
+        tt.append(time.perf_counter() - t0)
+    tt = tt[1:]
+    print(f"torch port (float32, {torch.get_num_threads()} threads): median {1e3 * np.median(tt):.1f} ms per batch = "
+          f"{NT * C / float(np.median(tt)) / 1e6:.2f} M ch*samples/s")
 
 
 if __name__ == "__main__":
