@@ -833,6 +833,8 @@ CHOSEN_CANDIDATES = [
      "bf16 splits (hi*hi + hi*lo + lo*hi on kind::f16), fp32 accumulate, FP32 matching loop"),
     ("bf16x3_keep16", {"gemm_path": 3, "match_keep": 16},
      "bf16 splits, matching loop on each sample's 16 templates of largest initial score"),
+    ("bf16x3_keep24", {"gemm_path": 3, "match_keep": 24},
+     "bf16 splits, matching loop on each sample's 24 templates of largest initial score"),
     ("bf16x1_rescore", {"gemm_path": 4, "match_keep": 0},
      "one BF16 product (kind::f16), fp32 accumulate, accepted candidates re-scored in FP32"),
     ("fp8_rescore", {"gemm_path": 5, "match_keep": 0},

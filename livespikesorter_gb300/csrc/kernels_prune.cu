@@ -51,6 +51,9 @@ template <int NJ>
 __global__ void __launch_bounds__(kSelWarps * 32)
 prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, int nb, int W, int T, int keep,
                     uint16_t* __restrict__ lrk, float* __restrict__ lsc) {
+    __shared__ float s_inm[32 * NJ];
+    for (int t = threadIdx.x; t < T; t += kSelWarps * 32) s_inm[t] = 1.f / nm[t];   // as the loop computes it
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int64_t g = (int64_t)blockIdx.x * kSelWarps + (threadIdx.x >> 5);
     if (g >= (int64_t)nb * W) return;
@@ -60,8 +63,8 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
     for (int j = 0; j < NJ; ++j) {
         const int t = lane + 32 * j;
         if (t < T) {
-            const float r = fmaxf(row[t], 0.f);
-            key[j] = desc_key(r * r * (1.f / nm[t]));   // the loop's Cf, bit for bit
+            const float r = fmaxf(__ldcs(row + t), 0.f);
+            key[j] = desc_key(r * r * s_inm[t]);   // the loop's Cf, bit for bit
         } else {
             key[j] = 0xffffffffu;                         // after every real key (keep <= T)
         }
@@ -111,11 +114,7 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
         const unsigned m = __ballot_sync(0xffffffffu, take);
         // the taken entry with index lane - pos among this j's taken lanes goes to this lane
         const int want = lane - pos;
-        if (want >= 0 && want < __popc(m)) {
-            unsigned mm = m;   // clear the lowest want set bits
-            for (int q = 0; q < want; ++q) mm &= mm - 1u;
-            my_t = __ffs(mm) - 1 + 32 * j;
-        }
+        if (want >= 0 && want < __popc(m)) my_t = (int)__fns(m, 0u, want + 1) + 32 * j;   // its (want+1)-th set bit
         pos += __popc(m);
     }
     if (lane < keep) {
@@ -871,17 +870,22 @@ static cudaError_t launch_pruned_cluster(const uint16_t* lrk, const float* lsc, 
 }
 
 // the cluster form when a CTA's share fits in shared memory: 4 CTAs of 512 threads per window for
-// groups (one wave for 64 windows), 8 CTAs for a few windows (latency)
+// groups (one wave for 64 windows at up to 24 listed templates), 8 CTAs for a few windows
+// (latency); lane groups of 16 (keep <= 16) or 32
 static cudaError_t try_pruned_cluster(const uint16_t* lrk, const float* lsc, int keep, const float* ctcP,
                                       const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
                                       const MatchOut& out, cudaStream_t s, bool* done) {
     *done = false;
     const int G = nb <= 8 ? 8 : 4;
-    if (keep > 16 || W < 2 * G * nt || prune_cl_smem(W, T, nt, keep, G) + 1024 > (size_t)prune_smem_max())
-        return cudaSuccess;
+    if (W < 2 * G * nt || prune_cl_smem(W, T, nt, keep, G) + 1024 > (size_t)prune_smem_max()) return cudaSuccess;
     *done = true;
-    if (G == 8) return launch_pruned_cluster<8, 512, 16>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
-    return launch_pruned_cluster<4, 512, 16>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+    if (keep <= 16) {
+        if (G == 8)
+            return launch_pruned_cluster<8, 512, 16>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+        return launch_pruned_cluster<4, 512, 16>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+    }
+    if (G == 8) return launch_pruned_cluster<8, 512, 32>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+    return launch_pruned_cluster<4, 512, 32>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
 }
 
 cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcP, const float* nm,
