@@ -68,6 +68,8 @@ def args_():
     ap.add_argument("--cpu-sample", type=int, default=6, help="batches timed on the CPU oracle")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--match-variant", type=int, default=0, help="0 auto, 1 scores in L2, 2 scores in SMEM")
+    ap.add_argument("--match-keep", type=int, default=0,
+                    help="match_keep of the measured path (0 = Kilosort's loop over every template)")
     ap.add_argument("--gemm-path", type=int, default=0,
                     help="0 tcgen05 FP32 (3xTF32), 1 FP32 SIMT, 2 tcgen05 with TF32 data (two products)")
     ap.add_argument("--no-tier", action="store_true", help="skip the chosen-tier measurement")
@@ -342,7 +344,7 @@ def run_gpu(a):
     base_ptr = d_data.data_ptr()
     row_bytes = C * 2
     s = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1,
-                           match_variant=a.match_variant, gemm_path=a.gemm_path)
+                           match_variant=a.match_variant, gemm_path=a.gemm_path, match_keep=a.match_keep)
     ext = torch.cuda.ExternalStream(s.cuda_stream(), device=f"cuda:{dev}")
     spikes_seen = [0]
 
@@ -522,7 +524,7 @@ def run_gpu(a):
 
     # ---- end to end through the host API ---------------------------------------------------
     s2 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
-                             match_variant=a.match_variant, gemm_path=a.gemm_path)
+                             match_variant=a.match_variant, gemm_path=a.gemm_path, match_keep=a.match_keep)
     chunk = G * NT
     pos = [0]
     # the caller's rows live in pinned host memory (the e2e contract); the API copies page-locked
@@ -570,7 +572,7 @@ def run_gpu(a):
     s2.close()
 
     # ---- per-batch latency (one batch per launch) --------------------------------------------
-    latency = batch_latency(a.gemm_path, a.latency_batches)
+    latency = batch_latency(a.gemm_path, a.latency_batches, a.match_keep)
 
     # ---- the chosen path on eight concurrent probe streams (rank 0) ----------------------------
     chosen_block = None

@@ -42,36 +42,11 @@ __device__ __forceinline__ uint32_t desc_key(float f) {
     return ~((u & 0x80000000u) ? ~u : (u | 0x80000000u));
 }
 
-// One warp per sample: the keep templates of largest Cf (ties: lower id), written in ascending
-// order with their scores.  NJ = templates per lane (T <= 32 NJ); template t = lane + 32 j.
-// The keep-th largest Cf is found by an MSB-first bitwise selection over the warp's keys (one
-// ballot-count per bit, stopping once a single key matches the prefix); every key above it is
-// taken, then the ties at it in ascending template order until keep are taken.
+// The k-th smallest (0-based) of the warp's keys (n live ones; padding keys 0xffffffff), MSB first,
+// one ballot-count per bit, stopping once a single key matches the prefix.
 template <int NJ>
-__global__ void __launch_bounds__(kSelWarps * 32)
-prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, int nb, int W, int T, int keep,
-                    uint16_t* __restrict__ lrk, float* __restrict__ lsc) {
-    __shared__ float s_inm[32 * NJ];
-    for (int t = threadIdx.x; t < T; t += kSelWarps * 32) s_inm[t] = 1.f / nm[t];   // as the loop computes it
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int64_t g = (int64_t)blockIdx.x * kSelWarps + (threadIdx.x >> 5);
-    if (g >= (int64_t)nb * W) return;
-    const float* row = Bt + g * T;
-    uint32_t key[NJ];
-#pragma unroll
-    for (int j = 0; j < NJ; ++j) {
-        const int t = lane + 32 * j;
-        if (t < T) {
-            const float r = fmaxf(__ldcs(row + t), 0.f);
-            key[j] = desc_key(r * r * s_inm[t]);   // the loop's Cf, bit for bit
-        } else {
-            key[j] = 0xffffffffu;                         // after every real key (keep <= T)
-        }
-    }
-    // the (keep - 1)-th smallest key
+__device__ __forceinline__ uint32_t kth_key_bits(const uint32_t (&key)[NJ], int k, int alive) {
     uint32_t prefix = 0;
-    int k = keep - 1, alive = 32 * NJ;
     for (int bit = 31; bit >= 0; --bit) {
         const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
         int cnt = 0;
@@ -91,9 +66,81 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
 #pragma unroll
             for (int j = 0; j < NJ; ++j)
                 if ((key[j] & m) == prefix) got = key[j];
-            prefix = __reduce_or_sync(0xffffffffu, got);
-            break;
+            return __reduce_or_sync(0xffffffffu, got);
         }
+    }
+    return prefix;
+}
+
+// One warp per sample: the keep templates of largest Cf (ties: lower id), written in ascending
+// order with their scores.  NJ = templates per lane (T <= 32 NJ); template t = lane + 32 j.
+// The keep-th largest Cf is found by an MSB-first bitwise selection over the warp's keys (one
+// ballot-count per bit, stopping once a single key matches the prefix); every key above it is
+// taken, then the ties at it in ascending template order until keep are taken.
+template <int NJ>
+__global__ void __launch_bounds__(kSelWarps * 32)
+prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, int nb, int W, int T, int keep,
+                    uint16_t* __restrict__ lrk, float* __restrict__ lsc) {
+    __shared__ float s_inm[32 * NJ];
+    __shared__ uint32_t s_cand[kSelWarps * 64];
+    for (int t = threadIdx.x; t < T; t += kSelWarps * 32) s_inm[t] = 1.f / nm[t];   // as the loop computes it
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t g = (int64_t)blockIdx.x * kSelWarps + (threadIdx.x >> 5);
+    if (g >= (int64_t)nb * W) return;
+    const float* row = Bt + g * T;
+    uint32_t key[NJ];
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+        const int t = lane + 32 * j;
+        if (t < T) {
+            const float r = fmaxf(__ldcs(row + t), 0.f);
+            key[j] = desc_key(r * r * s_inm[t]);   // the loop's Cf, bit for bit
+        } else {
+            key[j] = 0xffffffffu;                         // after every real key (keep <= T)
+        }
+    }
+    // the (keep - 1)-th smallest key.  Every lane's smallest key: the keep-th smallest of those 32
+    // bounds it from above (keep lanes hold a key at or below it), so it is the (keep - 1)-th
+    // smallest of the keys at or below that bound -- usually a few dozen, which the bitwise
+    // selection then runs on (two per lane); otherwise it runs on all of them.
+    uint32_t lmin = key[0];
+#pragma unroll
+    for (int j = 1; j < NJ; ++j) lmin = min(lmin, key[j]);
+    uint32_t v = lmin;   // bitonic sort of the lane minima, ascending by lane
+#pragma unroll
+    for (int k2 = 2; k2 <= 32; k2 <<= 1)
+#pragma unroll
+        for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
+            const uint32_t o = __shfl_xor_sync(0xffffffffu, v, j2);
+            const bool up = ((lane & k2) == 0) == ((lane & j2) == 0);
+            v = up ? min(v, o) : max(v, o);
+        }
+    const uint32_t bound = __shfl_sync(0xffffffffu, v, keep - 1);
+    int n_cand = 0;
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) n_cand += key[j] <= bound;
+    n_cand = __reduce_add_sync(0xffffffffu, n_cand);
+    uint32_t prefix = 0;
+    if (n_cand <= 64) {
+        uint32_t* cand = s_cand + (threadIdx.x >> 5) * 64;
+        int base = 0;
+        const uint32_t lt0 = (1u << lane) - 1u;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const bool c = key[j] <= bound;
+            const unsigned m = __ballot_sync(0xffffffffu, c);
+            if (c) cand[base + __popc(m & lt0)] = key[j];
+            base += __popc(m);
+        }
+        __syncwarp();
+        uint32_t ck[2];
+        ck[0] = lane < n_cand ? cand[lane] : 0xffffffffu;
+        ck[1] = lane + 32 < n_cand ? cand[lane + 32] : 0xffffffffu;
+        __syncwarp();
+        prefix = kth_key_bits<2>(ck, keep - 1, n_cand);
+    } else {
+        prefix = kth_key_bits<NJ>(key, keep - 1, 32 * NJ);
     }
     const uint32_t thr = prefix;
     int below = 0;   // keys strictly before the threshold (larger Cf): all taken
