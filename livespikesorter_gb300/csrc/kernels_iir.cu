@@ -19,6 +19,7 @@
 // enters from the previous group, or is the steady state of the first row at a segment start), or
 // each window alone on the windows API.
 #include "lss_kernels.cuh"
+#include "lss_select.cuh"
 
 #include <cuda_bf16.h>
 
@@ -301,45 +302,6 @@ iir_scan_windows_kernel(const int16_t* __restrict__ raw, int64_t row_stride, con
     }
 }
 
-__device__ __forceinline__ uint32_t iir_key(float f) {
-    const uint32_t u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float iir_unkey(uint32_t k) {
-    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
-}
-
-// the k-th smallest of the warp's 32 * NJ keys (padding keys 0xffffffff), MSB first, one bit per
-// pass; once a single key is left matching the prefix, that key is the answer
-template <int NJ>
-__device__ __forceinline__ uint32_t iir_kth_key(const uint32_t (&key)[NJ], int kth) {
-    uint32_t prefix = 0;
-    int alive = 32 * NJ;
-    for (int bit = 31; bit >= 0; --bit) {
-        const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
-        int cnt = 0;
-#pragma unroll
-        for (int j = 0; j < NJ; ++j) cnt += ((key[j] & hi_mask) == prefix) && !((key[j] >> bit) & 1u);
-        cnt = __reduce_add_sync(0xffffffffu, cnt);
-        if (kth >= cnt) {
-            kth -= cnt;
-            prefix |= (1u << bit);
-            alive -= cnt;
-        } else {
-            alive = cnt;
-        }
-        if (alive == 1) {
-            const uint32_t m = 0xffffffffu << bit;
-            uint32_t got = 0;
-#pragma unroll
-            for (int j = 0; j < NJ; ++j)
-                if ((key[j] & m) == prefix) got = key[j];
-            return __reduce_or_sync(0xffffffffu, got);
-        }
-    }
-    return prefix;
-}
-
 constexpr int kIirApplyThreads = 256;
 
 // OUT: 0 = FP32, 1 = TF32 split (Y = tf32(y), Ylo = y - Y when Ylo is given), 2 = BF16 split (Y /
@@ -372,9 +334,9 @@ iir_apply_car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const 
         for (int j = 0; j < NJ; ++j) {
             const int c = lane + 32 * j;
             v[j] = c < C ? s_y[rr * ld + c] : 0.f;
-            key[j] = c < C ? iir_key(v[j]) : 0xffffffffu;
+            key[j] = c < C ? float_key(v[j]) : 0xffffffffu;
         }
-        const float med = iir_unkey(iir_kth_key<NJ>(key, (C - 1) >> 1));
+        const float med = key_float(warp_kth_smallest<NJ>(key, (C - 1) >> 1));
         const int r = cr.r0 + rr;
         // the windows holding row r: b with 0 <= r - b NT < W (one, on the windows API)
         int b_lo, b_hi;

@@ -3,6 +3,7 @@
 // circular zero-phase high-pass as an FIR in registers, and the temporal-basis convolution
 // (Kilosort template_matching.py:145, conv1d with padding nt//2).
 #include "lss_kernels.cuh"
+#include "lss_select.cuh"
 
 #include <cuda_bf16.h>
 
@@ -62,15 +63,6 @@ void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, 
 // ---------------------------------------------------------------------------------------
 // mean removal + lower median across channels (torch.median semantics), one warp per row
 // ---------------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t f2key(float f) {
-    uint32_t u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float key2f(uint32_t k) {
-    uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
-    return __uint_as_float(u);
-}
-
 // tf32 split of an fp32 value: hi = tf32(x) (round to nearest, ties away), lo = x - hi
 __device__ __forceinline__ void tf32_split_(float x, float& hi, float& lo) {
     uint32_t h;
@@ -80,39 +72,6 @@ __device__ __forceinline__ void tf32_split_(float x, float& hi, float& lo) {
 }
 
 constexpr int kCarWarps = 8;
-
-// The k-th smallest of the warp's 32 * NJ keys (all lanes hold NJ; padding keys are 0xffffffff),
-// MSB first, one bit per pass.  The count of keys still matching the prefix is tracked, and once
-// it is one that key is the answer: after about log2(32 * NJ) passes for distinct values instead
-// of 32.  Ties simply run to bit 0.
-template <int NJ>
-__device__ __forceinline__ uint32_t warp_kth_key(const uint32_t (&key)[NJ], int k) {
-    uint32_t prefix = 0;
-    int alive = 32 * NJ;
-    for (int bit = 31; bit >= 0; --bit) {
-        const uint32_t hi_mask = (bit == 31) ? 0u : (0xffffffffu << (bit + 1));
-        int cnt = 0;
-#pragma unroll
-        for (int j = 0; j < NJ; ++j) cnt += ((key[j] & hi_mask) == prefix) && !((key[j] >> bit) & 1u);
-        cnt = __reduce_add_sync(0xffffffffu, cnt);
-        if (k >= cnt) {
-            k -= cnt;
-            prefix |= (1u << bit);
-            alive -= cnt;
-        } else {
-            alive = cnt;
-        }
-        if (alive == 1) {
-            const uint32_t m = 0xffffffffu << bit;
-            uint32_t got = 0;
-#pragma unroll
-            for (int j = 0; j < NJ; ++j)
-                if ((key[j] & m) == prefix) got = key[j];
-            return __reduce_or_sync(0xffffffffu, got);
-        }
-    }
-    return prefix;
-}
 
 // NJ = channels per lane (C <= 32 * NJ), so the selection loop runs over live registers only
 template <int NJ>
@@ -134,14 +93,13 @@ car_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t* _
         if (j < nj && c < C) {
             const float x = (float)raw[rowp + (chan ? chan[c] : c)] - mean[(int64_t)b * C + c];
             v[j] = x;
-            key[j] = f2key(x);
+            key[j] = float_key(x);
         } else {
             v[j] = 0.f;
             key[j] = 0xffffffffu;   // sorts after every real value, never selected (k < C)
         }
     }
-    // k-th smallest by MSB-first bit selection over order-preserving keys
-    const float med = key2f(warp_kth_key<kMaxChanPerLane>(key, (C - 1) >> 1));
+    const float med = key_float(warp_kth_smallest<kMaxChanPerLane>(key, (C - 1) >> 1));
     const int rows = W + L + R;
     float* xb = Xw + (int64_t)b * rows * C;
     const bool wrapL = (w >= W - L);   // also lands in the left pad
@@ -188,13 +146,13 @@ car_t_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t*
             if (c < C) {
                 const float x = (float)raw[rowp + (chan ? chan[c] : c)] - mean[(int64_t)b * C + c];
                 v[j] = x;
-                key[j] = f2key(x);
+                key[j] = float_key(x);
             } else {
                 v[j] = 0.f;
                 key[j] = 0xffffffffu;
             }
         }
-        const float med = key2f(warp_kth_key<NJ>(key, (C - 1) >> 1));
+        const float med = key_float(warp_kth_smallest<NJ>(key, (C - 1) >> 1));
 #pragma unroll
         for (int j = 0; j < NJ; ++j) {
             const int c = lane + 32 * j;

@@ -8,13 +8,15 @@
 // tier stores the data operand A once as tf32(x) and accumulates hi*hi + hi*lo (the fixed B keeps
 // its split), an error of about 2^-12 of |x*y| per product.
 //
-// One CTA (4 warps) computes a 128 x N tile: warp 0 / lane 0 streams A and B tiles into shared
-// memory with TMA (cp.async.bulk.tensor, 64-byte swizzle) through a 4-stage mbarrier pipeline;
-// warp 1 / lane 0 issues tcgen05.mma.kind::tf32 (M = 128, N = 128 or 256, K = 8) into an N-column
-// TMEM accumulator and releases each stage with tcgen05.commit; all four warps then read the
-// accumulator back with tcgen05.ld (each warp its 32 TMEM lanes = tile rows) and store it.
+// Persistent, warp-specialised CTAs (one per SM) walk the 128 x N output tiles: warp E / lane 0
+// streams A and B tiles into shared memory with TMA (cp.async.bulk.tensor, 64-byte swizzle)
+// through one mbarrier ring of stages that runs on across tiles; warp E + 1 / lane 0 issues
+// tcgen05.mma (M = 128, N = 128 or 256) into one of two N-column TMEM accumulators, releasing each
+// stage with tcgen05.commit; the E = kGemmEpiWarps warps read the other accumulator back with
+// tcgen05.ld (warp e its 32 TMEM lanes 32 (e % 4) .. = tile rows, every (E / 4)-th chunk of 32
+// columns) and store it while the next tile accumulates, then hand it back through an mbarrier.
 // Every wait is bounded (globaltimer); on a timeout the kernel sets an error word, waits (bounded)
-// for the copies it issued, frees its TMEM and returns.
+// for the copies it issued and the MMAs it started, frees its TMEM and returns.
 #include "lss_kernels.cuh"
 
 #include <cuda.h>
@@ -30,6 +32,8 @@ constexpr int kBM = 128, kBK = 16;
 constexpr int kTileA = kBM * kBK * 4;                   // 8 KB
 constexpr int kSmemBudget = 196 * 1024;                 // stage buffers per CTA
 constexpr uint64_t kWaitNs = 2000000000ull;             // 2 s
+constexpr int kGemmEpiWarps = 8;                        // a multiple of 4
+constexpr int kGemmThreads = (kGemmEpiWarps + 2) * 32;
 
 // Two uses of one kernel:
 //   kPlain     C[m][n] = sum_k A[m][k] B[n][k]; tile N = 256; B rows = n
@@ -53,6 +57,7 @@ struct UmmaArgs {
     int zpitch;
     int zt_bf16;      // zt as its BF16 split (bf16 arrays)
     const float* col_scale;   // kPlain, optional: C[m][n] *= col_scale[n] (the FP8 operands' scales)
+    int slices;       // kPlain: K split this many ways, slice z written to C + z M ldc (1: no split)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -65,6 +70,9 @@ __device__ __forceinline__ uint64_t gtimer() {
 }
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
@@ -163,29 +171,39 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 // (kind::f8f6f4, a K-step of 64 elements); only hi tiles are loaded, so a stage is half the bytes
 // and twice the stages fit.  The epilogue then scales column n by args.col_scale[n] when given.
 template <int BN, int MODE, bool ALO, bool BF16 = false, int LOWP = 0>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kGemmThreads, 1)
 umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
                  const __grid_constant__ CUtensorMap tB_hi, const __grid_constant__ CUtensorMap tB_lo, UmmaArgs args) {
     constexpr int kBN = BN;
+    constexpr int kTmemCols = 2 * kBN;   // two accumulators (256 or 512 columns, a power of two)
     constexpr int kKE = LOWP == 2 ? 4 * kBK : (BF16 ? 2 * kBK : kBK);   // elements per K-step (64 bytes of each row)
     constexpr int kTileB = kBN * kBK * 4;
     constexpr int kStageBytes = LOWP ? kTileA + kTileB : 2 * kTileA + 2 * kTileB;
     constexpr int kLoadBytes = LOWP ? kStageBytes : (ALO ? kStageBytes : kTileA + 2 * kTileB);   // bytes the TMA lands per stage
     constexpr int kStages = kSmemBudget / kStageBytes;
-    const int M = args.M, N = args.N, K = args.K;
+    const int M = args.M, N = args.N, K = args.K, S = args.slices;
     int* err = args.err;
     extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
+    __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], tfull_bar[2], tempty_bar[2], drain_bar;
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_raw;
     volatile int& abort_s = abort_raw;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n0 = blockIdx.x * kBN, m0 = blockIdx.y * kBM;
     const int nk = K / kKE;
-    // split K (plain mode, gridDim.z > 1): this CTA multiplies K-steps [kt0, kt0 + nkl) and writes its
-    // partial tile to output slice blockIdx.z (the caller sums the slices)
-    const int kt0 = (int)((int64_t)nk * blockIdx.z / gridDim.z);
-    const int nkl = (int)((int64_t)nk * (blockIdx.z + 1) / gridDim.z) - kt0;
+    const int tiles_n = (N + kBN - 1) / kBN, tiles_m = (M + kBM - 1) / kBM;
+    const int ntiles = tiles_n * tiles_m * S;
+    // tile t: output columns n0 = (t % tiles_n) kBN, rows m0 = ((t / tiles_n) % tiles_m) kBM, K slice
+    // z = t / (tiles_n tiles_m) -- the column tiles of one row block run on neighbouring CTAs and
+    // share its A tiles through L2.  Split K (S > 1, plain mode): slice z multiplies the K-steps
+    // [nk z / S, nk (z + 1) / S) and writes its partial tile to output slice z (the caller sums them).
+    auto tile_of = [&](int t, int& n0, int& m0, int& kt0, int& nkl) {
+        const int z = t / (tiles_n * tiles_m), r = t - z * tiles_n * tiles_m;
+        n0 = (r % tiles_n) * kBN;
+        m0 = (r / tiles_n) * kBM;
+        kt0 = (int)((int64_t)nk * z / S);
+        nkl = (int)((int64_t)nk * (z + 1) / S) - kt0;
+        return z;
+    };
     // 1024-byte aligned stage buffers: [A_hi][A_lo][B_hi][B_lo] per stage
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
     // (LOWP: [A_hi][B_hi] per stage)
@@ -199,13 +217,17 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
             mbar_init(smem_u32(&full_bar[s]), 1);
             mbar_init(smem_u32(&empty_bar[s]), 1);
         }
-        mbar_init(smem_u32(&done_bar), 1);
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(smem_u32(&tfull_bar[a]), 1);
+            mbar_init(smem_u32(&tempty_bar[a]), kGemmEpiWarps);   // one arrival per epilogue warp
+        }
+        mbar_init(smem_u32(&drain_bar), 1);
         abort_s = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
-                     "r"(kBN)
+                     "r"(kTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -214,157 +236,202 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_s;
 
-    if (warp == 0 && lane == 0) {
-        // ---- producer: TMA ----
-        int issued = 0;
-        for (int kt = 0; kt < nkl; ++kt) {
-            const int s = kt % kStages;
-            const uint32_t round = (uint32_t)(kt / kStages);
-            if (!mbar_wait(smem_u32(&empty_bar[s]), (round & 1u) ^ 1u) || abort_s) {
-                atomicOr(err, 1);
-                abort_s = 1;
-                break;
+    if (warp == kGemmEpiWarps && lane == 0) {
+        // ---- producer: TMA, one ring of stages across all tiles of this CTA ----
+        int q = 0;
+        bool stop = false;
+        for (int tile = blockIdx.x; tile < ntiles && !stop; tile += gridDim.x) {
+            int n0, m0, kt0, nkl;
+            tile_of(tile, n0, m0, kt0, nkl);
+            for (int kt = 0; kt < nkl; ++kt, ++q) {
+                const int s = q % kStages;
+                const uint32_t round = (uint32_t)(q / kStages);
+                if (!mbar_wait(smem_u32(&empty_bar[s]), (round & 1u) ^ 1u) || abort_s) {
+                    atomicOr(err, 1);
+                    abort_s = 1;
+                    stop = true;
+                    break;
+                }
+                const uint32_t fb = smem_u32(&full_bar[s]);
+                mbar_expect_tx(fb, kLoadBytes);
+                const int k0 = (kt0 + kt) * kKE;   // a multiple of 64 bytes
+                // Toeplitz: A columns start at the tile's output time n0 (a multiple of 128), B is the
+                // same band matrix for every tile
+                const int ax = (MODE == kToeplitz) ? n0 + k0 : k0;
+                const int by = (MODE == kToeplitz) ? 0 : n0;
+                tma_load_2d(sA_hi(s), &tA_hi, fb, ax, m0);
+                if constexpr (ALO && !LOWP) tma_load_2d(sA_lo(s), &tA_lo, fb, ax, m0);
+                tma_load_2d(sB_hi(s), &tB_hi, fb, k0, by);
+                if constexpr (!LOWP) tma_load_2d(sB_lo(s), &tB_lo, fb, k0, by);
             }
-            const uint32_t fb = smem_u32(&full_bar[s]);
-            mbar_expect_tx(fb, kLoadBytes);
-            const int k0 = (kt0 + kt) * kKE;   // a multiple of 64 bytes
-            // Toeplitz: A columns start at the tile's output time n0 (a multiple of 128), B is the
-            // same band matrix for every tile
-            const int ax = (MODE == kToeplitz) ? n0 + k0 : k0;
-            const int by = (MODE == kToeplitz) ? 0 : n0;
-            tma_load_2d(sA_hi(s), &tA_hi, fb, ax, m0);
-            if constexpr (ALO && !LOWP) tma_load_2d(sA_lo(s), &tA_lo, fb, ax, m0);
-            tma_load_2d(sB_hi(s), &tB_hi, fb, k0, by);
-            if constexpr (!LOWP) tma_load_2d(sB_lo(s), &tB_lo, fb, k0, by);
-            ++issued;
         }
         // the copies of the last rounds must have landed before the CTA may exit
-        for (int kt = (issued > kStages ? issued - kStages : 0); kt < issued; ++kt)
+        for (int kt = (q > kStages ? q - kStages : 0); kt < q; ++kt)
             if (!mbar_wait(smem_u32(&full_bar[kt % kStages]), (uint32_t)(kt / kStages) & 1u)) atomicOr(err, 4);
-    } else if (warp == 1 && lane == 0) {
-        // ---- MMA issuer ----
-        for (int kt = 0; kt < nkl; ++kt) {
-            const int s = kt % kStages;
-            const uint32_t round = (uint32_t)(kt / kStages);
-            if (!mbar_wait(smem_u32(&full_bar[s]), round & 1u) || abort_s) {
+    } else if (warp == kGemmEpiWarps + 1 && lane == 0) {
+        // ---- MMA issuer: tile i accumulates into TMEM columns (i % 2) kBN ----
+        int q = 0, i = 0;
+        for (int tile = blockIdx.x; tile < ntiles && !abort_s; tile += gridDim.x, ++i) {
+            const int ab = i & 1;
+            if (!mbar_wait(smem_u32(&tempty_bar[ab]), ((uint32_t)(i >> 1) & 1u) ^ 1u) || abort_s) {
                 atomicOr(err, 2);
                 abort_s = 1;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t d = tmem + (uint32_t)(ab * kBN);
+            int n0, m0, kt0, nkl;
+            tile_of(tile, n0, m0, kt0, nkl);
+            bool stop = false;
+            for (int kt = 0; kt < nkl; ++kt, ++q) {
+                const int s = q % kStages;
+                const uint32_t round = (uint32_t)(q / kStages);
+                if (!mbar_wait(smem_u32(&full_bar[s]), round & 1u) || abort_s) {
+                    atomicOr(err, 2);
+                    abort_s = 1;
+                    stop = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-            for (int kk = 0; kk < 2; ++kk) {          // 32 bytes (8 tf32 / 16 bf16) per MMA
-                const uint32_t off = (uint32_t)kk * 32u;
-                const uint64_t ah = smem_desc(sA_hi(s) + off), al = smem_desc(sA_lo(s) + off);
-                const uint64_t bh = smem_desc(sB_hi(s) + off), bl = smem_desc(sB_lo(s) + off);
-                if constexpr (LOWP == 1) {
-                    mma_bf16<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
-                } else if constexpr (LOWP == 2) {
-                    mma_e4m3<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
-                } else if constexpr (BF16) {
-                    mma_bf16<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
-                    mma_bf16<BN>(tmem, ah, bl, 1u);
-                    if constexpr (ALO) mma_bf16<BN>(tmem, al, bh, 1u);
-                } else {
-                    mma_tf32<BN>(tmem, ah, bh, (kt > 0 || kk > 0) ? 1u : 0u);
-                    mma_tf32<BN>(tmem, ah, bl, 1u);
-                    if constexpr (ALO) mma_tf32<BN>(tmem, al, bh, 1u);
+                for (int kk = 0; kk < 2; ++kk) {          // 32 bytes (8 tf32 / 16 bf16 / 32 e4m3) per MMA
+                    const uint32_t off = (uint32_t)kk * 32u;
+                    const uint64_t ah = smem_desc(sA_hi(s) + off), al = smem_desc(sA_lo(s) + off);
+                    const uint64_t bh = smem_desc(sB_hi(s) + off), bl = smem_desc(sB_lo(s) + off);
+                    const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+                    if constexpr (LOWP == 1) {
+                        mma_bf16<BN>(d, ah, bh, acc);
+                    } else if constexpr (LOWP == 2) {
+                        mma_e4m3<BN>(d, ah, bh, acc);
+                    } else if constexpr (BF16) {
+                        mma_bf16<BN>(d, ah, bh, acc);
+                        mma_bf16<BN>(d, ah, bl, 1u);
+                        if constexpr (ALO) mma_bf16<BN>(d, al, bh, 1u);
+                    } else {
+                        mma_tf32<BN>(d, ah, bh, acc);
+                        mma_tf32<BN>(d, ah, bl, 1u);
+                        if constexpr (ALO) mma_tf32<BN>(d, al, bh, 1u);
+                    }
+                }
+                mma_commit(smem_u32(&empty_bar[s]));        // frees the stage once these MMAs finish
+            }
+            if (stop) break;
+            mma_commit(smem_u32(&tfull_bar[ab]));           // the accumulator is complete
+        }
+        // every MMA issued has finished before the TMEM is released
+        mma_commit(smem_u32(&drain_bar));
+        if (!mbar_wait(smem_u32(&drain_bar), 0u)) atomicOr(err, 2);
+    } else if (warp < kGemmEpiWarps) {
+        // ---- epilogue: TMEM -> registers -> global, overlapping the next tile's MMAs ----
+        // warp e reads TMEM lanes 32 (e % 4) .. + 31 (its tile rows), column chunks e / 4, e / 4 +
+        // kGemmEpiWarps / 4, ... of 32
+        const int quad = warp & 3;
+        int i = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+            const int ab = i & 1;
+            // one decision per warp: the tcgen05.ld below is .sync.aligned
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[ab]), (uint32_t)(i >> 1) & 1u) && !abort_s);
+            if (!ok) {
+                if (lane == 0) atomicOr(err, 8);
+                abort_s = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            int n0, m0, kt0, nkl;
+            const int z = tile_of(tile, n0, m0, kt0, nkl);
+            const int row = m0 + quad * 32 + lane;
+            for (int c0 = 32 * (warp >> 2); c0 < kBN && n0 + c0 < N; c0 += 32 * (kGemmEpiWarps / 4)) {
+                uint32_t r[32];
+                const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(ab * kBN + c0);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+                    "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                      "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                      "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if constexpr (MODE == kToeplitz) {
+                    // row = (b, c); column j = output time n0 + c0 + j; lanes = consecutive channels
+                    if (row < M) {
+                        const int b = row / args.chans, c = row - b * args.chans;
+                        for (int j = 0; j < 32; ++j) {
+                            const int w = n0 + c0 + j;
+                            if (w < args.wlen) {
+                                const float v = __uint_as_float(r[j]);
+                                const int64_t o = ((int64_t)b * args.wlen + w) * args.chans + c;
+                                if constexpr (BF16) {
+                                    // the BF16 split, for the next GEMM on the BF16 tier
+                                    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                                    reinterpret_cast<__nv_bfloat16*>(args.out)[o] = h;
+                                    reinterpret_cast<__nv_bfloat16*>(args.out_lo)[o] =
+                                        __float2bfloat16_rn(v - __bfloat162float(h));
+                                } else {
+                                    uint32_t h;
+                                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+                                    args.out[o] = __uint_as_float(h);
+                                    if (args.out_lo) args.out_lo[o] = v - __uint_as_float(h);
+                                }
+                            }
+                        }
+                    }
+                    continue;
+                }
+                if (row < M) {
+                    float* crow = args.out + ((int64_t)z * M + row) * args.ldc + n0 + c0;
+                    const int ncol = min(32, N - (n0 + c0));
+                    if (args.col_scale) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (j < ncol) r[j] = __float_as_uint(__uint_as_float(r[j]) * __ldg(args.col_scale + n0 + c0 + j));
+                    }
+                    if (args.zt_hi) {
+                        // lanes hold consecutive rows = consecutive times of one channel row of zt
+                        const int b = row / args.wlen, w = row - b * args.wlen;
+                        const int64_t o = ((int64_t)b * N + n0 + c0) * args.zpitch + w;
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            if (j < ncol) {
+                                const float v = __uint_as_float(r[j]);
+                                const int64_t oj = o + (int64_t)j * args.zpitch;
+                                if (args.zt_bf16) {
+                                    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                                    reinterpret_cast<__nv_bfloat16*>(args.zt_hi)[oj] = h;
+                                    reinterpret_cast<__nv_bfloat16*>(args.zt_lo)[oj] =
+                                        __float2bfloat16_rn(v - __bfloat162float(h));
+                                } else {
+                                    uint32_t h;
+                                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+                                    args.zt_hi[oj] = __uint_as_float(h);
+                                    if (args.zt_lo) args.zt_lo[oj] = v - __uint_as_float(h);
+                                }
+                            }
+                        }
+                    }
+                    if (ncol == 32 && ((((uintptr_t)crow) & 15) == 0)) {
+#pragma unroll
+                        for (int j = 0; j < 32; j += 4)
+                            *reinterpret_cast<float4*>(crow + j) = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
+                                                                               __uint_as_float(r[j + 2]), __uint_as_float(r[j + 3]));
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (j < ncol) crow[j] = __uint_as_float(r[j]);
+                    }
                 }
             }
-            mma_commit(smem_u32(&empty_bar[s]));        // frees the stage once these MMAs finish
+            // the accumulator may be overwritten once every epilogue warp has read it
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&tempty_bar[ab]));
         }
-        mma_commit(smem_u32(&done_bar));
     }
     __syncwarp();
-
-    // ---- epilogue: TMEM -> registers -> global ----
-    const bool ok = mbar_wait(smem_u32(&done_bar), 0u) && !abort_s;
-    if (!ok && threadIdx.x == 0) atomicOr(err, 8);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int row = m0 + warp * 32 + lane;
-    for (int c0 = 0; c0 < kBN; c0 += 32) {
-        uint32_t r[32];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-            "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if constexpr (MODE == kToeplitz) {
-            // row = (b, c); column j = output time n0 + c0 + j; lanes = consecutive channels
-            if (ok && row < M) {
-                const int b = row / args.chans, c = row - b * args.chans;
-                for (int j = 0; j < 32; ++j) {
-                    const int w = n0 + c0 + j;
-                    if (w < args.wlen) {
-                        const float v = __uint_as_float(r[j]);
-                        const int64_t o = ((int64_t)b * args.wlen + w) * args.chans + c;
-                        if constexpr (BF16) {
-                            // the BF16 split, for the next GEMM on the BF16 tier
-                            const __nv_bfloat16 h = __float2bfloat16_rn(v);
-                            reinterpret_cast<__nv_bfloat16*>(args.out)[o] = h;
-                            reinterpret_cast<__nv_bfloat16*>(args.out_lo)[o] = __float2bfloat16_rn(v - __bfloat162float(h));
-                        } else {
-                            uint32_t h;
-                            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-                            args.out[o] = __uint_as_float(h);
-                            if (args.out_lo) args.out_lo[o] = v - __uint_as_float(h);
-                        }
-                    }
-                }
-            }
-            continue;
-        }
-        if (ok && row < M) {
-            float* crow = args.out + ((int64_t)blockIdx.z * M + row) * args.ldc + n0 + c0;
-            const int ncol = min(32, N - (n0 + c0));
-            if (args.col_scale) {
-#pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (j < ncol) r[j] = __float_as_uint(__uint_as_float(r[j]) * __ldg(args.col_scale + n0 + c0 + j));
-            }
-            if (args.zt_hi) {
-                // lanes hold consecutive rows = consecutive times of one channel row of zt
-                const int b = row / args.wlen, w = row - b * args.wlen;
-                const int64_t o = ((int64_t)b * N + n0 + c0) * args.zpitch + w;
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    if (j < ncol) {
-                        const float v = __uint_as_float(r[j]);
-                        const int64_t oj = o + (int64_t)j * args.zpitch;
-                        if (args.zt_bf16) {
-                            const __nv_bfloat16 h = __float2bfloat16_rn(v);
-                            reinterpret_cast<__nv_bfloat16*>(args.zt_hi)[oj] = h;
-                            reinterpret_cast<__nv_bfloat16*>(args.zt_lo)[oj] = __float2bfloat16_rn(v - __bfloat162float(h));
-                        } else {
-                            uint32_t h;
-                            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-                            args.zt_hi[oj] = __uint_as_float(h);
-                            if (args.zt_lo) args.zt_lo[oj] = v - __uint_as_float(h);
-                        }
-                    }
-                }
-            }
-            if (ncol == 32 && ((((uintptr_t)crow) & 15) == 0)) {
-#pragma unroll
-                for (int j = 0; j < 32; j += 4)
-                    *reinterpret_cast<float4*>(crow + j) = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
-                                                                       __uint_as_float(r[j + 2]), __uint_as_float(r[j + 3]));
-            } else {
-#pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (j < ncol) crow[j] = __uint_as_float(r[j]);
-            }
-        }
-    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kBN) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
 // hi = tf32(x) (round to nearest, ties away), lo = x - hi (exact in fp32)
@@ -420,10 +487,6 @@ struct ConvArgs {
     int out_bf16;   // store the BF16 split (two bf16 arrays) instead of fp32 / tf32
     int* err;
 };
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
 
 template <bool ALO, bool BF16>
 __global__ void __launch_bounds__(kConvThreads, 1)
@@ -838,6 +901,17 @@ UmmaOperands* umma_make_toeplitz(const float* x_hi, const float* x_lo, int64_t r
 
 void umma_free(UmmaOperands* u) { delete u; }
 
+// persistent GEMM grid: one CTA per SM (each holds 2 x BN TMEM columns and most of the shared
+// memory), fewer when there are fewer tiles
+static cudaError_t gemm_grid(int64_t ntiles, int& grid) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, std::max(sms, 1)));
+    return cudaSuccess;
+}
+
 cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, int* err, cudaStream_t s) {
     return launch_umma_gemm_zt(u, Cm, M, N, ldc, nullptr, nullptr, 1, 0, err, s);
 }
@@ -867,8 +941,11 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
     a.zpitch = zpitch;
     a.zt_bf16 = zt_bf16 ? 1 : 0;
     a.col_scale = u->col_scale;
-    dim3 grid((N + kPlainBN - 1) / kPlainBN, (M + kBM - 1) / kBM);
-    kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
+    a.slices = 1;
+    int grid = 0;
+    const cudaError_t ge = gemm_grid((int64_t)((N + kPlainBN - 1) / kPlainBN) * ((M + kBM - 1) / kBM), grid);
+    if (ge != cudaSuccess) return ge;
+    kern<<<grid, kGemmThreads, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     return cudaGetLastError();
 }
 
@@ -908,8 +985,11 @@ cudaError_t launch_umma_gemm_splitk(const UmmaOperands* u, float* Cm, int M, int
     a.err = err;
     a.wlen = 1;
     a.col_scale = u->col_scale;   // the slices are scaled before they are summed: sum(s x) = s sum(x) up to rounding
-    dim3 grid((N + kPlainBN - 1) / kPlainBN, (M + kBM - 1) / kBM, S);
-    kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
+    a.slices = S;
+    int grid = 0;
+    const cudaError_t ge = gemm_grid((int64_t)((N + kPlainBN - 1) / kPlainBN) * ((M + kBM - 1) / kBM) * S, grid);
+    if (ge != cudaSuccess) return ge;
+    kern<<<grid, kGemmThreads, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     const int blocks = (int)std::min<int64_t>(((int64_t)M * N + 255) / 256, 2048);
     sum_slices_kernel<<<blocks, 256, 0, s>>>(ws, Cm, M, N, ldc, S);
     return cudaGetLastError();
@@ -934,8 +1014,11 @@ static cudaError_t launch_highpass_tile(const UmmaOperands* u, float* Y_hi, floa
     a.chans = C;
     a.wlen = W;
     a.err = err;
-    dim3 grid((W + TILE - 1) / TILE, (nb * C + kBM - 1) / kBM);
-    kern<<<grid, 128, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
+    a.slices = 1;
+    int grid = 0;
+    const cudaError_t ge = gemm_grid((int64_t)((W + TILE - 1) / TILE) * ((nb * C + kBM - 1) / kBM), grid);
+    if (ge != cudaSuccess) return ge;
+    kern<<<grid, kGemmThreads, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     return cudaGetLastError();
 }
 

@@ -1,14 +1,18 @@
 """Reduced-precision and pruned variants of the matching loop -- TEST INFRASTRUCTURE ONLY.
 
-The checker and the study harness of precision tiers that the product does not have yet (an FP8
-projection, a pruned loop); nothing in the product calls this module.  Kilosort's loop
+The checker and the study harness of the product's precision tiers (the BF16 and FP8 projections
+with an exact re-score at acceptance, the pruned loop); nothing in the product calls this module.  Kilosort's loop
 (KS/template_matching.py:141-202, restated in ``ks_oracle.run_matching``) scores every template at
 every sample from an exact projection.  Here:
 
 * ``project_rounded``: the projection B = Wall3 . Bpc with both operands rounded to e4m3 / e5m2 /
   bf16 (round to nearest even, per-template scales on Wall3 and per-(component, channel) scales on
   Bpc, each the row's largest magnitude over the format's largest finite value), accumulated
-  exactly;
+  exactly.  Those activation scales see the whole window (dynamic, non-causal); with ``act_scale``
+  they are static instead, as the FP8 kernel runs them: per-(component, channel) scales fixed once
+  from a calibration window (``calibrate_act_scale``: twice the row's largest magnitude over the
+  format's largest finite value) and folded into the template operand, whose per-template scale
+  is then taken after the fold; values beyond the calibrated range saturate;
 * ``run_matching_variant``: Kilosort's loop on such scores, optionally re-scoring every accepted
   candidate exactly (exact initial score minus rounded initial score added to the running score;
   candidates whose exact score misses the threshold are dropped from then on), or restricted to
@@ -52,28 +56,43 @@ def operands(X, U, W):
     return np.asarray(U, np.float64).reshape(T, K * C), Bpc2
 
 
-def project_rounded(U2, Bpc2, fmt: str):
+def calibrate_act_scale(Bpc2, fmt: str = "e4m3"):
+    """Static per-(component, channel) activation scales [K*C, 1] from one calibration window's
+    Bpc2: twice each row's largest magnitude over the format's largest finite value (1 for an
+    all-zero row), so held-out values up to twice as large fit before saturating."""
+    m = np.abs(np.asarray(Bpc2, np.float64)).max(1, keepdims=True)
+    return np.where(m > 0, 2.0 * m / MAX_FINITE[fmt], 1.0)
+
+
+def project_rounded(U2, Bpc2, fmt: str, act_scale=None):
     if fmt == "exact":
         return U2 @ Bpc2
     if fmt == "bf16":
         return round_bf16(U2) @ round_bf16(Bpc2)
     m = MAX_FINITE[fmt]
+    if act_scale is not None:
+        s = np.asarray(act_scale, np.float64).reshape(-1, 1)
+        Uf = U2 * s.T                                            # the scale folded into the templates
+        r = np.maximum(np.abs(Uf).max(1, keepdims=True), 1e-300) / m
+        return (r * round_fp8(Uf / r, fmt)) @ round_fp8(Bpc2 / s, fmt)
     r = np.maximum(np.abs(U2).max(1, keepdims=True), 1e-300) / m
     s = np.maximum(np.abs(Bpc2).max(1, keepdims=True), 1e-300) / m
     return (r * (round_fp8(U2 / r, fmt) * s.T)) @ round_fp8(Bpc2 / s, fmt)
 
 
-def run_matching_variant(X, U, W, ctc, Th, fmt="exact", rescore=False, keep=None, max_iters=50, block=1):
+def run_matching_variant(X, U, W, ctc, Th, fmt="exact", rescore=False, keep=None, max_iters=50, block=1,
+                         act_scale=None):
     """-> (st [S, 2] (sample, template), amps [S]).  See the module docstring.  block > 1: one list
     per block of that many consecutive samples (from sample 0), the keep templates of largest Cq
-    maximum over the block's samples, scored at every sample of the block."""
+    maximum over the block's samples, scored at every sample of the block.  act_scale: static
+    activation scales (``calibrate_act_scale``) for an FP8 format."""
     U = np.asarray(U, np.float64)
     ctc = np.asarray(ctc, np.float64)
     nt = W.shape[1]
     nm = (U ** 2).sum(-1).sum(-1)
     U2, Bpc2 = operands(X, U, W)
     B0e = U2 @ Bpc2
-    B0q = project_rounded(U2, Bpc2, fmt)
+    B0q = project_rounded(U2, Bpc2, fmt, act_scale)
     if keep is not None:
         Cq = np.maximum(B0q, 0) ** 2 / nm[:, None]
         mask = np.zeros(B0e.shape, bool)
@@ -117,8 +136,10 @@ def run_matching_variant(X, U, W, ctc, Th, fmt="exact", rescore=False, keep=None
     return st, (np.concatenate(amp_l) if amp_l else np.zeros(0))
 
 
-def study(rates=(10.0, 40.0), windows: int = 8):
-    """Agreement with the exact loop of each variant on the 384-channel / 500-template shape."""
+def study(rates=(10.0, 40.0), windows: int = 8, only=None):
+    """Agreement with the exact loop of each variant on the 384-channel / 500-template shape
+    (``only``: names of the variants to run; all by default).  The static-scale variants take their
+    scales from window ``windows``, held out of the scored windows 0 .. windows-1."""
     import sys
     import tempfile
     from pathlib import Path
@@ -128,7 +149,11 @@ def study(rates=(10.0, 40.0), windows: int = 8):
     variants = [("bf16", dict(fmt="bf16")), ("bf16 re-scored", dict(fmt="bf16", rescore=True)),
                 ("e4m3", dict(fmt="e4m3")), ("e4m3 re-scored", dict(fmt="e4m3", rescore=True)),
                 ("e5m2 re-scored", dict(fmt="e5m2", rescore=True))] + \
-               [(f"e4m3 top-{k}, exact", dict(fmt="e4m3", keep=k)) for k in (4, 8, 16)]
+               [(f"e4m3 top-{k}, exact", dict(fmt="e4m3", keep=k)) for k in (4, 8, 16)] + \
+               [("e4m3 static re-scored", dict(fmt="e4m3", rescore=True, static=True)),
+                ("e4m3 static top-16", dict(fmt="e4m3", keep=16, static=True))]
+    if only is not None:
+        variants = [v for v in variants if v[0] in only]
     for rate in rates:
         cfg = synth.SynthConfig(n_chan=384, n_units=500, n_samples=(windows + 2) * 1500 + 300, drift_um=20.0,
                                 whiten_batch=3000, whiten_batches=3, seed=5, rate_hz=rate)
@@ -136,10 +161,16 @@ def study(rates=(10.0, 40.0), windows: int = 8):
         d = synth.write_oss_input(synth.build_oss_input(rec), Path(tempfile.mkdtemp()) / "oss_input")
         oss = ko.load_oss_input(d)
         tot = {name: [0.0, 0.0, 0] for name, _ in variants}
+        # static scales from a calibration window that is not one of the windows scored
+        Xc = ko.preprocess(rec.data[windows * 1500:windows * 1500 + 1622].T, oss)
+        act = calibrate_act_scale(operands(Xc, oss.Wall3, oss.wPCA)[1])
         for j in range(windows):
             X = ko.preprocess(rec.data[j * 1500:j * 1500 + 1622].T, oss)
             ref, refa = run_matching_variant(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned)
             for name, kw in variants:
+                kw = dict(kw)
+                if kw.pop("static", False):
+                    kw["act_scale"] = act
                 st, am = run_matching_variant(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned, **kw)
                 a, ok, _ = agreement(ref[:, 0], ref[:, 1], refa, st[:, 0], st[:, 1], am)
                 tot[name][0] += a * len(ref)

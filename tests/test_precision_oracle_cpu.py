@@ -47,3 +47,37 @@ def test_rescored_amplitudes_are_exact_for_the_spikes_kept(window):
         n += 1
     assert n > 0
     np.testing.assert_allclose(amps[:n], ref.amps[:n], rtol=1e-9)
+
+
+def test_static_scales_fold_into_the_templates_and_saturate(window):
+    """The static-scale projection (the FP8 kernel's form): scales calibrated on the window itself
+    stay within e4m3's relative error of the exact product, and a held-out value beyond twice the
+    calibrated range saturates at the largest finite value times its scale."""
+    X, oss, _ = window
+    U2, Bpc2 = po.operands(X, oss.Wall3, oss.wPCA)
+    s = po.calibrate_act_scale(Bpc2)
+    assert s.shape == (Bpc2.shape[0], 1) and np.all(s > 0)
+    np.testing.assert_allclose(s[:, 0], 2 * np.abs(Bpc2).max(1) / 448.0)
+    Bq = po.project_rounded(U2, Bpc2, "e4m3", act_scale=s)
+    Be = U2 @ Bpc2
+    # each product term carries at most (1 + 2^-4)^2 - 1 relative error, plus subnormal flushes
+    bound = (np.abs(U2) @ np.abs(Bpc2)) * ((1 + 2.0 ** -4) ** 2 - 1) + 1e-6 * np.abs(Be).max()
+    assert np.all(np.abs(Bq - Be) <= bound)
+    big = Bpc2.copy()
+    big[0, 0] = 10 * np.abs(Bpc2[0]).max()
+    e = np.zeros((1, U2.shape[1]))
+    e[0, 0] = 1.0
+    assert po.project_rounded(e, big[:, :1], "e4m3", act_scale=s)[0, 0] == pytest.approx(448.0 * s[0, 0], rel=2 ** -3)
+
+
+def test_static_rescored_variant_keeps_exact_amplitudes(window):
+    X, oss, it = window
+    ref = ko.run_matching(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned, max_iters=it)
+    s = po.calibrate_act_scale(po.operands(X, oss.Wall3, oss.wPCA)[1])
+    st, amps = po.run_matching_variant(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned, fmt="e4m3", rescore=True,
+                                       max_iters=it, act_scale=s)
+    n = 0
+    while n < min(len(st), len(ref.st)) and tuple(st[n]) == tuple(ref.st[n]):
+        n += 1
+    assert n > 0
+    np.testing.assert_allclose(amps[:n], ref.amps[:n], rtol=1e-9)
