@@ -861,7 +861,7 @@ int match_variant(int W, int T, int nt, bool* wide) {
 
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm, float th2,
                          int W, int T, int C, int nt, int max_iters, int nb, const MatchScratch& sc,
-                         const MatchOut& out, cudaStream_t s, int variant) {
+                         const MatchOut& out, cudaStream_t s, int variant, bool residual) {
     // variant: 0 = automatic -- for groups of at most 8 batches (latency), scores in shared memory
     // when they fit, else in L2 with 16-CTA clusters of 1024 threads (one CTA per SM); larger
     // groups (throughput) scores in L2 with 8-CTA clusters, two CTAs per SM.  1 = the 8-CTA L2
@@ -883,7 +883,7 @@ cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float*
     else
         e = launch_match_cfg<8, false, kMatchThreads>(Bt, Xres, ctcP, pre_wf, nm, th2, W, T, C, nt, max_iters, nb, sc,
                                                       out, s);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || !residual) return e;
     return launch_residual(Xres, pre_wf, out, W, C, nt, nb, s);
 }
 

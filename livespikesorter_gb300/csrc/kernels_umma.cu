@@ -379,7 +379,8 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
                     continue;
                 }
                 if (row < M) {
-                    float* crow = args.out + ((int64_t)z * M + row) * args.ldc + n0 + c0;
+                    // (out null: only the channel-major copy is wanted)
+                    float* crow = args.out ? args.out + ((int64_t)z * M + row) * args.ldc + n0 + c0 : nullptr;
                     const int ncol = min(32, N - (n0 + c0));
                     if (args.col_scale) {
 #pragma unroll
@@ -409,7 +410,8 @@ umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constan
                             }
                         }
                     }
-                    if (ncol == 32 && ((((uintptr_t)crow) & 15) == 0)) {
+                    if (!crow) {
+                    } else if (ncol == 32 && ((((uintptr_t)crow) & 15) == 0)) {
 #pragma unroll
                         for (int j = 0; j < 32; j += 4)
                             *reinterpret_cast<float4*>(crow + j) = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
@@ -448,30 +450,30 @@ __global__ void split_tf32_kernel(const float* __restrict__ x, float* __restrict
 }
 
 // ------------------------------------------------------------------------------------------
-// temporal basis convolution as a band GEMM per component:
+// temporal basis convolution as a band GEMM over all components of a group at once:
 //   Bpc[b][w][k][c] = sum_m wPCA[k][m] * Z[b][w + m - nt/2][c]
-// A = the channel-major whitened windows Zt[(b, c)][time] (M = 128 (b, c) rows per tile), B_k =
-// the band matrix of component k over the tile's input times.  A tile covers TW = kConvTileW output
-// times w0..w0+TW-1 of kg components and the K = 16 ks input times from x0 = w0 - hr on, so
-// B_k[j][u] = wPCA[k][u - j - d] (d = hr - nt/2).  Every K-step's band is the previous one 16 rows
-// further down one resident strip S_k[r][i] = wPCA[k][i - r + 16 (ks - 1) - d] (TW + 16 (ks - 1)
-// rows): the B descriptor of K-step s starts at strip row 16 (ks - 1 - s), a multiple of 1024
-// bytes, so no band tile is ever loaded twice.  Out-of-window input times (< 0 or >= W) come from
-// the TMA zero fill.
+// A = the channel-major whitened windows Zt[(b, c)][time] (M = 128 (b, c) rows per tile).  A tile
+// covers TW output times w0..w0+TW-1 of the kg components of its group and the ks K-steps of input
+// times from x0 = w0 - hr on.  B of K-step s stacks the components' band matrices along N:
+// B_s[g TW + j][i] = wPCA[cg kg + g][step s + i - j - d] (d = hr - nt/2), one resident tile per
+// K-step, so a K-step is one MMA of N = kg TW per product (three on the split operands) instead of
+// one narrow MMA per component: the tile count per unit of output, not the math, bounded the
+// narrow form.  Out-of-window input times (< 0 or >= W) come from the TMA zero fill.
 //
-// Persistent CTAs (one per SM), warp-specialised: warp E / lane 0 loads the strips once, then A
-// tiles through a kConvStages mbarrier ring; warp E + 1 / lane 0 issues tcgen05.mma (M = 128,
-// N = TW, K = 8; the per-instruction cost of narrower MMAs dominated) into one of two TMEM
-// accumulators of kg x TW columns; the E = kConvEpiWarps warps 0..E-1 drain the other accumulator
-// into Bpc while the next tile accumulates -- warp e reads TMEM lanes 32 (e % 4) .. + 31 (its
-// (b, c) rows) for the tile's components e / 4, e / 4 + E / 4, ...  The K components are split
-// into groups of kg (tiles of one (rows, times) block, one group each, run on neighbouring CTAs
-// and share its A tiles through L2).  Bounded waits as in the GEMM above.
+// Persistent CTAs (one per SM), warp-specialised: CTA b serves component group b % ncg; warp E /
+// lane 0 loads its group's bands once, then A tiles through a kConvStages mbarrier ring; warp
+// E + 1 / lane 0 issues tcgen05.mma (M = 128, N = ng TW) into one of two TMEM accumulators of
+// kg TW columns; the E = kConvEpiWarps warps 0..E-1 drain the other accumulator into Bpc while the
+// next tile accumulates -- warp e reads TMEM lanes 32 (e % 4) .. + 31 (its (b, c) rows), column
+// chunks of 32 (one component's 32 output times) e / 4, e / 4 + E / 4, ...  The CTAs of different
+// groups walk the same (rows, times) blocks in step and share their A tiles through L2.  Bounded
+// waits as in the GEMM above.
 // ------------------------------------------------------------------------------------------
 constexpr int kConvStages = 4;
 constexpr int kConvEpiWarps = 8;                        // a multiple of 4
 constexpr int kConvThreads = (kConvEpiWarps + 2) * 32;
-constexpr int kConvMaxK = 8;       // 2 x 8 x 32 TMEM columns
+constexpr int kConvMaxK = 8;
+constexpr int kConvSmemMax = 220 * 1024;
 
 struct ConvArgs {
     float* out_hi;
@@ -479,35 +481,97 @@ struct ConvArgs {
     int nrows;      // nb * C
     int chans, wlen;
     int kc;         // components
-    int ks, hr;     // ConvGeometry
-    int rows, kg;   // strip rows, components per tile
-    int ncg;        // component groups
+    int ks, hr, tw; // ConvGeometry
+    int kg, ncg;    // components per group, groups
     int ntiles_w;
-    int hi_only;
-    int out_bf16;   // store the BF16 split (two bf16 arrays) instead of fp32 / tf32
     int* err;
 };
 
-template <bool ALO, bool BF16>
+// instruction descriptors with N chosen at run time (N % 16 == 0, 16 <= N <= 256)
+__device__ __forceinline__ uint32_t idesc_n(uint32_t kind_bits, int n) {
+    return kind_bits | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+}
+__device__ __forceinline__ void mma_bf16_rt(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_tf32_rt(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// one chunk of the epilogue: element j (output time wh + j) of this lane's (b, c) row goes to
+// o0 + j step.  OUT: 0 = fp32, 1 = tf32 split (lo optional: tf32 alone), 2 = BF16 split
+template <int OUT, bool FULL>
+__device__ __forceinline__ void conv_store(const uint32_t (&r)[32], float* out_hi, float* out_lo, int64_t o0,
+                                           int64_t step, int nj) {
+    if constexpr (OUT == 2) {
+        __nv_bfloat16* ph = reinterpret_cast<__nv_bfloat16*>(out_hi) + o0;
+        __nv_bfloat16* pl = reinterpret_cast<__nv_bfloat16*>(out_lo) + o0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            if (FULL || j < nj) {
+                const float v = __uint_as_float(r[j]);
+                const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                *ph = h;
+                *pl = __float2bfloat16_rn(v - __bfloat162float(h));
+            }
+            ph += step;
+            pl += step;
+        }
+    } else if constexpr (OUT == 1) {
+        float* ph = out_hi + o0;
+        float* pl = out_lo ? out_lo + o0 : nullptr;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            if (FULL || j < nj) {
+                const float v = __uint_as_float(r[j]);
+                uint32_t h;
+                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+                ph[(int64_t)j * step] = __uint_as_float(h);
+                if (pl) pl[(int64_t)j * step] = v - __uint_as_float(h);
+            }
+        }
+    } else {
+        float* ph = out_hi + o0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (FULL || j < nj) ph[(int64_t)j * step] = __uint_as_float(r[j]);
+    }
+}
+
+template <bool ALO, bool BF16, int OUT>
 __global__ void __launch_bounds__(kConvThreads, 1)
 umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
                 const __grid_constant__ CUtensorMap tS_hi, const __grid_constant__ CUtensorMap tS_lo, ConvArgs args) {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[kConvStages], empty_bar[kConvStages], tfull_bar[2], tempty_bar[2];
-    __shared__ __align__(8) uint64_t strip_bar, drain_bar;
+    __shared__ __align__(8) uint64_t band_bar, drain_bar;
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_raw;
     volatile int& abort_s = abort_raw;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int TW = kConvTileW;
-    const int KC = args.kc, KS = args.ks, KG = args.kg, NCG = args.ncg;
-    const uint32_t sbytes = (uint32_t)args.rows * 64u;   // one component's strip (a multiple of 1024)
+    const int TW = args.tw, KC = args.kc, KS = args.ks, KG = args.kg, NCG = args.ncg;
+    const int NB = KG * TW;                               // band rows per K-step (N of a full group)
+    const uint32_t bbytes = (uint32_t)NB * 64u;           // one K-step's band tile (a multiple of 1024)
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
-    const uint32_t s_hi = base, s_lo = base + (uint32_t)KC * sbytes;
-    const uint32_t stage0 = base + 2u * (uint32_t)KC * sbytes;
+    const uint32_t b_hi = base, b_lo = base + (uint32_t)KS * bbytes;
+    const uint32_t stage0 = base + 2u * (uint32_t)KS * bbytes;
     auto sA_hi = [&](int s) { return stage0 + (uint32_t)s * 2u * kTileA; };
     auto sA_lo = [&](int s) { return stage0 + (uint32_t)s * 2u * kTileA + kTileA; };
-    const int ntiles = ((args.nrows + kBM - 1) / kBM) * args.ntiles_w * NCG;
+    // this CTA's component group and its walk over the (rows, times) blocks
+    const int cg = blockIdx.x % NCG, cta_step = gridDim.x / NCG;
+    const int nblocks = ((args.nrows + kBM - 1) / kBM) * args.ntiles_w;
+    const int blk0 = (int)(blockIdx.x / NCG);
+    const int ng = min(KG, KC - cg * KG);                 // components of this group
     int* err = args.err;
 
     if (threadIdx.x == 0) {
@@ -519,7 +583,7 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
             mbar_init(smem_u32(&tfull_bar[a]), 1);
             mbar_init(smem_u32(&tempty_bar[a]), kConvEpiWarps);   // one arrival per epilogue warp
         }
-        mbar_init(smem_u32(&strip_bar), 1);
+        mbar_init(smem_u32(&band_bar), 1);
         mbar_init(smem_u32(&drain_bar), 1);
         abort_s = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -536,17 +600,17 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
     const uint32_t tmem = tmem_base_s;
 
     if (warp == kConvEpiWarps && lane == 0) {
-        // ---- producer: the strips once, then the A tiles of every tile of this CTA ----
-        const uint32_t sb = smem_u32(&strip_bar);
-        mbar_expect_tx(sb, 2u * (uint32_t)KC * sbytes);
-        for (int c = 0; c < KC; ++c) {
-            tma_load_2d(s_hi + (uint32_t)c * sbytes, &tS_hi, sb, 0, c * args.rows);
-            tma_load_2d(s_lo + (uint32_t)c * sbytes, &tS_lo, sb, 0, c * args.rows);
+        // ---- producer: the group's band tiles once, then the A tiles of every block of this CTA ----
+        const uint32_t bb = smem_u32(&band_bar);
+        mbar_expect_tx(bb, 2u * (uint32_t)KS * bbytes);
+        for (int s = 0; s < KS; ++s) {
+            tma_load_2d(b_hi + (uint32_t)s * bbytes, &tS_hi, bb, 0, (cg * KS + s) * NB);
+            tma_load_2d(b_lo + (uint32_t)s * bbytes, &tS_lo, bb, 0, (cg * KS + s) * NB);
         }
         int q = 0;
-        for (int tile = blockIdx.x; tile < ntiles && !abort_s; tile += gridDim.x) {
-            const int blk = tile / NCG, mt = blk / args.ntiles_w, wt = blk - mt * args.ntiles_w;
-            const int m0 = mt * kBM, x0 = wt * TW - args.hr;   // 16-byte aligned (hr is)
+        for (int blk = blk0; blk < nblocks && !abort_s; blk += cta_step) {
+            const int mt = blk / args.ntiles_w, wt = blk - mt * args.ntiles_w;
+            const int m0 = mt * kBM, x0 = wt * TW - args.hr;   // 16-byte aligned (hr and TW are)
             constexpr int kStep = BF16 ? 2 * kBK : kBK;         // input times per K-step
             bool stop = false;
             for (int ks = 0; ks < KS; ++ks, ++q) {
@@ -565,19 +629,20 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
             }
             if (stop) break;
         }
-        // the copies of the last rounds and the strips land before the CTA may exit
+        // the copies of the last rounds and the bands land before the CTA may exit
         for (int kt = (q > kConvStages ? q - kConvStages : 0); kt < q; ++kt)
             if (!mbar_wait(smem_u32(&full_bar[kt % kConvStages]), (uint32_t)(kt / kConvStages) & 1u)) atomicOr(err, 4);
-        if (!mbar_wait(sb, 0u)) atomicOr(err, 4);
+        if (!mbar_wait(bb, 0u)) atomicOr(err, 4);
     } else if (warp == kConvEpiWarps + 1 && lane == 0) {
-        // ---- MMA issuer ----
-        const uint64_t dsh = smem_desc(s_hi), dsl = smem_desc(s_lo);   // the strips' base descriptors
-        if (!mbar_wait(smem_u32(&strip_bar), 0u)) {
+        // ---- MMA issuer: per K-step one MMA of N = ng TW per product ----
+        const uint32_t idesc = idesc_n(BF16 ? ((1u << 4) | (1u << 7) | (1u << 10)) : ((1u << 4) | (2u << 7) | (2u << 10)),
+                                       ng * TW);
+        if (!mbar_wait(smem_u32(&band_bar), 0u)) {
             atomicOr(err, 2);
             abort_s = 1;
         }
         int q = 0, i = 0;
-        for (int tile = blockIdx.x; tile < ntiles && !abort_s; tile += gridDim.x, ++i) {
+        for (int blk = blk0; blk < nblocks && !abort_s; blk += cta_step, ++i) {
             const int ab = i & 1;
             if (!mbar_wait(smem_u32(&tempty_bar[ab]), ((uint32_t)(i >> 1) & 1u) ^ 1u) || abort_s) {
                 atomicOr(err, 2);
@@ -585,8 +650,7 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t dcol = tmem + (uint32_t)(ab * KG * TW);
-            const int cg0 = (tile % NCG) * KG, ng = min(KG, KC - cg0);
+            const uint32_t d = tmem + (uint32_t)(ab * NB);
             bool stop = false;
             for (int ks = 0; ks < KS; ++ks, ++q) {
                 const int s = q % kConvStages;
@@ -598,33 +662,21 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                // strip row step (ks - 1 - s): 16 or 32 rows of 64 bytes per K-step.  The start
-                // address sits in the descriptors' low bits (address >> 4, every shared address here
-                // is below 256 KB), so offsets are added to descriptors built once: the single
-                // issuing thread spends its instructions on the 18 MMAs of the K-step, not on
-                // rebuilding their operands
-                const uint64_t ah0 = smem_desc(sA_hi(s)), al0 = smem_desc(sA_lo(s));
-                const uint64_t band = ((uint64_t)(KS - 1 - ks) * (BF16 ? 2048u : 1024u) + cg0 * sbytes) >> 4;
 #pragma unroll
                 for (int kk = 0; kk < 2; ++kk) {          // 32 bytes (8 tf32 / 16 bf16) per MMA
-                    const uint64_t ah = ah0 + 2u * kk, al = al0 + 2u * kk;
+                    const uint32_t off = (uint32_t)kk * 32u;
+                    const uint64_t ah = smem_desc(sA_hi(s) + off), al = smem_desc(sA_lo(s) + off);
+                    const uint64_t bh = smem_desc(b_hi + (uint32_t)ks * bbytes + off);
+                    const uint64_t bl = smem_desc(b_lo + (uint32_t)ks * bbytes + off);
                     const uint32_t acc = (ks > 0 || kk > 0) ? 1u : 0u;
-#pragma unroll
-                    for (int g = 0; g < kConvMaxK / 2; ++g) {
-                        if (g < ng) {
-                            const uint64_t boff = band + (uint64_t)g * (sbytes >> 4) + 2u * kk;
-                            const uint64_t bh = dsh + boff, bl = dsl + boff;
-                            const uint32_t d = dcol + (uint32_t)(g * TW);
-                            if constexpr (BF16) {
-                                mma_bf16<TW>(d, ah, bh, acc);
-                                mma_bf16<TW>(d, ah, bl, 1u);
-                                if constexpr (ALO) mma_bf16<TW>(d, al, bh, 1u);
-                            } else {
-                                mma_tf32<TW>(d, ah, bh, acc);
-                                mma_tf32<TW>(d, ah, bl, 1u);
-                                if constexpr (ALO) mma_tf32<TW>(d, al, bh, 1u);
-                            }
-                        }
+                    if constexpr (BF16) {
+                        mma_bf16_rt(d, ah, bh, idesc, acc);
+                        mma_bf16_rt(d, ah, bl, idesc, 1u);
+                        if constexpr (ALO) mma_bf16_rt(d, al, bh, idesc, 1u);
+                    } else {
+                        mma_tf32_rt(d, ah, bh, idesc, acc);
+                        mma_tf32_rt(d, ah, bl, idesc, 1u);
+                        if constexpr (ALO) mma_tf32_rt(d, al, bh, idesc, 1u);
                     }
                 }
                 mma_commit(smem_u32(&empty_bar[s]));
@@ -636,10 +688,11 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
         mma_commit(smem_u32(&drain_bar));
         if (!mbar_wait(smem_u32(&drain_bar), 0u)) atomicOr(err, 2);
     } else if (warp < kConvEpiWarps) {
-        // ---- epilogue: accumulator -> Bpc (tf32 split) ----
-        const int quad = warp & 3, c_first = warp >> 2;
+        // ---- epilogue: accumulator -> Bpc ----
+        const int quad = warp & 3;
+        const int cpc = TW / 32;                          // 32-column chunks per component
         int i = 0;
-        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+        for (int blk = blk0; blk < nblocks; blk += cta_step, ++i) {
             const int ab = i & 1;
             // one decision per warp: the tcgen05.ld below is .sync.aligned
             const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[ab]), (uint32_t)(i >> 1) & 1u) && !abort_s);
@@ -649,17 +702,15 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int blk = tile / NCG, mt = blk / args.ntiles_w, wt = blk - mt * args.ntiles_w;
-            const int cg0 = (tile % NCG) * KG, ng = min(KG, KC - cg0);
+            const int mt = blk / args.ntiles_w, wt = blk - mt * args.ntiles_w;
             const int row = mt * kBM + quad * 32 + lane, w0 = wt * TW;
             const int b = row / args.chans, ch = row - b * args.chans;
-            for (int cc = c_first; cc < 2 * ng; cc += kConvEpiWarps / 4) {
-                // 32 output times of one component per pass: (g, half) = (cc / 2, cc % 2)
-                const int g = cc >> 1, c = cg0 + g, wh = w0 + 32 * (cc & 1);
+            for (int cc = warp >> 2; cc < ng * cpc; cc += kConvEpiWarps / 4) {
+                // 32 output times of one component per chunk: (g, part) = (cc / cpc, cc % cpc)
+                const int g = cc / cpc, c = cg * KG + g, wh = w0 + 32 * (cc - g * cpc);
                 const int nj = min(32, args.wlen - wh);
                 uint32_t r[32];
-                const uint32_t taddr =
-                    tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)((ab * KG + g) * TW + 32 * (cc & 1));
+                const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(ab * NB + cc * 32);
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
                     "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
@@ -672,29 +723,13 @@ umma_basis_conv(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant
                     : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 if (row < args.nrows) {
-                    // lanes = consecutive channels of one (w, k): 128-byte stores
+                    // lanes = consecutive channels of one (w, k): 64- or 128-byte stores
                     const int64_t o0 = (((int64_t)b * args.wlen + wh) * KC + c) * args.chans + ch;
                     const int64_t step = (int64_t)KC * args.chans;
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        if (j < nj) {
-                            const float v = __uint_as_float(r[j]);
-                            const int64_t o = o0 + (int64_t)j * step;
-                            if (args.out_bf16) {
-                                const __nv_bfloat16 h = __float2bfloat16_rn(v);
-                                reinterpret_cast<__nv_bfloat16*>(args.out_hi)[o] = h;
-                                reinterpret_cast<__nv_bfloat16*>(args.out_lo)[o] =
-                                    __float2bfloat16_rn(v - __bfloat162float(h));
-                            } else if (args.out_lo || args.hi_only) {
-                                uint32_t h;
-                                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-                                args.out_hi[o] = __uint_as_float(h);
-                                if (args.out_lo) args.out_lo[o] = v - __uint_as_float(h);
-                            } else {
-                                args.out_hi[o] = v;
-                            }
-                        }
-                    }
+                    if (nj == 32)
+                        conv_store<OUT, true>(r, args.out_hi, args.out_lo, o0, step, 32);
+                    else
+                        conv_store<OUT, false>(r, args.out_hi, args.out_lo, o0, step, nj);
                 }
             }
             // the accumulator may be overwritten once every epilogue warp has read it
@@ -920,6 +955,7 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
                                 float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s, bool zt_bf16) {
     if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
     if (zt_hi && (wlen <= 0 || zpitch < wlen || (zt_bf16 && !zt_lo))) return cudaErrorInvalidValue;
+    if (!Cm && !zt_hi) return cudaErrorInvalidValue;
     auto kern = u->lowp == 2  ? umma_gemm_3xtf32<kPlainBN, kPlain, true, false, 2>
                 : u->lowp == 1 ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true, 1>
                 : u->bf16     ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
@@ -1034,27 +1070,52 @@ cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo
 bool conv_tc_geometry(int nt, int K, ConvGeometry& g, bool bf16) {
     if (K < 1 || K > kConvMaxK || nt < 1) return false;
     const int H = nt / 2;
-    g.bf16 = bf16;
-    g.step = bf16 ? 2 * kBK : kBK;
+    const int step = bf16 ? 2 * kBK : kBK;
     const int al = bf16 ? 8 : 4;                       // elements in 16 bytes
-    g.hr = (H + al - 1) / al * al;                     // tile inputs start 16-byte aligned
-    const int need = kConvTileW + nt - 1 + (g.hr - H);  // input times one tile reads
-    g.ks = (need + g.step - 1) / g.step;
-    g.rows = kConvTileW + g.step * (g.ks - 1);
-    if (g.rows > 256) return false;                     // one TMA box per strip
-    const int ncg = (K * kConvTileW * 2 + 511) / 512;   // component groups that fit two accumulators
-    g.kg = (K + ncg - 1) / ncg;
-    const size_t smem = 1024 + 2 * (size_t)K * g.rows * 64 + (size_t)kConvStages * 2 * kTileA;
-    return smem <= 220 * 1024;
+    const int hr = (H + al - 1) / al * al;             // tile inputs start 16-byte aligned
+    // the tile width and component grouping with the fewest MMAs per output (K-steps per tile over
+    // the kg TW outputs a K-step's MMA covers), within N <= 256 (two accumulators fit the 512 TMEM
+    // columns) and the shared-memory budget; ties go to the wider tile
+    bool found = false;
+    double best = 0.0;
+    for (int tw : {64, 32}) {
+        const int ks = (tw + nt - 1 + (hr - H) + step - 1) / step;
+        for (int ncg = 1; ncg <= K; ++ncg) {
+            const int kg = (K + ncg - 1) / ncg;
+            if (kg * tw > 256) continue;
+            const size_t smem = 1024 + 2 * (size_t)ks * kg * tw * 64 + (size_t)kConvStages * 2 * kTileA;
+            if (smem > (size_t)kConvSmemMax) continue;
+            const double cost = (double)ks / (kg * tw);
+            if (!found || cost < best) {
+                found = true;
+                best = cost;
+                g.bf16 = bf16;
+                g.step = step;
+                g.tw = tw;
+                g.ks = ks;
+                g.hr = hr;
+                g.kg = kg;
+                g.ncg = ncg;
+                g.rows = ncg * ks * kg * tw;
+            }
+            break;   // more groups only narrow the MMA
+        }
+    }
+    return found;
 }
 
-void conv_tc_strips(const float* wPCA, int K, int nt, const ConvGeometry& g, float* strips) {
+void conv_tc_bands(const float* wPCA, int K, int nt, const ConvGeometry& g, float* bands) {
     const int d = g.hr - nt / 2;
-    for (int k = 0; k < K; ++k)
-        for (int r = 0; r < g.rows; ++r)
-            for (int i = 0; i < g.step; ++i) {
-                const int m = i - r + g.step * (g.ks - 1) - d;
-                strips[((size_t)k * g.rows + r) * g.step + i] = (m >= 0 && m < nt) ? wPCA[(size_t)k * nt + m] : 0.f;
+    const int nb = g.kg * g.tw;
+    for (int cg = 0; cg < g.ncg; ++cg)
+        for (int s = 0; s < g.ks; ++s)
+            for (int n = 0; n < nb; ++n) {
+                const int k = cg * g.kg + n / g.tw, j = n % g.tw;
+                float* row = bands + ((size_t)(cg * g.ks + s) * nb + n) * g.step;
+                for (int i = 0; i < g.step; ++i) {
+                    const int m = g.step * s + i - j - d;
+                    row[i] = (k < K && m >= 0 && m < nt) ? wPCA[(size_t)k * nt + m] : 0.f;
+                }
             }
 }
 
@@ -1107,8 +1168,8 @@ ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows,
         u->wlen = wlen;
         if (!make_map_pitched_bf16(&u->a_hi, zt_hi, rows, wlen, zpitch, kBM) ||
             !make_map_pitched_bf16(&u->a_lo, zt_lo, rows, wlen, zpitch, kBM) ||
-            !make_map_bf16(&u->s_hi, s_hi, (uint64_t)K * g.rows, g.step, g.rows) ||
-            !make_map_bf16(&u->s_lo, s_lo, (uint64_t)K * g.rows, g.step, g.rows)) {
+            !make_map_bf16(&u->s_hi, s_hi, (uint64_t)g.rows, g.step, g.kg * g.tw) ||
+            !make_map_bf16(&u->s_lo, s_lo, (uint64_t)g.rows, g.step, g.kg * g.tw)) {
             delete u;
             return nullptr;
         }
@@ -1123,8 +1184,8 @@ ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows,
     if (!zt_lo) zt_lo = zt_hi;   // the map is never used
     if (!make_map_pitched(&u->a_hi, zt_hi, rows, wlen, zpitch, kBM) ||
         !make_map_pitched(&u->a_lo, zt_lo, rows, wlen, zpitch, kBM) ||
-        !make_map(&u->s_hi, s_hi, (uint64_t)K * g.rows, 16, g.rows) ||
-        !make_map(&u->s_lo, s_lo, (uint64_t)K * g.rows, 16, g.rows)) {
+        !make_map(&u->s_hi, s_hi, (uint64_t)g.rows, 16, g.kg * g.tw) ||
+        !make_map(&u->s_lo, s_lo, (uint64_t)g.rows, 16, g.kg * g.tw)) {
         delete u;
         return nullptr;
     }
@@ -1137,10 +1198,14 @@ cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* 
                                    int W, int* err, cudaStream_t s, bool out_bf16) {
     if (!u || (int64_t)nb * C > u->rows || W != u->wlen || nb <= 0 || (out_bf16 && !out_lo))
         return cudaErrorInvalidValue;
-    auto kern = u->g.bf16 ? umma_basis_conv<true, true>
-                : u->has_a_lo ? umma_basis_conv<true, false> : umma_basis_conv<false, false>;
+    // the BF16 operands always come with the BF16 split output (the BF16 projection reads it)
+    if (u->g.bf16 != out_bf16) return cudaErrorInvalidValue;
+    auto kern = u->g.bf16 ? umma_basis_conv<true, true, 2>
+                : (out_lo || hi_only) ? (u->has_a_lo ? umma_basis_conv<true, false, 1> : umma_basis_conv<false, false, 1>)
+                                      : (u->has_a_lo ? umma_basis_conv<true, false, 0> : umma_basis_conv<false, false, 0>);
     // at least 120 KB, so that one CTA (holding all 512 TMEM columns) runs per SM
-    const int smem = std::max<int>(120 * 1024, 1024 + 2 * u->K * u->g.rows * 64 + kConvStages * 2 * kTileA);
+    const ConvGeometry& g = u->g;
+    const int smem = std::max<int>(120 * 1024, 1024 + 2 * g.ks * g.kg * g.tw * 64 + kConvStages * 2 * kTileA);
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
     int dev = 0, sms = 0;
@@ -1154,17 +1219,17 @@ cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* 
     a.chans = C;
     a.wlen = W;
     a.kc = u->K;
-    a.ks = u->g.ks;
-    a.rows = u->g.rows;
-    a.kg = u->g.kg;
-    a.ncg = (u->K + u->g.kg - 1) / u->g.kg;
-    a.hr = u->g.hr;
-    a.ntiles_w = (W + kConvTileW - 1) / kConvTileW;
-    a.hi_only = hi_only ? 1 : 0;
-    a.out_bf16 = out_bf16 ? 1 : 0;
+    a.ks = g.ks;
+    a.hr = g.hr;
+    a.tw = g.tw;
+    a.kg = g.kg;
+    a.ncg = g.ncg;
+    a.ntiles_w = (W + g.tw - 1) / g.tw;
     a.err = err;
-    const int64_t ntiles = (int64_t)((nb * C + kBM - 1) / kBM) * a.ntiles_w * a.ncg;
-    const int grid = (int)std::min<int64_t>(ntiles, std::max(sms, 1));
+    // a multiple of ncg CTAs: CTA b serves group b % ncg over every ncg-th block
+    const int64_t nblocks = (int64_t)((nb * C + kBM - 1) / kBM) * a.ntiles_w;
+    const int64_t per_group = std::max<int64_t>(1, std::min<int64_t>(nblocks, std::max(sms, g.ncg) / g.ncg));
+    const int grid = (int)(per_group * g.ncg);
     kern<<<grid, kConvThreads, smem, s>>>(u->a_hi, u->a_lo, u->s_hi, u->s_lo, a);
     return cudaGetLastError();
 }

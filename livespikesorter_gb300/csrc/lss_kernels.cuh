@@ -175,15 +175,17 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
 struct ConvGeometry {
     bool bf16 = false;  // operands are BF16 splits (kind::f16) instead of TF32 splits
     int step = 16;      // input times per K-step: 64-byte rows, 16 fp32 or 32 bf16
-    int ks = 0;         // K-steps per tile of kConvTileW output times
+    int tw = 32;        // output times per tile
+    int ks = 0;         // K-steps per tile
     int hr = 0;         // a tile's first input time is its first output time - hr (16-byte aligned)
-    int rows = 0;       // strip rows per component, kConvTileW + step * (ks - 1)
-    int kg = 0;         // components per tile (two accumulators of kg x kConvTileW TMEM columns)
+    int kg = 0;         // components per tile: one MMA of N = kg * tw columns per K-step and product
+    int ncg = 0;        // component groups (tiles of one (rows, times) block)
+    int rows = 0;       // band rows, ncg * ks * kg * tw (the band array is [rows][step])
 };
-constexpr int kConvTileW = 64;   // output times per tile
 bool conv_tc_geometry(int nt, int K, ConvGeometry& g, bool bf16 = false);
-// strip[k][r][i] = wPCA[k][i - r + step (ks - 1) - (hr - nt / 2)] (zero outside 0..nt-1), [K][rows][step]
-void conv_tc_strips(const float* wPCA, int K, int nt, const ConvGeometry& g, float* strips);
+// band[cg][s][g tw + j][i] = wPCA[cg kg + g][step s + i - j - (hr - nt / 2)] (zero outside
+// 0..nt-1 and for components >= K): the B operand of K-step s, [rows][step]
+void conv_tc_bands(const float* wPCA, int K, int nt, const ConvGeometry& g, float* bands);
 struct ConvOperands;
 ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows, int wlen, int zpitch,
                            const float* s_hi, const float* s_lo, int K, const ConvGeometry& g);
@@ -194,7 +196,8 @@ cudaError_t launch_umma_basis_conv(const ConvOperands* u, float* out_hi, float* 
                                    int W, int* err, cudaStream_t s, bool out_bf16 = false);
 cudaError_t launch_match(float* Bt, float* Xres, const float* ctcP, const float* pre_wf, const float* nm,
                          float th2, int W, int T, int C, int nt, int max_iters, int nb,
-                         const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0);
+                         const MatchScratch& sc, const MatchOut& out, cudaStream_t s, int variant = 0,
+                         bool residual = true);
 // the residual after a matching loop: Xres[w][:] -= amp * waveform[t][w - w_s + nt/2][:] for the
 // spikes of out, in list order
 cudaError_t launch_residual(float* Xres, const float* pre_wf, const MatchOut& out, int W, int C, int nt, int nb,
@@ -220,6 +223,15 @@ void launch_features(const float* Xres, const MatchOut& out, int nb, int W, int 
                      const float* wPCA, const int64_t* iCC, const int64_t* iU, const float* Ucc, const float* xc,
                      const float* yc, const float* centroids, int n_final, const float* cpca, const float* cpca_nm,
                      float r2, const int* rec_offset, SpikeRec* recs, int batch_base, cudaStream_t s);
+// the same records from the basis convolution Bpc [b][w][k][c] (fmt 0: fp32; 1: fp32 pair hi + lo;
+// 2: BF16 pair) and the accepted spikes, without the residual; xcorr = basis_xcorr(wPCA) on the
+// device, wall3t = Wall3 channel-major [T][C][K]
+void basis_xcorr(const float* wPCA, int K, int nt, float* P);   // P [K][K][2 nt - 1]
+void launch_features_direct(const void* bpc_hi, const void* bpc_lo, int fmt, const MatchOut& out, int nb, int W,
+                            int C, int T, int K, int nt, int nC, const float* wall3t, const float* xcorr,
+                            const int64_t* iCC, const int64_t* iU, const float* Ucc, const float* xc, const float* yc,
+                            const float* centroids, int n_final, const float* cpca, const float* cpca_nm, float r2,
+                            const int* rec_offset, SpikeRec* recs, int batch_base, cudaStream_t s);
 void launch_rec_offsets(const MatchOut& out, int nb, int* rec_offset, cudaStream_t s);
 
 }  // namespace lss

@@ -160,9 +160,19 @@ struct Handle {
     uint8_t* d_W8 = nullptr;            // [T][K*C] e4m3 templates (scales folded)
     float *d_tau = nullptr, *d_sig = nullptr, *d_isig = nullptr;   // [T] template, [K*C] activation scales
     unsigned* d_colmax = nullptr;       // [K*C] calibration scratch
+    // PC features straight from the basis convolution and the accepted spikes, without the
+    // residual, whenever Bpc holds the convolution to FP32 accuracy (fp32, or an fp32 / BF16 pair:
+    // feat_fmt 0 / 1 / 2); the whitened windows and the residual are then written only for the
+    // proposal gate and lss_debug_stage (debug_run)
+    bool direct_feat = false;
+    int feat_fmt = 0;
+    float* d_xcorr = nullptr;           // basis cross-correlation [K][K][2 nt - 1]
+    float* d_Wall3T = nullptr;          // Wall3 channel-major [T][C][K]
+    bool debug_run = false;
+    bool need_z() const { return !direct_feat || gate || debug_run || !tc_whiten || !tc_conv; }
     bool tc_conv = false;     // basis convolution as per-component band GEMMs on the tensor cores
     ConvGeometry conv_g;
-    float *d_S_hi = nullptr, *d_S_lo = nullptr;   // its band strips (tf32 split)
+    float *d_S_hi = nullptr, *d_S_lo = nullptr;   // its band tiles (tf32 or BF16 split)
     // PC-score cluster rule: centroid features [T_final][nC*K], their squared norms, radius^2
     float *d_cpca = nullptr, *d_cpca_nm = nullptr;
     float cl_r2 = 0.f;
@@ -286,7 +296,7 @@ Handle::~Handle() {
             if (kv.second.g_lo[v]) cudaFree(kv.second.g_lo[v]);
         }
     }
-    for (void* p : {(void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
+    for (void* p : {(void*)d_xcorr, (void*)d_Wall3T, (void*)d_WD, (void*)d_Wall3, (void*)d_ctcP, (void*)d_pre_wf, (void*)d_nm, (void*)d_wPCA,
                     (void*)d_Ucc, (void*)d_xc, (void*)d_yc, (void*)d_cent, (void*)d_iCC, (void*)d_iU,
                     (void*)d_chan, (void*)d_WD_hi, (void*)d_WD_lo, (void*)d_Wall3_hi, (void*)d_Wall3_lo,
                     (void*)d_S_hi, (void*)d_S_lo, (void*)d_cpca, (void*)d_cpca_nm, (void*)d_iir_state,
@@ -527,8 +537,8 @@ void Handle::init(const char* dir, const lss_params* prm) {
     bf16_pre = bf16_tier && tc_whiten && C % 32 == 0;
     tc_conv = tc_whiten && tc_project && conv_tc_geometry(nt, K, conv_g, bf16_tier);
     if (tc_conv) {
-        std::vector<float> S((size_t)K * conv_g.rows * conv_g.step);
-        conv_tc_strips(m.wPCA.data(), K, nt, conv_g, S.data());
+        std::vector<float> S((size_t)conv_g.rows * conv_g.step);
+        conv_tc_bands(m.wPCA.data(), K, nt, conv_g, S.data());
         float* d = dev_upload(S, dev_bytes, st);
         d_S_hi = dev_alloc<float>(S.size(), dev_bytes);
         d_S_lo = dev_alloc<float>(S.size(), dev_bytes);
@@ -563,6 +573,18 @@ void Handle::init(const char* dir, const lss_params* prm) {
         }
         LSS_CUDA(cudaGetLastError());
         LSS_CUDA(cudaStreamSynchronize(st));
+    }
+    direct_feat = !tf32_data;
+    feat_fmt = bf16_proj ? 2 : (tc_project ? 1 : 0);
+    if (direct_feat) {
+        std::vector<float> P((size_t)K * K * (2 * nt - 1));
+        basis_xcorr(m.wPCA.data(), K, nt, P.data());
+        d_xcorr = dev_upload(P, dev_bytes, st);
+        std::vector<float> UT((size_t)T * C * K);
+        for (int t = 0; t < T; ++t)
+            for (int k = 0; k < K; ++k)
+                for (int c = 0; c < C; ++c) UT[((size_t)t * C + c) * K + k] = m.Wall3[((size_t)t * K + k) * C + c];
+        d_Wall3T = dev_upload(UT, dev_bytes, st);
     }
     if (lowp) {
         if (!bf16_proj || (lowp == 2 && (K * C) % 64 != 0))
@@ -850,7 +872,7 @@ void Handle::run_stages_to_scores(const int16_t* raw, int nb, int Wn, int NTs, c
         run_zero_phase(raw, nb, Wn, NTs, ts, nl, mark);
     }
     if (tc_whiten)
-        LSS_CUDA(launch_umma_gemm_zt(um_whiten, d_Z, nb * Wn, C, C, tc_conv ? d_Zt_hi : nullptr,
+        LSS_CUDA(launch_umma_gemm_zt(um_whiten, need_z() ? d_Z : nullptr, nb * Wn, C, C, tc_conv ? d_Zt_hi : nullptr,
                                      tc_conv ? d_Zt_lo : nullptr, Wn, ts.zpitch, d_gemm_err, st,
                                      tc_conv && conv_g.bf16));
     else
@@ -928,8 +950,13 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     run_match(nb, Wn, nl);
     mark();
     launch_rec_offsets(mo, nb, s.d_off, st), ++nl;
-    launch_features(d_Z, mo, nb, Wn, C, T, K, nt, nC, d_wPCA, d_iCC, d_iU, d_Ucc, d_xc, d_yc, d_cent, Tf, d_cpca,
-                    d_cpca_nm, cl_r2, s.d_off, s.d_recs, 0, st), ++nl;
+    if (direct_feat)
+        launch_features_direct(d_Bpc, d_Bpc_lo, feat_fmt, mo, nb, Wn, C, T, K, nt, nC, d_Wall3T, d_xcorr, d_iCC, d_iU,
+                               d_Ucc, d_xc, d_yc, d_cent, Tf, d_cpca, d_cpca_nm, cl_r2, s.d_off, s.d_recs, 0, st);
+    else
+        launch_features(d_Z, mo, nb, Wn, C, T, K, nt, nC, d_wPCA, d_iCC, d_iU, d_Ucc, d_xc, d_yc, d_cent, Tf, d_cpca,
+                        d_cpca_nm, cl_r2, s.d_off, s.d_recs, 0, st);
+    ++nl;
     LSS_CUDA(cudaGetLastError());
     mark();
     LSS_CUDA(cudaMemcpyAsync(s.h_nsp, mo.n_spikes, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
@@ -942,26 +969,30 @@ void Handle::launch_group(Slot& s, int nb, int Wn, int NTs, const TapSet& ts, in
     launches_last += nl;
 }
 
-// The matching loop of nb windows on d_Bt (scores) and d_Z (becomes the residual): Kilosort's loop
-// over every template, or the pruned tier (per-sample lists of the keep best templates, then the
-// loop on them); the residual follows either way.
+// The matching loop of nb windows on d_Bt (scores): Kilosort's loop over every template, or the
+// pruned tier (per-sample lists of the keep best templates, then the loop on them); then d_Z
+// becomes the residual, when the features or lss_debug_stage read it.
 void Handle::run_match(int nb, int Wn, int64_t& nl) {
     LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
+    const bool resid = !direct_feat || debug_run;
     if (keep > 0) {
         launch_prune_select(d_Bt, d_nm, nb, Wn, T, keep, d_lid, d_lsc, st);
         LSS_CUDA(cudaGetLastError());
         LSS_CUDA(launch_match_pruned(d_lid, d_lsc, keep, d_ctcP, d_nm, th * th, Wn, T, nt, max_iters, nb, d_pcf,
                                      d_pslot, mo, st));
-        LSS_CUDA(launch_residual(d_Z, d_pre_wf, mo, Wn, C, nt, nb, st));
-        nl += 3;   // selection, loop, residual
+        nl += 2;   // selection, loop
+        if (resid) {
+            LSS_CUDA(launch_residual(d_Z, d_pre_wf, mo, Wn, C, nt, nb, st));
+            ++nl;
+        }
     } else {
         MatchScratch scr = sc;
         if (lowp)
             scr.rs = MatchRescore{d_Bt0, reinterpret_cast<const uint16_t*>(d_Bpc),
                                   reinterpret_cast<const uint16_t*>(d_Bpc_lo), d_Wall3, K * C};
         LSS_CUDA(launch_match(d_Bt, d_Z, d_ctcP, d_pre_wf, d_nm, th * th, Wn, T, C, nt, max_iters, nb, scr, mo, st,
-                              p.match_variant));
-        nl += 2;   // the loop and the residual
+                              p.match_variant, resid));
+        nl += resid ? 2 : 1;   // the loop (and the residual)
     }
 }
 
@@ -1486,6 +1517,12 @@ int lss_debug_stage(lss_handle* hp, const int16_t* window, int32_t W, int32_t st
         cudaSetDevice(h.dev);
         h.drain_all();
         h.ensure_work(W, 1);
+        // the whitened window and the residual are written for this call
+        struct DebugRun {
+            lss::Handle& h;
+            explicit DebugRun(lss::Handle& hh) : h(hh) { h.debug_run = true; }
+            ~DebugRun() { h.debug_run = false; }
+        } debug_run(h);
         const int si = h.acquire_slot();
         lss::Slot& s = h.slots[si];
         std::memcpy(s.h_stage, window, (size_t)W * h.Cin * sizeof(int16_t));
