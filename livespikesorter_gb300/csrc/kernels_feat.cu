@@ -216,7 +216,7 @@ __device__ __forceinline__ float bpc_value(const void* hi, const void* lo, int64
     }
 }
 
-template <int FMT>
+template <int FMT, int KC>
 __global__ void __launch_bounds__(kFeatWarps * 32)
 features_direct_kernel(const void* __restrict__ bpc_hi, const void* __restrict__ bpc_lo, MatchOut out, int nb, int W,
                        int C, int T, int K, int nt, int nC, const float* __restrict__ wall3t,
@@ -225,6 +225,9 @@ features_direct_kernel(const void* __restrict__ bpc_hi, const void* __restrict__
                        const float* __restrict__ yc, const float* __restrict__ centroids, int n_final,
                        const float* __restrict__ cpca, const float* __restrict__ cpca_nm, float r2,
                        const int* __restrict__ rec_offset, SpikeRec* __restrict__ recs, int batch_base) {
+    // KC: the component count when known at compile time (0: K at run time, up to kFeatMaxK)
+    constexpr int KM = KC > 0 ? KC : kFeatMaxK;
+    if (KC > 0 && K != KC) return;
     extern __shared__ float s_p[];   // P[d + nt - 1][k][k'], (2 nt - 1) K K
     __shared__ float s_f[kFeatWarps][64];
     const int nd = 2 * nt - 1;
@@ -249,16 +252,16 @@ features_direct_kernel(const void* __restrict__ bpc_hi, const void* __restrict__
         const float amp = out.sp_amp[so];
         const int64_t peak = iU[t];
         const int64_t ch = iCC[(int64_t)n * C + peak];
-        float acc[kFeatMaxK];
+        float acc[KM];
 #pragma unroll
-        for (int k = 0; k < kFeatMaxK; ++k) acc[k] = 0.f;
+        for (int k = 0; k < KM; ++k) acc[k] = 0.f;
         // every accepted spike of the batch whose waveform overlaps this spike's nt samples
         // (itself included); slice j takes the ones whose rank among them is j mod J
         const int n_sp = min(out.n_spikes[b], out.cap);
         const int* sw = out.sp_w + (int64_t)b * out.cap;
         const int* st = out.sp_t + (int64_t)b * out.cap;
         const float* sa = out.sp_amp + (int64_t)b * out.cap;
-        int rank = 0;
+        int slice = 0;   // rank of the next overlapping spike, mod J
         for (int i0 = 0; i0 < n_sp; i0 += 32) {
             const int i = i0 + lane;
             const int d = i < n_sp ? w - sw[i] : nt;
@@ -272,29 +275,30 @@ features_direct_kernel(const void* __restrict__ bpc_hi, const void* __restrict__
                 const int dd = __shfl_sync(0xffffffffu, d, src);
                 const int t2 = __shfl_sync(0xffffffffu, ti, src);
                 const float a2 = __shfl_sync(0xffffffffu, ai, src);
-                if (act && rank % J == jj) {
+                if (act && slice == jj) {
                     // the neighbour's template at channel ch: Wall3[t2][k'][ch], k' = 0 .. K-1 (contiguous)
-                    const float* u = wall3t + ((int64_t)t2 * C + ch) * K;
-                    const float* pd = s_p + (dd + nt - 1) * K * K;
-                    float uk[kFeatMaxK];
+                    const int kd = KC > 0 ? KC : K;
+                    const float* u = wall3t + ((int64_t)t2 * C + ch) * kd;
+                    const float* pd = s_p + (dd + nt - 1) * kd * kd;
+                    float uk[KM];
 #pragma unroll
-                    for (int k2 = 0; k2 < kFeatMaxK; ++k2) uk[k2] = k2 < K ? __ldg(u + k2) : 0.f;
+                    for (int k2 = 0; k2 < KM; ++k2) uk[k2] = (KC > 0 || k2 < K) ? __ldg(u + k2) : 0.f;
 #pragma unroll
-                    for (int k = 0; k < kFeatMaxK; ++k) {
-                        if (k >= K) break;
+                    for (int k = 0; k < KM; ++k) {
+                        if (KC == 0 && k >= K) break;
                         float sum = 0.f;
 #pragma unroll
-                        for (int k2 = 0; k2 < kFeatMaxK; ++k2)
-                            if (k2 < K) sum = fmaf(uk[k2], pd[k * K + k2], sum);
+                        for (int k2 = 0; k2 < KM; ++k2)
+                            if (KC > 0 || k2 < K) sum = fmaf(uk[k2], pd[k * kd + k2], sum);
                         acc[k] = fmaf(-a2, sum, acc[k]);
                     }
                 }
-                ++rank;
+                if (++slice == J) slice = 0;
             }
         }
         // slices summed in slice order into lane n, then the convolution and the amplitude term
 #pragma unroll
-        for (int k = 0; k < kFeatMaxK; ++k) {
+        for (int k = 0; k < KM; ++k) {
             float tot = acc[k];
             for (int q = 1; q < J; ++q) tot += __shfl_sync(0xffffffffu, acc[k], (lane + q * nC) & 31);
             acc[k] = tot;
@@ -304,7 +308,9 @@ features_direct_kernel(const void* __restrict__ bpc_hi, const void* __restrict__
         sf[lane + 32] = 0.f;
         __syncwarp();
         if (act && jj == 0) {
-            for (int k = 0; k < K; ++k) {
+#pragma unroll
+            for (int k = 0; k < KM; ++k) {
+                if (KC == 0 && k >= K) break;
                 const float base = bpc_value<FMT>(bpc_hi, bpc_lo, (((int64_t)b * W + w) * K + k) * C + ch);
                 sf[n * K + k] = (base + acc[k]) + amp * Ucc[((int64_t)n * T + t) * K + k];   // acc = -(overlaps)
             }
@@ -334,7 +340,11 @@ void launch_features_direct(const void* bpc_hi, const void* bpc_lo, int fmt, con
     const int max_recs = nb * out.cap;
     const int blocks = std::min((max_recs + kFeatWarps - 1) / kFeatWarps, 2048);
     const size_t smem = sizeof(float) * (size_t)K * K * (2 * nt - 1);
-    auto kern = fmt == 2 ? features_direct_kernel<2> : (fmt == 1 ? features_direct_kernel<1> : features_direct_kernel<0>);
+    // six components (Kilosort's default basis) unrolled exactly, any other count up to 8 generic
+    auto kern = K == 6 ? (fmt == 2 ? features_direct_kernel<2, 6>
+                                   : (fmt == 1 ? features_direct_kernel<1, 6> : features_direct_kernel<0, 6>))
+                       : (fmt == 2 ? features_direct_kernel<2, 0>
+                                   : (fmt == 1 ? features_direct_kernel<1, 0> : features_direct_kernel<0, 0>));
     kern<<<blocks, kFeatWarps * 32, smem, s>>>(bpc_hi, bpc_lo, out, nb, W, C, T, K, nt, nC, wall3t, xcorr, iCC, iU, Ucc,
                                                xc, yc, centroids, n_final, cpca, cpca_nm, r2, rec_offset, recs,
                                                batch_base);
