@@ -227,7 +227,8 @@ def roofline(stage_ms, n_groups, group, C, T, K, nt, W, ntaps, spikes_per_batch,
     """Achieved vs peak for the dominant kernel (per-launch algorithmic work / mean duration).  For
     the matching loop the algorithmic bytes are one score scan plus, per spike, the ctc read and score
     read-modify-write of the templates it updates (mean_reach of them on average -- all T in Kilosort's
-    dense subtraction) and the residual update."""
+    dense subtraction); the residual is not part of the sorting path (the features come from the
+    convolution)."""
     hbm, tflops, src = peaks()
     per = {k: v / max(n_groups, 1) for k, v in stage_ms.items()}
     kern = max((k for k in per if k not in ("h2d", "d2h")), key=lambda k: per[k])
@@ -242,19 +243,19 @@ def roofline(stage_ms, n_groups, group, C, T, K, nt, W, ntaps, spikes_per_batch,
         work, unit, bound, peak = 2.0 * C * K * nt * W * group / 1e12, "TFLOP/s", "tensor", tflops
     elif kern == "match":
         reach = T if mean_reach is None else mean_reach
-        per_spike = reach * (2 * nt + 1) * (4 + 8) + nt * C * (4 + 8)
+        per_spike = reach * (2 * nt + 1) * (4 + 8)
         work = group * (4.0 * T * W + spikes_per_batch * per_spike) / 1e9
-        dense = group * (4.0 * T * W + spikes_per_batch * (T * (2 * nt + 1) * 12 + nt * C * 12)) / 1e9
+        dense = group * (4.0 * T * W + spikes_per_batch * T * (2 * nt + 1) * 12) / 1e9
         unit, bound, peak = "GB/s", "hbm", hbm
     else:
         work = group * (2.0 * W * C + 4.0 * W * C) / 1e9
         unit, bound, peak = "GB/s", "hbm", hbm
     achieved = work / (ms / 1e3)
-    # DRAM bytes (read + write) per batch of each stage's kernels (match: loop + residual) from ncu captures of the
-    # 64-batch group (profiles/match_kernel_interleaved_64batches.md, profiles/residual_and_features_64batches.md,
+    # DRAM bytes (read + write) per batch of each stage's kernel on the FP32 path from ncu captures of the
+    # 64-batch group (profiles/match_kernel_interleaved_64batches.md,
     # profiles/preprocess_and_gemm_kernels_64batches.md), scaled to this launch's batches
-    traffic_per_batch = {"match": (8.476e9 + 0.371e9) / 64, "project": 2.214e9 / 64, "basis_conv": 2.171e9 / 64,
-                         "highpass": 0.798e9 / 64, "whiten": 0.742e9 / 64, "car": 0.514e9 / 64}
+    traffic_per_batch = {"match": 8.477e9 / 64, "project": 2.216e9 / 64, "basis_conv": 2.172e9 / 64,
+                         "highpass": 0.796e9 / 64, "whiten": 0.597e9 / 64, "car": 0.515e9 / 64}
     traffic = traffic_per_batch.get(kern)
     out = {"kernel": kern, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
            "frac": achieved / peak, "peak_source": src, "algorithmic_gb_per_launch": work if unit == "GB/s" else None,
