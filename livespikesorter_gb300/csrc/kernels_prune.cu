@@ -568,14 +568,18 @@ __host__ __device__ inline size_t prune_cl_smem(int W, int T, int nt, int keep, 
     return b + span * ks * 4;
 }
 
-template <int G, int NTHR, int LPS>
+// EPL: list entries per lane (entry e = gl + LPS h, h < EPL), so 24 or 32 entries run on lane
+// groups of 16 -- two samples per warp, as at 16 entries -- instead of groups of 32
+template <int G, int NTHR, int LPS, int EPL>
 __global__ void __launch_bounds__(NTHR, 2)
 match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __restrict__ lsc_g, int keep,
                             const float* __restrict__ ctcP, const float* __restrict__ nm, float th2, int W, int T,
                             int nt, int max_iters, MatchOut out) {
     constexpr int kWarps = NTHR / 32;
     constexpr int kGroups = 32 / LPS;
+    constexpr int kItems = kClItems / EPL;        // samples a lane group updates at once
     static_assert(G <= LPS, "the lanes of a group push one CTA each");
+    static_assert(LPS * EPL <= KP && kItems >= 1, "entries per group");
     extern __shared__ __align__(16) unsigned char smraw[];
     const int b = blockIdx.x / G;
     const int rank = (int)prune_cluster_rank();
@@ -630,22 +634,33 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
     // every CTA of the cluster has started before any pushes into another's shared memory
     cluster_sync_all<G>();
 
-    // the group's own sample w (own index j), lane gl holding entry gl (score x, template r): the
-    // (Cf, template, slot) maximum of the list -- largest Cf, then the lower template -- pushed into
-    // every CTA (lane g < G of the group writes CTA g)
-    auto finish_push = [&](int w, float x, int r, bool valid) {
+    // the group's own sample w (own index j), lane gl holding entries gl + LPS h (scores x[h],
+    // templates r[h]): the (Cf, template, slot) maximum of the list -- largest Cf, then the lower
+    // template -- pushed into every CTA (lane g < G of the group writes CTA g)
+    auto finish_push = [&](int w, const float (&x)[EPL], const int (&r)[EPL], bool valid) {
         unsigned long long key = 0ull;
-        if (valid && gl < keep) {
-            const float q = fmaxf(x, 0.f);
-            key = ((unsigned long long)__float_as_uint(q * q * s_inm[r]) << 32) |
-                  ((unsigned long long)(0xffffu - (unsigned)r) << 8) | (unsigned)gl;
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            const int e = gl + LPS * h;
+            if (valid && e < keep) {
+                const float q = fmaxf(x[h], 0.f);
+                const unsigned long long kh = ((unsigned long long)__float_as_uint(q * q * s_inm[r[h]]) << 32) |
+                                              ((unsigned long long)(0xffffu - (unsigned)r[h]) << 8) | (unsigned)e;
+                key = kh > key ? kh : key;
+            }
         }
 #pragma unroll
         for (int o = LPS / 2; o > 0; o >>= 1) {
             const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
             key = ok > key ? ok : key;
         }
-        const float xw = __shfl_sync(0xffffffffu, x, grp * LPS + (int)(key & 0xffu));
+        const int es = (int)(key & 0xffu);                 // the winning entry: lane es % LPS, slot es / LPS
+        float xw = 0.f;
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            const float xh = __shfl_sync(0xffffffffu, x[h], grp * LPS + es % LPS);
+            if (es / LPS == h) xw = xh;
+        }
         if (valid && gl < G) {
             const bool inner = w >= nt && w < W - nt;
             const float v = inner ? __uint_as_float((unsigned)(key >> 32)) : 0.f;
@@ -662,8 +677,14 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
         const int j = j0 + grp;
         const bool valid = j < own;
         const int w = rank + G * j;
-        const int r = valid && gl < keep ? RK[(size_t)j * ks + gl] : 0;
-        const float x = valid && gl < keep ? SC[(size_t)j * ks + gl] : 0.f;
+        int r[EPL];
+        float x[EPL];
+#pragma unroll
+        for (int h = 0; h < EPL; ++h) {
+            const int e = gl + LPS * h;
+            r[h] = valid && e < keep ? RK[(size_t)j * ks + e] : 0;
+            x[h] = valid && e < keep ? SC[(size_t)j * ks + e] : 0.f;
+        }
         finish_push(w, x, r, valid);
     }
     cluster_sync_all<G>();
@@ -774,13 +795,13 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
         __syncthreads();
         // ---- C: subtract the spikes from the listed scores of the own samples near them ----
         const int n_items = s_pre[total];
-        constexpr int kPerWarp = kClItems * kGroups;
+        constexpr int kPerWarp = kItems * kGroups;
         for (int q0 = warp * kPerWarp; q0 < n_items; q0 += kWarps * kPerWarp) {
-            int wv[kClItems], kv[kClItems], rv[kClItems], jv[kClItems];
-            float xv[kClItems], cv[kClItems], cv2[kClItems];
-            bool two[kClItems];
+            int wv[kItems], kv[kItems], jv[kItems], rv[kItems][EPL];
+            float xv[kItems][EPL], cv[kItems][EPL], cv2[kItems][EPL];
+            bool two[kItems];
 #pragma unroll
-            for (int u = 0; u < kClItems; ++u) {
+            for (int u = 0; u < kItems; ++u) {
                 const int q = q0 + u * kGroups + grp;
                 int w = -1, k = 0;
                 if (q < n_items) {
@@ -797,40 +818,54 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                 kv[u] = k;
                 jv[u] = w >= 0 ? (w - rank) / G : 0;
                 two[u] = w >= 0 && k + 1 < total && s_sw[k + 1] - nt <= w;
-                rv[u] = 0;
-                xv[u] = 0.f;
-                if (w >= 0 && gl < keep) {
-                    rv[u] = RK[(size_t)jv[u] * ks + gl];
-                    xv[u] = SC[(size_t)jv[u] * ks + gl];
+#pragma unroll
+                for (int h = 0; h < EPL; ++h) {
+                    const int e = gl + LPS * h;
+                    rv[u][h] = 0;
+                    xv[u][h] = 0.f;
+                    if (w >= 0 && e < keep) {
+                        rv[u][h] = RK[(size_t)jv[u] * ks + e];
+                        xv[u][h] = SC[(size_t)jv[u] * ks + e];
+                    }
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kClItems; ++u) {
-                cv[u] = cv2[u] = 0.f;
-                if (wv[u] >= 0 && gl < keep) {
-                    const int k = kv[u];
-                    cv[u] = __ldg(ctcP + ((int64_t)s_st[k] * L2 + (wv[u] - s_sw[k] + nt)) * T + rv[u]);
-                    if (two[u]) cv2[u] = __ldg(ctcP + ((int64_t)s_st[k + 1] * L2 + (wv[u] - s_sw[k + 1] + nt)) * T + rv[u]);
+            for (int u = 0; u < kItems; ++u) {
+#pragma unroll
+                for (int h = 0; h < EPL; ++h) {
+                    cv[u][h] = cv2[u][h] = 0.f;
+                    if (wv[u] >= 0 && gl + LPS * h < keep) {
+                        const int k = kv[u];
+                        cv[u][h] = __ldg(ctcP + ((int64_t)s_st[k] * L2 + (wv[u] - s_sw[k] + nt)) * T + rv[u][h]);
+                        if (two[u])
+                            cv2[u][h] = __ldg(ctcP + ((int64_t)s_st[k + 1] * L2 + (wv[u] - s_sw[k + 1] + nt)) * T + rv[u][h]);
+                    }
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kClItems; ++u) {
+            for (int u = 0; u < kItems; ++u) {
                 const int w = wv[u];
                 if (!__any_sync(0xffffffffu, w >= 0)) continue;
-                float x = 0.f;
-                if (w >= 0) {
-                    const int k = kv[u];
-                    x = fmaf(-s_sa[k], cv[u], xv[u]);
-                    if (two[u]) {
-                        x = fmaf(-s_sa[k + 1], cv2[u], x);
-                        for (int kk = k + 2; kk < total && s_sw[kk] - nt <= w; ++kk) {   // rare: a third
-                            const float c = gl < keep
-                                                ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u])
-                                                : 0.f;
-                            x = fmaf(-s_sa[kk], c, x);
+                float x[EPL];
+#pragma unroll
+                for (int h = 0; h < EPL; ++h) {
+                    x[h] = 0.f;
+                    const int e = gl + LPS * h;
+                    if (w >= 0) {
+                        const int k = kv[u];
+                        float xe = fmaf(-s_sa[k], cv[u][h], xv[u][h]);
+                        if (two[u]) {
+                            xe = fmaf(-s_sa[k + 1], cv2[u][h], xe);
+                            for (int kk = k + 2; kk < total && s_sw[kk] - nt <= w; ++kk) {   // rare: a third
+                                const float c = e < keep
+                                                    ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u][h])
+                                                    : 0.f;
+                                xe = fmaf(-s_sa[kk], c, xe);
+                            }
                         }
+                        if (e < keep) SC[(size_t)jv[u] * ks + e] = xe;
+                        x[h] = xe;
                     }
-                    if (gl < keep) SC[(size_t)jv[u] * ks + gl] = x;
                 }
                 finish_push(w, x, rv[u], w >= 0);
             }
@@ -893,12 +928,12 @@ static cudaError_t launch_pruned_lps(const uint16_t* lrk, float* lsc, int keep, 
     return cudaGetLastError();
 }
 
-template <int G, int NTHR, int LPS>
+template <int G, int NTHR, int LPS, int EPL>
 static cudaError_t launch_pruned_cluster(const uint16_t* lrk, const float* lsc, int keep, const float* ctcP,
                                          const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
                                          const MatchOut& out, cudaStream_t s) {
     const size_t smem = prune_cl_smem(W, T, nt, keep, G);
-    auto kern = match_pruned_cluster_kernel<G, NTHR, LPS>;
+    auto kern = match_pruned_cluster_kernel<G, NTHR, LPS, EPL>;
     cudaError_t e = raise_smem_limit((const void*)kern, smem);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
@@ -918,7 +953,7 @@ static cudaError_t launch_pruned_cluster(const uint16_t* lrk, const float* lsc, 
 
 // the cluster form when a CTA's share fits in shared memory: 4 CTAs of 512 threads per window for
 // groups (one wave for 64 windows at up to 24 listed templates), 8 CTAs for a few windows
-// (latency); lane groups of 16 (keep <= 16) or 32
+// (latency); lane groups of 16, one list entry per lane up to 16 entries, two up to 32
 static cudaError_t try_pruned_cluster(const uint16_t* lrk, const float* lsc, int keep, const float* ctcP,
                                       const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
                                       const MatchOut& out, cudaStream_t s, bool* done) {
@@ -928,11 +963,12 @@ static cudaError_t try_pruned_cluster(const uint16_t* lrk, const float* lsc, int
     *done = true;
     if (keep <= 16) {
         if (G == 8)
-            return launch_pruned_cluster<8, 512, 16>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
-        return launch_pruned_cluster<4, 512, 16>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+            return launch_pruned_cluster<8, 512, 16, 1>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+        return launch_pruned_cluster<4, 512, 16, 1>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
     }
-    if (G == 8) return launch_pruned_cluster<8, 512, 32>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
-    return launch_pruned_cluster<4, 512, 32>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+    if (G == 8)
+        return launch_pruned_cluster<8, 512, 16, 2>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
+    return launch_pruned_cluster<4, 512, 16, 2>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s);
 }
 
 cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcP, const float* nm,

@@ -65,7 +65,7 @@ def test_pruned_tier_agrees_with_full_loop_384ch(cfg_stream):
     assert a >= AGREE and amp_ok >= AGREE, (a, amp_ok, amax)
 
 
-@pytest.mark.parametrize("keep", [16, 32])
+@pytest.mark.parametrize("keep", [16, 24, 32])
 def test_pruned_tier_against_oracle_pruned_loop(cfg_stream, keep):
     """Window by window against the float64 oracle's pruned loop with the same list rule."""
     d, data, _ = cfg_stream
