@@ -558,14 +558,18 @@ constexpr int kClItems = 4;   // samples a lane group of the cluster form update
 // shared memory of one CTA: [1/nm, nm: 2T f32][accepted lists: 6 x cap][own-item starts and
 // prefix: 2 x (cap + 1) int], to 16 B; [cf, block prefix, block suffix: 3 (W + 2nt) f32][winner
 // score W f32][winner template W i32][own lists: span x ks u16, to 16 B][own scores: span x ks f32]
-__host__ __device__ inline size_t prune_cl_smem(int W, int T, int nt, int keep, int G) {
+// [the iteration's items: sample and spike, 2 x span i32]
+__host__ __device__ inline size_t prune_cl_fixed(int W, int T, int nt) {
     const size_t cap = (size_t)prune_iter_cap(W, nt);
+    return ((size_t)T * 8 + cap * 24 + (cap + 1) * 8 + cap * 4 + 15) & ~(size_t)15;
+}
+__host__ __device__ inline size_t prune_cl_smem(int W, int T, int nt, int keep, int G) {
     const size_t span = (size_t)(W + G - 1) / G;
     const size_t ks = (size_t)prune_stride(keep);
-    size_t b = ((size_t)T * 8 + cap * 24 + (cap + 1) * 8 + 15) & ~(size_t)15;
+    size_t b = prune_cl_fixed(W, T, nt);
     b += (size_t)(W + 2 * nt) * 12 + (size_t)W * 8;
     b += (span * ks * 2 + 15) & ~(size_t)15;
-    return b + span * ks * 4;
+    return b + span * ks * 4 + span * 8;
 }
 
 // EPL: list entries per lane (entry e = gl + LPS h, h < EPL), so 24 or 32 entries run on lane
@@ -600,7 +604,8 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
     float* s_sa = reinterpret_cast<float*>(s_st + cap_it);
     int* s_lo = reinterpret_cast<int*>(s_sa + cap_it);     // [cap + 1] first own sample of spike k's items
     int* s_pre = s_lo + cap_it + 1;                        // [cap + 1] own items before spike k
-    unsigned char* next = smraw + ((((size_t)T * 8 + (size_t)cap_it * 24 + (size_t)(cap_it + 1) * 8) + 15) & ~(size_t)15);
+    int* s_cb = s_pre + cap_it + 1;                        // [cap] ctcP offset of spike k's rows, less w T
+    unsigned char* next = smraw + prune_cl_fixed(W, T, nt);
     float* cf = reinterpret_cast<float*>(next);            // [n] maximum of w at cf[w + nt]
     float* pg = cf + n;
     float* ph = pg + n;
@@ -609,6 +614,8 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
     uint16_t* RK = reinterpret_cast<uint16_t*>(wt + W);    // [span][ks] own lists
     float* SC = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(RK) +
                                          ((((size_t)span * ks * 2) + 15) & ~(size_t)15));   // [span][ks]
+    int* s_itw = reinterpret_cast<int*>(SC + (size_t)span * ks);   // [span] item q's own sample
+    int* s_itk = s_itw + span;                                     // [span] and the spike that takes it
     __shared__ int s_cnt, s_over;
 
     const uint16_t* rk_g = lrk_g + (int64_t)b * W * KP;
@@ -634,42 +641,54 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
     // every CTA of the cluster has started before any pushes into another's shared memory
     cluster_sync_all<G>();
 
-    // the group's own sample w (own index j), lane gl holding entries gl + LPS h (scores x[h],
-    // templates r[h]): the (Cf, template, slot) maximum of the list -- largest Cf, then the lower
-    // template -- pushed into every CTA (lane g < G of the group writes CTA g)
+    // this layout in CTA gl of the cluster (the lanes gl < G of a group push into CTA gl): the same
+    // offsets from its shared-memory window
+    const unsigned sm_base = (unsigned)__cvta_generic_to_shared(smraw);
+    const unsigned rem = gl < G ? prune_dsmem(smraw, (unsigned)gl) : 0u;
+    const unsigned off_cf = (unsigned)__cvta_generic_to_shared(cf) - sm_base + 4u * (unsigned)nt;
+    const unsigned off_wsc = (unsigned)__cvta_generic_to_shared(wsc) - sm_base;
+    const unsigned off_wt = (unsigned)__cvta_generic_to_shared(wt) - sm_base;
+    const unsigned gmask = LPS == 32 ? 0xffffffffu : (((1u << LPS) - 1u) << (grp * LPS));
+    // the group's own sample w, lane gl holding entries gl + LPS h (scores x[h], templates r[h]):
+    // the maximum of the list -- largest Cf, then the lower template -- pushed into every CTA.
+    // Cf bits + 1 order the valid entries above every padding entry (0); the group maximum is
+    // taken on those 32 bits, and only when several lanes share it does a second reduction pick
+    // the lowest template among them.
     auto finish_push = [&](int w, const float (&x)[EPL], const int (&r)[EPL], bool valid) {
-        unsigned long long key = 0ull;
+        unsigned u = 0u, rr = 0xffffffffu;
+        float xb = 0.f;
 #pragma unroll
         for (int h = 0; h < EPL; ++h) {
             const int e = gl + LPS * h;
             if (valid && e < keep) {
                 const float q = fmaxf(x[h], 0.f);
-                const unsigned long long kh = ((unsigned long long)__float_as_uint(q * q * s_inm[r[h]]) << 32) |
-                                              ((unsigned long long)(0xffffu - (unsigned)r[h]) << 8) | (unsigned)e;
-                key = kh > key ? kh : key;
+                const unsigned uh = __float_as_uint(q * q * s_inm[r[h]]) + 1u;
+                if (uh > u || (uh == u && (unsigned)r[h] < rr)) {
+                    u = uh;
+                    rr = (unsigned)r[h];
+                    xb = x[h];
+                }
             }
         }
+        unsigned m = u;
 #pragma unroll
-        for (int o = LPS / 2; o > 0; o >>= 1) {
-            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
-            key = ok > key ? ok : key;
-        }
-        const int es = (int)(key & 0xffu);                 // the winning entry: lane es % LPS, slot es / LPS
-        float xw = 0.f;
+        for (int o = LPS / 2; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        const unsigned cand = __ballot_sync(0xffffffffu, u == m) & gmask;
+        unsigned rmin = rr;
+        if (__any_sync(0xffffffffu, __popc(cand) > 1)) {
+            rmin = u == m ? rr : 0xffffffffu;
 #pragma unroll
-        for (int h = 0; h < EPL; ++h) {
-            const float xh = __shfl_sync(0xffffffffu, x[h], grp * LPS + es % LPS);
-            if (es / LPS == h) xw = xh;
+            for (int o = LPS / 2; o > 0; o >>= 1) rmin = min(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
         }
+        const int win = __ffs(__ballot_sync(0xffffffffu, u == m && (__popc(cand) == 1 || rr == rmin)) & gmask) - 1;
+        const float xw = __shfl_sync(0xffffffffu, xb, win);
+        const unsigned tw = __shfl_sync(0xffffffffu, rr, win);
         if (valid && gl < G) {
             const bool inner = w >= nt && w < W - nt;
-            const float v = inner ? __uint_as_float((unsigned)(key >> 32)) : 0.f;
-            const int tw = (int)(0xffffu - (unsigned)((key >> 8) & 0xffffu));
-            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(prune_dsmem(cf + w + nt, (unsigned)gl)), "f"(v)
-                         : "memory");
-            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(prune_dsmem(wsc + w, (unsigned)gl)), "f"(xw)
-                         : "memory");
-            asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(prune_dsmem(wt + w, (unsigned)gl)), "r"(tw)
+            const float v = inner && m > 0u ? __uint_as_float(m - 1u) : 0.f;
+            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(rem + off_cf + 4u * (unsigned)w), "f"(v) : "memory");
+            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(rem + off_wsc + 4u * (unsigned)w), "f"(xw) : "memory");
+            asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(rem + off_wt + 4u * (unsigned)w), "r"((int)tw)
                          : "memory");
         }
     };
@@ -752,6 +771,7 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
             s_sw[r] = w;
             s_st[r] = s_at[k];
             s_sa[r] = s_aa[k];
+            s_cb[r] = (s_at[k] * L2 + nt - w) * T;   // ctcP[t_k][w' - w + nt][t] at s_cb + w' T + t
             const int o = n_total + r;
             if (rank == 0 && o < out.cap) {
                 sp_w[o] = w;
@@ -793,6 +813,16 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
             }
         }
         __syncthreads();
+        // the item table: item q = own sample s_lo[k] + G (q - s_pre[k]) of the spike k whose
+        // items hold q (32 threads per spike)
+        for (int idx = tid; idx < total * 32; idx += NTHR) {
+            const int k = idx >> 5;
+            for (int q = s_pre[k] + (idx & 31); q < s_pre[k + 1]; q += 32) {
+                s_itw[q] = s_lo[k] + G * (q - s_pre[k]);
+                s_itk[q] = k;
+            }
+        }
+        __syncthreads();
         // ---- C: subtract the spikes from the listed scores of the own samples near them ----
         const int n_items = s_pre[total];
         constexpr int kPerWarp = kItems * kGroups;
@@ -805,14 +835,8 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                 const int q = q0 + u * kGroups + grp;
                 int w = -1, k = 0;
                 if (q < n_items) {
-                    int lo_k = 0, hi_k = total - 1;   // the last spike with s_pre[k] <= q
-                    while (lo_k < hi_k) {
-                        const int mid = (lo_k + hi_k + 1) >> 1;
-                        if (s_pre[mid] <= q) lo_k = mid;
-                        else hi_k = mid - 1;
-                    }
-                    k = lo_k;
-                    w = s_lo[k] + G * (q - s_pre[k]);
+                    w = s_itw[q];
+                    k = s_itk[q];
                 }
                 wv[u] = w;
                 kv[u] = k;
@@ -836,9 +860,9 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                     cv[u][h] = cv2[u][h] = 0.f;
                     if (wv[u] >= 0 && gl + LPS * h < keep) {
                         const int k = kv[u];
-                        cv[u][h] = __ldg(ctcP + ((int64_t)s_st[k] * L2 + (wv[u] - s_sw[k] + nt)) * T + rv[u][h]);
-                        if (two[u])
-                            cv2[u][h] = __ldg(ctcP + ((int64_t)s_st[k + 1] * L2 + (wv[u] - s_sw[k + 1] + nt)) * T + rv[u][h]);
+                        const int wo = wv[u] * T + rv[u][h];
+                        cv[u][h] = __ldg(ctcP + (s_cb[k] + wo));
+                        if (two[u]) cv2[u][h] = __ldg(ctcP + (s_cb[k + 1] + wo));
                     }
                 }
             }
@@ -857,9 +881,7 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                         if (two[u]) {
                             xe = fmaf(-s_sa[k + 1], cv2[u][h], xe);
                             for (int kk = k + 2; kk < total && s_sw[kk] - nt <= w; ++kk) {   // rare: a third
-                                const float c = e < keep
-                                                    ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u][h])
-                                                    : 0.f;
+                                const float c = e < keep ? __ldg(ctcP + (s_cb[kk] + w * T + rv[u][h])) : 0.f;
                                 xe = fmaf(-s_sa[kk], c, xe);
                             }
                         }
