@@ -54,8 +54,73 @@ colsum_kernel(const int16_t* __restrict__ raw, int64_t row_stride, const int32_t
     }
 }
 
+// The same sums with 16-byte loads, when the channels are the row's first C values (no channel
+// map), C % 8 == 0 and rows start 16-byte aligned: thread (g, p) of a block adds channels
+// 8g .. 8g+7 over the block's rows r = p (mod P), P = 256 / (C / 8); the P partial sums of a channel
+// group are added in shared memory in p order, then one 64-bit atomic per channel; one ticket per
+// window (the last row block takes the means).
+constexpr int kSumRowsV = 64;
+__global__ void __launch_bounds__(kSumThreads)
+colsum_vec_kernel(const int16_t* __restrict__ raw, int64_t row_stride, int C, int W, int NT,
+                  long long* __restrict__ colsum, int* __restrict__ ticket, float* __restrict__ mean) {
+    extern __shared__ int s_part[];   // [P][C]
+    __shared__ int s_last;
+    const int b = blockIdx.y;
+    const int r0 = blockIdx.x * kSumRowsV, r1 = min(W, r0 + kSumRowsV);
+    const int CG = C >> 3, P = kSumThreads / CG;
+    const int g = threadIdx.x % CG, p = threadIdx.x / CG;
+    if (p < P) {
+        int acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const int16_t* base = raw + (int64_t)b * NT * row_stride + 8 * g;
+        for (int r = r0 + p; r < r1; r += P) {
+            const uint4 v = __ldcs(reinterpret_cast<const uint4*>(base + (int64_t)r * row_stride));
+            const uint32_t u[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                acc[2 * e] += (int)(int16_t)(u[e] & 0xffffu);
+                acc[2 * e + 1] += (int)(int16_t)(u[e] >> 16);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s_part[p * C + 8 * g + e] = acc[e];
+    }
+    __syncthreads();
+    long long* cs = colsum + (int64_t)b * C;
+    for (int c = threadIdx.x; c < C; c += kSumThreads) {
+        int tot = 0;
+        for (int q = 0; q < P; ++q) tot += s_part[q * C + c];
+        atomicAdd(reinterpret_cast<unsigned long long*>(cs + c), (unsigned long long)(long long)tot);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int* tk = ticket + b;
+        s_last = atomicAdd(tk, 1) == (int)gridDim.x - 1;
+        if (s_last) *tk = 0;
+    }
+    __syncthreads();
+    if (s_last) {
+        for (int c = threadIdx.x; c < C; c += kSumThreads) {
+            const long long sum = __ldcg(cs + c);
+            const long long q = sum / W;
+            const int r = (int)(sum - q * W);
+            mean[(int64_t)b * C + c] = (float)q + __fdiv_rn((float)r, (float)W);
+            cs[c] = 0;
+        }
+    }
+}
+
 void launch_colsum(const int16_t* raw, int64_t row_stride, const int32_t* chan, int C, int W, int NT, int nb,
                    long long* colsum, int* ticket, float* mean, cudaStream_t s) {
+    const bool vec = !chan && C % 8 == 0 && C / 8 <= kSumThreads && (row_stride * 2) % 16 == 0 &&
+                     (reinterpret_cast<uintptr_t>(raw) & 15) == 0;
+    if (vec) {
+        const int P = kSumThreads / (C / 8);
+        dim3 grid((W + kSumRowsV - 1) / kSumRowsV, nb);
+        colsum_vec_kernel<<<grid, kSumThreads, sizeof(int) * P * C, s>>>(raw, row_stride, C, W, NT, colsum, ticket,
+                                                                          mean);
+        return;
+    }
     dim3 grid((C + kSumThreads - 1) / kSumThreads, (W + kSumRows - 1) / kSumRows, nb);
     colsum_kernel<<<grid, kSumThreads, 0, s>>>(raw, row_stride, chan, C, W, NT, colsum, ticket, mean);
 }
