@@ -216,8 +216,10 @@ __device__ __forceinline__ float bpc_value(const void* hi, const void* lo, int64
     }
 }
 
+constexpr int kNearCap = 64;   // overlapping spikes gathered per round (a multiple of 32 more than J - 1)
+
 template <int FMT, int KC>
-__global__ void __launch_bounds__(kFeatWarps * 32)
+__global__ void __launch_bounds__(kFeatWarps * 32, 4)
 features_direct_kernel(const void* __restrict__ bpc_hi, const void* __restrict__ bpc_lo, MatchOut out, int nb, int W,
                        int C, int T, int K, int nt, int nC, const float* __restrict__ wall3t,
                        const float* __restrict__ xcorr, const int64_t* __restrict__ iCC,
@@ -230,6 +232,8 @@ features_direct_kernel(const void* __restrict__ bpc_hi, const void* __restrict__
     if (KC > 0 && K != KC) return;
     extern __shared__ float s_p[];   // P[d + nt - 1][k][k'], (2 nt - 1) K K
     __shared__ float s_f[kFeatWarps][64];
+    __shared__ int s_nd[kFeatWarps][kNearCap + 32], s_ntp[kFeatWarps][kNearCap + 32];
+    __shared__ float s_na[kFeatWarps][kNearCap + 32];
     const int nd = 2 * nt - 1;
     for (int i = threadIdx.x; i < K * K * nd; i += blockDim.x) {
         const int d = i / (K * K), kk = i - d * K * K;      // xcorr is [k][k'][d]
@@ -256,28 +260,23 @@ features_direct_kernel(const void* __restrict__ bpc_hi, const void* __restrict__
 #pragma unroll
         for (int k = 0; k < KM; ++k) acc[k] = 0.f;
         // every accepted spike of the batch whose waveform overlaps this spike's nt samples
-        // (itself included); slice j takes the ones whose rank among them is j mod J
+        // (itself included), gathered in list order into the warp's table (kNearCap at a time);
+        // slice j then takes the ones whose rank among them is j mod J, all slices at once
         const int n_sp = min(out.n_spikes[b], out.cap);
         const int* sw = out.sp_w + (int64_t)b * out.cap;
         const int* st = out.sp_t + (int64_t)b * out.cap;
         const float* sa = out.sp_amp + (int64_t)b * out.cap;
-        int slice = 0;   // rank of the next overlapping spike, mod J
-        for (int i0 = 0; i0 < n_sp; i0 += 32) {
-            const int i = i0 + lane;
-            const int d = i < n_sp ? w - sw[i] : nt;
-            const bool near = d > -nt && d < nt;
-            const int ti = near ? st[i] : 0;
-            const float ai = near ? sa[i] : 0.f;
-            unsigned m = __ballot_sync(0xffffffffu, near);
-            while (m) {
-                const int src = __ffs(m) - 1;
-                m &= m - 1;
-                const int dd = __shfl_sync(0xffffffffu, d, src);
-                const int t2 = __shfl_sync(0xffffffffu, ti, src);
-                const float a2 = __shfl_sync(0xffffffffu, ai, src);
-                if (act && slice == jj) {
-                    // the neighbour's template at channel ch: Wall3[t2][k'][ch], k' = 0 .. K-1 (contiguous)
-                    const int kd = KC > 0 ? KC : K;
+        int* nd = s_nd[threadIdx.x >> 5];
+        int* ntp = s_ntp[threadIdx.x >> 5];
+        float* na = s_na[threadIdx.x >> 5];
+        const int kd = KC > 0 ? KC : K;
+        auto apply = [&](int cnt) {
+            // entries jj, jj + J, ... of the table, in order
+            if (act) {
+#pragma unroll 2
+                for (int e = jj; e < cnt; e += J) {
+                    const int dd = nd[e], t2 = ntp[e];
+                    const float a2 = na[e];
                     const float* u = wall3t + ((int64_t)t2 * C + ch) * kd;
                     const float* pd = s_p + (dd + nt - 1) * kd * kd;
                     float uk[KM];
@@ -293,9 +292,41 @@ features_direct_kernel(const void* __restrict__ bpc_hi, const void* __restrict__
                         acc[k] = fmaf(-a2, sum, acc[k]);
                     }
                 }
-                if (++slice == J) slice = 0;
             }
+            __syncwarp();
+        };
+        // the table restarts at a multiple of J entries, so an entry's rank mod J is its slice
+        int cnt = 0;
+        for (int i0 = 0; i0 < n_sp; i0 += 32) {
+            const int i = i0 + lane;
+            const int d = i < n_sp ? w - sw[i] : nt;
+            const bool near = d > -nt && d < nt;
+            const unsigned m = __ballot_sync(0xffffffffu, near);
+            if (cnt + __popc(m) > kNearCap) {
+                const int full = cnt - cnt % J;   // apply whole rounds of J, keep the rest
+                apply(full);
+                const int rest = cnt - full;
+                const int sd = lane < rest ? nd[full + lane] : 0, stt = lane < rest ? ntp[full + lane] : 0;
+                const float sav = lane < rest ? na[full + lane] : 0.f;
+                __syncwarp();
+                if (lane < rest) {
+                    nd[lane] = sd;
+                    ntp[lane] = stt;
+                    na[lane] = sav;
+                }
+                __syncwarp();
+                cnt = rest;
+            }
+            if (near) {
+                const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                nd[pos] = d;
+                ntp[pos] = st[i];
+                na[pos] = sa[i];
+            }
+            __syncwarp();
+            cnt += __popc(m);
         }
+        apply(cnt);
         // slices summed in slice order into lane n, then the convolution and the amplitude term
 #pragma unroll
         for (int k = 0; k < KM; ++k) {
