@@ -838,6 +838,9 @@ CHOSEN_CANDIDATES = [
      "bf16 splits, matching loop on each sample's 16 templates of largest initial score"),
     ("bf16x3_keep24", {"gemm_path": 3, "match_keep": 24},
      "bf16 splits, matching loop on each sample's 24 templates of largest initial score"),
+    ("bf16x3_keep16w24", {"gemm_path": 3, "match_keep": 16, "match_keep_wide": 24, "match_keep_crowd": 0.5},
+     "bf16 splits, matching loop on each sample's 16 templates of largest initial score, 24 where the 16th "
+     "largest initial Cf exceeds Th^2 / 2 (crowded samples)"),
     ("bf16x1_rescore", {"gemm_path": 4, "match_keep": 0},
      "one BF16 product (kind::f16), fp32 accumulate, accepted candidates re-scored in FP32"),
     ("fp8_rescore", {"gemm_path": 5, "match_keep": 0},

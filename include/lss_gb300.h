@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define LSS_ABI_VERSION 2
+#define LSS_ABI_VERSION 3
 #define LSS_MAX_PCFEAT 64 /* nearest channels x PCs carried per spike */
 
 enum lss_status {
@@ -88,6 +88,11 @@ typedef struct lss_params {
                                filters each window alone. */
     float highpass_hz;      /* edge of mode 1 (default 300, Kilosort's) */
     float sample_rate_hz;   /* sample rate of mode 1 (default 30000) */
+    int32_t match_keep_wide;  /* 0 = every sample lists match_keep templates; match_keep < n <= 32 = a crowded
+                                 sample lists n: one whose match_keep-th largest initial Cf exceeds
+                                 match_keep_crowd * Th^2 (the templates a larger overlapping spike outranks
+                                 there are the ones a short list misses) */
+    float match_keep_crowd;   /* the crowding threshold of match_keep_wide, in units of Th^2 (default 0.5) */
 } lss_params;
 
 /* One sorted spike.  time is the stream sample (Kilosort template_matching.py:68). */

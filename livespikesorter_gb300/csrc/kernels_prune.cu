@@ -77,10 +77,13 @@ __device__ __forceinline__ uint32_t kth_key_bits(const uint32_t (&key)[NJ], int 
 // The keep-th largest Cf is found by an MSB-first bitwise selection over the warp's keys (one
 // ballot-count per bit, stopping once a single key matches the prefix); every key above it is
 // taken, then the ties at it in ascending template order until keep are taken.
+// Widened lists (keep_wide > keep): a crowded sample -- its keep-th largest Cf above crowd_cf --
+// takes keep_wide templates by the same rule; the others take keep, their entries keep ..
+// keep_wide-1 marked kListPad.
 template <int NJ>
 __global__ void __launch_bounds__(kSelWarps * 32)
 prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, int nb, int W, int T, int keep,
-                    uint16_t* __restrict__ lrk, float* __restrict__ lsc) {
+                    int keep_wide, float crowd_cf, uint16_t* __restrict__ lrk, float* __restrict__ lsc) {
     __shared__ float s_inm[32 * NJ];
     __shared__ uint32_t s_cand[kSelWarps * 64];
     for (int t = threadIdx.x; t < T; t += kSelWarps * 32) s_inm[t] = 1.f / nm[t];   // as the loop computes it
@@ -116,12 +119,13 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
             const bool up = ((lane & k2) == 0) == ((lane & j2) == 0);
             v = up ? min(v, o) : max(v, o);
         }
-    const uint32_t bound = __shfl_sync(0xffffffffu, v, keep - 1);
+    const int kw = max(keep, keep_wide);   // the longest list a sample may take
+    const uint32_t bound = __shfl_sync(0xffffffffu, v, kw - 1);
     int n_cand = 0;
 #pragma unroll
     for (int j = 0; j < NJ; ++j) n_cand += key[j] <= bound;
     n_cand = __reduce_add_sync(0xffffffffu, n_cand);
-    uint32_t prefix = 0;
+    uint32_t prefix = 0, prefix_w = 0;
     if (n_cand <= 64) {
         uint32_t* cand = s_cand + (threadIdx.x >> 5) * 64;
         int base = 0;
@@ -139,15 +143,20 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
         ck[1] = lane + 32 < n_cand ? cand[lane + 32] : 0xffffffffu;
         __syncwarp();
         prefix = kth_key_bits<2>(ck, keep - 1, n_cand);
+        if (kw > keep) prefix_w = kth_key_bits<2>(ck, kw - 1, n_cand);
     } else {
         prefix = kth_key_bits<NJ>(key, keep - 1, 32 * NJ);
+        if (kw > keep) prefix_w = kth_key_bits<NJ>(key, kw - 1, 32 * NJ);
     }
-    const uint32_t thr = prefix;
+    // crowded: the keep-th largest Cf (the key's value, Cf >= 0) above crowd_cf
+    const bool crowded = kw > keep && __uint_as_float(~prefix & 0x7fffffffu) > crowd_cf;
+    const int cnt = crowded ? kw : keep;
+    const uint32_t thr = crowded ? prefix_w : prefix;
     int below = 0;   // keys strictly before the threshold (larger Cf): all taken
 #pragma unroll
     for (int j = 0; j < NJ; ++j) below += key[j] < thr;
     below = __reduce_add_sync(0xffffffffu, below);
-    int ties_left = keep - below;
+    int ties_left = cnt - below;
     // compaction of the taken templates into lanes 0..keep-1, in template order
     int pos = 0, my_t = -1;
     const uint32_t lt = (1u << lane) - 1u;
@@ -164,20 +173,24 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
         if (want >= 0 && want < __popc(m)) my_t = (int)__fns(m, 0u, want + 1) + 32 * j;   // its (want+1)-th set bit
         pos += __popc(m);
     }
-    if (lane < keep) {
+    if (lane < cnt) {
         const int64_t o = g * KP + lane;
         lrk[o] = (uint16_t)my_t;
         lsc[o] = row[my_t];
+    } else if (lane < kw) {
+        const int64_t o = g * KP + lane;
+        lrk[o] = kListPad;
+        lsc[o] = 0.f;
     }
 }
 
 void launch_prune_select(const float* Bt, const float* nm, int nb, int W, int T, int keep, uint16_t* lrk, float* lsc,
-                         cudaStream_t s) {
+                         cudaStream_t s, int keep_wide, float crowd_cf) {
     const int64_t warps = (int64_t)nb * W;
     const dim3 grid((unsigned)((warps + kSelWarps - 1) / kSelWarps));
     const int nj = (T + 31) / 32;
 #define LSS_SEL(N) \
-    prune_select_kernel<N><<<grid, kSelWarps * 32, 0, s>>>(Bt, nm, nb, W, T, keep, lrk, lsc)
+    prune_select_kernel<N><<<grid, kSelWarps * 32, 0, s>>>(Bt, nm, nb, W, T, keep, keep_wide, crowd_cf, lrk, lsc)
     if (nj <= 4) LSS_SEL(4);
     else if (nj <= 8) LSS_SEL(8);
     else if (nj <= 16) LSS_SEL(16);
@@ -301,7 +314,7 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
     auto finish = [&](int w, float x, int r, bool valid) {
         float best = -1.f;
         int bt = INT_MAX, bs = 0;
-        if (valid && gl < keep) {
+        if (valid && gl < keep && r != kListPad) {
             const float q = fmaxf(x, 0.f);
             best = q * q * s_inm[r];
             bt = r;
@@ -467,7 +480,7 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
 #pragma unroll
             for (int u = 0; u < kItemsPerGroup; ++u) {
                 cv[u] = cv2[u] = 0.f;
-                if (wv[u] >= 0 && gl < keep) {
+                if (wv[u] >= 0 && gl < keep && rv[u] != kListPad) {
                     const int k = kv[u];
                     cv[u] = __ldg(ctcP + ((int64_t)s_st[k] * L2 + (wv[u] - s_sw[k] + nt)) * T + rv[u]);
                     if (two[u]) cv2[u] = __ldg(ctcP + ((int64_t)s_st[k + 1] * L2 + (wv[u] - s_sw[k + 1] + nt)) * T + rv[u]);
@@ -486,12 +499,13 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
                 if (two[u]) {
                     x = fmaf(-s_sa[k + 1], cv2[u], x);
                     for (int kk = k + 2; kk < total && s_sw[kk] - nt <= w; ++kk) {   // rare: a third
-                        const float c =
-                            gl < keep ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u]) : 0.f;
+                        const float c = gl < keep && rv[u] != kListPad
+                                            ? __ldg(ctcP + ((int64_t)s_st[kk] * L2 + (w - s_sw[kk] + nt)) * T + rv[u])
+                                            : 0.f;
                         x = fmaf(-s_sa[kk], c, x);
                     }
                 }
-                if (gl < keep) {
+                if (gl < keep && rv[u] != kListPad) {
                     SC[(size_t)w * ss + gl] = x;
                     const float qv = fmaxf(x, 0.f);
                     const float cfv = qv * qv * s_inm[rv[u]];
@@ -654,13 +668,15 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
     // Cf bits + 1 order the valid entries above every padding entry (0); the group maximum is
     // taken on those 32 bits, and only when several lanes share it does a second reduction pick
     // the lowest template among them.
-    auto finish_push = [&](int w, const float (&x)[EPL], const int (&r)[EPL], bool valid) {
+    // hn: the entry slots in use (warp-uniform; the second slot of widened lists is all padding at
+    // most samples, and then skipped)
+    auto finish_push = [&](int w, const float (&x)[EPL], const int (&r)[EPL], bool valid, int hn) {
         unsigned u = 0u, rr = 0xffffffffu;
         float xb = 0.f;
 #pragma unroll
         for (int h = 0; h < EPL; ++h) {
             const int e = gl + LPS * h;
-            if (valid && e < keep) {
+            if (h < hn && valid && e < keep && r[h] != kListPad) {
                 const float q = fmaxf(x[h], 0.f);
                 const unsigned uh = __float_as_uint(q * q * s_inm[r[h]]) + 1u;
                 if (uh > u || (uh == u && (unsigned)r[h] < rr)) {
@@ -704,7 +720,7 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
             r[h] = valid && e < keep ? RK[(size_t)j * ks + e] : 0;
             x[h] = valid && e < keep ? SC[(size_t)j * ks + e] : 0.f;
         }
-        finish_push(w, x, r, valid);
+        finish_push(w, x, r, valid, EPL);
     }
     cluster_sync_all<G>();
 
@@ -827,7 +843,7 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
         const int n_items = s_pre[total];
         constexpr int kPerWarp = kItems * kGroups;
         for (int q0 = warp * kPerWarp; q0 < n_items; q0 += kWarps * kPerWarp) {
-            int wv[kItems], kv[kItems], jv[kItems], rv[kItems][EPL];
+            int wv[kItems], kv[kItems], jv[kItems], rv[kItems][EPL], hn[kItems];
             float xv[kItems][EPL], cv[kItems][EPL], cv2[kItems][EPL];
             bool two[kItems];
 #pragma unroll
@@ -852,13 +868,18 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                         xv[u][h] = SC[(size_t)jv[u] * ks + e];
                     }
                 }
+                // the slots any lane of the warp uses for this item
+                hn[u] = 1;
+#pragma unroll
+                for (int h = 1; h < EPL; ++h)
+                    if (__any_sync(0xffffffffu, w >= 0 && gl + LPS * h < keep && rv[u][h] != kListPad)) hn[u] = h + 1;
             }
 #pragma unroll
             for (int u = 0; u < kItems; ++u) {
 #pragma unroll
                 for (int h = 0; h < EPL; ++h) {
                     cv[u][h] = cv2[u][h] = 0.f;
-                    if (wv[u] >= 0 && gl + LPS * h < keep) {
+                    if (h < hn[u] && wv[u] >= 0 && gl + LPS * h < keep && rv[u][h] != kListPad) {
                         const int k = kv[u];
                         const int wo = wv[u] * T + rv[u][h];
                         cv[u][h] = __ldg(ctcP + (s_cb[k] + wo));
@@ -875,21 +896,23 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                 for (int h = 0; h < EPL; ++h) {
                     x[h] = 0.f;
                     const int e = gl + LPS * h;
-                    if (w >= 0) {
+                    if (h < hn[u] && w >= 0) {
                         const int k = kv[u];
                         float xe = fmaf(-s_sa[k], cv[u][h], xv[u][h]);
                         if (two[u]) {
                             xe = fmaf(-s_sa[k + 1], cv2[u][h], xe);
                             for (int kk = k + 2; kk < total && s_sw[kk] - nt <= w; ++kk) {   // rare: a third
-                                const float c = e < keep ? __ldg(ctcP + (s_cb[kk] + w * T + rv[u][h])) : 0.f;
+                                const float c = e < keep && rv[u][h] != kListPad
+                                                    ? __ldg(ctcP + (s_cb[kk] + w * T + rv[u][h]))
+                                                    : 0.f;
                                 xe = fmaf(-s_sa[kk], c, xe);
                             }
                         }
-                        if (e < keep) SC[(size_t)jv[u] * ks + e] = xe;
+                        if (e < keep && rv[u][h] != kListPad) SC[(size_t)jv[u] * ks + e] = xe;
                         x[h] = xe;
                     }
                 }
-                finish_push(w, x, rv[u], w >= 0);
+                finish_push(w, x, rv[u], w >= 0, hn[u]);
             }
         }
         n_total += total;

@@ -206,9 +206,10 @@ cudaError_t launch_residual(float* Xres, const float* pre_wf, const MatchOut& ou
 // pruned matching tier (kernels_prune.cu): per sample the keep (<= kPruneKeepMax) templates of
 // largest initial Cf, lists lrk / lsc [nb][W][kPruneKeepMax]; the loop on those lists
 constexpr int kPruneKeepMax = 32;
+constexpr uint16_t kListPad = 0xffffu;   // an unused list entry (a sample whose list is shorter)
 constexpr int kPruneThreads = 1024;
 void launch_prune_select(const float* Bt, const float* nm, int nb, int W, int T, int keep, uint16_t* lrk, float* lsc,
-                         cudaStream_t s);
+                         cudaStream_t s, int keep_wide = 0, float crowd_cf = 0.f);
 // cf_scratch [nb][W + 2nt] and slot_scratch [nb][W] hold the per-sample maxima of windows whose
 // maxima do not fit in shared memory (prune_mode without bit 0); may be null otherwise
 cudaError_t launch_match_pruned(const uint16_t* lrk, float* lsc, int keep, const float* ctcP, const float* nm,

@@ -247,8 +247,10 @@ struct Handle {
     // templates are numbered internally by their position along the probe (tmpl_orig[internal] =
     // the oss_input row), so templates that overlap in space have nearby numbers
     std::vector<int32_t> tmpl_orig;
-    // pruned matching tier (match_keep > 0): per-sample lists of internal ids and scores
-    int keep = 0;
+    // pruned matching tier (match_keep > 0): per-sample lists of internal ids and scores; crowded
+    // samples list keep_list (> keep) templates when match_keep_wide is set
+    int keep = 0, keep_list = 0;
+    float crowd_cf = 0.f;
     uint16_t* d_lid = nullptr;          // [nb][W][kPruneKeepMax] internal template ids
     float* d_lsc = nullptr;             // [nb][W][kPruneKeepMax] scores
     float* d_pcf = nullptr;             // [nb][W + 2nt] per-sample maxima of windows too long for shared memory
@@ -603,6 +605,12 @@ void Handle::init(const char* dir, const lss_params* prm) {
         throw LoadError{LSS_ERR_ARG, "lss_params.match_keep must be 0 (full loop) or 1.." + std::to_string(kPruneKeepMax)};
     keep = std::min(p.match_keep, T);
     if (keep > 0 && T > 1024) throw LoadError{LSS_ERR_ARG, "the pruned matching tier takes at most 1024 templates"};
+    if (p.match_keep_wide != 0 && (p.match_keep <= 0 || p.match_keep_wide <= p.match_keep ||
+                                   p.match_keep_wide > kPruneKeepMax || !(p.match_keep_crowd >= 0.f)))
+        throw LoadError{LSS_ERR_ARG, "lss_params.match_keep_wide must be 0 or in (match_keep, " +
+                                         std::to_string(kPruneKeepMax) + "], with match_keep_crowd >= 0"};
+    keep_list = keep > 0 && p.match_keep_wide > 0 ? std::min(p.match_keep_wide, T) : keep;
+    crowd_cf = p.match_keep_crowd * th * th;
     if (iir) {
         d_iir_state = dev_alloc<float4>((size_t)C, dev_bytes);
         d_iir_pow = dev_upload(iir_pow, dev_bytes, st);
@@ -743,7 +751,7 @@ void Handle::ensure_work(int Wn, int nb) {
     if (keep > 0) {
         d_lid = dev_alloc<uint16_t>((size_t)nba * Wa * kPruneKeepMax, dev_bytes);
         d_lsc = dev_alloc<float>((size_t)nba * Wa * kPruneKeepMax, dev_bytes);
-        const int pm = prune_mode(Wa, T, nt, keep);
+        const int pm = prune_mode(Wa, T, nt, keep_list);
         if (pm < 0) throw LoadError{LSS_ERR_ARG, "window too long for the pruned matching tier"};
         if (!(pm & 1)) {
             d_pcf = dev_alloc<float>((size_t)nba * (Wa + 2 * nt), dev_bytes);
@@ -976,9 +984,9 @@ void Handle::run_match(int nb, int Wn, int64_t& nl) {
     LSS_CUDA(cudaMemsetAsync(mo.status, 0, sizeof(int) * nb, st));
     const bool resid = !direct_feat || debug_run;
     if (keep > 0) {
-        launch_prune_select(d_Bt, d_nm, nb, Wn, T, keep, d_lid, d_lsc, st);
+        launch_prune_select(d_Bt, d_nm, nb, Wn, T, keep, d_lid, d_lsc, st, keep_list, crowd_cf);
         LSS_CUDA(cudaGetLastError());
-        LSS_CUDA(launch_match_pruned(d_lid, d_lsc, keep, d_ctcP, d_nm, th * th, Wn, T, nt, max_iters, nb, d_pcf,
+        LSS_CUDA(launch_match_pruned(d_lid, d_lsc, keep_list, d_ctcP, d_nm, th * th, Wn, T, nt, max_iters, nb, d_pcf,
                                      d_pslot, mo, st));
         nl += 2;   // selection, loop
         if (resid) {
@@ -1318,6 +1326,8 @@ int lss_default_params(lss_params* p) {
     p->highpass_mode = 0;
     p->highpass_hz = 300.f;
     p->sample_rate_hz = 30000.f;
+    p->match_keep_wide = 0;
+    p->match_keep_crowd = 0.5f;
     return LSS_OK;
 }
 

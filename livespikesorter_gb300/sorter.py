@@ -19,7 +19,7 @@ import numpy as np
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = Path(os.environ.get("LSS_GB300_LIB", _PKG / "lib" / "liblss_gb300.so"))
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_PCFEAT = 64
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_FORMAT", 4: "ERR_CUDA", 5: "ERR_NOMEM",
           6: "ERR_OVERFLOW", 7: "ERR_STATE", 8: "ERR_INTERNAL"}
@@ -33,7 +33,8 @@ class Params(ct.Structure):
                 ("spike_cap", ct.c_int32), ("mem_budget", ct.c_int64), ("profile", ct.c_int32),
                 ("match_variant", ct.c_int32), ("gemm_path", ct.c_int32), ("cluster_rule", ct.c_int32),
                 ("cluster_radius_um", ct.c_float), ("match_keep", ct.c_int32),
-                ("highpass_mode", ct.c_int32), ("highpass_hz", ct.c_float), ("sample_rate_hz", ct.c_float)]
+                ("highpass_mode", ct.c_int32), ("highpass_hz", ct.c_float), ("sample_rate_hz", ct.c_float),
+                ("match_keep_wide", ct.c_int32), ("match_keep_crowd", ct.c_float)]
 
 
 class Spike(ct.Structure):

@@ -81,11 +81,13 @@ def project_rounded(U2, Bpc2, fmt: str, act_scale=None):
 
 
 def run_matching_variant(X, U, W, ctc, Th, fmt="exact", rescore=False, keep=None, max_iters=50, block=1,
-                         act_scale=None):
+                         act_scale=None, keep_wide=None, crowd=0.5):
     """-> (st [S, 2] (sample, template), amps [S]).  See the module docstring.  block > 1: one list
     per block of that many consecutive samples (from sample 0), the keep templates of largest Cq
     maximum over the block's samples, scored at every sample of the block.  act_scale: static
-    activation scales (``calibrate_act_scale``) for an FP8 format."""
+    activation scales (``calibrate_act_scale``) for an FP8 format.  keep_wide (> keep): a crowded
+    sample -- its keep-th largest Cq above crowd * Th^2 -- lists keep_wide templates instead of keep
+    (the sorter's match_keep_wide / match_keep_crowd)."""
     U = np.asarray(U, np.float64)
     ctc = np.asarray(ctc, np.float64)
     nt = W.shape[1]
@@ -104,8 +106,12 @@ def run_matching_variant(X, U, W, ctc, Th, fmt="exact", rescore=False, keep=None
                 mask[np.ix_(top, np.arange(w0, min(nw, w0 + block)))] = True
         else:
             # the keep largest per sample, ties to the lower template (a stable sort of -Cq)
-            top = np.argsort(-Cq, axis=0, kind="stable")[:keep]
-            mask[top, np.arange(B0e.shape[1])[None, :]] = True
+            order = np.argsort(-Cq, axis=0, kind="stable")
+            cols = np.arange(B0e.shape[1])
+            mask[order[:keep], cols[None, :]] = True
+            if keep_wide is not None and keep_wide > keep:
+                crowded = Cq[order[keep - 1], cols] > crowd * Th ** 2
+                mask[order[keep:keep_wide][:, crowded], cols[crowded][None, :]] = True
         B, D = np.where(mask, B0e, -1e30), None
     else:
         B, D = B0q.copy(), B0e - B0q

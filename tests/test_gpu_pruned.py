@@ -86,6 +86,35 @@ def test_pruned_tier_against_oracle_pruned_loop(cfg_stream, keep):
     assert n_match / n_ref >= AGREE and n_amp / n_match >= AGREE, (n_match / n_ref, n_amp / n_match)
 
 
+def test_widened_lists(cfg_stream):
+    """match_keep_wide: with no sample crowded the spikes are the 16-entry lists' bit for bit (the
+    widened loop skips the padding entries); with crowded samples at Th^2 / 2 they agree with the
+    float64 oracle's pruned loop under the same rule at >= 99.5 %."""
+    d, data, _ = cfg_stream
+    oss = ko.load_oss_input(d)
+    nt, nt0 = oss.wPCA.shape[1], oss.nt0min
+    wins = np.stack([data[k * 1500: k * 1500 + 1622] for k in (1, 2, 3)])
+    outs = {}
+    for name, kw in (("k16", {}), ("none", dict(match_keep_wide=24, match_keep_crowd=1e30)),
+                     ("half", dict(match_keep_wide=24, match_keep_crowd=0.5))):
+        with sorter.OnlineSorter(d, max_iters=50, group_batches=3, match_keep=16, **kw) as s:
+            outs[name] = s.sort_windows(wins)
+    for a, b in zip(outs["k16"], outs["none"]):
+        for f in ("time", "tmpl", "amp", "iter", "x", "y", "pcfeat"):
+            np.testing.assert_array_equal(a[f], b[f], err_msg=f)
+    n_ref = n_match = n_amp = 0.0
+    for win, sp in zip(wins, outs["half"]):
+        X = ko.preprocess(win.T, oss)
+        st, amps = po.run_matching_variant(X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned, keep=16, keep_wide=24,
+                                           crowd=0.5, max_iters=50)
+        a, amp_ok, _ = agreement(st[:, 0] - nt // 2 + nt0, st[:, 1], amps, sp["time"], sp["tmpl"], sp["amp"])
+        n_ref += len(st)
+        n_match += a * max(len(st), len(sp))
+        n_amp += amp_ok * a * max(len(st), len(sp))
+    assert n_ref > 300
+    assert n_match / n_ref >= AGREE and n_amp / n_match >= AGREE, (n_match / n_ref, n_amp / n_match)
+
+
 def test_pruned_tier_dense_overlapping(cfg_dense):
     """30 Hz with 30 % of the spikes overlapping: against the float64 oracle's full loop."""
     d, data, _ = cfg_dense
@@ -126,3 +155,8 @@ def test_match_keep_is_validated(golden_dir, tmp_path):
     with pytest.raises(sorter.SorterError) as e:
         sorter.OnlineSorter(d, match_keep=33)
     assert e.value.status == 1
+    for bad in (dict(match_keep=16, match_keep_wide=16), dict(match_keep=16, match_keep_wide=33),
+                dict(match_keep=0, match_keep_wide=24), dict(match_keep=16, match_keep_wide=24, match_keep_crowd=-1.0)):
+        with pytest.raises(sorter.SorterError) as e:
+            sorter.OnlineSorter(d, **bad)
+        assert e.value.status == 1, bad

@@ -81,3 +81,21 @@ def test_static_rescored_variant_keeps_exact_amplitudes(window):
         n += 1
     assert n > 0
     np.testing.assert_allclose(amps[:n], ref.amps[:n], rtol=1e-9)
+
+
+def test_widened_lists_between_the_fixed_lengths(window):
+    """Widened lists (keep_wide at crowded samples): with no sample crowded they are the keep-entry
+    lists, with every sample crowded the keep_wide-entry ones."""
+    X, oss, it = window
+    T = oss.Wall3.shape[0]
+    k, kw = 4, 8
+    assert T > kw
+    args = (X, oss.Wall3, oss.wPCA, oss.ctc, oss.th_learned)
+    fixed_k = po.run_matching_variant(*args, keep=k, max_iters=it)
+    fixed_kw = po.run_matching_variant(*args, keep=kw, max_iters=it)
+    none = po.run_matching_variant(*args, keep=k, keep_wide=kw, crowd=np.inf, max_iters=it)
+    every = po.run_matching_variant(*args, keep=k, keep_wide=kw, crowd=-1.0, max_iters=it)
+    np.testing.assert_array_equal(none[0], fixed_k[0])
+    np.testing.assert_array_equal(none[1], fixed_k[1])
+    np.testing.assert_array_equal(every[0], fixed_kw[0])
+    np.testing.assert_array_equal(every[1], fixed_kw[1])
