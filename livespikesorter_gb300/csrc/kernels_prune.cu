@@ -567,7 +567,7 @@ __device__ __forceinline__ unsigned prune_dsmem(const void* local, unsigned rank
     return r;
 }
 
-constexpr int kClItems = 4;   // samples a lane group of the cluster form updates at once
+constexpr int kClItems = 2;   // samples a lane group of the cluster form updates at once (2, 3, 4 measured: 2 best)
 
 // shared memory of one CTA: [1/nm, nm: 2T f32][accepted lists: 6 x cap][own-item starts and
 // prefix: 2 x (cap + 1) int], to 16 B; [cf, block prefix, block suffix: 3 (W + 2nt) f32][winner
@@ -595,7 +595,7 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                             int nt, int max_iters, MatchOut out) {
     constexpr int kWarps = NTHR / 32;
     constexpr int kGroups = 32 / LPS;
-    constexpr int kItems = kClItems / EPL;        // samples a lane group updates at once
+    constexpr int kItems = kClItems;              // samples a lane group updates at once
     static_assert(G <= LPS, "the lanes of a group push one CTA each");
     static_assert(LPS * EPL <= KP && kItems >= 1, "entries per group");
     extern __shared__ __align__(16) unsigned char smraw[];
