@@ -70,6 +70,8 @@ def args_():
     ap.add_argument("--match-variant", type=int, default=0, help="0 auto, 1 scores in L2, 2 scores in SMEM")
     ap.add_argument("--match-keep", type=int, default=0,
                     help="match_keep of the measured path (0 = Kilosort's loop over every template)")
+    ap.add_argument("--match-keep-wide", type=int, default=0,
+                    help="match_keep_wide of the measured path (crowded samples' list length; 0 = fixed lists)")
     ap.add_argument("--gemm-path", type=int, default=0,
                     help="0 tcgen05 FP32 (3xTF32), 1 FP32 SIMT, 2 tcgen05 with TF32 data (two products)")
     ap.add_argument("--no-tier", action="store_true", help="skip the chosen-tier measurement")
@@ -345,7 +347,8 @@ def run_gpu(a):
     base_ptr = d_data.data_ptr()
     row_bytes = C * 2
     s = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1,
-                           match_variant=a.match_variant, gemm_path=a.gemm_path, match_keep=a.match_keep)
+                           match_variant=a.match_variant, gemm_path=a.gemm_path, match_keep=a.match_keep,
+                           match_keep_wide=a.match_keep_wide if a.match_keep else 0)
     ext = torch.cuda.ExternalStream(s.cuda_stream(), device=f"cuda:{dev}")
     spikes_seen = [0]
 
@@ -396,7 +399,8 @@ def run_gpu(a):
     def batch_latency(path, n, keep=0):
         """push-to-spikes wall time of single 1500-sample batches (one batch per launch)"""
         s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1, profile=1,
-                                 match_variant=a.match_variant, gemm_path=path, match_keep=keep)
+                                 match_variant=a.match_variant, gemm_path=path, match_keep=keep,
+                                 match_keep_wide=a.match_keep_wide if keep else 0)
         lat = []
         s3.push(data[:NT + 2 * nt], 0)
         drain(s3)
@@ -525,7 +529,8 @@ def run_gpu(a):
 
     # ---- end to end through the host API ---------------------------------------------------
     s2 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
-                             match_variant=a.match_variant, gemm_path=a.gemm_path, match_keep=a.match_keep)
+                             match_variant=a.match_variant, gemm_path=a.gemm_path, match_keep=a.match_keep,
+                             match_keep_wide=a.match_keep_wide if a.match_keep else 0)
     chunk = G * NT
     pos = [0]
     # the caller's rows live in pinned host memory (the e2e contract); the API copies page-locked
