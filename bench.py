@@ -72,6 +72,8 @@ def args_():
                     help="match_keep of the measured path (0 = Kilosort's loop over every template)")
     ap.add_argument("--match-keep-wide", type=int, default=0,
                     help="match_keep_wide of the measured path (crowded samples' list length; 0 = fixed lists)")
+    ap.add_argument("--match-keep-crowd", type=float, default=0.5,
+                    help="match_keep_crowd of the measured path (crowded: the match_keep-th largest Cf above this x Th^2)")
     ap.add_argument("--gemm-path", type=int, default=0,
                     help="0 tcgen05 FP32 (3xTF32), 1 FP32 SIMT, 2 tcgen05 with TF32 data (two products)")
     ap.add_argument("--no-tier", action="store_true", help="skip the chosen-tier measurement")
@@ -348,7 +350,8 @@ def run_gpu(a):
     row_bytes = C * 2
     s = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G, profile=1,
                            match_variant=a.match_variant, gemm_path=a.gemm_path, match_keep=a.match_keep,
-                           match_keep_wide=a.match_keep_wide if a.match_keep else 0)
+                           match_keep_wide=a.match_keep_wide if a.match_keep else 0,
+                           match_keep_crowd=a.match_keep_crowd)
     ext = torch.cuda.ExternalStream(s.cuda_stream(), device=f"cuda:{dev}")
     spikes_seen = [0]
 
@@ -400,7 +403,8 @@ def run_gpu(a):
         """push-to-spikes wall time of single 1500-sample batches (one batch per launch)"""
         s3 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=1, profile=1,
                                  match_variant=a.match_variant, gemm_path=path, match_keep=keep,
-                                 match_keep_wide=a.match_keep_wide if keep else 0)
+                                 match_keep_wide=a.match_keep_wide if keep else 0,
+                                 match_keep_crowd=a.match_keep_crowd)
         lat = []
         s3.push(data[:NT + 2 * nt], 0)
         drain(s3)
@@ -530,7 +534,8 @@ def run_gpu(a):
     # ---- end to end through the host API ---------------------------------------------------
     s2 = sorter.OnlineSorter(oss_dir, device=dev, batch_samples=NT, max_iters=50, group_batches=G,
                              match_variant=a.match_variant, gemm_path=a.gemm_path, match_keep=a.match_keep,
-                             match_keep_wide=a.match_keep_wide if a.match_keep else 0)
+                             match_keep_wide=a.match_keep_wide if a.match_keep else 0,
+                           match_keep_crowd=a.match_keep_crowd)
     chunk = G * NT
     pos = [0]
     # the caller's rows live in pinned host memory (the e2e contract); the API copies page-locked

@@ -143,13 +143,23 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
         ck[1] = lane + 32 < n_cand ? cand[lane + 32] : 0xffffffffu;
         __syncwarp();
         prefix = kth_key_bits<2>(ck, keep - 1, n_cand);
-        if (kw > keep) prefix_w = kth_key_bits<2>(ck, kw - 1, n_cand);
     } else {
         prefix = kth_key_bits<NJ>(key, keep - 1, 32 * NJ);
-        if (kw > keep) prefix_w = kth_key_bits<NJ>(key, kw - 1, 32 * NJ);
     }
-    // crowded: the keep-th largest Cf (the key's value, Cf >= 0) above crowd_cf
+    // crowded: the keep-th largest Cf (the key's value, Cf >= 0) above crowd_cf; only then the
+    // kw-th key (the warp's decision: one sample per warp)
     const bool crowded = kw > keep && __uint_as_float(~prefix & 0x7fffffffu) > crowd_cf;
+    if (crowded) {
+        if (n_cand <= 64) {
+            uint32_t* cand = s_cand + (threadIdx.x >> 5) * 64;
+            uint32_t ck[2];
+            ck[0] = lane < n_cand ? cand[lane] : 0xffffffffu;
+            ck[1] = lane + 32 < n_cand ? cand[lane + 32] : 0xffffffffu;
+            prefix_w = kth_key_bits<2>(ck, kw - 1, n_cand);
+        } else {
+            prefix_w = kth_key_bits<NJ>(key, kw - 1, 32 * NJ);
+        }
+    }
     const int cnt = crowded ? kw : keep;
     const uint32_t thr = crowded ? prefix_w : prefix;
     int below = 0;   // keys strictly before the threshold (larger Cf): all taken
