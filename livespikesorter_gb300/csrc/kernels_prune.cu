@@ -587,20 +587,24 @@ __host__ __device__ inline size_t prune_cl_fixed(int W, int T, int nt) {
     const size_t cap = (size_t)prune_iter_cap(W, nt);
     return ((size_t)T * 8 + cap * 24 + (cap + 1) * 8 + cap * 4 + 15) & ~(size_t)15;
 }
+// the cluster form's lane groups: 16 lanes, one list entry each in shared memory; entries 16 and
+// up (24- or 32-entry lists, or widened lists at crowded samples) stay in the global lists, so the
+// shared-memory footprint -- and the L1 left for the ctc gathers -- is the 16-entry one
+constexpr int kClLanes = 16;
 __host__ __device__ inline size_t prune_cl_smem(int W, int T, int nt, int keep, int G) {
     const size_t span = (size_t)(W + G - 1) / G;
-    const size_t ks = (size_t)prune_stride(keep);
+    const size_t ks = (size_t)prune_stride(keep < kClLanes ? keep : kClLanes);
     size_t b = prune_cl_fixed(W, T, nt);
     b += (size_t)(W + 2 * nt) * 12 + (size_t)W * 8;
     b += (span * ks * 2 + 15) & ~(size_t)15;
-    return b + span * ks * 4 + span * 8;
+    return b + span * ks * 4 + span * 8 + span;
 }
 
 // EPL: list entries per lane (entry e = gl + LPS h, h < EPL), so 24 or 32 entries run on lane
 // groups of 16 -- two samples per warp, as at 16 entries -- instead of groups of 32
 template <int G, int NTHR, int LPS, int EPL>
 __global__ void __launch_bounds__(NTHR, 2)
-match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __restrict__ lsc_g, int keep,
+match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_g, int keep,
                             const float* __restrict__ ctcP, const float* __restrict__ nm, float th2, int W, int T,
                             int nt, int max_iters, MatchOut out) {
     constexpr int kWarps = NTHR / 32;
@@ -608,6 +612,7 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
     constexpr int kItems = kClItems;              // samples a lane group updates at once
     static_assert(G <= LPS, "the lanes of a group push one CTA each");
     static_assert(LPS * EPL <= KP && kItems >= 1, "entries per group");
+    static_assert(LPS == kClLanes, "shared-memory list width");
     extern __shared__ __align__(16) unsigned char smraw[];
     const int b = blockIdx.x / G;
     const int rank = (int)prune_cluster_rank();
@@ -617,7 +622,7 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
     const int cap_it = prune_iter_cap(W, nt);
     const int span = (W + G - 1) / G;
     const int own = rank < W ? (W - rank + G - 1) / G : 0;
-    const int ks = prune_stride(keep);
+    const int ks = prune_stride(min(keep, LPS));   // shared-memory list stride: entries < LPS
     float* s_inm = reinterpret_cast<float*>(smraw);
     float* s_nm = s_inm + T;
     int* s_aw = reinterpret_cast<int*>(s_nm + T);
@@ -640,16 +645,19 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                                          ((((size_t)span * ks * 2) + 15) & ~(size_t)15));   // [span][ks]
     int* s_itw = reinterpret_cast<int*>(SC + (size_t)span * ks);   // [span] item q's own sample
     int* s_itk = s_itw + span;                                     // [span] and the spike that takes it
+    unsigned char* s_wide = reinterpret_cast<unsigned char*>(s_itk + span);   // [span] entries >= LPS in use
     __shared__ int s_cnt, s_over;
 
     const uint16_t* rk_g = lrk_g + (int64_t)b * W * KP;
-    const float* sc_g = lsc_g + (int64_t)b * W * KP;
+    float* sc_g = lsc_g + (int64_t)b * W * KP;   // entries >= LPS are read and updated here
     for (int q = tid; q < own * ks; q += NTHR) {
         const int j = q / ks, i = q - j * ks;
         const int w = rank + G * j;
         RK[q] = i < keep ? rk_g[(size_t)w * KP + i] : (uint16_t)0;
         SC[q] = i < keep ? sc_g[(size_t)w * KP + i] : 0.f;
     }
+    for (int j = tid; j < own; j += NTHR)
+        s_wide[j] = keep > LPS && rk_g[(size_t)(rank + G * j) * KP + LPS] != kListPad;
     for (int t = tid; t < T; t += NTHR) {
         s_nm[t] = nm[t];
         s_inm[t] = 1.f / nm[t];
@@ -727,8 +735,9 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
 #pragma unroll
         for (int h = 0; h < EPL; ++h) {
             const int e = gl + LPS * h;
-            r[h] = valid && e < keep ? RK[(size_t)j * ks + e] : 0;
-            x[h] = valid && e < keep ? SC[(size_t)j * ks + e] : 0.f;
+            const bool in = valid && e < keep && (h == 0 || s_wide[j]);
+            r[h] = !in ? (int)kListPad : h == 0 ? RK[(size_t)j * ks + e] : rk_g[(size_t)w * KP + e];
+            x[h] = !in ? 0.f : h == 0 ? SC[(size_t)j * ks + e] : sc_g[(size_t)w * KP + e];
         }
         finish_push(w, x, r, valid, EPL);
     }
@@ -868,21 +877,19 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                 kv[u] = k;
                 jv[u] = w >= 0 ? (w - rank) / G : 0;
                 two[u] = w >= 0 && k + 1 < total && s_sw[k + 1] - nt <= w;
+                const bool wide = w >= 0 && s_wide[jv[u]];
 #pragma unroll
                 for (int h = 0; h < EPL; ++h) {
                     const int e = gl + LPS * h;
-                    rv[u][h] = 0;
+                    rv[u][h] = kListPad;
                     xv[u][h] = 0.f;
-                    if (w >= 0 && e < keep) {
-                        rv[u][h] = RK[(size_t)jv[u] * ks + e];
-                        xv[u][h] = SC[(size_t)jv[u] * ks + e];
+                    if (w >= 0 && e < keep && (h == 0 || wide)) {
+                        rv[u][h] = h == 0 ? RK[(size_t)jv[u] * ks + e] : rk_g[(size_t)w * KP + e];
+                        xv[u][h] = h == 0 ? SC[(size_t)jv[u] * ks + e] : sc_g[(size_t)w * KP + e];
                     }
                 }
                 // the slots any lane of the warp uses for this item
-                hn[u] = 1;
-#pragma unroll
-                for (int h = 1; h < EPL; ++h)
-                    if (__any_sync(0xffffffffu, w >= 0 && gl + LPS * h < keep && rv[u][h] != kListPad)) hn[u] = h + 1;
+                hn[u] = EPL > 1 && __any_sync(0xffffffffu, wide) ? EPL : 1;
             }
 #pragma unroll
             for (int u = 0; u < kItems; ++u) {
@@ -918,7 +925,10 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, const float* __r
                                 xe = fmaf(-s_sa[kk], c, xe);
                             }
                         }
-                        if (e < keep && rv[u][h] != kListPad) SC[(size_t)jv[u] * ks + e] = xe;
+                        if (e < keep && rv[u][h] != kListPad) {
+                            if (h == 0) SC[(size_t)jv[u] * ks + e] = xe;
+                            else sc_g[(size_t)w * KP + e] = xe;
+                        }
                         x[h] = xe;
                     }
                 }
@@ -984,7 +994,7 @@ static cudaError_t launch_pruned_lps(const uint16_t* lrk, float* lsc, int keep, 
 }
 
 template <int G, int NTHR, int LPS, int EPL>
-static cudaError_t launch_pruned_cluster(const uint16_t* lrk, const float* lsc, int keep, const float* ctcP,
+static cudaError_t launch_pruned_cluster(const uint16_t* lrk, float* lsc, int keep, const float* ctcP,
                                          const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
                                          const MatchOut& out, cudaStream_t s) {
     const size_t smem = prune_cl_smem(W, T, nt, keep, G);
@@ -1009,7 +1019,7 @@ static cudaError_t launch_pruned_cluster(const uint16_t* lrk, const float* lsc, 
 // the cluster form when a CTA's share fits in shared memory: 4 CTAs of 512 threads per window for
 // groups (one wave for 64 windows at up to 24 listed templates), 8 CTAs for a few windows
 // (latency); lane groups of 16, one list entry per lane up to 16 entries, two up to 32
-static cudaError_t try_pruned_cluster(const uint16_t* lrk, const float* lsc, int keep, const float* ctcP,
+static cudaError_t try_pruned_cluster(const uint16_t* lrk, float* lsc, int keep, const float* ctcP,
                                       const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
                                       const MatchOut& out, cudaStream_t s, bool* done) {
     *done = false;
