@@ -175,7 +175,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 umma_gemm_3xtf32(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
                  const __grid_constant__ CUtensorMap tB_hi, const __grid_constant__ CUtensorMap tB_lo, UmmaArgs args) {
     constexpr int kBN = BN;
-    constexpr int kTmemCols = 2 * kBN;   // two accumulators (256 or 512 columns, a power of two)
+    // two accumulators at columns 0 and kBN; the allocation is a power of two (256 or 512)
+    constexpr int kTmemCols = 2 * kBN <= 256 ? 256 : 512;
     constexpr int kKE = LOWP == 2 ? 4 * kBK : (BF16 ? 2 * kBK : kBK);   // elements per K-step (64 bytes of each row)
     constexpr int kTileB = kBN * kBK * 4;
     constexpr int kStageBytes = LOWP ? kTileA + kTileB : 2 * kTileA + 2 * kTileB;
@@ -830,9 +831,14 @@ struct UmmaOperands {
     const float* col_scale = nullptr;   // per output column (B row) scale applied in the epilogue
     int rows_a = 0, rows_b = 0, K = 0;
     int cols_a = 0;           // Toeplitz: columns of A (wrapped window length, padded)
+    int bn = 256;             // plain mode: output columns per tile (the B map's box rows)
 };
 
 constexpr int kPlainBN = 256;
+constexpr int kNarrowBN = 192;
+// output columns per tile of a plain GEMM with N columns: 192 where it tiles N exactly (192, 384:
+// the whitening of 384 channels wastes no quarter of its MMAs on padding), else 256
+static int plain_bn(int64_t n) { return (n == kNarrowBN || n == 2 * kNarrowBN) ? kNarrowBN : kPlainBN; }
 template <int BN>
 constexpr int smem_bytes() {
     return (kSmemBudget / (2 * kTileA + 2 * BN * kBK * 4)) * (2 * kTileA + 2 * BN * kBK * 4) + 1024;
@@ -849,10 +855,11 @@ UmmaOperands* umma_make(const float* a_hi, const float* a_lo, int64_t rows_a, co
     u->rows_a = (int)rows_a;
     u->rows_b = (int)rows_b;
     u->K = K;
+    u->bn = plain_bn(rows_b);
     u->has_a_lo = a_lo != nullptr;
     if (!a_lo) a_lo = a_hi;   // the map is never used
     if (!make_map(&u->a_hi, a_hi, rows_a, K, kBM) || !make_map(&u->a_lo, a_lo, rows_a, K, kBM) ||
-        !make_map(&u->b_hi, b_hi, rows_b, K, kPlainBN) || !make_map(&u->b_lo, b_lo, rows_b, K, kPlainBN)) {
+        !make_map(&u->b_hi, b_hi, rows_b, K, u->bn) || !make_map(&u->b_lo, b_lo, rows_b, K, u->bn)) {
         delete u;
         return nullptr;
     }
@@ -867,8 +874,9 @@ UmmaOperands* umma_make_bf16(const void* a_hi, const void* a_lo, int64_t rows_a,
     u->rows_a = (int)rows_a;
     u->rows_b = (int)rows_b;
     u->K = K;
+    u->bn = plain_bn(rows_b);
     if (!make_map_bf16(&u->a_hi, a_hi, rows_a, K, kBM) || !make_map_bf16(&u->a_lo, a_lo, rows_a, K, kBM) ||
-        !make_map_bf16(&u->b_hi, b_hi, rows_b, K, kPlainBN) || !make_map_bf16(&u->b_lo, b_lo, rows_b, K, kPlainBN)) {
+        !make_map_bf16(&u->b_hi, b_hi, rows_b, K, u->bn) || !make_map_bf16(&u->b_lo, b_lo, rows_b, K, u->bn)) {
         delete u;
         return nullptr;
     }
@@ -951,17 +959,23 @@ cudaError_t launch_umma_gemm(const UmmaOperands* u, float* Cm, int M, int N, int
     return launch_umma_gemm_zt(u, Cm, M, N, ldc, nullptr, nullptr, 1, 0, err, s);
 }
 
-cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* zt_hi,
+template <int BN>
+static cudaError_t launch_zt_bn(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* zt_hi,
                                 float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s, bool zt_bf16) {
-    if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
-    if (zt_hi && (wlen <= 0 || zpitch < wlen || (zt_bf16 && !zt_lo))) return cudaErrorInvalidValue;
-    if (!Cm && !zt_hi) return cudaErrorInvalidValue;
-    auto kern = u->lowp == 2  ? umma_gemm_3xtf32<kPlainBN, kPlain, true, false, 2>
-                : u->lowp == 1 ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true, 1>
-                : u->bf16     ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
-                : u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true>
-                              : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
-    const int smem = u->lowp ? smem_bytes_lowp<kPlainBN>() : smem_bytes<kPlainBN>();
+    void (*kern)(CUtensorMap, CUtensorMap, CUtensorMap, CUtensorMap, UmmaArgs) = nullptr;
+    if constexpr (BN == kPlainBN) {
+        kern = u->lowp == 2  ? umma_gemm_3xtf32<BN, kPlain, true, false, 2>
+               : u->lowp == 1 ? umma_gemm_3xtf32<BN, kPlain, true, true, 1>
+               : u->bf16     ? umma_gemm_3xtf32<BN, kPlain, true, true>
+               : u->has_a_lo ? umma_gemm_3xtf32<BN, kPlain, true>
+                             : umma_gemm_3xtf32<BN, kPlain, false>;
+    } else {
+        if (u->lowp) return cudaErrorInvalidValue;   // the low-precision operands are made with 256-row tiles
+        kern = u->bf16 ? umma_gemm_3xtf32<BN, kPlain, true, true>
+               : u->has_a_lo ? umma_gemm_3xtf32<BN, kPlain, true>
+                             : umma_gemm_3xtf32<BN, kPlain, false>;
+    }
+    const int smem = u->lowp ? smem_bytes_lowp<BN>() : smem_bytes<BN>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
     UmmaArgs a{};
@@ -979,10 +993,20 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
     a.col_scale = u->col_scale;
     a.slices = 1;
     int grid = 0;
-    const cudaError_t ge = gemm_grid((int64_t)((N + kPlainBN - 1) / kPlainBN) * ((M + kBM - 1) / kBM), grid);
+    const cudaError_t ge = gemm_grid((int64_t)((N + BN - 1) / BN) * ((M + kBM - 1) / kBM), grid);
     if (ge != cudaSuccess) return ge;
     kern<<<grid, kGemmThreads, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     return cudaGetLastError();
+}
+
+cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* zt_hi,
+                                float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s, bool zt_bf16) {
+    if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN) return cudaErrorInvalidValue;
+    if (zt_hi && (wlen <= 0 || zpitch < wlen || (zt_bf16 && !zt_lo))) return cudaErrorInvalidValue;
+    if (!Cm && !zt_hi) return cudaErrorInvalidValue;
+    if (u->bn == kNarrowBN)
+        return launch_zt_bn<kNarrowBN>(u, Cm, M, N, ldc, zt_hi, zt_lo, wlen, zpitch, err, s, zt_bf16);
+    return launch_zt_bn<kPlainBN>(u, Cm, M, N, ldc, zt_hi, zt_lo, wlen, zpitch, err, s, zt_bf16);
 }
 
 // C[m][n] = sum over the slices of ws[s][m][n], in slice order
@@ -997,19 +1021,23 @@ __global__ void sum_slices_kernel(const float* __restrict__ ws, float* __restric
     }
 }
 
-cudaError_t launch_umma_gemm_splitk(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* ws, int S,
-                                    int* err, cudaStream_t s) {
-    if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN || S < 1 || !ws)
-        return cudaErrorInvalidValue;
-    const int nk = u->K / (u->lowp == 2 ? 4 * kBK : (u->bf16 ? 2 * kBK : kBK));
-    S = std::min(S, nk);
-    if (S <= 1) return launch_umma_gemm(u, Cm, M, N, ldc, err, s);
-    auto kern = u->lowp == 2  ? umma_gemm_3xtf32<kPlainBN, kPlain, true, false, 2>
-                : u->lowp == 1 ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true, 1>
-                : u->bf16     ? umma_gemm_3xtf32<kPlainBN, kPlain, true, true>
-                : u->has_a_lo ? umma_gemm_3xtf32<kPlainBN, kPlain, true>
-                              : umma_gemm_3xtf32<kPlainBN, kPlain, false>;
-    const int smem = u->lowp ? smem_bytes_lowp<kPlainBN>() : smem_bytes<kPlainBN>();
+template <int BN>
+static cudaError_t launch_splitk_bn(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* ws, int S,
+                                   int* err, cudaStream_t s) {
+    void (*kern)(CUtensorMap, CUtensorMap, CUtensorMap, CUtensorMap, UmmaArgs) = nullptr;
+    if constexpr (BN == kPlainBN) {
+        kern = u->lowp == 2  ? umma_gemm_3xtf32<BN, kPlain, true, false, 2>
+               : u->lowp == 1 ? umma_gemm_3xtf32<BN, kPlain, true, true, 1>
+               : u->bf16     ? umma_gemm_3xtf32<BN, kPlain, true, true>
+               : u->has_a_lo ? umma_gemm_3xtf32<BN, kPlain, true>
+                             : umma_gemm_3xtf32<BN, kPlain, false>;
+    } else {
+        if (u->lowp) return cudaErrorInvalidValue;
+        kern = u->bf16 ? umma_gemm_3xtf32<BN, kPlain, true, true>
+               : u->has_a_lo ? umma_gemm_3xtf32<BN, kPlain, true>
+                             : umma_gemm_3xtf32<BN, kPlain, false>;
+    }
+    const int smem = u->lowp ? smem_bytes_lowp<BN>() : smem_bytes<BN>();
     const cudaError_t attr_err = raise_smem_limit((const void*)kern, smem);
     if (attr_err != cudaSuccess) return attr_err;
     UmmaArgs a{};
@@ -1023,12 +1051,23 @@ cudaError_t launch_umma_gemm_splitk(const UmmaOperands* u, float* Cm, int M, int
     a.col_scale = u->col_scale;   // the slices are scaled before they are summed: sum(s x) = s sum(x) up to rounding
     a.slices = S;
     int grid = 0;
-    const cudaError_t ge = gemm_grid((int64_t)((N + kPlainBN - 1) / kPlainBN) * ((M + kBM - 1) / kBM) * S, grid);
+    const cudaError_t ge = gemm_grid((int64_t)((N + BN - 1) / BN) * ((M + kBM - 1) / kBM) * S, grid);
     if (ge != cudaSuccess) return ge;
     kern<<<grid, kGemmThreads, smem, s>>>(u->a_hi, u->a_lo, u->b_hi, u->b_lo, a);
     const int blocks = (int)std::min<int64_t>(((int64_t)M * N + 255) / 256, 2048);
     sum_slices_kernel<<<blocks, 256, 0, s>>>(ws, Cm, M, N, ldc, S);
     return cudaGetLastError();
+}
+
+cudaError_t launch_umma_gemm_splitk(const UmmaOperands* u, float* Cm, int M, int N, int64_t ldc, float* ws, int S,
+                                    int* err, cudaStream_t s) {
+    if (!u || M > u->rows_a || N > u->rows_b || N > 2 * kPlainBN || S < 1 || !ws)
+        return cudaErrorInvalidValue;
+    const int nk = u->K / (u->lowp == 2 ? 4 * kBK : (u->bf16 ? 2 * kBK : kBK));
+    S = std::min(S, nk);
+    if (S <= 1) return launch_umma_gemm(u, Cm, M, N, ldc, err, s);
+    if (u->bn == kNarrowBN) return launch_splitk_bn<kNarrowBN>(u, Cm, M, N, ldc, ws, S, err, s);
+    return launch_splitk_bn<kPlainBN>(u, Cm, M, N, ldc, ws, S, err, s);
 }
 
 // Y[b][w][c] (tf32 split) = circular high-pass of nb windows held channel-major in the operands
