@@ -17,14 +17,21 @@
 // warp (its lanes on the listed entries of one sample) reads a few neighbouring cache lines of one
 // row of ctcP instead of one line per entry.
 //
+// Widened lists: a sample whose keep-th largest initial Cf is high (crowded -- a larger spike
+// nearby outranks the templates a short list misses) lists keep_wide templates; the others list
+// keep and mark the rest kListPad, which both loop forms skip.
+//
 // Layouts (device):
-//   lrk   u16 [nb][W][KP]     listed templates of sample w, ascending (KP = kPruneKeepMax slots, keep used)
+//   lrk   u16 [nb][W][KP]     listed templates of sample w, ascending (KP = kPruneKeepMax slots, keep used;
+//                             kListPad past a short list)
 //   lsc   f32 [nb][W][KP]     their running scores (initial B on entry), updated in place
 //   ctcP  f32 [T][2nt+1][T]   ctcP[s][l][t] = ctc[t][s][l]
 //
-// The loop kernel runs one CTA of 1024 threads per window; the per-sample maxima, the listed
-// templates and their scores live in shared memory as far as they fit (all three for windows up
-// to ~1700 samples at 16 entries), the rest in global memory (L2).
+// The loop runs on a thread-block cluster per window where a CTA's share fits in shared memory
+// (4 CTAs of 512 threads for groups, 8 for a few windows; each CTA owns every G-th sample and its
+// first 16 list entries, the rest of a list staying in lsc), else on one CTA of 1024 threads per
+// window with the per-sample maxima, the listed templates and their scores in shared memory as far
+// as they fit (all three for windows up to ~1700 samples at 16 entries), the rest in global memory.
 #include "lss_kernels.cuh"
 
 #include <cfloat>

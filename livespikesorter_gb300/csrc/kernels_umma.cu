@@ -1105,7 +1105,7 @@ cudaError_t launch_umma_highpass(const UmmaOperands* u, float* Y_hi, float* Y_lo
     return launch_highpass_tile<kHighpassTileSmall>(u, Y_hi, Y_lo, nb, C, W, err, s);
 }
 
-// ---- tensor-core basis convolution: geometry, strips, maps, launch ----
+// ---- tensor-core basis convolution: geometry, band tiles, maps, launch ----
 bool conv_tc_geometry(int nt, int K, ConvGeometry& g, bool bf16) {
     if (K < 1 || K > kConvMaxK || nt < 1) return false;
     const int H = nt / 2;
@@ -1198,7 +1198,7 @@ static bool make_map_pitched_bf16(CUtensorMap* m, const void* ptr, uint64_t rows
 ConvOperands* conv_tc_make(const float* zt_hi, const float* zt_lo, int64_t rows, int wlen, int zpitch,
                            const float* s_hi, const float* s_lo, int K, const ConvGeometry& g) {
     if (g.bf16) {
-        // BF16 splits: A and the strips are bf16 arrays (the three products need both lo parts)
+        // BF16 splits: A and the band tiles are bf16 arrays (the three products need both lo parts)
         if (!zt_lo) return nullptr;
         auto* u = new ConvOperands();
         u->K = K;

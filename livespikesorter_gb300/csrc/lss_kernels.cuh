@@ -171,7 +171,7 @@ cudaError_t launch_umma_gemm_zt(const UmmaOperands* u, float* Cm, int M, int N, 
                                 float* zt_lo, int wlen, int zpitch, int* err, cudaStream_t s, bool zt_bf16 = false);
 
 // temporal basis convolution on the tensor cores (kernels_umma.cu): Bpc[b][w][k][c] from the
-// channel-major whitened windows Zt[(b, c)][time] and one band strip per component
+// channel-major whitened windows Zt[(b, c)][time] and the components' band tiles of every K-step
 struct ConvGeometry {
     bool bf16 = false;  // operands are BF16 splits (kind::f16) instead of TF32 splits
     int step = 16;      // input times per K-step: 64-byte rows, 16 fp32 or 32 bf16

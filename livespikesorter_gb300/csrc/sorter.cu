@@ -94,7 +94,7 @@ struct TapSet {
     int pitch = 0;
     UmmaOperands* um[2] = {};
     // tensor-core basis convolution: maps over the channel-major whitened windows (row pitch
-    // zpitch = W rounded up to 4) and the component strips
+    // zpitch = W rounded up to 8) and the band tiles
     int zpitch = 0;
     ConvOperands* conv = nullptr;
 };
