@@ -93,6 +93,7 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
                     int keep_wide, float crowd_cf, uint16_t* __restrict__ lrk, float* __restrict__ lsc) {
     __shared__ float s_inm[32 * NJ];
     __shared__ uint32_t s_cand[kSelWarps * 64];
+    __shared__ uint16_t s_cand_t[kSelWarps * 64];   // their templates (candidate order = template order)
     for (int t = threadIdx.x; t < T; t += kSelWarps * 32) s_inm[t] = 1.f / nm[t];   // as the loop computes it
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -141,7 +142,10 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
         for (int j = 0; j < NJ; ++j) {
             const bool c = key[j] <= bound;
             const unsigned m = __ballot_sync(0xffffffffu, c);
-            if (c) cand[base + __popc(m & lt0)] = key[j];
+            if (c) {
+                cand[base + __popc(m & lt0)] = key[j];
+                s_cand_t[(threadIdx.x >> 5) * 64 + base + __popc(m & lt0)] = (uint16_t)(lane + 32 * j);
+            }
             base += __popc(m);
         }
         __syncwarp();
@@ -169,6 +173,38 @@ prune_select_kernel(const float* __restrict__ Bt, const float* __restrict__ nm, 
     }
     const int cnt = crowded ? kw : keep;
     const uint32_t thr = crowded ? prefix_w : prefix;
+    if (n_cand <= 64) {
+        // the taken keys are all among the candidates (kept in template order): those before the
+        // threshold, then its ties in template order until cnt, each written at its rank
+        const uint32_t* cand = s_cand + (threadIdx.x >> 5) * 64;
+        const uint16_t* cand_t = s_cand_t + (threadIdx.x >> 5) * 64;
+        uint32_t ck[2];
+        ck[0] = lane < n_cand ? cand[lane] : 0xffffffffu;
+        ck[1] = lane + 32 < n_cand ? cand[lane + 32] : 0xffffffffu;
+        const int below_c = __reduce_add_sync(0xffffffffu, (int)(ck[0] < thr) + (int)(ck[1] < thr));
+        int ties_c = cnt - below_c, pos = 0;
+        const uint32_t ltc = (1u << lane) - 1u;
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const bool tie = ck[i] == thr;
+            const unsigned tm = __ballot_sync(0xffffffffu, tie);
+            const bool take = ck[i] < thr || (tie && __popc(tm & ltc) < ties_c);
+            ties_c -= min(__popc(tm), max(ties_c, 0));
+            const unsigned m = __ballot_sync(0xffffffffu, take);
+            if (take) {
+                const int t = cand_t[lane + 32 * i];
+                const int64_t o = g * KP + pos + __popc(m & ltc);
+                lrk[o] = (uint16_t)t;
+                lsc[o] = row[t];
+            }
+            pos += __popc(m);
+        }
+        if (lane >= cnt && lane < kw) {
+            lrk[g * KP + lane] = kListPad;
+            lsc[g * KP + lane] = 0.f;
+        }
+        return;
+    }
     int below = 0;   // keys strictly before the threshold (larger Cf): all taken
 #pragma unroll
     for (int j = 0; j < NJ; ++j) below += key[j] < thr;
