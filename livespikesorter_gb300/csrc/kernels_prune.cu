@@ -1060,10 +1060,6 @@ static cudaError_t launch_pruned_cluster(const uint16_t* lrk, float* lsc, int ke
     auto kern = match_pruned_cluster_kernel<G, NTHR, LPS, EPL>;
     cudaError_t e = raise_smem_limit((const void*)kern, smem);
     if (e != cudaSuccess) return e;
-    if (G > 8) {
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        if (e != cudaSuccess) return e;
-    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(nb * G));
     cfg.blockDim = dim3(NTHR);
@@ -1079,58 +1075,20 @@ static cudaError_t launch_pruned_cluster(const uint16_t* lrk, float* lsc, int ke
     return cudaLaunchKernelEx(&cfg, kern, lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, out);
 }
 
-// Can a cluster of 16 CTAs of the pruned loop (EPL list entries per lane) be resident on this
-// device at this shape?  (16 is above the portable cluster size; the answer is kept per shape.)
-template <int EPL>
-static bool pruned16_ok(int W, int T, int nt, int keep) {
-    static thread_local int cW = -1, cT = -1, cnt = -1, ckeep = -1;
-    static thread_local bool cres = false;
-    if (W == cW && T == cT && nt == cnt && keep == ckeep) return cres;
-    cW = W, cT = T, cnt = nt, ckeep = keep;
-    cres = false;
-    const size_t smem = prune_cl_smem(W, T, nt, keep, 16);
-    if (smem + 1024 > (size_t)prune_smem_max()) return cres;
-    auto kern = match_pruned_cluster_kernel<16, 512, 16, EPL>;
-    if (raise_smem_limit((const void*)kern, smem) != cudaSuccess ||
-        cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-        cudaGetLastError();
-        return cres;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(16);
-    cfg.blockDim = dim3(512);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 16;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
-        cudaGetLastError();
-        return cres;
-    }
-    cres = n > 0;
-    return cres;
-}
-
 // the cluster form when a CTA's share fits in shared memory: 4 CTAs of 512 threads per window for
-// groups (one wave for 64 windows at up to 24 listed templates), 8 CTAs for a few windows and 16
-// for one or two (latency: a CTA updates a sixteenth of the window's samples per iteration); lane
-// groups of 16, one list entry per lane up to 16 entries, two up to 32
+// groups (one wave for 64 windows at up to 24 listed templates), 8 CTAs for a few windows
+// (latency); lane groups of 16, one list entry per lane up to 16 entries, two up to 32
 static cudaError_t try_pruned_cluster(const uint16_t* lrk, float* lsc, int keep, const float* ctcP,
                                       const float* nm, float th2, int W, int T, int nt, int max_iters, int nb,
                                       const MatchOut& out, cudaStream_t s, bool* done) {
     *done = false;
-    int G = nb <= 8 ? 8 : 4;
+    const int G = nb <= 8 ? 8 : 4;
     if (W < 2 * G * nt || prune_cl_smem(W, T, nt, keep, G) + 1024 > (size_t)prune_smem_max()) return cudaSuccess;
     *done = true;
 #define LSS_PCL(GG, EE) \
     launch_pruned_cluster<GG, 512, 16, EE>(lrk, lsc, keep, ctcP, nm, th2, W, T, nt, max_iters, nb, out, s)
-    if (keep <= 16) return G == 16 ? LSS_PCL(16, 1) : G == 8 ? LSS_PCL(8, 1) : LSS_PCL(4, 1);
-    return G == 16 ? LSS_PCL(16, 2) : G == 8 ? LSS_PCL(8, 2) : LSS_PCL(4, 2);
+    if (keep <= 16) return G == 8 ? LSS_PCL(8, 1) : LSS_PCL(4, 1);
+    return G == 8 ? LSS_PCL(8, 2) : LSS_PCL(4, 2);
 #undef LSS_PCL
 }
 
