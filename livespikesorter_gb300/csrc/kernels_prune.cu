@@ -600,8 +600,10 @@ match_pruned_kernel(const uint16_t* __restrict__ lrk_g, float* __restrict__ lsc_
 // scores.  Every CTA keeps a replica of every sample's maximum Cf and of the template and score
 // behind it; an owner pushes the new values of the samples it updates into all G CTAs through
 // distributed shared memory.  So every CTA finds the same accepted spikes (max pool, threshold)
-// and ranks them the same way on its own, and phase C updates the own samples near them: one
-// cluster barrier per iteration.
+// and ranks them the same way on its own, and phase C updates the own samples near them.  Two
+// cluster barriers per iteration: one between the acceptance and the first push (its arrival
+// and wait split around the ranking), so that no CTA's replica changes while it is read, and one
+// after phase C, so that every replica is whole before the next max pool.
 // ---------------------------------------------------------------------------------------------
 template <int G>
 __device__ __forceinline__ void cluster_sync_all() {
