@@ -181,6 +181,11 @@ class ClockSampler:
                  "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once nvidia-smi has initialised and sampled once: its start-up
+            # competes with the timed launches otherwise
+            t_end = time.perf_counter() + 3.0
+            while not self.lines and self.proc.poll() is None and time.perf_counter() < t_end:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
