@@ -115,6 +115,47 @@ def test_widened_lists(cfg_stream):
     assert n_match / n_ref >= AGREE and n_amp / n_match >= AGREE, (n_match / n_ref, n_amp / n_match)
 
 
+def test_concurrent_pruned_streams_equal_alone(cfg_stream):
+    """Eight handles of the chosen tier's arithmetic (BF16 splits, 16 listed templates, 24 at
+    crowded samples) pushing single batches from their own host threads at once -- cluster loops of
+    different streams sharing SMs, so CTAs of one cluster run at different speeds -- give, bit for
+    bit, the spikes one handle gives alone."""
+    import threading
+    d, data, _ = cfg_stream
+    kw = dict(batch_samples=1500, max_iters=50, gemm_path=3, match_keep=16, match_keep_wide=24, match_keep_crowd=0.5)
+    with sorter.OnlineSorter(d, **kw) as s:
+        alone = s.sort_stream(data, chunk=1500)
+    assert len(alone) > 300
+    n = 8
+    results, errors = [None] * n, []
+    barrier = threading.Barrier(n)
+
+    def run(i):
+        try:
+            with sorter.OnlineSorter(d, **kw) as s:
+                barrier.wait()
+                got = []
+                for pos in range(0, data.shape[0], 1500):
+                    s.push(data[pos:pos + 1500])
+                    got.append(s.poll())
+                s.flush()
+                got.append(s.poll_all())
+                results[i] = np.concatenate(got)
+        except Exception as e:   # surfaced below, after every thread finished
+            errors.append(e)
+
+    th = [threading.Thread(target=run, args=(i,)) for i in range(n)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+    for got in results:
+        assert len(got) == len(alone)
+        for f in ("time", "tmpl", "cluster", "amp", "x", "y", "pcfeat"):
+            np.testing.assert_array_equal(got[f], alone[f], err_msg=f)
+
+
 def test_pruned_tier_dense_overlapping(cfg_dense):
     """30 Hz with 30 % of the spikes overlapping: against the float64 oracle's full loop."""
     d, data, _ = cfg_dense
