@@ -1006,19 +1006,19 @@ match_pruned_cluster_kernel(const uint16_t* __restrict__ lrk_g, float* __restric
     }
 }
 
-static int g_prune_smem_max = -1;
-
+// the opt-in shared memory per block, queried once (a function-local static: initialised once even
+// when several host threads drive handles at the same time)
 static int prune_smem_max() {
-    if (g_prune_smem_max < 0) {
-        int dev = 0, v = 0;
+    static const int v = [] {
+        int dev = 0, r = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+            cudaDeviceGetAttribute(&r, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
             cudaGetLastError();
-            v = 0;
+            r = 0;
         }
-        g_prune_smem_max = v;
-    }
-    return g_prune_smem_max;
+        return r;
+    }();
+    return v;
 }
 
 // where the per-sample state of a window goes: bit 0 = maxima and slots in shared memory, bit 1 =

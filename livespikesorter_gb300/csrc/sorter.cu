@@ -1281,7 +1281,6 @@ namespace lss {
 // message of the last failure of a call that has no handle (lss_open, lss_match_noalloc)
 thread_local std::string g_handleless_error;
 }
-static std::string& g_open_error = lss::g_handleless_error;
 
 #define LSS_TRY(hptr, ...)                                                                         \
     try {                                                                                          \
@@ -1341,15 +1340,15 @@ int lss_open(const char* oss_dir, const lss_params* p, lss_handle** out) {
         *out = h;
         return LSS_OK;
     } catch (const lss::LoadError& e) {
-        g_open_error = e.msg;
+        lss::g_handleless_error = e.msg;
         delete h;
         return e.status;
     } catch (const lss::CudaError& e) {
-        g_open_error = e.msg;
+        lss::g_handleless_error = e.msg;
         delete h;
         return LSS_ERR_CUDA;
     } catch (const std::exception& e) {
-        g_open_error = e.what();
+        lss::g_handleless_error = e.what();
         delete h;
         return LSS_ERR_INTERNAL;
     }
@@ -1393,16 +1392,16 @@ int lss_validate_oss_input(const char* oss_dir, lss_info* info) {
             info->dup_bins = (int32_t)m.dup_bins;
             info->th = m.th;
         }
-        g_open_error.clear();
+        lss::g_handleless_error.clear();
         return LSS_OK;
     } catch (const lss::LoadError& e) {
-        g_open_error = e.msg;
+        lss::g_handleless_error = e.msg;
         return e.status;
     } catch (const std::bad_alloc&) {
-        g_open_error = "host allocation failed";
+        lss::g_handleless_error = "host allocation failed";
         return LSS_ERR_NOMEM;
     } catch (const std::exception& e) {
-        g_open_error = e.what();
+        lss::g_handleless_error = e.what();
         return LSS_ERR_INTERNAL;
     }
 }
@@ -1470,7 +1469,7 @@ int lss_close(lss_handle* hp) {
 }
 
 const char* lss_last_error(const lss_handle* hp) {
-    if (!hp) return g_open_error.c_str();
+    if (!hp) return lss::g_handleless_error.c_str();
     return hp->h.err.c_str();
 }
 

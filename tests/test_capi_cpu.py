@@ -94,6 +94,26 @@ def test_missing_dir_is_io_error(lib, tmp_path):
     assert st == 2 and "misc.txt" in msg
 
 
+def test_open_error_message_is_per_thread(lib, tmp_path):
+    """lss_last_error(NULL) is the message of this thread's last failed call without a handle: a
+    failure on another thread does not replace it."""
+    import threading
+    st, msg = _open_status(lib, tmp_path / "nope")
+    assert st == 2 and "misc.txt" in msg
+    other = {}
+
+    def run():
+        other["st"], other["msg"] = _open_status(lib, small := tmp_path / "also_missing_dir_x")
+        other["dir"] = str(small)
+
+    t = threading.Thread(target=run)
+    t.start()
+    t.join()
+    assert other["st"] == 2 and "also_missing_dir_x" in other["msg"]
+    again = (lib.lss_last_error(None) or b"").decode()
+    assert again == msg
+
+
 def test_missing_misc_key(lib, small_oss, tmp_path):
     d = tmp_path / "o"
     shutil.copytree(small_oss, d)
