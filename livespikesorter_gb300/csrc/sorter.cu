@@ -17,6 +17,8 @@
 #include "proposal.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -24,6 +26,7 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <thread>
 #include <string>
@@ -60,17 +63,111 @@ static T* dev_upload(const std::vector<T>& v, int64_t& tally, cudaStream_t s) {
     return p;
 }
 
+namespace {
+// Host copies of a few hundred kB to a few MB (one batch of pageable rows into the pinned staging)
+// go through a small process-wide pool of copy helpers: the copy is cut into chunks that the
+// calling thread and the helpers claim from a shared counter, so a call never waits for a busy
+// pool -- the caller copies whatever the helpers have not taken -- and only for chunks already
+// being copied.
+struct CopyJob {
+    char* dst;
+    const char* src;
+    size_t bytes, chunk, nchunks;
+    std::atomic<size_t> next{0}, done{0};
+};
+
+void copy_chunks(CopyJob& j) {
+    for (size_t c; (c = j.next.fetch_add(1, std::memory_order_relaxed)) < j.nchunks;) {
+        const size_t off = c * j.chunk;
+        std::memcpy(j.dst + off, j.src + off, std::min(j.chunk, j.bytes - off));
+        j.done.fetch_add(1, std::memory_order_release);
+    }
+}
+
+class CopyPool {
+  public:
+    static CopyPool& get() {
+        static CopyPool pool;
+        return pool;
+    }
+    size_t helpers() const { return th_.size(); }
+    void run(void* dst, const void* src, size_t bytes, size_t chunk) {
+        auto j = std::make_shared<CopyJob>();
+        j->dst = static_cast<char*>(dst);
+        j->src = static_cast<const char*>(src);
+        j->bytes = bytes;
+        j->chunk = chunk;
+        j->nchunks = (bytes + chunk - 1) / chunk;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            q_.push_back(j);
+        }
+        cv_.notify_all();
+        copy_chunks(*j);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            auto it = std::find(q_.begin(), q_.end(), j);
+            if (it != q_.end()) q_.erase(it);
+        }
+        // chunks a helper claimed are a memcpy each from being done
+        while (j->done.load(std::memory_order_acquire) < j->nchunks) std::this_thread::yield();
+    }
+
+  private:
+    CopyPool() {
+        const unsigned hw = std::thread::hardware_concurrency();
+        const unsigned n = std::min(4u, hw / 4);
+        for (unsigned i = 0; i < n; ++i) th_.emplace_back([this] { work(); });
+    }
+    ~CopyPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : th_) t.join();
+    }
+    void work() {
+        std::unique_lock<std::mutex> lk(mu_);
+        for (;;) {
+            cv_.wait(lk, [this] { return stop_ || !q_.empty(); });
+            if (stop_) return;
+            std::shared_ptr<CopyJob> j = q_.front();
+            lk.unlock();
+            copy_chunks(*j);
+            lk.lock();
+            if (!q_.empty() && q_.front() == j) q_.pop_front();   // every chunk is claimed
+        }
+    }
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<std::shared_ptr<CopyJob>> q_;
+    bool stop_ = false;
+    std::vector<std::thread> th_;
+};
+}  // namespace
+
 // memcpy split across threads for large host copies (pinned staging fills at several GB/s per
-// core; one thread alone is the bottleneck of the host path for multi-MB groups)
+// core; one thread alone is the bottleneck of the host path): copies of 8 MB and more on threads
+// of their own, from 512 kB on the copy pool
 void par_memcpy(void* dst, const void* src, size_t bytes) {
     constexpr size_t kChunk = 4u << 20;
+    constexpr size_t kPoolMin = 512u << 10, kPoolChunk = 256u << 10;
     const size_t nthr = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency() / 2), 16);
-    if (bytes < 2 * kChunk || nthr < 2) {
+    if (bytes < 2 * kChunk) {
+        if (bytes >= kPoolMin && CopyPool::get().helpers() > 0) {
+            CopyPool::get().run(dst, src, bytes, kPoolChunk);
+            return;
+        }
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    if (nthr < 2) {
         std::memcpy(dst, src, bytes);
         return;
     }
     const size_t k = std::min(nthr, bytes / kChunk);
-    const size_t per = (bytes / k + 63) / 64 * 64;
+    const size_t per = ((bytes + k - 1) / k + 63) / 64 * 64;   // k * per >= bytes: nothing left over
     std::vector<std::thread> th;
     th.reserve(k);
     for (size_t i = 1; i < k; ++i) {
