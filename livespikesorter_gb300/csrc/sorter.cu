@@ -1590,7 +1590,7 @@ int lss_sort_windows(lss_handle* hp, const int16_t* windows, int32_t n_windows, 
             const int g = std::min(per, n_windows - w0);
             const int si = h.acquire_slot();
             lss::Slot& s = h.slots[si];
-            std::memcpy(s.h_stage, windows + (size_t)w0 * W * h.Cin, (size_t)g * W * h.Cin * sizeof(int16_t));
+            lss::par_memcpy(s.h_stage, windows + (size_t)w0 * W * h.Cin, (size_t)g * W * h.Cin * sizeof(int16_t));
             s.windows_api = true;
             s.win_start.assign(g, 0);
             s.drop_before.assign(g, INT64_MIN);
